@@ -1,0 +1,129 @@
+"""ctypes binding of libbhtsne_gpu.so (the C ABI in include/bhtsne_gpu.h).
+
+The library is built in-tree (bhtsne_gb300/build.py). There is no fallback:
+if the library cannot be built or loaded, every call raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import threading
+
+from . import build as _build
+
+OK, ENOMEM, EINVAL, ETIMEDOUT, ECUDA, EINTERNAL = 0, 12, 22, 110, 1001, 1002
+F32, F64 = 0, 1
+METHOD_EXACT, METHOD_BARNES_HUT, METHOD_FIT_SNE = 1, 2, 3
+
+EPOCH_CB = C.CFUNCTYPE(None, C.c_int64, C.c_void_p, C.c_void_p)
+
+# Every symbol declared in include/bhtsne_gpu.h with its (restype, argtypes).
+_vp, _i64, _i32, _dbl, _u64p, _u32p, _i32p, _i64p, _dblp = (
+    C.c_void_p, C.c_int64, C.c_int32, C.c_double, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p)
+SIGNATURES = {
+    "bhtsne_version": (C.c_char_p, []),
+    "bhtsne_ctx_create": (C.c_int, [C.c_int, C.POINTER(C.c_void_p)]),
+    "bhtsne_ctx_destroy": (C.c_int, [_vp]),
+    "bhtsne_ctx_last_error": (C.c_char_p, [_vp]),
+    "bhtsne_tsne_new": (C.c_int, [_vp, C.c_int, _i32, _i64, C.POINTER(C.c_void_p)]),
+    "bhtsne_tsne_free": (C.c_int, [_vp]),
+    "bhtsne_tsne_last_error": (C.c_char_p, [_vp]),
+    "bhtsne_tsne_learning_rate": (C.c_int, [_vp, _dbl]),
+    "bhtsne_tsne_epochs": (C.c_int, [_vp, _i64]),
+    "bhtsne_tsne_momentum": (C.c_int, [_vp, _dbl]),
+    "bhtsne_tsne_final_momentum": (C.c_int, [_vp, _dbl]),
+    "bhtsne_tsne_momentum_switch_epoch": (C.c_int, [_vp, _i64]),
+    "bhtsne_tsne_stop_lying_epoch": (C.c_int, [_vp, _i64]),
+    "bhtsne_tsne_early_exaggeration": (C.c_int, [_vp, _dbl]),
+    "bhtsne_tsne_perplexity": (C.c_int, [_vp, _dbl]),
+    "bhtsne_tsne_epoch_callback": (C.c_int, [_vp, _vp, _vp]),
+    "bhtsne_tsne_initial_embedding": (C.c_int, [_vp, _vp, _i64]),
+    "bhtsne_tsne_random_seed": (C.c_int, [_vp, C.c_uint64]),
+    "bhtsne_tsne_exact_euclidean": (C.c_int, [_vp, _vp, _i32, _i32]),
+    "bhtsne_tsne_exact_distances": (C.c_int, [_vp, _vp]),
+    "bhtsne_tsne_barnes_hut_euclidean": (C.c_int, [_vp, _dbl, _vp, _i32]),
+    "bhtsne_tsne_barnes_hut_with_neighbors": (C.c_int, [_vp, _dbl, _u64p, _vp, _i64, _i64]),
+    "bhtsne_tsne_fit_sne_euclidean": (C.c_int, [_vp, _vp, _i32]),
+    "bhtsne_tsne_fit_sne_with_neighbors": (C.c_int, [_vp, _u64p, _vp, _i64, _i64]),
+    "bhtsne_tsne_embedding": (C.c_int, [_vp, _vp]),
+    "bhtsne_tsne_kl_divergence": (C.c_int, [_vp, _i32, _dblp, _i32p]),
+    "bhtsne_tsne_affinities": (C.c_int, [_vp, _u64p, _u32p, _vp, _i64p, _dblp, _i32p]),
+    "bhtsne_tsne_with_affinities": (C.c_int, [_vp, _u64p, _i64, _u32p, _vp, _i64, _dbl]),
+    "bhtsne_tsne_advance": (C.c_int, [_vp, _i64]),
+    "bhtsne_tsne_timings": (C.c_int, [_vp, _dblp, _dblp, _i64p]),
+    "bhtsne_knn_euclidean": (C.c_int, [_vp, C.c_int, _vp, _i64, _i32, _i32, _u32p, _vp]),
+    "bhtsne_conditional_p": (C.c_int, [_vp, C.c_int, _vp, _i64, _i32, _dbl, _vp, _i32p]),
+    "bhtsne_symmetrize": (C.c_int, [_vp, C.c_int, _u32p, _vp, _i64, _i32, _u64p, _u32p, _vp, _i64p]),
+    "bhtsne_gradient": (C.c_int, [_vp, C.c_int, _i32, _i32, _vp, _i64, _u64p, _u32p, _vp, _i64, _dbl, _vp, _vp,
+                                  _dblp]),
+    "bhtsne_update": (C.c_int, [_vp, C.c_int, _i32, _vp, _vp, _vp, _vp, _vp, _i64, _dbl, _dbl, _dbl]),
+}
+
+_lock = threading.Lock()
+_lib = None
+
+
+def library_path() -> str:
+    return _build.LIB
+
+
+def load(build_if_needed: bool = True):
+    """Loads (building first if needed) the CUDA library. Raises on failure."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        path = _build.build() if build_if_needed else _build.LIB
+        if not os.path.exists(path):
+            raise RuntimeError(f"libbhtsne_gpu.so is missing at {path}; run bhtsne_gb300/build.py")
+        lib = C.CDLL(path)
+        for name, (res, args) in SIGNATURES.items():
+            f = getattr(lib, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = lib
+        return _lib
+
+
+class BhtsneError(RuntimeError):
+    def __init__(self, code: int, message: str):
+        super().__init__(message)
+        self.code = code
+
+
+class Context:
+    """One CUDA device and stream (bhtsne_ctx)."""
+
+    def __init__(self, device: int = 0):
+        self.lib = load()
+        h = C.c_void_p()
+        rc = self.lib.bhtsne_ctx_create(int(device), C.byref(h))
+        if rc != OK:
+            raise BhtsneError(rc, f"bhtsne_ctx_create failed with status {rc} (is a CUDA device visible?)")
+        self.handle = h
+        self.device = device
+
+    def check(self, rc: int) -> None:
+        if rc != OK:
+            raise BhtsneError(rc, self.lib.bhtsne_ctx_last_error(self.handle).decode())
+
+    def close(self) -> None:
+        if getattr(self, "handle", None):
+            self.lib.bhtsne_ctx_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+_default_ctx = None
+
+
+def default_context() -> Context:
+    global _default_ctx
+    if _default_ctx is None:
+        _default_ctx = Context(0)
+    return _default_ctx

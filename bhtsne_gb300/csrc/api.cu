@@ -1,0 +1,1023 @@
+// C ABI of the library (include/bhtsne_gpu.h): the tSNE builder state machine
+// and the stage entry points.
+//
+// The handle mirrors the reference builder (bhtsne 0.7.10, src/lib.rs):
+// fields :149-176, defaults :241-266, setters :277-435, finishers :489-951,
+// affinity cache :1019-1051 and :1192-1248, epoch tail :1162-1179. Device
+// state (P, y, velocity, gains and every scratch buffer) stays resident in the
+// handle; host memory is touched only for the caller's inputs and outputs and
+// for the optional per-epoch callback snapshot.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <functional>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/bhtsne_gpu.h"
+#include "affinity.h"
+#include "bh.h"
+#include "epoch.h"
+#include "fitsne.h"
+#include "knn.h"
+
+using namespace bhg;
+
+struct bhtsne_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::string err;
+};
+
+namespace {
+
+const char* kVersion = "bhtsne-gb300 0.1.0 (restates bhtsne 0.7.10)";
+
+template <class T>
+struct State {
+  int D = 2;
+  int64_t n = 0;
+  // sparse P (CSR)
+  bool has_sparse = false;
+  int64_t sparse_rows = 0;  // number of row offsets held (n + 1 when usable)
+  int64_t nnz = 0;
+  DevBuf rows, cols, vals;
+  // dense P (exact)
+  bool has_dense = false;
+  DevBuf pdense;
+  // optimisation state
+  DevBuf y, uy, gains, pos, neg, zbuf, klbuf, tmp, tmp2;
+  DevBuf kidx, kdist, kp, xin;
+  BhWorkspace<T> bh;
+  FitWorkspace<T> fit;
+  UpdateScratch us;
+  SymWorkspace<T> sym;
+  KnnWorkspace knn;
+};
+
+template <class T>
+void upload(DevBuf& b, const void* src, size_t bytes, cudaStream_t s) {
+  b.ensure(bytes);
+  if (bytes) BHG_CUDA(cudaMemcpyAsync(b.ptr, src, bytes, cudaMemcpyHostToDevice, s));
+}
+
+template <class T>
+__global__ void fill_kernel(T* p, int64_t n, T v) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) p[i] = v;
+}
+
+__global__ void match_neighbors_kernel(const uint64_t* __restrict__ rows, const uint32_t* __restrict__ cols, int64_t n,
+                                       int64_t k, const uint32_t* __restrict__ idx, int* __restrict__ mismatch) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n * k) return;
+  const int64_t i = e / k, j = e % k;
+  const uint64_t s = rows[i], t = rows[i + 1];
+  if ((int64_t)(t - s) != k || cols[s + j] != idx[e]) *mismatch = 1;
+}
+
+uint64_t lcg_next(uint64_t& s) {
+  s = s * 6364136223846793005ULL + 1442695040888963407ULL;
+  return s;
+}
+
+}  // namespace
+
+struct bhtsne_tsne {
+  bhtsne_ctx* ctx = nullptr;
+  int dtype = BHTSNE_F32;
+  int D = 2;
+  int64_t n = 0;
+  // builder fields (values rounded through T at the setter)
+  bool has_lr = false;
+  double lr = 0;
+  int64_t epochs = 1000;
+  double momentum = 0.5, final_momentum = 0.8;
+  int64_t momentum_switch_epoch = 250, stop_lying_epoch = 250;
+  double early_exaggeration = 12.0, perplexity = 20.0;
+  bhtsne_epoch_cb cb = nullptr;
+  void* user = nullptr;
+  bool has_init = false;
+  std::vector<unsigned char> init;
+  int64_t init_len = 0;
+  bool stop_lying_fired = false;
+  bool has_cached_perplexity = false;
+  double cached_perplexity = 0;
+  int fit = 0;
+  double fit_theta = 0;
+  uint64_t seed = 0x6268747336e65ULL;
+  // armed loop (for advance)
+  bool armed = false;
+  int loop_kind = 0;
+  double loop_theta = 0, loop_lr = 0;
+  int64_t cursor = 0;
+  // timings
+  double aff_ms = 0, loop_ms = 0;
+  int64_t loop_epochs = 0;
+  std::string err;
+  State<float>* sf = nullptr;
+  State<double>* sd = nullptr;
+};
+
+namespace {
+
+double tcast(const bhtsne_tsne* t, double v) { return t->dtype == BHTSNE_F32 ? (double)(float)v : v; }
+
+[[noreturn]] void invalid(const std::string& m) { throw Error(ST_EINVAL, m); }
+
+template <class F>
+int guard_ctx(bhtsne_ctx* ctx, F&& f) {
+  if (!ctx) return BHTSNE_EINVAL;
+  try {
+    BHG_CUDA(cudaSetDevice(ctx->device));
+    f();
+    ctx->err.clear();
+    return BHTSNE_OK;
+  } catch (const Error& e) {
+    ctx->err = e.what();
+    return e.code;
+  } catch (const std::exception& e) {
+    ctx->err = e.what();
+    return BHTSNE_EINTERNAL;
+  }
+}
+
+template <class F>
+int guard(bhtsne_tsne* t, F&& f) {
+  if (!t) return BHTSNE_EINVAL;
+  try {
+    BHG_CUDA(cudaSetDevice(t->ctx->device));
+    f();
+    return BHTSNE_OK;
+  } catch (const Error& e) {
+    t->err = e.what();
+    return e.code;
+  } catch (const std::exception& e) {
+    t->err = e.what();
+    return BHTSNE_EINTERNAL;
+  }
+}
+
+// check_perplexity: src/tsne/mod.rs:55-59.
+void check_perplexity(const bhtsne_tsne* t) {
+  const double perp = t->perplexity;
+  const int64_t as_usize = perp > 0 ? (int64_t)perp : 0;
+  if (t->n < 1 || (t->n - 1) < 3 * as_usize)
+    invalid("error: the provided perplexity is too large for the number of data points.\n");
+}
+
+// validate_fit_params: src/lib.rs:1182-1189.
+void validate_fit_params(const bhtsne_tsne* t, double theta) {
+  if (!(theta > 0))
+    invalid(
+        "error: theta value must be greater than 0.0.\n            A value of 0.0 corresponds to using the exact "
+        "version of the algorithm.");
+  check_perplexity(t);
+}
+
+template <class T>
+State<T>& st(bhtsne_tsne* t);
+template <>
+State<float>& st<float>(bhtsne_tsne* t) {
+  return *t->sf;
+}
+template <>
+State<double>& st<double>(bhtsne_tsne* t) {
+  return *t->sd;
+}
+
+template <class T>
+T resolve_lr(const bhtsne_tsne* t) {
+  if (t->has_lr) return (T)t->lr;
+  const T a = (T)(double)t->n / (T)t->early_exaggeration / (T)4.0;
+  return a > (T)50.0 ? a : (T)50.0;
+}
+
+template <class T>
+void host_random_init(const bhtsne_tsne* t, std::vector<T>& y) {
+  uint64_t s = t->seed;
+  for (size_t e = 0; e < y.size(); e += 2) {
+    const double u1 = ((lcg_next(s) >> 11) + 0.5) * (1.0 / 9007199254740992.0);
+    const double u2 = ((lcg_next(s) >> 11) + 0.5) * (1.0 / 9007199254740992.0);
+    const double r = std::sqrt(-2.0 * std::log(u1));
+    y[e] = (T)(1e-4 * r * std::cos(2 * M_PI * u2));
+    if (e + 1 < y.size()) y[e + 1] = (T)(1e-4 * r * std::sin(2 * M_PI * u2));
+  }
+}
+
+// finalize_p_and_seed: src/lib.rs:663-685 (plus the optimisation buffers that
+// the reference resizes in build_affinities / prepare_cached).
+template <class T>
+void finalize_p_and_seed(bhtsne_tsne* t, bool dense) {
+  State<T>& S = st<T>(t);
+  cudaStream_t s = t->ctx->stream;
+  const int64_t ge = t->n * t->D;
+  T* p = dense ? S.pdense.template as<T>() : S.vals.template as<T>();
+  const int64_t np = dense ? t->n * t->n : S.nnz;
+  launch_normalize<T>(p, np, (T)t->early_exaggeration, S.zbuf.template as<double>() + 2, S.tmp, s);
+  if (t->stop_lying_epoch == 0) launch_scale<T>(p, np, T(1) / (T)t->early_exaggeration, s);
+  S.y.ensure(ge * sizeof(T));
+  if (t->has_init) {
+    t->has_init = false;
+    if (t->init_len != ge) {
+      const int64_t got = t->init_len;
+      t->init.clear();
+      invalid("error: initial embedding has " + std::to_string(got) + " values, expected n_samples * D = " +
+              std::to_string(ge));
+    }
+    BHG_CUDA(cudaMemcpyAsync(S.y.ptr, t->init.data(), ge * sizeof(T), cudaMemcpyHostToDevice, s));
+    BHG_CUDA(cudaStreamSynchronize(s));
+    t->init.clear();
+  } else {
+    std::vector<T> h(ge);
+    host_random_init<T>(t, h);
+    BHG_CUDA(cudaMemcpyAsync(S.y.ptr, h.data(), ge * sizeof(T), cudaMemcpyHostToDevice, s));
+    BHG_CUDA(cudaStreamSynchronize(s));
+  }
+  S.uy.ensure(ge * sizeof(T));
+  S.gains.ensure(ge * sizeof(T));
+  BHG_CUDA(cudaMemsetAsync(S.uy.ptr, 0, ge * sizeof(T), s));
+  fill_kernel<T><<<256, 256, 0, s>>>(S.gains.template as<T>(), ge, T(1));
+  BHG_LAUNCH_CHECK();
+}
+
+template <class T>
+void ensure_state(bhtsne_tsne* t) {
+  State<T>& S = st<T>(t);
+  S.D = t->D;
+  S.n = t->n;
+  const int64_t ge = std::max<int64_t>(t->n * t->D, 1);
+  S.pos.ensure(ge * sizeof(T));
+  S.neg.ensure(ge * sizeof(T));
+  S.zbuf.ensure(16 * sizeof(double));
+  S.klbuf.ensure(16 * sizeof(double));
+}
+
+// build_affinities: src/lib.rs:1061-1127, from a device kNN table in S.kidx / S.kdist.
+template <class T>
+void build_affinities(bhtsne_tsne* t, int64_t k) {
+  State<T>& S = st<T>(t);
+  cudaStream_t s = t->ctx->stream;
+  const int64_t n = t->n;
+  S.kp.ensure(n * k * sizeof(T));
+  launch_search_beta<T>(S.kdist.template as<T>(), n, k, (T)t->perplexity, S.kp.template as<T>(), nullptr, s);
+  const int64_t nnz = symmetrize<T>(S.kidx.template as<uint32_t>(), S.kp.template as<T>(), n, (int)k, S.sym, s);
+  S.rows.ensure((n + 1) * 8);
+  S.cols.ensure(std::max<int64_t>(nnz, 1) * 4);
+  S.vals.ensure(std::max<int64_t>(nnz, 1) * sizeof(T));
+  symmetrize_finish<T>(S.sym, n, nnz, S.rows.template as<uint64_t>(), S.cols.template as<uint32_t>(),
+                       S.vals.template as<T>(), s);
+  BHG_CUDA(cudaStreamSynchronize(s));
+  S.sym.release();
+  S.kp.release();
+  S.nnz = nnz;
+  S.has_sparse = true;
+  S.sparse_rows = n + 1;
+  t->has_cached_perplexity = true;
+  t->cached_perplexity = t->perplexity;
+}
+
+template <class T>
+void epoch_tail(bhtsne_tsne* t, int64_t epoch, std::vector<T>& snap) {
+  State<T>& S = st<T>(t);
+  cudaStream_t s = t->ctx->stream;
+  if (epoch == t->stop_lying_epoch && epoch != 0) {
+    const T scale = T(1) / (T)t->early_exaggeration;
+    if (t->loop_kind == BHTSNE_METHOD_EXACT) launch_scale<T>(S.pdense.template as<T>(), t->n * t->n, scale, s);
+    else launch_scale<T>(S.vals.template as<T>(), S.nnz, scale, s);
+    t->stop_lying_fired = true;
+  }
+  if (epoch == t->momentum_switch_epoch) t->momentum = t->final_momentum;
+  if (t->cb) {
+    snap.resize(t->n * t->D);
+    BHG_CUDA(cudaMemcpyAsync(snap.data(), S.y.ptr, snap.size() * sizeof(T), cudaMemcpyDeviceToHost, s));
+    BHG_CUDA(cudaStreamSynchronize(s));
+    t->cb(epoch, snap.data(), t->user);
+  }
+}
+
+template <class T>
+int bits_for_method(const bhtsne_tsne* t) {
+  return (t->loop_kind == BHTSNE_METHOD_BARNES_HUT) ? bh_bits<T>(t->D) : 32;
+}
+
+// The epoch loop body of run_loop (src/lib.rs:961-1014) and of exact's loop
+// (src/lib.rs:567-638), on device-resident state.
+template <class T>
+void advance_impl(bhtsne_tsne* t, int64_t epochs) {
+  State<T>& S = st<T>(t);
+  cudaStream_t s = t->ctx->stream;
+  const int64_t n = t->n;
+  const int D = t->D;
+  const T lr = (T)t->loop_lr;
+  const int bits = bits_for_method<T>(t);
+  std::vector<T> snap;
+  S.bh.reserve(n, D);
+  cudaEvent_t e0, e1;
+  BHG_CUDA(cudaEventCreate(&e0));
+  BHG_CUDA(cudaEventCreate(&e1));
+  BHG_CUDA(cudaEventRecord(e0, s));
+  T* y = S.y.template as<T>();
+  double* z = S.zbuf.template as<double>();
+  for (int64_t k = 0; k < epochs; ++k) {
+    const int64_t epoch = t->cursor;
+    if (epoch == 0) launch_recenter_bbox<T>(D, y, n, nullptr, false, S.bh, bits, s);
+    const T mom = (T)t->momentum;
+    if (t->loop_kind == BHTSNE_METHOD_BARNES_HUT) {
+      bh_build<T>(S.bh, D, y, n, s);
+      bh_traverse<T>(S.bh, D, y, n, (T)t->loop_theta, S.neg.template as<T>(), nullptr, s);
+      launch_attractive<T>(D, S.rows.template as<uint64_t>(), S.cols.template as<uint32_t>(), S.vals.template as<T>(), y, n,
+                           S.pos.template as<T>(), s);
+      launch_update<T>(D, y, S.pos.template as<T>(), S.neg.template as<T>(), S.uy.template as<T>(),
+                       S.gains.template as<T>(), n, S.bh.z(), T(0), lr, mom, S.us, s);
+    } else if (t->loop_kind == BHTSNE_METHOD_FIT_SNE) {
+      fit_repulsion<T>(S.fit, D, y, n, S.bh.params.template as<BoxParams<T>>(), S.neg.template as<T>(), z, s);
+      launch_attractive<T>(D, S.rows.template as<uint64_t>(), S.cols.template as<uint32_t>(), S.vals.template as<T>(), y, n,
+                           S.pos.template as<T>(), s);
+      launch_update<T>(D, y, S.pos.template as<T>(), S.neg.template as<T>(), S.uy.template as<T>(),
+                       S.gains.template as<T>(), n, z, T(0), lr, mom, S.us, s);
+    } else {
+      launch_exact_z<T>(D, y, n, z, S.tmp, s);
+      launch_exact_grad<T>(D, y, S.pdense.template as<T>(), n, z, S.pos.template as<T>(), s);
+      launch_update<T>(D, y, S.pos.template as<T>(), nullptr, S.uy.template as<T>(), S.gains.template as<T>(), n,
+                       nullptr, T(0), lr, mom, S.us, s);
+    }
+    launch_recenter_bbox<T>(D, y, n, S.us.mean(), true, S.bh, bits, s);
+    epoch_tail<T>(t, epoch, snap);
+    t->cursor += 1;
+  }
+  BHG_CUDA(cudaEventRecord(e1, s));
+  BHG_CUDA(cudaEventSynchronize(e1));
+  float ms = 0;
+  BHG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+  BHG_CUDA(cudaEventDestroy(e0));
+  BHG_CUDA(cudaEventDestroy(e1));
+  t->loop_ms = ms;
+  t->loop_epochs = epochs;
+}
+
+template <class T>
+void run_loop(bhtsne_tsne* t, int kind, double theta) {
+  t->armed = true;
+  t->loop_kind = kind;
+  t->loop_theta = theta;
+  t->loop_lr = (double)resolve_lr<T>(t);
+  t->cursor = 0;
+  advance_impl<T>(t, t->epochs);
+  t->fit = kind;
+  t->fit_theta = theta;
+}
+
+template <class T>
+bool has_cached_affinities(bhtsne_tsne* t) {
+  State<T>& S = st<T>(t);
+  return S.has_sparse && S.sparse_rows == t->n + 1 && t->has_cached_perplexity &&
+         t->cached_perplexity == t->perplexity;
+}
+
+// prepare_cached + run_cached: src/lib.rs:1227-1248.
+template <class T>
+void run_cached(bhtsne_tsne* t, int kind, double theta) {
+  t->stop_lying_fired = false;
+  ensure_state<T>(t);
+  finalize_p_and_seed<T>(t, false);
+  run_loop<T>(t, kind, theta);
+}
+
+template <class T>
+void timed_affinities(bhtsne_tsne* t, const std::function<void()>& f) {
+  cudaStream_t s = t->ctx->stream;
+  cudaEvent_t e0, e1;
+  BHG_CUDA(cudaEventCreate(&e0));
+  BHG_CUDA(cudaEventCreate(&e1));
+  BHG_CUDA(cudaEventRecord(e0, s));
+  f();
+  BHG_CUDA(cudaEventRecord(e1, s));
+  BHG_CUDA(cudaEventSynchronize(e1));
+  float ms = 0;
+  BHG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  t->aff_ms = ms;
+}
+
+// barnes_hut / fit_sne over a dense Euclidean dataset: src/lib.rs:701-742, :835-871.
+template <class T>
+void fit_euclidean(bhtsne_tsne* t, int kind, double theta, const void* data, int32_t dim) {
+  if (kind == BHTSNE_METHOD_BARNES_HUT) validate_fit_params(t, theta);
+  else check_perplexity(t);
+  if (has_cached_affinities<T>(t)) {
+    run_cached<T>(t, kind, theta);
+    return;
+  }
+  if (!data || dim <= 0) invalid("error: data must be a non-empty n_samples x dim array.");
+  State<T>& S = st<T>(t);
+  ensure_state<T>(t);
+  cudaStream_t s = t->ctx->stream;
+  const int64_t n = t->n;
+  const int64_t k = (int64_t)((T)3.0 * (T)t->perplexity);
+  timed_affinities<T>(t, [&] {
+    upload<T>(S.xin, data, (size_t)n * dim * sizeof(T), s);
+    S.kidx.ensure(n * k * 4);
+    S.kdist.ensure(n * k * sizeof(T));
+    knn_euclidean<T>(S.xin.template as<T>(), n, dim, (int)k, S.kidx.template as<uint32_t>(), S.kdist.template as<T>(),
+                     S.knn, s);
+    S.xin.release();
+    S.knn.release();
+    build_affinities<T>(t, k);
+  });
+  S.kidx.release();
+  S.kdist.release();
+  finalize_p_and_seed<T>(t, false);
+  run_loop<T>(t, kind, theta);
+}
+
+// *_with_neighbors: src/lib.rs:757-772, :884-894, :922-951.
+template <class T>
+void fit_with_neighbors(bhtsne_tsne* t, int kind, double theta, const uint64_t* idx, const void* dist, int64_t rows,
+                        int64_t k) {
+  if (kind == BHTSNE_METHOD_BARNES_HUT) validate_fit_params(t, theta);
+  const int64_t n = t->n;
+  if (rows != n)
+    invalid("error: neighbors has " + std::to_string(rows) + " rows, expected one per sample = " + std::to_string(n));
+  if (k <= 0 || !idx || !dist) invalid("error: every neighbors row must have the same length, greater than zero.");
+  State<T>& S = st<T>(t);
+  ensure_state<T>(t);
+  cudaStream_t s = t->ctx->stream;
+  // Indices are compared and stored as u32 (the reference's `index as u32`).
+  std::vector<uint32_t> idx32((size_t)(n * k));
+  bool in_range = true;
+  for (int64_t e = 0; e < n * k; ++e) {
+    idx32[e] = (uint32_t)idx[e];
+    in_range &= idx[e] < (uint64_t)n;
+  }
+  S.kidx.ensure(n * k * 4);
+  BHG_CUDA(cudaMemcpyAsync(S.kidx.ptr, idx32.data(), n * k * 4, cudaMemcpyHostToDevice, s));
+  // cached_affinities_match_neighbors: src/lib.rs:1201-1220.
+  if (S.has_sparse && S.sparse_rows == n + 1 && t->has_cached_perplexity && t->cached_perplexity == t->perplexity) {
+    int* mm = static_cast<int*>(S.tmp2.ensure(64));
+    BHG_CUDA(cudaMemsetAsync(mm, 0, 4, s));
+    match_neighbors_kernel<<<(unsigned)ceil_div(n * k, 256), 256, 0, s>>>(S.rows.template as<uint64_t>(),
+                                                                          S.cols.template as<uint32_t>(), n, k,
+                                                                          S.kidx.template as<uint32_t>(), mm);
+    BHG_LAUNCH_CHECK();
+    int h = 1;
+    BHG_CUDA(cudaMemcpyAsync(&h, mm, 4, cudaMemcpyDeviceToHost, s));
+    BHG_CUDA(cudaStreamSynchronize(s));
+    if (h == 0) {
+      S.kidx.release();
+      run_cached<T>(t, kind, theta);
+      return;
+    }
+  }
+  if (!in_range)
+    invalid("error: a neighbor index is out of range, every index must be < n_samples = " + std::to_string(n) + ".");
+  timed_affinities<T>(t, [&] {
+    upload<T>(S.kdist, dist, (size_t)n * k * sizeof(T), s);
+    build_affinities<T>(t, k);
+  });
+  S.kidx.release();
+  S.kdist.release();
+  finalize_p_and_seed<T>(t, false);
+  run_loop<T>(t, kind, theta);
+}
+
+// exact: src/lib.rs:489-646, given the dense distance matrix on the device in S.pdense.
+template <class T>
+void exact_from_device_distances(bhtsne_tsne* t) {
+  State<T>& S = st<T>(t);
+  cudaStream_t s = t->ctx->stream;
+  const int64_t n = t->n;
+  timed_affinities<T>(t, [&] {
+    // search_beta over full rows, diagonal (distance 0) included.
+    S.kp.ensure(n * n * sizeof(T));
+    launch_search_beta<T>(S.pdense.template as<T>(), n, n, (T)t->perplexity, S.kp.template as<T>(), nullptr, s);
+    std::swap(S.pdense.ptr, S.kp.ptr);
+    std::swap(S.pdense.bytes, S.kp.bytes);
+    S.kp.release();
+    launch_dense_symmetrize<T>(S.pdense.template as<T>(), n, s);
+  });
+  S.has_dense = true;
+  // The reference reuses p_values for the dense matrix; the sparse cache is
+  // no longer valid after an exact fit.
+  S.has_sparse = false;
+  finalize_p_and_seed<T>(t, true);
+  run_loop<T>(t, BHTSNE_METHOD_EXACT, 0.0);
+}
+
+template <class T>
+void exact_euclidean(bhtsne_tsne* t, const void* data, int32_t dim, int32_t squared) {
+  check_perplexity(t);
+  if (!data || dim <= 0) invalid("error: data must be a non-empty n_samples x dim array.");
+  State<T>& S = st<T>(t);
+  ensure_state<T>(t);
+  cudaStream_t s = t->ctx->stream;
+  const int64_t n = t->n;
+  upload<T>(S.xin, data, (size_t)n * dim * sizeof(T), s);
+  S.pdense.ensure(n * n * sizeof(T));
+  launch_dense_distance<T>(S.xin.template as<T>(), n, dim, squared != 0, S.pdense.template as<T>(), s);
+  S.xin.release();
+  exact_from_device_distances<T>(t);
+}
+
+template <class T>
+__global__ void mirror_upper_kernel(T* d, int64_t n) {
+  const int64_t i = blockIdx.y;
+  const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n || j >= n) return;
+  if (j == i) d[i * n + j] = T(0);
+  else if (j < i) d[i * n + j] = d[j * n + i];
+}
+
+template <class T>
+void exact_distances(bhtsne_tsne* t, const void* dist) {
+  check_perplexity(t);
+  State<T>& S = st<T>(t);
+  ensure_state<T>(t);
+  cudaStream_t s = t->ctx->stream;
+  const int64_t n = t->n;
+  upload<T>(S.pdense, dist, (size_t)n * n * sizeof(T), s);
+  dim3 g((unsigned)ceil_div(n, 256), (unsigned)n);
+  mirror_upper_kernel<T><<<g, 256, 0, s>>>(S.pdense.template as<T>(), n);
+  BHG_LAUNCH_CHECK();
+  exact_from_device_distances<T>(t);
+}
+
+// kl_divergence: src/lib.rs:448-477.
+template <class T>
+bool kl(bhtsne_tsne* t, bool quirk, double* out) {
+  if (t->fit == 0) return false;
+  State<T>& S = st<T>(t);
+  cudaStream_t s = t->ctx->stream;
+  const int64_t n = t->n;
+  const int D = t->D;
+  T* y = S.y.template as<T>();
+  double* z = S.klbuf.template as<double>();
+  double* res = z + 1;
+  if (t->fit == BHTSNE_METHOD_EXACT) {
+    launch_exact_z<T>(D, y, n, z, S.tmp, s);
+    launch_exact_kl<T>(D, y, S.pdense.template as<T>(), n, z, res, S.tmp2, s);
+  } else {
+    S.bh.reserve(n, D);
+    if (t->fit == BHTSNE_METHOD_BARNES_HUT) {
+      launch_recenter_bbox<T>(D, y, n, nullptr, false, S.bh, bh_bits<T>(D), s);
+      bh_build<T>(S.bh, D, y, n, s);
+      bh_traverse<T>(S.bh, D, y, n, (T)t->fit_theta, S.neg.template as<T>(), nullptr, s);
+      BHG_CUDA(cudaMemcpyAsync(z, S.bh.z(), sizeof(double), cudaMemcpyDeviceToDevice, s));
+    } else {
+      launch_recenter_bbox<T>(D, y, n, nullptr, false, S.bh, 32, s);
+      fit_repulsion<T>(S.fit, D, y, n, S.bh.params.template as<BoxParams<T>>(), S.neg.template as<T>(), z, s);
+    }
+    launch_kl_sparse<T>(D, S.rows.template as<uint64_t>(), S.cols.template as<uint32_t>(), S.vals.template as<T>(), y, n,
+                        z, quirk, res, S.tmp2, s);
+  }
+  BHG_CUDA(cudaMemcpyAsync(out, res, sizeof(double), cudaMemcpyDeviceToHost, s));
+  BHG_CUDA(cudaStreamSynchronize(s));
+  return true;
+}
+
+template <class T>
+void new_state(bhtsne_tsne* t);
+template <>
+void new_state<float>(bhtsne_tsne* t) {
+  t->sf = new State<float>();
+}
+template <>
+void new_state<double>(bhtsne_tsne* t) {
+  t->sd = new State<double>();
+}
+
+#define DISPATCH(t, ...)            \
+  do {                              \
+    if ((t)->dtype == BHTSNE_F32) { \
+      typedef float T;              \
+      __VA_ARGS__;                  \
+    } else {                        \
+      typedef double T;             \
+      __VA_ARGS__;                  \
+    }                               \
+  } while (0)
+
+#define DISPATCH_DT(dt, ...)   \
+  do {                         \
+    if ((dt) == BHTSNE_F32) {  \
+      typedef float T;         \
+      __VA_ARGS__;             \
+    } else {                   \
+      typedef double T;        \
+      __VA_ARGS__;             \
+    }                          \
+  } while (0)
+
+}  // namespace
+
+// ===========================================================================
+extern "C" {
+
+const char* bhtsne_version(void) { return kVersion; }
+
+int bhtsne_ctx_create(int device, bhtsne_ctx** out) {
+  if (!out) return BHTSNE_EINVAL;
+  *out = nullptr;
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || count <= 0) return BHTSNE_ECUDA;
+  if (device < 0 || device >= count) return BHTSNE_EINVAL;
+  bhtsne_ctx* c = new bhtsne_ctx();
+  c->device = device;
+  if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete c;
+    return BHTSNE_ECUDA;
+  }
+  *out = c;
+  return BHTSNE_OK;
+}
+
+int bhtsne_ctx_destroy(bhtsne_ctx* ctx) {
+  if (!ctx) return BHTSNE_OK;
+  cudaSetDevice(ctx->device);
+  if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  delete ctx;
+  return BHTSNE_OK;
+}
+
+const char* bhtsne_ctx_last_error(const bhtsne_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+int bhtsne_tsne_new(bhtsne_ctx* ctx, int dtype, int32_t embed_dim, int64_t n_samples, bhtsne_tsne** out) {
+  if (!ctx || !out) return BHTSNE_EINVAL;
+  *out = nullptr;
+  if (dtype != BHTSNE_F32 && dtype != BHTSNE_F64) {
+    ctx->err = "error: dtype must be BHTSNE_F32 or BHTSNE_F64.";
+    return BHTSNE_EINVAL;
+  }
+  if (embed_dim < 1 || embed_dim > 3) {
+    ctx->err = "error: the embedding dimension must be 1, 2 or 3.";
+    return BHTSNE_EINVAL;
+  }
+  if (n_samples < 0 || n_samples > 0x7fffffffLL) {
+    ctx->err = "error: n_samples must be in [0, 2^31).";
+    return BHTSNE_EINVAL;
+  }
+  bhtsne_tsne* t = new bhtsne_tsne();
+  t->ctx = ctx;
+  t->dtype = dtype;
+  t->D = embed_dim;
+  t->n = n_samples;
+  t->momentum = tcast(t, 0.5);
+  t->final_momentum = tcast(t, 0.8);
+  t->early_exaggeration = tcast(t, 12.0);
+  t->perplexity = tcast(t, 20.0);
+  DISPATCH(t, new_state<T>(t));
+  *out = t;
+  return BHTSNE_OK;
+}
+
+int bhtsne_tsne_free(bhtsne_tsne* t) {
+  if (!t) return BHTSNE_OK;
+  cudaSetDevice(t->ctx->device);
+  delete t->sf;
+  delete t->sd;
+  delete t;
+  return BHTSNE_OK;
+}
+
+const char* bhtsne_tsne_last_error(const bhtsne_tsne* t) { return t ? t->err.c_str() : "null handle"; }
+
+int bhtsne_tsne_learning_rate(bhtsne_tsne* t, double v) {
+  if (!t) return BHTSNE_EINVAL;
+  t->has_lr = true;
+  t->lr = tcast(t, v);
+  return BHTSNE_OK;
+}
+int bhtsne_tsne_epochs(bhtsne_tsne* t, int64_t v) {
+  if (!t || v < 0) return BHTSNE_EINVAL;
+  t->epochs = v;
+  return BHTSNE_OK;
+}
+int bhtsne_tsne_momentum(bhtsne_tsne* t, double v) {
+  if (!t) return BHTSNE_EINVAL;
+  t->momentum = tcast(t, v);
+  return BHTSNE_OK;
+}
+int bhtsne_tsne_final_momentum(bhtsne_tsne* t, double v) {
+  if (!t) return BHTSNE_EINVAL;
+  t->final_momentum = tcast(t, v);
+  return BHTSNE_OK;
+}
+int bhtsne_tsne_momentum_switch_epoch(bhtsne_tsne* t, int64_t v) {
+  if (!t || v < 0) return BHTSNE_EINVAL;
+  t->momentum_switch_epoch = v;
+  return BHTSNE_OK;
+}
+int bhtsne_tsne_stop_lying_epoch(bhtsne_tsne* t, int64_t v) {
+  if (!t || v < 0) return BHTSNE_EINVAL;
+  t->stop_lying_epoch = v;
+  return BHTSNE_OK;
+}
+int bhtsne_tsne_early_exaggeration(bhtsne_tsne* t, double v) {
+  if (!t) return BHTSNE_EINVAL;
+  t->early_exaggeration = tcast(t, v);
+  return BHTSNE_OK;
+}
+int bhtsne_tsne_perplexity(bhtsne_tsne* t, double v) {
+  if (!t) return BHTSNE_EINVAL;
+  t->perplexity = tcast(t, v);
+  return BHTSNE_OK;
+}
+int bhtsne_tsne_epoch_callback(bhtsne_tsne* t, bhtsne_epoch_cb cb, void* user) {
+  if (!t) return BHTSNE_EINVAL;
+  t->cb = cb;
+  t->user = user;
+  return BHTSNE_OK;
+}
+int bhtsne_tsne_initial_embedding(bhtsne_tsne* t, const void* y, int64_t len) {
+  if (!t || len < 0 || (len > 0 && !y)) return BHTSNE_EINVAL;
+  const size_t es = t->dtype == BHTSNE_F32 ? 4 : 8;
+  t->init.assign((const unsigned char*)y, (const unsigned char*)y + (size_t)len * es);
+  t->init_len = len;
+  t->has_init = true;
+  return BHTSNE_OK;
+}
+int bhtsne_tsne_random_seed(bhtsne_tsne* t, uint64_t seed) {
+  if (!t) return BHTSNE_EINVAL;
+  t->seed = seed;
+  return BHTSNE_OK;
+}
+
+int bhtsne_tsne_exact_euclidean(bhtsne_tsne* t, const void* data, int32_t dim, int32_t squared) {
+  return guard(t, [&] { DISPATCH(t, exact_euclidean<T>(t, data, dim, squared)); });
+}
+int bhtsne_tsne_exact_distances(bhtsne_tsne* t, const void* distances) {
+  return guard(t, [&] {
+    if (!distances) invalid("error: distances must be an n_samples x n_samples array.");
+    DISPATCH(t, exact_distances<T>(t, distances));
+  });
+}
+int bhtsne_tsne_barnes_hut_euclidean(bhtsne_tsne* t, double theta, const void* data, int32_t dim) {
+  return guard(t, [&] {
+    if (t->D < 2 || t->D > 3) invalid("error: the GPU Barnes-Hut path covers D in {2, 3}.");
+    DISPATCH(t, fit_euclidean<T>(t, BHTSNE_METHOD_BARNES_HUT, tcast(t, theta), data, dim));
+  });
+}
+int bhtsne_tsne_barnes_hut_with_neighbors(bhtsne_tsne* t, double theta, const uint64_t* indices, const void* distances,
+                                          int64_t rows, int64_t k) {
+  return guard(t, [&] {
+    if (t->D < 2 || t->D > 3) invalid("error: the GPU Barnes-Hut path covers D in {2, 3}.");
+    DISPATCH(t, fit_with_neighbors<T>(t, BHTSNE_METHOD_BARNES_HUT, tcast(t, theta), indices, distances, rows, k));
+  });
+}
+int bhtsne_tsne_fit_sne_euclidean(bhtsne_tsne* t, const void* data, int32_t dim) {
+  return guard(t, [&] {
+    if (t->D < 1 || t->D > 2) invalid("error: FIt-SNE is restricted to D in {1, 2}.");
+    DISPATCH(t, fit_euclidean<T>(t, BHTSNE_METHOD_FIT_SNE, 0.0, data, dim));
+  });
+}
+int bhtsne_tsne_fit_sne_with_neighbors(bhtsne_tsne* t, const uint64_t* indices, const void* distances, int64_t rows,
+                                       int64_t k) {
+  return guard(t, [&] {
+    if (t->D < 1 || t->D > 2) invalid("error: FIt-SNE is restricted to D in {1, 2}.");
+    DISPATCH(t, fit_with_neighbors<T>(t, BHTSNE_METHOD_FIT_SNE, 0.0, indices, distances, rows, k));
+  });
+}
+
+int bhtsne_tsne_embedding(bhtsne_tsne* t, void* out) {
+  return guard(t, [&] {
+    if (!out) invalid("error: output buffer is null.");
+    DISPATCH(t, {
+      State<T>& S = st<T>(t);
+      const size_t bytes = (size_t)t->n * t->D * sizeof(T);
+      if (!S.y.ptr || S.y.bytes < bytes) {
+        // The reference returns an empty vector before a fit.
+        return;
+      }
+      BHG_CUDA(cudaMemcpyAsync(out, S.y.ptr, bytes, cudaMemcpyDeviceToHost, t->ctx->stream));
+      BHG_CUDA(cudaStreamSynchronize(t->ctx->stream));
+    });
+  });
+}
+
+int bhtsne_tsne_kl_divergence(bhtsne_tsne* t, int32_t quirk, double* out, int32_t* has_value) {
+  return guard(t, [&] {
+    double v = 0;
+    bool has = false;
+    DISPATCH(t, has = kl<T>(t, quirk != 0, &v));
+    if (has_value) *has_value = has ? 1 : 0;
+    if (out && has) *out = v;
+  });
+}
+
+int bhtsne_tsne_affinities(bhtsne_tsne* t, uint64_t* rows, uint32_t* columns, void* values, int64_t* nnz,
+                           double* perplexity, int32_t* has_value) {
+  return guard(t, [&] {
+    DISPATCH(t, {
+      State<T>& S = st<T>(t);
+      if (has_value) *has_value = S.has_sparse ? 1 : 0;
+      if (!S.has_sparse) return;
+      if (nnz) *nnz = S.nnz;
+      if (perplexity) *perplexity = t->perplexity;
+      cudaStream_t s = t->ctx->stream;
+      if (rows) BHG_CUDA(cudaMemcpyAsync(rows, S.rows.ptr, S.sparse_rows * 8, cudaMemcpyDeviceToHost, s));
+      if (columns) BHG_CUDA(cudaMemcpyAsync(columns, S.cols.ptr, S.nnz * 4, cudaMemcpyDeviceToHost, s));
+      if (values) {
+        if (t->stop_lying_fired) {
+          BHG_CUDA(cudaMemcpyAsync(values, S.vals.ptr, S.nnz * sizeof(T), cudaMemcpyDeviceToHost, s));
+        } else {
+          T* tmp = static_cast<T*>(S.tmp2.ensure(std::max<int64_t>(S.nnz, 1) * sizeof(T)));
+          launch_scaled_copy<T>(S.vals.template as<T>(), S.nnz, T(1) / (T)t->early_exaggeration, tmp, s);
+          BHG_CUDA(cudaMemcpyAsync(values, tmp, S.nnz * sizeof(T), cudaMemcpyDeviceToHost, s));
+        }
+      }
+      BHG_CUDA(cudaStreamSynchronize(s));
+    });
+  });
+}
+
+int bhtsne_tsne_with_affinities(bhtsne_tsne* t, const uint64_t* rows, int64_t n_rows, const uint32_t* columns,
+                                const void* values, int64_t nnz, double perplexity) {
+  return guard(t, [&] {
+    if (n_rows < 1 || nnz < 0 || !rows || (nnz > 0 && (!columns || !values)))
+      invalid("error: affinities must hold row offsets, columns and values.");
+    DISPATCH(t, {
+      State<T>& S = st<T>(t);
+      ensure_state<T>(t);
+      cudaStream_t s = t->ctx->stream;
+      upload<T>(S.rows, rows, n_rows * 8, s);
+      S.cols.ensure(std::max<int64_t>(nnz, 1) * 4);
+      S.vals.ensure(std::max<int64_t>(nnz, 1) * sizeof(T));
+      if (nnz > 0) {
+        BHG_CUDA(cudaMemcpyAsync(S.cols.ptr, columns, nnz * 4, cudaMemcpyHostToDevice, s));
+        BHG_CUDA(cudaMemcpyAsync(S.vals.ptr, values, nnz * sizeof(T), cudaMemcpyHostToDevice, s));
+      }
+      BHG_CUDA(cudaStreamSynchronize(s));
+      S.nnz = nnz;
+      S.sparse_rows = n_rows;
+      S.has_sparse = true;
+      t->perplexity = tcast(t, perplexity);
+      t->has_cached_perplexity = true;
+      t->cached_perplexity = t->perplexity;
+    });
+  });
+}
+
+int bhtsne_tsne_advance(bhtsne_tsne* t, int64_t epochs) {
+  return guard(t, [&] {
+    if (!t->armed) invalid("error: advance needs a completed fit on this handle.");
+    if (epochs < 0) invalid("error: epochs must be >= 0.");
+    DISPATCH(t, advance_impl<T>(t, epochs));
+  });
+}
+
+int bhtsne_tsne_timings(const bhtsne_tsne* t, double* affinity_ms, double* loop_ms, int64_t* loop_epochs) {
+  if (!t) return BHTSNE_EINVAL;
+  if (affinity_ms) *affinity_ms = t->aff_ms;
+  if (loop_ms) *loop_ms = t->loop_ms;
+  if (loop_epochs) *loop_epochs = t->loop_epochs;
+  return BHTSNE_OK;
+}
+
+// ---- stage entry points ----------------------------------------------------
+int bhtsne_knn_euclidean(bhtsne_ctx* ctx, int dtype, const void* data, int64_t n, int32_t dim, int32_t k,
+                         uint32_t* indices, void* distances) {
+  return guard_ctx(ctx, [&] {
+    if (!data || !indices || !distances || n < 2 || dim <= 0) invalid("error: invalid kNN arguments.");
+    DISPATCH_DT(dtype, {
+      cudaStream_t s = ctx->stream;
+      DevBuf x, idx, dist;
+      KnnWorkspace ws;
+      upload<T>(x, data, (size_t)n * dim * sizeof(T), s);
+      idx.ensure((size_t)n * k * 4);
+      dist.ensure((size_t)n * k * sizeof(T));
+      knn_euclidean<T>(x.as<T>(), n, dim, k, idx.as<uint32_t>(), dist.as<T>(), ws, s);
+      BHG_CUDA(cudaMemcpyAsync(indices, idx.ptr, (size_t)n * k * 4, cudaMemcpyDeviceToHost, s));
+      BHG_CUDA(cudaMemcpyAsync(distances, dist.ptr, (size_t)n * k * sizeof(T), cudaMemcpyDeviceToHost, s));
+      BHG_CUDA(cudaStreamSynchronize(s));
+    });
+  });
+}
+
+int bhtsne_conditional_p(bhtsne_ctx* ctx, int dtype, const void* distances, int64_t n, int32_t k, double perplexity,
+                         void* p, int32_t* iterations) {
+  return guard_ctx(ctx, [&] {
+    if (!distances || !p || n < 0 || k <= 0) invalid("error: invalid conditional P arguments.");
+    DISPATCH_DT(dtype, {
+      cudaStream_t s = ctx->stream;
+      DevBuf d, out, it;
+      upload<T>(d, distances, (size_t)n * k * sizeof(T), s);
+      out.ensure((size_t)n * k * sizeof(T));
+      if (iterations) it.ensure((size_t)n * 4);
+      launch_search_beta<T>(d.as<T>(), n, k, (T)perplexity, out.as<T>(), iterations ? it.as<int32_t>() : nullptr, s);
+      BHG_CUDA(cudaMemcpyAsync(p, out.ptr, (size_t)n * k * sizeof(T), cudaMemcpyDeviceToHost, s));
+      if (iterations) BHG_CUDA(cudaMemcpyAsync(iterations, it.ptr, (size_t)n * 4, cudaMemcpyDeviceToHost, s));
+      BHG_CUDA(cudaStreamSynchronize(s));
+    });
+  });
+}
+
+int bhtsne_symmetrize(bhtsne_ctx* ctx, int dtype, const uint32_t* columns, const void* p, int64_t n, int32_t k,
+                      uint64_t* rows_out, uint32_t* columns_out, void* values_out, int64_t* nnz) {
+  return guard_ctx(ctx, [&] {
+    if (!columns || !p || n < 1 || k <= 0) invalid("error: invalid symmetrize arguments.");
+    DISPATCH_DT(dtype, {
+      cudaStream_t s = ctx->stream;
+      DevBuf c, v, r, co, vo;
+      SymWorkspace<T> ws;
+      upload<T>(c, columns, (size_t)n * k * 4, s);
+      upload<T>(v, p, (size_t)n * k * sizeof(T), s);
+      const int64_t m = symmetrize<T>(c.as<uint32_t>(), v.as<T>(), n, k, ws, s);
+      if (nnz) *nnz = m;
+      if (rows_out || columns_out || values_out) {
+        r.ensure((n + 1) * 8);
+        co.ensure(std::max<int64_t>(m, 1) * 4);
+        vo.ensure(std::max<int64_t>(m, 1) * sizeof(T));
+        symmetrize_finish<T>(ws, n, m, r.as<uint64_t>(), co.as<uint32_t>(), vo.as<T>(), s);
+        if (rows_out) BHG_CUDA(cudaMemcpyAsync(rows_out, r.ptr, (n + 1) * 8, cudaMemcpyDeviceToHost, s));
+        if (columns_out && m) BHG_CUDA(cudaMemcpyAsync(columns_out, co.ptr, m * 4, cudaMemcpyDeviceToHost, s));
+        if (values_out && m) BHG_CUDA(cudaMemcpyAsync(values_out, vo.ptr, m * sizeof(T), cudaMemcpyDeviceToHost, s));
+      }
+      BHG_CUDA(cudaStreamSynchronize(s));
+    });
+  });
+}
+
+int bhtsne_gradient(bhtsne_ctx* ctx, int dtype, int32_t method, int32_t embed_dim, const void* y, int64_t n,
+                    const uint64_t* rows, const uint32_t* columns, const void* values, int64_t nnz, double theta,
+                    void* pos, void* neg, double* z) {
+  return guard_ctx(ctx, [&] {
+    if (!y || n < 1 || !pos) invalid("error: invalid gradient arguments.");
+    if (embed_dim < 1 || embed_dim > 3) invalid("error: the embedding dimension must be 1, 2 or 3.");
+    DISPATCH_DT(dtype, {
+      cudaStream_t s = ctx->stream;
+      const int D = embed_dim;
+      DevBuf yd, rd, cd, vd, pd, nd, zd, tmp;
+      BhWorkspace<T> bh;
+      FitWorkspace<T> fw;
+      upload<T>(yd, y, (size_t)n * D * sizeof(T), s);
+      pd.ensure((size_t)n * D * sizeof(T));
+      nd.ensure((size_t)n * D * sizeof(T));
+      zd.ensure(64);
+      if (method == BHTSNE_METHOD_EXACT) {
+        upload<T>(vd, values, (size_t)n * n * sizeof(T), s);
+        launch_exact_z<T>(D, yd.as<T>(), n, zd.as<double>(), tmp, s);
+        launch_exact_grad<T>(D, yd.as<T>(), vd.as<T>(), n, zd.as<double>(), pd.as<T>(), s);
+      } else {
+        if (!rows || (nnz > 0 && (!columns || !values))) invalid("error: the sparse affinities are required.");
+        upload<T>(rd, rows, (size_t)(n + 1) * 8, s);
+        upload<T>(cd, columns, (size_t)std::max<int64_t>(nnz, 0) * 4, s);
+        upload<T>(vd, values, (size_t)std::max<int64_t>(nnz, 0) * sizeof(T), s);
+        bh.reserve(n, D);
+        if (method == BHTSNE_METHOD_BARNES_HUT) {
+          if (D < 2) invalid("error: the GPU Barnes-Hut path covers D in {2, 3}.");
+          if (!(theta > 0)) invalid("error: theta value must be greater than 0.0.");
+          launch_recenter_bbox<T>(D, yd.as<T>(), n, nullptr, false, bh, bh_bits<T>(D), s);
+          bh_build<T>(bh, D, yd.as<T>(), n, s);
+          bh_traverse<T>(bh, D, yd.as<T>(), n, (T)theta, nd.as<T>(), nullptr, s);
+          BHG_CUDA(cudaMemcpyAsync(zd.ptr, bh.z(), 8, cudaMemcpyDeviceToDevice, s));
+        } else if (method == BHTSNE_METHOD_FIT_SNE) {
+          if (D > 2) invalid("error: FIt-SNE is restricted to D in {1, 2}.");
+          launch_recenter_bbox<T>(D, yd.as<T>(), n, nullptr, false, bh, 32, s);
+          fit_repulsion<T>(fw, D, yd.as<T>(), n, bh.params.template as<BoxParams<T>>(), nd.as<T>(), zd.as<double>(), s);
+        } else {
+          invalid("error: unknown method.");
+        }
+        launch_attractive<T>(D, rd.as<uint64_t>(), cd.as<uint32_t>(), vd.as<T>(), yd.as<T>(), n, pd.as<T>(), s);
+        if (neg) BHG_CUDA(cudaMemcpyAsync(neg, nd.ptr, (size_t)n * D * sizeof(T), cudaMemcpyDeviceToHost, s));
+      }
+      BHG_CUDA(cudaMemcpyAsync(pos, pd.ptr, (size_t)n * D * sizeof(T), cudaMemcpyDeviceToHost, s));
+      double zh = 0;
+      BHG_CUDA(cudaMemcpyAsync(&zh, zd.ptr, 8, cudaMemcpyDeviceToHost, s));
+      BHG_CUDA(cudaStreamSynchronize(s));
+      if (z) *z = zh;
+    });
+  });
+}
+
+int bhtsne_update(bhtsne_ctx* ctx, int dtype, int32_t embed_dim, void* y, const void* pos, const void* neg, void* uy,
+                  void* gains, int64_t n, double learning_rate, double momentum, double inverse_z) {
+  return guard_ctx(ctx, [&] {
+    if (!y || !pos || !uy || !gains || n < 1) invalid("error: invalid update arguments.");
+    if (embed_dim < 1 || embed_dim > 3) invalid("error: the embedding dimension must be 1, 2 or 3.");
+    DISPATCH_DT(dtype, {
+      cudaStream_t s = ctx->stream;
+      const int D = embed_dim;
+      const size_t bytes = (size_t)n * D * sizeof(T);
+      DevBuf yd, pd, nd, ud, gd;
+      UpdateScratch us;
+      BhWorkspace<T> bh;
+      bh.reserve(n, D);
+      upload<T>(yd, y, bytes, s);
+      upload<T>(pd, pos, bytes, s);
+      if (neg) upload<T>(nd, neg, bytes, s);
+      upload<T>(ud, uy, bytes, s);
+      upload<T>(gd, gains, bytes, s);
+      launch_update<T>(D, yd.as<T>(), pd.as<T>(), neg ? nd.as<T>() : nullptr, ud.as<T>(), gd.as<T>(), n, nullptr,
+                       (T)inverse_z, (T)learning_rate, (T)momentum, us, s);
+      launch_recenter_bbox<T>(D, yd.as<T>(), n, us.mean(), true, bh, 32, s);
+      BHG_CUDA(cudaMemcpyAsync(y, yd.ptr, bytes, cudaMemcpyDeviceToHost, s));
+      BHG_CUDA(cudaMemcpyAsync(uy, ud.ptr, bytes, cudaMemcpyDeviceToHost, s));
+      BHG_CUDA(cudaMemcpyAsync(gains, gd.ptr, bytes, cudaMemcpyDeviceToHost, s));
+      BHG_CUDA(cudaStreamSynchronize(s));
+    });
+  });
+}
+
+}  // extern "C"

@@ -1,0 +1,659 @@
+// Barnes-Hut repulsion on the GPU: bounding box, Morton codes, radix sort,
+// a parallel build of the reference's compressed 2^D-tree, centre-of-mass
+// summaries, and a stackless per-point traversal.
+//
+// Reference behaviour restated (bhtsne 0.7.10):
+//  * bounding box, quantisation scale and per-level half widths:
+//    src/tsne/arena.rs:65-94, :154-174; quantize: src/tsne/morton.rs:103-120;
+//    encoders: src/tsne/morton/d2.rs:5-47, src/tsne/morton/d3.rs:5-50.
+//  * tree shape: src/tsne/arena.rs:197-259. A node whose Morton range holds
+//    more than one distinct code becomes internal at the tightest D-bit level
+//    that splits the range; its children are the non-empty orthants at that
+//    level; a run of equal codes is a leaf.
+//  * leaf centre of mass = mean of members (:264-284); internal = count
+//    weighted mean (:289-309).
+//  * traversal: :338-392 (skip the leaf at zero distance; descend while
+//    half_width^2[level] >= theta^2 * dist^2; accumulate count/(1+d^2)).
+//
+// GPU construction (no sequential breadth-first walk):
+//  * For sorted codes c[0..N), the boundary between s-1 and s (c[s-1] != c[s])
+//    has level l = bits-1 - msb(c[s-1]^c[s])/D. The internal node that owns
+//    the boundary is the Morton cell at depth l holding c[s]; its range
+//    [a, e) is found by binary search for the cell's first and one-past-last
+//    codes. The boundary is the node's representative when c[s-1] lies in the
+//    first child of that cell, so every internal node is emitted exactly once.
+//  * Nodes are laid out in depth-first preorder, i.e. by (range start, level).
+//    A bitmask per start position records the levels of the internal nodes
+//    starting there; an exclusive scan of (popcount + run-start flag) gives
+//    every node its index, and the index one past a node's subtree ("skip")
+//    is simply the scan value at the node's range end.
+//  * Internal centres of mass come from FP64 prefix sums of the Z-ordered
+//    points, (S[e] - S[a]) / (e - a), which equals the count-weighted mean of
+//    the children. Leaves are summed in T exactly like the reference so that
+//    a singleton leaf's centre is bit-identical to its point (the self test).
+#include "bh.h"
+
+namespace bhg {
+
+namespace {
+
+constexpr int kThreads = 256;
+
+template <int D>
+struct MortonD;
+template <>
+struct MortonD<2> {
+  static constexpr int BITS = 32;
+  __device__ static uint64_t part(uint64_t x) {
+    x &= 0x00000000ffffffffULL;
+    x = (x | (x << 16)) & 0x0000ffff0000ffffULL;
+    x = (x | (x << 8)) & 0x00ff00ff00ff00ffULL;
+    x = (x | (x << 4)) & 0x0f0f0f0f0f0f0f0fULL;
+    x = (x | (x << 2)) & 0x3333333333333333ULL;
+    return (x | (x << 1)) & 0x5555555555555555ULL;
+  }
+  __device__ static uint64_t encode(const uint32_t* c) { return part(c[0]) | (part(c[1]) << 1); }
+};
+template <>
+struct MortonD<3> {
+  static constexpr int BITS = 21;
+  __device__ static uint64_t part(uint64_t x) {
+    x &= 0x1fffffULL;
+    x = (x | (x << 32)) & 0x001f00000000ffffULL;
+    x = (x | (x << 16)) & 0x001f0000ff0000ffULL;
+    x = (x | (x << 8)) & 0x100f00f00f00f00fULL;
+    x = (x | (x << 4)) & 0x10c30c30c30c30c3ULL;
+    return (x | (x << 2)) & 0x1249249249249249ULL;
+  }
+  __device__ static uint64_t encode(const uint32_t* c) {
+    return part(c[0]) | (part(c[1]) << 1) | (part(c[2]) << 2);
+  }
+};
+
+template <class T>
+__device__ __forceinline__ uint32_t quantize(T v, T mn, T inv_scale, uint32_t max_bucket) {
+  const T scaled = floor((v - mn) * inv_scale);
+  if (scaled > T(0)) {
+    if (!(scaled < T(18446744073709551616.0))) return max_bucket;
+    const uint64_t q = (uint64_t)scaled;
+    return q < (uint64_t)max_bucket ? (uint32_t)q : max_bucket;
+  }
+  return 0u;
+}
+
+// ---------------------------------------------------------------------------
+// Recentre (optional) + per-axis bounding box; the last block to finish
+// derives the tree parameters. Also used by the FIt-SNE path (min/max only).
+// ---------------------------------------------------------------------------
+template <class T, int D>
+__global__ void recenter_bbox_kernel(T* __restrict__ y, int64_t n, const double* __restrict__ mean_sum,
+                                     int apply_mean, T* __restrict__ part_min, T* __restrict__ part_max,
+                                     unsigned* __restrict__ done, BoxParams<T>* __restrict__ out, int bits) {
+  __shared__ T smin[D][32], smax[D][32];
+  __shared__ bool last;
+  T mean[D];
+  if (apply_mean) {
+#pragma unroll
+    for (int a = 0; a < D; ++a) mean[a] = (T)mean_sum[a] / (T)n;
+  }
+  T mn[D], mx[D];
+#pragma unroll
+  for (int a = 0; a < D; ++a) {
+    mn[a] = Lim<T>::max();
+    mx[a] = -Lim<T>::max();
+  }
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+      T v = y[i * D + a];
+      if (apply_mean) {
+        v = v - mean[a];
+        y[i * D + a] = v;
+      }
+      mn[a] = fmin(mn[a], v);
+      mx[a] = fmax(mx[a], v);
+    }
+  }
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int a = 0; a < D; ++a) {
+    T m0 = warp_min(mn[a]), m1 = warp_max(mx[a]);
+    if (lane == 0) {
+      smin[a][w] = m0;
+      smax[a][w] = m1;
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const int nw = blockDim.x >> 5;
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+      T m0 = smin[a][0], m1 = smax[a][0];
+      for (int q = 1; q < nw; ++q) {
+        m0 = fmin(m0, smin[a][q]);
+        m1 = fmax(m1, smax[a][q]);
+      }
+      part_min[blockIdx.x * D + a] = m0;
+      part_max[blockIdx.x * D + a] = m1;
+    }
+    __threadfence();
+    last = atomicAdd(done, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  if (threadIdx.x == 0) {
+    T fmn[D], fmx[D];
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+      fmn[a] = Lim<T>::max();
+      fmx[a] = -Lim<T>::max();
+    }
+    for (unsigned b = 0; b < gridDim.x; ++b) {
+#pragma unroll
+      for (int a = 0; a < D; ++a) {
+        fmn[a] = fmin(fmn[a], ((volatile T*)part_min)[b * D + a]);
+        fmx[a] = fmax(fmx[a], ((volatile T*)part_max)[b * D + a]);
+      }
+    }
+    const T scale = (T)(double)(1ULL << bits);
+    T max_extent = T(0);
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+      const T ext = fmx[a] - fmn[a];
+      out->mn[a] = fmn[a];
+      out->mx[a] = fmx[a];
+      out->inv_scale[a] = ext > T(0) ? scale / ext : T(0);
+      max_extent = fmax(max_extent, ext);
+    }
+    for (int a = D; a < 3; ++a) {
+      out->mn[a] = T(0);
+      out->mx[a] = T(0);
+      out->inv_scale[a] = T(0);
+    }
+    out->max_extent = max_extent;
+    for (int l = 0; l <= bits; ++l) {
+      const T hw = max_extent / (T)(double)(1ULL << (l + 1));
+      out->hw2[l] = hw * hw;
+    }
+    *done = 0;
+  }
+}
+
+template <class T, int D>
+__global__ void morton_kernel(const T* __restrict__ y, int64_t n, const BoxParams<T>* __restrict__ prm,
+                              uint64_t* __restrict__ keys, uint32_t* __restrict__ idx) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  constexpr int B = MortonD<D>::BITS;
+  const uint32_t max_bucket = (uint32_t)((1ULL << B) - 1);
+  uint32_t q[D];
+#pragma unroll
+  for (int a = 0; a < D; ++a) q[a] = quantize<T>(y[i * D + a], prm->mn[a], prm->inv_scale[a], max_bucket);
+  keys[i] = MortonD<D>::encode(q);
+  idx[i] = (uint32_t)i;
+}
+
+// ---------------------------------------------------------------------------
+// FP64 prefix sums of the Z-ordered points (for internal centres of mass).
+// ---------------------------------------------------------------------------
+constexpr int kPsThreads = 256;
+constexpr int kPsItems = 8;
+constexpr int kPsTile = kPsThreads * kPsItems;
+
+template <class T, int D>
+__global__ void prefix_reduce_kernel(const T* __restrict__ y, const uint32_t* __restrict__ perm, int64_t n,
+                                     double* __restrict__ part) {
+  __shared__ double sh[D][kPsThreads / 32];
+  const int64_t base = (int64_t)blockIdx.x * kPsTile;
+  double s[D];
+#pragma unroll
+  for (int a = 0; a < D; ++a) s[a] = 0.0;
+  for (int i = 0; i < kPsItems; ++i) {
+    const int64_t p = base + (int64_t)i * kPsThreads + threadIdx.x;
+    if (p < n) {
+      const int64_t src = perm[p];
+#pragma unroll
+      for (int a = 0; a < D; ++a) s[a] += (double)y[src * D + a];
+    }
+  }
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int a = 0; a < D; ++a) {
+    double v = warp_sum(s[a]);
+    if (lane == 0) sh[a][w] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < D) {
+    double t = 0.0;
+    for (int q = 0; q < kPsThreads / 32; ++q) t += sh[threadIdx.x][q];
+    part[blockIdx.x * D + threadIdx.x] = t;
+  }
+}
+
+template <int D>
+__global__ void prefix_partials_kernel(double* __restrict__ part, int64_t nparts) {
+  if (threadIdx.x < D) {
+    double run = 0.0;
+    for (int64_t b = 0; b < nparts; ++b) {
+      const double v = part[b * D + threadIdx.x];
+      part[b * D + threadIdx.x] = run;
+      run += v;
+    }
+    part[nparts * D + threadIdx.x] = run;
+  }
+}
+
+// Writes the Z-ordered points (T) and their exclusive FP64 prefix sums S[0..n].
+template <class T, int D>
+__global__ void prefix_apply_kernel(const T* __restrict__ y, const uint32_t* __restrict__ perm, int64_t n,
+                                    const double* __restrict__ part, int64_t nparts, T* __restrict__ ys,
+                                    double* __restrict__ pre) {
+  __shared__ double sh[D][kPsThreads / 32];
+  const int64_t base = (int64_t)blockIdx.x * kPsTile + (int64_t)threadIdx.x * kPsItems;
+  double v[kPsItems][D];
+  double s[D];
+#pragma unroll
+  for (int a = 0; a < D; ++a) s[a] = 0.0;
+#pragma unroll
+  for (int i = 0; i < kPsItems; ++i) {
+    const int64_t p = base + i;
+    if (p < n) {
+      const int64_t src = perm[p];
+#pragma unroll
+      for (int a = 0; a < D; ++a) {
+        const T t = y[src * D + a];
+        ys[p * D + a] = t;
+        v[i][a] = (double)t;
+        s[a] += v[i][a];
+      }
+    } else {
+#pragma unroll
+      for (int a = 0; a < D; ++a) v[i][a] = 0.0;
+    }
+  }
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  double x[D];
+#pragma unroll
+  for (int a = 0; a < D; ++a) {
+    x[a] = s[a];
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const double t = __shfl_up_sync(kFull, x[a], o);
+      if (lane >= o) x[a] += t;
+    }
+    if (lane == 31) sh[a][w] = x[a];
+  }
+  __syncthreads();
+  if (threadIdx.x < D) {
+    double run = 0.0;
+    for (int q = 0; q < kPsThreads / 32; ++q) {
+      const double t = sh[threadIdx.x][q];
+      sh[threadIdx.x][q] = run;
+      run += t;
+    }
+  }
+  __syncthreads();
+  double run[D];
+#pragma unroll
+  for (int a = 0; a < D; ++a) run[a] = x[a] - s[a] + sh[a][w] + part[blockIdx.x * D + a];
+#pragma unroll
+  for (int i = 0; i < kPsItems; ++i) {
+    const int64_t p = base + i;
+    if (p < n) {
+#pragma unroll
+      for (int a = 0; a < D; ++a) {
+        pre[p * D + a] = run[a];
+        run[a] += v[i][a];
+      }
+    }
+  }
+  if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) {
+#pragma unroll
+    for (int a = 0; a < D; ++a) pre[n * D + a] = part[nparts * D + a];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Tree build.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int64_t lower_bound_u64(const uint64_t* __restrict__ c, int64_t lo, int64_t hi,
+                                                   uint64_t key) {
+  while (lo < hi) {
+    const int64_t mid = (lo + hi) >> 1;
+    if (c[mid] < key) lo = mid + 1;
+    else hi = mid;
+  }
+  return lo;
+}
+
+template <int D>
+__device__ __forceinline__ int boundary_level(uint64_t c0, uint64_t c1) {
+  constexpr int B = MortonD<D>::BITS;
+  const int highest = 63 - __clzll((long long)(c0 ^ c1));
+  return (B - 1) - highest / D;
+}
+
+// Range [a, e) of the depth-l Morton cell holding code c.
+template <int D>
+__device__ __forceinline__ void cell_range(const uint64_t* __restrict__ codes, int64_t n, uint64_t c, int l,
+                                           int64_t* a, int64_t* e) {
+  constexpr int B = MortonD<D>::BITS;
+  if (l == 0) {
+    *a = 0;
+    *e = n;
+    return;
+  }
+  const int shift = D * (B - l);
+  const uint64_t prefix = c >> shift;
+  *a = lower_bound_u64(codes, 0, n, prefix << shift);
+  const uint64_t limit = ~0ULL >> shift;  // largest prefix representable
+  if (prefix >= limit) *e = n;
+  else *e = lower_bound_u64(codes, *a, n, (prefix + 1) << shift);
+}
+
+template <int D>
+__global__ void tree_mark_kernel(const uint64_t* __restrict__ codes, int64_t n, uint32_t* __restrict__ mask) {
+  const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s <= 0 || s >= n) return;
+  const uint64_t c0 = codes[s - 1], c1 = codes[s];
+  if (c0 == c1) return;
+  constexpr int B = MortonD<D>::BITS;
+  const int l = boundary_level<D>(c0, c1);
+  int64_t a, e;
+  cell_range<D>(codes, n, c1, l, &a, &e);
+  const int sh1 = D * (B - l - 1);
+  if ((c0 >> sh1) == (codes[a] >> sh1)) atomicOr(&mask[a], 1u << l);
+}
+
+__global__ void tree_count_kernel(const uint64_t* __restrict__ codes, int64_t n, const uint32_t* __restrict__ mask,
+                                  uint32_t* __restrict__ cnt) {
+  const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  const bool run_start = s == 0 || codes[s - 1] != codes[s];
+  cnt[s] = (uint32_t)__popc(mask[s]) + (run_start ? 1u : 0u);
+}
+
+template <class T, int D>
+__global__ void tree_emit_kernel(const uint64_t* __restrict__ codes, int64_t n, const uint32_t* __restrict__ mask,
+                                 const uint64_t* __restrict__ base, const T* __restrict__ ys,
+                                 const double* __restrict__ pre, const BoxParams<T>* __restrict__ prm,
+                                 TreeNodes<T, D> nodes) {
+  const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  constexpr int B = MortonD<D>::BITS;
+  const uint64_t c1 = codes[s];
+  const bool run_start = s == 0 || codes[s - 1] != c1;
+  if (s > 0 && run_start) {
+    const uint64_t c0 = codes[s - 1];
+    const int l = boundary_level<D>(c0, c1);
+    int64_t a, e;
+    cell_range<D>(codes, n, c1, l, &a, &e);
+    const int sh1 = D * (B - l - 1);
+    if ((c0 >> sh1) == (codes[a] >> sh1)) {
+      const uint32_t m = mask[a];
+      const int64_t idx = (int64_t)base[a] + __popc(m & ((1u << l) - 1u));
+      const double cnt = (double)(e - a);
+      T com[D];
+#pragma unroll
+      for (int q = 0; q < D; ++q) com[q] = (T)((pre[e * D + q] - pre[a * D + q]) / cnt);
+      nodes.write(idx, com, (T)(uint32_t)(e - a), prm->hw2[l], (uint32_t)base[e]);
+    }
+  }
+  if (run_start) {
+    int64_t e = s + 1;
+    if (e < n && codes[e] == c1) {
+      // duplicate codes: find the run end
+      int64_t lo = e, hi = n;
+      while (lo < hi) {
+        const int64_t mid = (lo + hi) >> 1;
+        if (codes[mid] <= c1) lo = mid + 1;
+        else hi = mid;
+      }
+      e = lo;
+    }
+    const uint32_t m = mask[s];
+    const int64_t idx = (int64_t)base[s] + __popc(m);
+    const uint32_t count = (uint32_t)(e - s);
+    T com[D];
+    if (count == 1) {
+#pragma unroll
+      for (int q = 0; q < D; ++q) com[q] = ys[s * D + q];
+    } else {
+      T acc[D];
+#pragma unroll
+      for (int q = 0; q < D; ++q) acc[q] = T(0);
+      for (int64_t p = s; p < e; ++p) {
+#pragma unroll
+        for (int q = 0; q < D; ++q) acc[q] += ys[p * D + q];
+      }
+      const T inv = T(1) / (T)count;
+#pragma unroll
+      for (int q = 0; q < D; ++q) com[q] = acc[q] * inv;
+    }
+    nodes.write(idx, com, (T)count, T(-1), (uint32_t)base[e]);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Traversal: one thread per query point, queries taken in Z-order so that a
+// warp walks neighbouring paths. Writes the repulsive force and per-point q,
+// and reduces Z = sum q in FP64 (deterministic: per-block partials reduced in
+// block order by the last block).
+// ---------------------------------------------------------------------------
+template <class T, int D>
+__global__ void __launch_bounds__(kThreads) bh_traverse_kernel(const T* __restrict__ y, const uint32_t* __restrict__ perm,
+                                                               int64_t n, TreeNodes<T, D> nodes, const uint64_t* __restrict__ n_nodes_p,
+                                                               T theta_sq, T* __restrict__ neg, T* __restrict__ qout,
+                                                               double* __restrict__ zpart, unsigned* __restrict__ done,
+                                                               double* __restrict__ z_out) {
+  __shared__ double sh[32];
+  __shared__ bool last;
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  double qd = 0.0;
+  if (t < n) {
+    const int64_t pi = perm[t];
+    T qv[D];
+#pragma unroll
+    for (int a = 0; a < D; ++a) qv[a] = y[pi * D + a];
+    const uint32_t M = (uint32_t)*n_nodes_p;
+    T f[D];
+#pragma unroll
+    for (int a = 0; a < D; ++a) f[a] = T(0);
+    T q = T(0);
+    uint32_t i = 0;
+    while (i < M) {
+      T com[D], mass, r2;
+      uint32_t skip;
+      nodes.read(i, com, &mass, &r2, &skip);
+      T disp[D];
+      T dist = T(0);
+#pragma unroll
+      for (int a = 0; a < D; ++a) {
+        disp[a] = qv[a] - com[a];
+        dist += disp[a] * disp[a];
+      }
+      if (r2 >= theta_sq * dist) {
+        ++i;
+        continue;
+      }
+      i = skip;
+      if (r2 < T(0) && dist == T(0)) continue;
+      const T inv = T(1) / (T(1) + dist);
+      T m = mass * inv;
+      q += m;
+      m = m * inv;
+#pragma unroll
+      for (int a = 0; a < D; ++a) f[a] += m * disp[a];
+    }
+#pragma unroll
+    for (int a = 0; a < D; ++a) neg[pi * D + a] = f[a];
+    if (qout) qout[pi] = q;
+    qd = (double)q;
+  }
+  const double bs = block_sum(qd, sh);
+  if (threadIdx.x == 0) {
+    zpart[blockIdx.x] = bs;
+    __threadfence();
+    last = atomicAdd(done, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (last && threadIdx.x == 0) {
+    __threadfence();
+    double z = 0.0;
+    for (unsigned b = 0; b < gridDim.x; ++b) z += ((volatile double*)zpart)[b];
+    *z_out = z;
+    *done = 0;
+  }
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Host orchestration.
+// ---------------------------------------------------------------------------
+template <class T>
+void launch_recenter_bbox(int D, T* y, int64_t n, const double* mean_sum, bool apply_mean, BhWorkspace<T>& ws,
+                          int bits, cudaStream_t s) {
+  const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(n, kThreads), 2 * 152));
+  T* pmin = ws.part_min.template as<T>();
+  T* pmax = ws.part_max.template as<T>();
+  if (D == 1)
+    recenter_bbox_kernel<T, 1><<<grid, kThreads, 0, s>>>(y, n, mean_sum, apply_mean ? 1 : 0, pmin, pmax,
+                                                         ws.done.template as<unsigned>(), ws.params.template as<BoxParams<T>>(), bits);
+  else if (D == 2)
+    recenter_bbox_kernel<T, 2><<<grid, kThreads, 0, s>>>(y, n, mean_sum, apply_mean ? 1 : 0, pmin, pmax,
+                                                         ws.done.template as<unsigned>(), ws.params.template as<BoxParams<T>>(), bits);
+  else
+    recenter_bbox_kernel<T, 3><<<grid, kThreads, 0, s>>>(y, n, mean_sum, apply_mean ? 1 : 0, pmin, pmax,
+                                                         ws.done.template as<unsigned>(), ws.params.template as<BoxParams<T>>(), bits);
+  BHG_LAUNCH_CHECK();
+}
+
+template <class T>
+void BhWorkspace<T>::reserve(int64_t n_, int D_) {
+  n = n_;
+  D = D_;
+  const int64_t nn = std::max<int64_t>(n, 1);
+  keys.ensure(nn * 8);
+  keys_alt.ensure(nn * 8);
+  perm.ensure(nn * 4);
+  perm_alt.ensure(nn * 4);
+  ys.ensure(nn * D * sizeof(T));
+  pre.ensure((nn + 1) * D * sizeof(double));
+  pre_part.ensure((ceil_div(nn, kPsTile) + 1) * D * sizeof(double));
+  mask.ensure(nn * 4);
+  cnt.ensure(nn * 4);
+  base.ensure((nn + 1) * 8);
+  const int64_t max_nodes = 2 * nn;
+  if (D == 2) {
+    geom.ensure(max_nodes * sizeof(Quad<T>));
+    aux.ensure(max_nodes * sizeof(uint32_t));
+  } else {
+    geom.ensure(max_nodes * sizeof(Quad<T>));
+    aux.ensure(max_nodes * sizeof(RSkip<T>));
+  }
+  part_min.ensure(2 * 152 * 3 * sizeof(T));
+  part_max.ensure(2 * 152 * 3 * sizeof(T));
+  done.ensure(64);
+  zdone.ensure(64);
+  params.ensure(sizeof(BoxParams<T>));
+  zpart.ensure((ceil_div(nn, kThreads) + 1) * sizeof(double));
+  zval.ensure(sizeof(double));
+  if (!zeroed) {
+    BHG_CUDA(cudaMemset(done.ptr, 0, 64));
+    BHG_CUDA(cudaMemset(zdone.ptr, 0, 64));
+    zeroed = true;
+  }
+}
+
+template <class T, int D>
+static TreeNodes<T, D> nodes_of(BhWorkspace<T>& ws) {
+  TreeNodes<T, D> t;
+  t.geom = ws.geom.template as<Quad<T>>();
+  if constexpr (D == 2) t.skip = ws.aux.template as<uint32_t>();
+  else t.rs = ws.aux.template as<RSkip<T>>();
+  return t;
+}
+
+template <class T, int D>
+static void bh_build_impl(BhWorkspace<T>& ws, const T* y, int64_t n, cudaStream_t s) {
+  constexpr int B = MortonD<D>::BITS;
+  const unsigned g = (unsigned)ceil_div(n, kThreads);
+  morton_kernel<T, D><<<g, kThreads, 0, s>>>(y, n, ws.params.template as<BoxParams<T>>(), ws.keys.template as<uint64_t>(),
+                                             ws.perm.template as<uint32_t>());
+  BHG_LAUNCH_CHECK();
+  radix_sort_pairs<uint32_t>(ws.keys.template as<uint64_t>(), ws.perm.template as<uint32_t>(),
+                             ws.keys_alt.template as<uint64_t>(), ws.perm_alt.template as<uint32_t>(), n, 0, D * B,
+                             ws.sort_tmp, s);
+  const int64_t np = ceil_div(n, kPsTile);
+  prefix_reduce_kernel<T, D><<<(unsigned)np, kPsThreads, 0, s>>>(y, ws.perm.template as<uint32_t>(), n,
+                                                                  ws.pre_part.template as<double>());
+  BHG_LAUNCH_CHECK();
+  prefix_partials_kernel<D><<<1, 32, 0, s>>>(ws.pre_part.template as<double>(), np);
+  BHG_LAUNCH_CHECK();
+  prefix_apply_kernel<T, D><<<(unsigned)np, kPsThreads, 0, s>>>(y, ws.perm.template as<uint32_t>(), n,
+                                                                 ws.pre_part.template as<double>(), np,
+                                                                 ws.ys.template as<T>(), ws.pre.template as<double>());
+  BHG_LAUNCH_CHECK();
+  BHG_CUDA(cudaMemsetAsync(ws.mask.ptr, 0, (size_t)n * 4, s));
+  tree_mark_kernel<D><<<g, kThreads, 0, s>>>(ws.keys.template as<uint64_t>(), n, ws.mask.template as<uint32_t>());
+  BHG_LAUNCH_CHECK();
+  tree_count_kernel<<<g, kThreads, 0, s>>>(ws.keys.template as<uint64_t>(), n, ws.mask.template as<uint32_t>(),
+                                           ws.cnt.template as<uint32_t>());
+  BHG_LAUNCH_CHECK();
+  scan_u32_to_u64(ws.cnt.template as<uint32_t>(), ws.base.template as<uint64_t>(), n, ws.scan_tmp, s);
+  tree_emit_kernel<T, D><<<g, kThreads, 0, s>>>(ws.keys.template as<uint64_t>(), n, ws.mask.template as<uint32_t>(),
+                                                ws.base.template as<uint64_t>(), ws.ys.template as<T>(),
+                                                ws.pre.template as<double>(), ws.params.template as<BoxParams<T>>(),
+                                                nodes_of<T, D>(ws));
+  BHG_LAUNCH_CHECK();
+}
+
+template <class T>
+void bh_build(BhWorkspace<T>& ws, int D, const T* y, int64_t n, cudaStream_t s) {
+  if (n <= 0) return;
+  if (D == 2) bh_build_impl<T, 2>(ws, y, n, s);
+  else if (D == 3) bh_build_impl<T, 3>(ws, y, n, s);
+  else throw Error(ST_EINVAL, "error: the GPU Barnes-Hut path covers D in {2, 3}.");
+}
+
+template <class T>
+void bh_traverse(BhWorkspace<T>& ws, int D, const T* y, int64_t n, T theta, T* neg, T* qout, cudaStream_t s) {
+  if (n <= 0) {
+    BHG_CUDA(cudaMemsetAsync(ws.zval.ptr, 0, sizeof(double), s));
+    return;
+  }
+  const unsigned g = (unsigned)ceil_div(n, kThreads);
+  const T theta_sq = theta * theta;
+  const uint64_t* M = ws.base.template as<uint64_t>() + n;
+  if (D == 2)
+    bh_traverse_kernel<T, 2><<<g, kThreads, 0, s>>>(y, ws.perm.template as<uint32_t>(), n, nodes_of<T, 2>(ws), M, theta_sq, neg,
+                                                    qout, ws.zpart.template as<double>(), ws.zdone.template as<unsigned>(),
+                                                    ws.zval.template as<double>());
+  else
+    bh_traverse_kernel<T, 3><<<g, kThreads, 0, s>>>(y, ws.perm.template as<uint32_t>(), n, nodes_of<T, 3>(ws), M, theta_sq, neg,
+                                                    qout, ws.zpart.template as<double>(), ws.zdone.template as<unsigned>(),
+                                                    ws.zval.template as<double>());
+  BHG_LAUNCH_CHECK();
+}
+
+template <class T>
+int bh_bits(int D) {
+  return D == 2 ? MortonD<2>::BITS : MortonD<3>::BITS;
+}
+
+template struct BhWorkspace<float>;
+template struct BhWorkspace<double>;
+template void launch_recenter_bbox<float>(int, float*, int64_t, const double*, bool, BhWorkspace<float>&, int, cudaStream_t);
+template void launch_recenter_bbox<double>(int, double*, int64_t, const double*, bool, BhWorkspace<double>&, int,
+                                           cudaStream_t);
+template void bh_build<float>(BhWorkspace<float>&, int, const float*, int64_t, cudaStream_t);
+template void bh_build<double>(BhWorkspace<double>&, int, const double*, int64_t, cudaStream_t);
+template void bh_traverse<float>(BhWorkspace<float>&, int, const float*, int64_t, float, float*, float*, cudaStream_t);
+template void bh_traverse<double>(BhWorkspace<double>&, int, const double*, int64_t, double, double*, double*,
+                                  cudaStream_t);
+template int bh_bits<float>(int);
+template int bh_bits<double>(int);
+
+}  // namespace bhg

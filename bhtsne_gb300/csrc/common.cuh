@@ -1,0 +1,118 @@
+// Shared device/host helpers for the bhtsne GB300 library.
+//
+// Every translation unit is compiled with -fmad=false so that, like the Rust
+// reference (which never contracts a*b+c), each product and sum is rounded on
+// its own; kernels that want a fused multiply-add ask for it explicitly.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstdio>
+#include <stdexcept>
+#include <string>
+
+namespace bhg {
+
+// Status codes of the C ABI (errno-like values).
+enum : int {
+  ST_OK = 0,
+  ST_ENOMEM = 12,
+  ST_EINVAL = 22,
+  ST_ETIMEDOUT = 110,
+  ST_ECUDA = 1001,
+  ST_EINTERNAL = 1002,
+};
+
+struct Error : std::runtime_error {
+  int code;
+  Error(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+[[noreturn]] inline void throw_cuda(cudaError_t e, const char* what, const char* file, int line) {
+  char buf[512];
+  snprintf(buf, sizeof buf, "CUDA error %s (%s) at %s:%d: %s", cudaGetErrorName(e), cudaGetErrorString(e),
+           file, line, what);
+  throw Error(e == cudaErrorMemoryAllocation ? ST_ENOMEM : ST_ECUDA, buf);
+}
+
+#define BHG_CUDA(call)                                                   \
+  do {                                                                   \
+    cudaError_t e_ = (call);                                             \
+    if (e_ != cudaSuccess) ::bhg::throw_cuda(e_, #call, __FILE__, __LINE__); \
+  } while (0)
+
+#define BHG_LAUNCH_CHECK() BHG_CUDA(cudaGetLastError())
+
+inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
+
+constexpr int kWarp = 32;
+constexpr unsigned kFull = 0xffffffffu;
+
+// Numeric limits usable on the device.
+template <class T>
+struct Lim;
+template <>
+struct Lim<float> {
+  __host__ __device__ static constexpr float max() { return 3.40282347e+38f; }
+  __host__ __device__ static constexpr float min_pos() { return 1.17549435e-38f; }
+  __host__ __device__ static constexpr float eps() { return 1.1920929e-07f; }
+};
+template <>
+struct Lim<double> {
+  __host__ __device__ static constexpr double max() { return 1.7976931348623157e+308; }
+  __host__ __device__ static constexpr double min_pos() { return 2.2250738585072014e-308; }
+  __host__ __device__ static constexpr double eps() { return 2.220446049250313e-16; }
+};
+
+__device__ __forceinline__ float dexp(float x) { return expf(x); }
+__device__ __forceinline__ double dexp(double x) { return exp(x); }
+__device__ __forceinline__ float dlog(float x) { return logf(x); }
+__device__ __forceinline__ double dlog(double x) { return log(x); }
+__device__ __forceinline__ float dsqrt(float x) { return sqrtf(x); }
+__device__ __forceinline__ double dsqrt(double x) { return sqrt(x); }
+
+template <class V>
+__device__ __forceinline__ V warp_sum(V v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
+  return v;
+}
+
+template <class V>
+__device__ __forceinline__ V warp_min(V v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(kFull, v, o));
+  return v;
+}
+
+template <class V>
+__device__ __forceinline__ V warp_max(V v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(kFull, v, o));
+  return v;
+}
+
+// Block-wide sum of a double, result valid in thread 0. `sh` holds >= 32 doubles.
+__device__ __forceinline__ double block_sum(double v, double* sh) {
+  v = warp_sum(v);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) sh[w] = v;
+  __syncthreads();
+  double r = 0.0;
+  if (w == 0) {
+    const int nw = (blockDim.x + 31) >> 5;
+    r = lane < nw ? sh[lane] : 0.0;
+    r = warp_sum(r);
+  }
+  return r;
+}
+
+// Rust `signum`: +1 for +0.0 and positives, -1 for -0.0 and negatives, NaN for NaN.
+template <class T>
+__device__ __forceinline__ T signum(T x) {
+  return isnan(x) ? x : copysign(T(1), x);
+}
+
+}  // namespace bhg

@@ -1,0 +1,378 @@
+// Per-epoch kernels shared by every fitting method: the attractive CSR pass,
+// the fused gains/momentum update with the FP64 mean for recentring, the
+// sparse KL divergence, and the dense O(N^2) kernels of the exact method.
+//
+// Reference behaviour restated (bhtsne 0.7.10):
+//  * compute_edge_forces: src/tsne/arena.rs:398-427,
+//    pos_i = sum_{j in row i} p_ij / (1 + |y_i - y_j|^2) (y_i - y_j).
+//  * gradient_descent_step: src/tsne/mod.rs:470-516 (g = pos - neg / Z;
+//    gain + 0.2 on a sign change of (g, u), else * 0.8, floored at 0.01;
+//    u = mu u - lr gain g; y += u), update_solution: :423-451 (exact method,
+//    g = dy), zero_mean: :534-568, constants :29-31.
+//  * sparse_kl_divergence: src/tsne/mod.rs:738-775, including the indexing of
+//    the value array by row number (:768-770) when `quirk` is set.
+//  * exact epoch: src/lib.rs:567-638 (Q includes the diagonal, Z includes N,
+//    dy_i = sum_j (p_ij - q_ij / Z) q_ij (y_i - y_j)); evaluate_error:
+//    src/tsne/mod.rs:579-618; dense symmetrisation: src/lib.rs:548-554.
+#include "epoch.h"
+
+namespace bhg {
+
+namespace {
+
+template <class T, int D>
+__global__ void __launch_bounds__(256) attractive_kernel(const uint64_t* __restrict__ rows, const uint32_t* __restrict__ cols,
+                                                         const T* __restrict__ vals, const T* __restrict__ y, int64_t n,
+                                                         T* __restrict__ pos) {
+  const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (row >= n) return;
+  T yi[D], acc[D];
+#pragma unroll
+  for (int a = 0; a < D; ++a) {
+    yi[a] = y[row * D + a];
+    acc[a] = T(0);
+  }
+  const int64_t e0 = (int64_t)rows[row], e1 = (int64_t)rows[row + 1];
+  for (int64_t e = e0 + lane; e < e1; e += 32) {
+    const int64_t j = cols[e];
+    const T p = vals[e];
+    T disp[D];
+    T dist = T(0);
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+      disp[a] = yi[a] - y[j * D + a];
+      dist += disp[a] * disp[a];
+    }
+    const T factor = p / (dist + T(1));
+#pragma unroll
+    for (int a = 0; a < D; ++a) acc[a] += factor * disp[a];
+  }
+#pragma unroll
+  for (int a = 0; a < D; ++a) acc[a] = warp_sum(acc[a]);
+  if (lane == 0) {
+#pragma unroll
+    for (int a = 0; a < D; ++a) pos[row * D + a] = acc[a];
+  }
+}
+
+// Fused update over points; neg may be null (exact method: pos holds dy).
+// Accumulates sum(y_new) per axis in FP64 into mean_sum (deterministic: the
+// last block reduces the per-block partials in block order).
+template <class T, int D>
+__global__ void __launch_bounds__(256) update_kernel(T* __restrict__ y, const T* __restrict__ pos, const T* __restrict__ neg,
+                                                     T* __restrict__ uy, T* __restrict__ gains, int64_t n,
+                                                     const double* __restrict__ z, T inv_norm_arg, T lr, T momentum,
+                                                     double* __restrict__ part, unsigned* __restrict__ done,
+                                                     double* __restrict__ mean_sum) {
+  __shared__ double sh[D][32];
+  __shared__ bool last;
+  const T inc = (T)0.2, dec = (T)0.8, floor_ = (T)0.01;
+  const T inv_norm = neg ? (z ? T(1) / (T)(*z) : inv_norm_arg) : T(0);
+  double s[D];
+#pragma unroll
+  for (int a = 0; a < D; ++a) s[a] = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+      const int64_t e = i * D + a;
+      const T g = neg ? pos[e] - neg[e] * inv_norm : pos[e];
+      const T u = uy[e];
+      T gn = (signum(g) != signum(u)) ? gains[e] + inc : gains[e] * dec;
+      if (gn < floor_) gn = floor_;
+      gains[e] = gn;
+      const T un = momentum * u - lr * gn * g;
+      uy[e] = un;
+      const T yn = y[e] + un;
+      y[e] = yn;
+      s[a] += (double)yn;
+    }
+  }
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int a = 0; a < D; ++a) {
+    const double v = warp_sum(s[a]);
+    if (lane == 0) sh[a][w] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const int nw = blockDim.x >> 5;
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+      double t = 0.0;
+      for (int q = 0; q < nw; ++q) t += sh[a][q];
+      part[blockIdx.x * D + a] = t;
+    }
+    __threadfence();
+    last = atomicAdd(done, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (last && threadIdx.x == 0) {
+    __threadfence();
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+      double t = 0.0;
+      for (unsigned b = 0; b < gridDim.x; ++b) t += ((volatile double*)part)[b * D + a];
+      mean_sum[a] = t;
+    }
+    *done = 0;
+  }
+}
+
+template <class T, int D>
+__global__ void kl_sparse_kernel(const uint64_t* __restrict__ rows, const uint32_t* __restrict__ cols,
+                                 const T* __restrict__ vals, const T* __restrict__ y, int64_t n,
+                                 const double* __restrict__ z, int quirk, double* __restrict__ part) {
+  __shared__ double sh[32];
+  const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  const T inv_q_sum = T(1) / (T)(*z);
+  double acc = 0.0;
+  for (int64_t row = gw; row < n; row += nw) {
+    T cost = T(0);
+    const int64_t e0 = (int64_t)rows[row], e1 = (int64_t)rows[row + 1];
+    for (int64_t e = e0 + lane; e < e1; e += 32) {
+      const int64_t j = cols[e];
+      T q = T(0);
+#pragma unroll
+      for (int a = 0; a < D; ++a) {
+        const T d = y[row * D + a] - y[j * D + a];
+        q = q + d * d;
+      }
+      q = (T(1) / (T(1) + q)) * inv_q_sum;
+      const T p = quirk ? vals[row] : vals[e];
+      cost += p * dlog((p + Lim<T>::min_pos()) / (q + Lim<T>::min_pos()));
+    }
+    acc += (double)cost;
+  }
+  const double bs = block_sum(acc, sh);
+  if (threadIdx.x == 0) part[blockIdx.x] = bs;
+}
+
+__global__ void reduce_parts_kernel(const double* __restrict__ part, int nparts, double* __restrict__ out) {
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int b = 0; b < nparts; ++b) s += part[b];
+    *out = s;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Exact (dense) method.
+// ---------------------------------------------------------------------------
+template <class T>
+__global__ void dense_distance_kernel(const T* __restrict__ X, int64_t n, int dim, int squared, T* __restrict__ dist) {
+  const int64_t i = blockIdx.y;
+  const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n || j >= n) return;
+  if (j == i) {
+    dist[i * n + j] = T(0);
+    return;
+  }
+  // Evaluate on the upper triangle only and mirror (src/tsne/mod.rs:161-189).
+  const int64_t a = j > i ? i : j, b = j > i ? j : i;
+  T s = T(0);
+  for (int c = 0; c < dim; ++c) {
+    const T d = X[a * dim + c] - X[b * dim + c];
+    s = s + d * d;
+  }
+  dist[i * n + j] = squared ? s : dsqrt(s);
+}
+
+template <class T>
+__global__ void dense_symmetrize_kernel(T* __restrict__ p, int64_t n) {
+  const int64_t i = blockIdx.y;
+  const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n || j >= n || j <= i) return;
+  const T v = p[i * n + j] + p[j * n + i];
+  p[i * n + j] = v;
+  p[j * n + i] = v;
+}
+
+// Z = sum over all (i, j) including the diagonal of 1 / (1 + |y_i - y_j|^2).
+template <class T, int D>
+__global__ void exact_z_kernel(const T* __restrict__ y, int64_t n, double* __restrict__ part) {
+  __shared__ double sh[32];
+  const int64_t i = blockIdx.x;
+  T yi[D];
+#pragma unroll
+  for (int a = 0; a < D; ++a) yi[a] = y[i * D + a];
+  double acc = 0.0;
+  for (int64_t j = threadIdx.x; j < n; j += blockDim.x) {
+    T d = T(0);
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+      const T t = yi[a] - y[j * D + a];
+      d = d + t * t;
+    }
+    acc += (double)(T(1) / (T(1) + d));
+  }
+  const double bs = block_sum(acc, sh);
+  if (threadIdx.x == 0) part[i] = bs;
+}
+
+template <class T, int D>
+__global__ void exact_grad_kernel(const T* __restrict__ y, const T* __restrict__ p, int64_t n,
+                                  const double* __restrict__ z, T* __restrict__ dy) {
+  __shared__ double sh[32];
+  const int64_t i = blockIdx.x;
+  const T inv = T(1) / (T)(*z);
+  T yi[D], acc[D];
+#pragma unroll
+  for (int a = 0; a < D; ++a) {
+    yi[a] = y[i * D + a];
+    acc[a] = T(0);
+  }
+  for (int64_t j = threadIdx.x; j < n; j += blockDim.x) {
+    T d = T(0);
+    T diff[D];
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+      diff[a] = yi[a] - y[j * D + a];
+      d = d + diff[a] * diff[a];
+    }
+    const T q = T(1) / (T(1) + d);
+    const T m = (p[i * n + j] - q * inv) * q;
+#pragma unroll
+    for (int a = 0; a < D; ++a) acc[a] += diff[a] * m;
+  }
+#pragma unroll
+  for (int a = 0; a < D; ++a) {
+    const double bs = block_sum((double)acc[a], sh);
+    if (threadIdx.x == 0) dy[i * D + a] = (T)bs;
+    __syncthreads();
+  }
+}
+
+template <class T, int D>
+__global__ void exact_kl_kernel(const T* __restrict__ y, const T* __restrict__ p, int64_t n,
+                                const double* __restrict__ z, double* __restrict__ part) {
+  __shared__ double sh[32];
+  const int64_t i = blockIdx.x;
+  const T inv = T(1) / (T)(*z);
+  T yi[D];
+#pragma unroll
+  for (int a = 0; a < D; ++a) yi[a] = y[i * D + a];
+  double acc = 0.0;
+  for (int64_t j = threadIdx.x; j < n; j += blockDim.x) {
+    T d = T(0);
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+      const T t = yi[a] - y[j * D + a];
+      d = d + t * t;
+    }
+    const T q = T(1) / (T(1) + d) * inv;
+    const T pv = p[i * n + j];
+    acc += (double)(pv * dlog((pv + Lim<T>::min_pos()) / (q + Lim<T>::min_pos())));
+  }
+  const double bs = block_sum(acc, sh);
+  if (threadIdx.x == 0) part[i] = bs;
+}
+
+constexpr int kUpdBlocks = 2 * 152;
+
+}  // namespace
+
+template <class T>
+void launch_attractive(int D, const uint64_t* rows, const uint32_t* cols, const T* vals, const T* y, int64_t n, T* pos,
+                       cudaStream_t s) {
+  if (n <= 0) return;
+  const unsigned g = (unsigned)ceil_div(n * 32, 256);
+  if (D == 1) attractive_kernel<T, 1><<<g, 256, 0, s>>>(rows, cols, vals, y, n, pos);
+  else if (D == 2) attractive_kernel<T, 2><<<g, 256, 0, s>>>(rows, cols, vals, y, n, pos);
+  else attractive_kernel<T, 3><<<g, 256, 0, s>>>(rows, cols, vals, y, n, pos);
+  BHG_LAUNCH_CHECK();
+}
+
+template <class T>
+void launch_update(int D, T* y, const T* pos, const T* neg, T* uy, T* gains, int64_t n, const double* z, T inv_norm,
+                   T lr, T momentum, UpdateScratch& us, cudaStream_t s) {
+  double* part = static_cast<double*>(us.part.ensure(kUpdBlocks * 3 * sizeof(double)));
+  unsigned* done = static_cast<unsigned*>(us.done.ensure(64));
+  if (!us.zeroed) {
+    BHG_CUDA(cudaMemset(done, 0, 64));
+    us.zeroed = true;
+  }
+  double* mean_sum = static_cast<double*>(us.mean_sum.ensure(3 * sizeof(double)));
+  const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(n, 256), kUpdBlocks));
+  if (D == 1) update_kernel<T, 1><<<grid, 256, 0, s>>>(y, pos, neg, uy, gains, n, z, inv_norm, lr, momentum, part, done, mean_sum);
+  else if (D == 2) update_kernel<T, 2><<<grid, 256, 0, s>>>(y, pos, neg, uy, gains, n, z, inv_norm, lr, momentum, part, done, mean_sum);
+  else update_kernel<T, 3><<<grid, 256, 0, s>>>(y, pos, neg, uy, gains, n, z, inv_norm, lr, momentum, part, done, mean_sum);
+  BHG_LAUNCH_CHECK();
+}
+
+template <class T>
+void launch_kl_sparse(int D, const uint64_t* rows, const uint32_t* cols, const T* vals, const T* y, int64_t n,
+                      const double* z, bool quirk, double* out, DevBuf& tmp, cudaStream_t s) {
+  const int blocks = 2 * 152;
+  double* part = static_cast<double*>(tmp.ensure(blocks * sizeof(double)));
+  if (D == 1) kl_sparse_kernel<T, 1><<<blocks, 256, 0, s>>>(rows, cols, vals, y, n, z, quirk ? 1 : 0, part);
+  else if (D == 2) kl_sparse_kernel<T, 2><<<blocks, 256, 0, s>>>(rows, cols, vals, y, n, z, quirk ? 1 : 0, part);
+  else kl_sparse_kernel<T, 3><<<blocks, 256, 0, s>>>(rows, cols, vals, y, n, z, quirk ? 1 : 0, part);
+  BHG_LAUNCH_CHECK();
+  reduce_parts_kernel<<<1, 32, 0, s>>>(part, blocks, out);
+  BHG_LAUNCH_CHECK();
+}
+
+template <class T>
+void launch_dense_distance(const T* X, int64_t n, int dim, bool squared, T* dist, cudaStream_t s) {
+  dim3 g((unsigned)ceil_div(n, 256), (unsigned)n);
+  dense_distance_kernel<T><<<g, 256, 0, s>>>(X, n, dim, squared ? 1 : 0, dist);
+  BHG_LAUNCH_CHECK();
+}
+
+template <class T>
+void launch_dense_symmetrize(T* p, int64_t n, cudaStream_t s) {
+  dim3 g((unsigned)ceil_div(n, 256), (unsigned)n);
+  dense_symmetrize_kernel<T><<<g, 256, 0, s>>>(p, n);
+  BHG_LAUNCH_CHECK();
+}
+
+template <class T>
+void launch_exact_z(int D, const T* y, int64_t n, double* z, DevBuf& tmp, cudaStream_t s) {
+  double* part = static_cast<double*>(tmp.ensure(n * sizeof(double)));
+  if (D == 1) exact_z_kernel<T, 1><<<(unsigned)n, 256, 0, s>>>(y, n, part);
+  else if (D == 2) exact_z_kernel<T, 2><<<(unsigned)n, 256, 0, s>>>(y, n, part);
+  else exact_z_kernel<T, 3><<<(unsigned)n, 256, 0, s>>>(y, n, part);
+  BHG_LAUNCH_CHECK();
+  reduce_parts_kernel<<<1, 32, 0, s>>>(part, (int)n, z);
+  BHG_LAUNCH_CHECK();
+}
+
+template <class T>
+void launch_exact_grad(int D, const T* y, const T* p, int64_t n, const double* z, T* dy, cudaStream_t s) {
+  if (D == 1) exact_grad_kernel<T, 1><<<(unsigned)n, 256, 0, s>>>(y, p, n, z, dy);
+  else if (D == 2) exact_grad_kernel<T, 2><<<(unsigned)n, 256, 0, s>>>(y, p, n, z, dy);
+  else exact_grad_kernel<T, 3><<<(unsigned)n, 256, 0, s>>>(y, p, n, z, dy);
+  BHG_LAUNCH_CHECK();
+}
+
+template <class T>
+void launch_exact_kl(int D, const T* y, const T* p, int64_t n, const double* z, double* out, DevBuf& tmp,
+                     cudaStream_t s) {
+  double* part = static_cast<double*>(tmp.ensure(n * sizeof(double)));
+  if (D == 1) exact_kl_kernel<T, 1><<<(unsigned)n, 256, 0, s>>>(y, p, n, z, part);
+  else if (D == 2) exact_kl_kernel<T, 2><<<(unsigned)n, 256, 0, s>>>(y, p, n, z, part);
+  else exact_kl_kernel<T, 3><<<(unsigned)n, 256, 0, s>>>(y, p, n, z, part);
+  BHG_LAUNCH_CHECK();
+  reduce_parts_kernel<<<1, 32, 0, s>>>(part, (int)n, out);
+  BHG_LAUNCH_CHECK();
+}
+
+#define BHG_INST(T)                                                                                                  \
+  template void launch_attractive<T>(int, const uint64_t*, const uint32_t*, const T*, const T*, int64_t, T*,         \
+                                     cudaStream_t);                                                                  \
+  template void launch_update<T>(int, T*, const T*, const T*, T*, T*, int64_t, const double*, T, T, T, UpdateScratch&,  \
+                                 cudaStream_t);                                                                      \
+  template void launch_kl_sparse<T>(int, const uint64_t*, const uint32_t*, const T*, const T*, int64_t,             \
+                                    const double*, bool, double*, DevBuf&, cudaStream_t);                            \
+  template void launch_dense_distance<T>(const T*, int64_t, int, bool, T*, cudaStream_t);                            \
+  template void launch_dense_symmetrize<T>(T*, int64_t, cudaStream_t);                                               \
+  template void launch_exact_z<T>(int, const T*, int64_t, double*, DevBuf&, cudaStream_t);                           \
+  template void launch_exact_grad<T>(int, const T*, const T*, int64_t, const double*, T*, cudaStream_t);             \
+  template void launch_exact_kl<T>(int, const T*, const T*, int64_t, const double*, double*, DevBuf&, cudaStream_t);
+BHG_INST(float)
+BHG_INST(double)
+
+}  // namespace bhg

@@ -1,0 +1,515 @@
+// FIt-SNE repulsion on the GPU: Lagrange spread onto an equispaced grid, FFT
+// convolution with the squared Cauchy kernel, gather, and reconstruction of
+// the forces and Z.
+//
+// Reference behaviour restated (bhtsne 0.7.10, src/tsne/interpolation.rs):
+//  * square domain over the joint coordinate range, extent floored at
+//    min_positive (:115-116); boxes = clamp(ceil(extent / 1), 10, 1000)
+//    (:353-358); 3 Lagrange nodes per box at (k + 1/2)/3 (:395-441);
+//    locate_points (:162-187); charges [1, y_1..y_D, |y|^2] (:446-456);
+//    tensor-product weights, axis 0 the slow grid index (:462-481);
+//    kernel (1 + spacing^2 lag^2)^-2 over signed lags (:198-226);
+//    reconstruct (:305-332): F_i = y_i phi_0 - phi_{1+d},
+//    Z = sum_i [(1 + |y_i|^2) phi_0 - 2 y_i . phi_1 + phi_{D+1}] - N.
+//
+// GPU choices:
+//  * The transform length is the next power of two >= 2 nodes - 1 rather than
+//    the reference's 7-smooth length. Any length >= 2 nodes - 1 yields the
+//    same linear convolution on the node window (charges are zero padded and
+//    wrapped lags are never read), so only rounding differs.
+//  * The kernel is real and even, so its spectrum is real: two real charge
+//    grids are packed as the real and imaginary parts of one complex grid and
+//    convolved together (D + 2 terms -> 2 complex transforms).
+//  * 2-D transforms are row FFTs in shared memory plus tiled transposes; the
+//    spectrum stays in transposed layout, which is harmless because the
+//    kernel spectrum is symmetric in its two axes. Rows that are known to be
+//    zero (charges) or unused (potentials) are skipped.
+//  * The spread scatters with atomics; the gather re-derives each point's
+//    boxes and weights instead of storing them.
+#include "fitsne.h"
+
+#include <cmath>
+#include <vector>
+
+namespace bhg {
+
+namespace {
+
+template <class T>
+struct Cx;
+template <>
+struct Cx<float> {
+  typedef float2 type;
+};
+template <>
+struct Cx<double> {
+  typedef double2 type;
+};
+
+template <class T2>
+__device__ __forceinline__ T2 cmul(T2 a, T2 b) {
+  T2 r;
+  r.x = a.x * b.x - a.y * b.y;
+  r.y = a.x * b.y + a.y * b.x;
+  return r;
+}
+
+template <class T>
+struct Lagrange3 {
+  T node[3];
+  T inv_denom[3];
+  __device__ Lagrange3() {
+    const T half = T(0.5);
+    const T p_recip = T(1) / T(3);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) node[k] = (T(k) + half) * p_recip;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      T denom = T(1);
+#pragma unroll
+      for (int m = 0; m < 3; ++m)
+        if (m != k) denom = denom * (node[k] - node[m]);
+      inv_denom[k] = T(1) / denom;
+    }
+  }
+  __device__ __forceinline__ void weights(T local, T* out) const {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      T num = T(1);
+#pragma unroll
+      for (int m = 0; m < 3; ++m)
+        if (m != k) num = num * (local - node[m]);
+      out[k] = num * inv_denom[k];
+    }
+  }
+};
+
+template <class T, int D>
+__global__ void fit_params_kernel(const BoxParams<T>* __restrict__ box, FitParams<T>* __restrict__ out) {
+  if (threadIdx.x != 0) return;
+  T lo = box->mn[0], hi = box->mx[0];
+#pragma unroll
+  for (int a = 1; a < D; ++a) {
+    lo = fmin(lo, box->mn[a]);
+    hi = fmax(hi, box->mx[a]);
+  }
+  const T extent = fmax(hi - lo, Lim<T>::min_pos());
+  const T scaled = ceil(extent / T(1.0));
+  int64_t boxes = 0;
+  if (scaled > T(0)) boxes = scaled >= T(9.0e18) ? INT64_MAX : (int64_t)scaled;
+  boxes = boxes < 10 ? 10 : (boxes > 1000 ? 1000 : boxes);
+  const int nodes = (int)boxes * 3;
+  int L = 16;
+  while (L < 2 * nodes - 1) L <<= 1;
+  const T box_width = extent / (T)(double)boxes;
+  out->lo = lo;
+  out->extent = extent;
+  out->box_width = box_width;
+  out->inv_box_width = T(1) / box_width;
+  out->spacing = box_width / T(3);
+  out->boxes = (int)boxes;
+  out->nodes = nodes;
+  out->L = L;
+}
+
+template <class T>
+__device__ __forceinline__ void locate(T v, const FitParams<T>& p, const Lagrange3<T>& lb, int* box, T* w) {
+  const T offset = (v - p.lo) * p.inv_box_width;
+  const T b = floor(offset);
+  const int64_t last = p.boxes - 1;
+  int64_t id = 0;
+  if (b > T(0)) {
+    id = b >= T(9.0e18) ? last : (int64_t)b;
+    if (id > last) id = last;
+  }
+  *box = (int)id;
+  const T local = offset - (T)(double)id;
+  lb.weights(local, w);
+}
+
+template <class T, int D>
+__global__ void spread_kernel(const T* __restrict__ y, int64_t n, const FitParams<T>* __restrict__ prm,
+                              typename Cx<T>::type* __restrict__ g0, typename Cx<T>::type* __restrict__ g1) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const FitParams<T> p = *prm;
+  const Lagrange3<T> lb;
+  const int L = p.L;
+  int box[D];
+  T w[D][3];
+  T yv[D];
+#pragma unroll
+  for (int a = 0; a < D; ++a) {
+    yv[a] = y[i * D + a];
+    locate<T>(yv[a], p, lb, &box[a], w[a]);
+  }
+  T sq = T(0);
+#pragma unroll
+  for (int a = 0; a < D; ++a) sq = sq + yv[a] * yv[a];
+  constexpr int combos = D == 1 ? 3 : 9;
+#pragma unroll
+  for (int c = 0; c < combos; ++c) {
+    int rem = c;
+    int64_t flat = 0;
+    T wt = T(1);
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+      const int k = rem % 3;
+      rem /= 3;
+      flat = flat * L + (box[a] * 3 + k);
+      wt = wt * w[a][k];
+    }
+    T* c0 = reinterpret_cast<T*>(g0 + flat);
+    T* c1 = reinterpret_cast<T*>(g1 + flat);
+    if (D == 2) {
+      atomicAdd(c0, wt * T(1));
+      atomicAdd(c0 + 1, wt * yv[0]);
+      atomicAdd(c1, wt * yv[D - 1]);
+      atomicAdd(c1 + 1, wt * sq);
+    } else {
+      atomicAdd(c0, wt * T(1));
+      atomicAdd(c0 + 1, wt * yv[0]);
+      atomicAdd(c1, wt * sq);
+    }
+  }
+}
+
+template <class T, int D>
+__global__ void kernel_grid_kernel(const FitParams<T>* __restrict__ prm, typename Cx<T>::type* __restrict__ g) {
+  const int L = prm->L;
+  const T spacing = prm->spacing;
+  const int64_t total = D == 1 ? L : (int64_t)L * L;
+  for (int64_t flat = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; flat < total;
+       flat += (int64_t)gridDim.x * blockDim.x) {
+    T sq = T(0);
+    int64_t rem = flat;
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+      const int64_t coord = rem % L;
+      rem /= L;
+      const int64_t lag = coord <= L / 2 ? coord : coord - L;
+      const T disp = spacing * (T)(double)lag;
+      sq = sq + disp * disp;
+    }
+    const T cauchy = T(1) / (T(1) + sq);
+    typename Cx<T>::type v;
+    v.x = cauchy * cauchy;
+    v.y = T(0);
+    g[flat] = v;
+  }
+}
+
+template <class T>
+__global__ void take_real_scaled_kernel(const typename Cx<T>::type* __restrict__ g, int64_t total,
+                                        const FitParams<T>* __restrict__ prm, int D, T* __restrict__ khat) {
+  const int L = prm->L;
+  const T inv_total = T(1) / (T)(D == 1 ? (double)L : (double)L * (double)L);
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x)
+    khat[e] = g[e].x * inv_total;
+}
+
+template <class T>
+__global__ void multiply_kernel(typename Cx<T>::type* __restrict__ a, typename Cx<T>::type* __restrict__ b,
+                                const T* __restrict__ khat, int64_t total) {
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    const T k = khat[e];
+    typename Cx<T>::type u = a[e], v = b[e];
+    u.x *= k;
+    u.y *= k;
+    v.x *= k;
+    v.y *= k;
+    a[e] = u;
+    b[e] = v;
+  }
+}
+
+// Radix-2 FFT of `rows` rows of length L held in shared memory.
+template <class T>
+__global__ void fft_rows_kernel(typename Cx<T>::type* __restrict__ data, int L, int log2L, int64_t stride,
+                                const typename Cx<T>::type* __restrict__ tw, int inverse) {
+  typedef typename Cx<T>::type T2;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T2* s = reinterpret_cast<T2*>(smem_raw);
+  T2* d = data + (int64_t)blockIdx.x * stride;
+  for (int i = threadIdx.x; i < L; i += blockDim.x) s[__brev((unsigned)i) >> (32 - log2L)] = d[i];
+  __syncthreads();
+  for (int lg = 1; lg <= log2L; ++lg) {
+    const int half = 1 << (lg - 1);
+    const int tstep = L >> lg;
+    for (int b = threadIdx.x; b < (L >> 1); b += blockDim.x) {
+      const int pos = b & (half - 1);
+      const int i = ((b >> (lg - 1)) << lg) + pos;
+      const int j = i + half;
+      T2 w = tw[pos * tstep];
+      if (inverse) w.y = -w.y;
+      const T2 u = s[i];
+      const T2 v = cmul(s[j], w);
+      T2 r0, r1;
+      r0.x = u.x + v.x;
+      r0.y = u.y + v.y;
+      r1.x = u.x - v.x;
+      r1.y = u.y - v.y;
+      s[i] = r0;
+      s[j] = r1;
+    }
+    __syncthreads();
+  }
+  for (int i = threadIdx.x; i < L; i += blockDim.x) d[i] = s[i];
+}
+
+// out[c][r] = in[r][c] for r < rows_in (zero for rows_in <= r < out_cols),
+// c < cols; out row length ld_out.
+template <class T>
+__global__ void transpose_kernel(const typename Cx<T>::type* __restrict__ in, int rows_in, int cols, int64_t ld_in,
+                                 typename Cx<T>::type* __restrict__ out, int out_cols, int64_t ld_out) {
+  typedef typename Cx<T>::type T2;
+  __shared__ T2 tile[32][33];
+  const int c0 = blockIdx.x * 32, r0 = blockIdx.y * 32;
+  for (int k = threadIdx.y; k < 32; k += blockDim.y) {
+    const int r = r0 + k, c = c0 + threadIdx.x;
+    T2 v;
+    v.x = T(0);
+    v.y = T(0);
+    if (r < rows_in && c < cols) v = in[(int64_t)r * ld_in + c];
+    tile[k][threadIdx.x] = v;
+  }
+  __syncthreads();
+  for (int k = threadIdx.y; k < 32; k += blockDim.y) {
+    const int c = c0 + k, r = r0 + threadIdx.x;
+    if (c < cols && r < out_cols) out[(int64_t)c * ld_out + r] = tile[threadIdx.x][k];
+  }
+}
+
+template <class T, int D>
+__global__ void gather_kernel(const T* __restrict__ y, int64_t n, const FitParams<T>* __restrict__ prm,
+                              const typename Cx<T>::type* __restrict__ g0, const typename Cx<T>::type* __restrict__ g1,
+                              T* __restrict__ neg, double* __restrict__ zpart, unsigned* __restrict__ done,
+                              double* __restrict__ z_out) {
+  __shared__ double sh[32];
+  __shared__ bool last;
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  double zi = 0.0;
+  if (i < n) {
+    const FitParams<T> p = *prm;
+    const Lagrange3<T> lb;
+    const int L = p.L;
+    int box[D];
+    T w[D][3];
+    T yv[D];
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+      yv[a] = y[i * D + a];
+      locate<T>(yv[a], p, lb, &box[a], w[a]);
+    }
+    constexpr int combos = D == 1 ? 3 : 9;
+    T phi[D + 2];
+#pragma unroll
+    for (int t = 0; t < D + 2; ++t) phi[t] = T(0);
+#pragma unroll
+    for (int c = 0; c < combos; ++c) {
+      int rem = c;
+      int64_t flat = 0;
+      T wt = T(1);
+#pragma unroll
+      for (int a = 0; a < D; ++a) {
+        const int k = rem % 3;
+        rem /= 3;
+        flat = flat * L + (box[a] * 3 + k);
+        wt = wt * w[a][k];
+      }
+      const typename Cx<T>::type a0 = g0[flat], a1 = g1[flat];
+      phi[0] = phi[0] + wt * a0.x;
+      phi[1] = phi[1] + wt * a0.y;
+      phi[2] = phi[2] + wt * a1.x;
+      if (D == 2) phi[3] = phi[3] + wt * a1.y;
+    }
+    const T density = phi[0];
+    const T sqp = phi[D + 1];
+    T norm_sq = T(0), cross = T(0);
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+      const T fm = phi[1 + a];
+      neg[i * D + a] = yv[a] * density - fm;
+      norm_sq = norm_sq + yv[a] * yv[a];
+      cross = cross + yv[a] * fm;
+    }
+    zi = (double)((T(1) + norm_sq) * density - T(2) * cross + sqp);
+  }
+  const double bs = block_sum(zi, sh);
+  if (threadIdx.x == 0) {
+    zpart[blockIdx.x] = bs;
+    __threadfence();
+    last = atomicAdd(done, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (last && threadIdx.x == 0) {
+    __threadfence();
+    double z = 0.0;
+    for (unsigned b = 0; b < gridDim.x; ++b) z += ((volatile double*)zpart)[b];
+    *z_out = z - (double)n;
+    *done = 0;
+  }
+}
+
+int ilog2(int L) {
+  int r = 0;
+  while ((1 << r) < L) ++r;
+  return r;
+}
+
+}  // namespace
+
+template <class T>
+const typename FitWorkspace<T>::T2* FitWorkspace<T>::twiddles(int L) {
+  if (tw_len != L) {
+    std::vector<T2> h(L / 2 > 0 ? L / 2 : 1);
+    for (int k = 0; k < L / 2; ++k) {
+      const double ang = -2.0 * M_PI * (double)k / (double)L;
+      h[k].x = (T)std::cos(ang);
+      h[k].y = (T)std::sin(ang);
+    }
+    tw.ensure(h.size() * sizeof(T2));
+    BHG_CUDA(cudaMemcpy(tw.ptr, h.data(), h.size() * sizeof(T2), cudaMemcpyHostToDevice));
+    tw_len = L;
+  }
+  return tw.template as<T2>();
+}
+
+template <class T>
+static void fft_rows(FitWorkspace<T>& ws, typename Cx<T>::type* data, int L, int rows, int64_t stride, bool inverse,
+                     cudaStream_t s) {
+  if (rows <= 0) return;
+  const int threads = std::min(512, std::max(32, L / 2));
+  const size_t smem = (size_t)L * sizeof(typename Cx<T>::type);
+  static bool attr_set[2] = {false, false};
+  if (smem > 48 * 1024 && !attr_set[sizeof(T) == 8]) {
+    BHG_CUDA(cudaFuncSetAttribute(fft_rows_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    attr_set[sizeof(T) == 8] = true;
+  }
+  fft_rows_kernel<T><<<rows, threads, smem, s>>>(data, L, ilog2(L), stride, ws.twiddles(L), inverse ? 1 : 0);
+  BHG_LAUNCH_CHECK();
+}
+
+template <class T>
+static void transpose(const typename Cx<T>::type* in, int rows_in, int cols, int64_t ld_in, typename Cx<T>::type* out,
+                      int out_cols, int64_t ld_out, cudaStream_t s) {
+  dim3 b(32, 8);
+  dim3 g((unsigned)ceil_div(cols, 32), (unsigned)ceil_div(out_cols, 32));
+  transpose_kernel<T><<<g, b, 0, s>>>(in, rows_in, cols, ld_in, out, out_cols, ld_out);
+  BHG_LAUNCH_CHECK();
+}
+
+template <class T>
+FitGrid fit_repulsion(FitWorkspace<T>& ws, int D, const T* y, int64_t n, const BoxParams<T>* box, T* neg, double* z_out,
+                      cudaStream_t s) {
+  typedef typename Cx<T>::type T2;
+  ws.params.ensure(sizeof(FitParams<T>));
+  FitParams<T>* dp = ws.params.template as<FitParams<T>>();
+  if (D == 1) fit_params_kernel<T, 1><<<1, 32, 0, s>>>(box, dp);
+  else fit_params_kernel<T, 2><<<1, 32, 0, s>>>(box, dp);
+  BHG_LAUNCH_CHECK();
+  FitParams<T> hp;
+  BHG_CUDA(cudaMemcpyAsync(&hp, dp, sizeof(hp), cudaMemcpyDeviceToHost, s));
+  BHG_CUDA(cudaStreamSynchronize(s));
+  const int L = hp.L, nodes = hp.nodes;
+  const int64_t total = D == 1 ? (int64_t)L : (int64_t)L * L;
+  T2* g0 = static_cast<T2*>(ws.g0.ensure(total * sizeof(T2)));
+  T2* g1 = static_cast<T2*>(ws.g1.ensure(total * sizeof(T2)));
+  T2* h0 = static_cast<T2*>(ws.h0.ensure(total * sizeof(T2)));
+  T2* h1 = static_cast<T2*>(ws.h1.ensure(total * sizeof(T2)));
+  T* khat = static_cast<T*>(ws.khat.ensure(total * sizeof(T)));
+  const int eb = (int)std::min<int64_t>(ceil_div(total, 256), 4 * 152);
+
+  // kernel spectrum (real, pre-scaled by 1/L^D); symmetric in its axes, so it
+  // serves the transposed spectrum layout unchanged.
+  if (D == 1) kernel_grid_kernel<T, 1><<<eb, 256, 0, s>>>(dp, g0);
+  else kernel_grid_kernel<T, 2><<<eb, 256, 0, s>>>(dp, g0);
+  BHG_LAUNCH_CHECK();
+  if (D == 1) {
+    fft_rows<T>(ws, g0, L, 1, L, false, s);
+    take_real_scaled_kernel<T><<<eb, 256, 0, s>>>(g0, total, dp, D, khat);
+  } else {
+    fft_rows<T>(ws, g0, L, L, L, false, s);
+    transpose<T>(g0, L, L, L, h0, L, L, s);
+    fft_rows<T>(ws, h0, L, L, L, false, s);
+    take_real_scaled_kernel<T><<<eb, 256, 0, s>>>(h0, total, dp, D, khat);
+  }
+  BHG_LAUNCH_CHECK();
+
+  // charges: zero the rows that receive them, spread
+  const int64_t charge_rows = D == 1 ? 1 : nodes;
+  BHG_CUDA(cudaMemsetAsync(g0, 0, (size_t)charge_rows * (D == 1 ? L : L) * sizeof(T2), s));
+  BHG_CUDA(cudaMemsetAsync(g1, 0, (size_t)charge_rows * (D == 1 ? L : L) * sizeof(T2), s));
+  if (n > 0) {
+    if (D == 1) spread_kernel<T, 1><<<(unsigned)ceil_div(n, 256), 256, 0, s>>>(y, n, dp, g0, g1);
+    else spread_kernel<T, 2><<<(unsigned)ceil_div(n, 256), 256, 0, s>>>(y, n, dp, g0, g1);
+    BHG_LAUNCH_CHECK();
+  }
+
+  T2 *r0, *r1;
+  if (D == 1) {
+    fft_rows<T>(ws, g0, L, 1, L, false, s);
+    fft_rows<T>(ws, g1, L, 1, L, false, s);
+    multiply_kernel<T><<<eb, 256, 0, s>>>(g0, g1, khat, total);
+    BHG_LAUNCH_CHECK();
+    fft_rows<T>(ws, g0, L, 1, L, true, s);
+    fft_rows<T>(ws, g1, L, 1, L, true, s);
+    r0 = g0;
+    r1 = g1;
+  } else {
+    // forward: rows n0 < nodes, transpose to [k1][n0], rows over n0
+    fft_rows<T>(ws, g0, L, nodes, L, false, s);
+    fft_rows<T>(ws, g1, L, nodes, L, false, s);
+    transpose<T>(g0, nodes, L, L, h0, L, L, s);
+    transpose<T>(g1, nodes, L, L, h1, L, L, s);
+    fft_rows<T>(ws, h0, L, L, L, false, s);
+    fft_rows<T>(ws, h1, L, L, L, false, s);
+    multiply_kernel<T><<<eb, 256, 0, s>>>(h0, h1, khat, total);
+    BHG_LAUNCH_CHECK();
+    // inverse: rows over k0, transpose back (rows n0 < nodes only), rows over k1
+    fft_rows<T>(ws, h0, L, L, L, true, s);
+    fft_rows<T>(ws, h1, L, L, L, true, s);
+    transpose<T>(h0, L, nodes, L, g0, L, L, s);
+    transpose<T>(h1, L, nodes, L, g1, L, L, s);
+    fft_rows<T>(ws, g0, L, nodes, L, true, s);
+    fft_rows<T>(ws, g1, L, nodes, L, true, s);
+    r0 = g0;
+    r1 = g1;
+  }
+
+  ws.zpart.ensure((ceil_div(std::max<int64_t>(n, 1), 256) + 1) * sizeof(double));
+  if (!ws.done_zeroed) {
+    ws.done.ensure(64);
+    BHG_CUDA(cudaMemset(ws.done.ptr, 0, 64));
+    ws.done_zeroed = true;
+  }
+  if (n > 0) {
+    const unsigned g = (unsigned)ceil_div(n, 256);
+    if (D == 1)
+      gather_kernel<T, 1><<<g, 256, 0, s>>>(y, n, dp, r0, r1, neg, ws.zpart.template as<double>(),
+                                            ws.done.template as<unsigned>(), z_out);
+    else
+      gather_kernel<T, 2><<<g, 256, 0, s>>>(y, n, dp, r0, r1, neg, ws.zpart.template as<double>(),
+                                            ws.done.template as<unsigned>(), z_out);
+    BHG_LAUNCH_CHECK();
+  } else {
+    BHG_CUDA(cudaMemsetAsync(z_out, 0, sizeof(double), s));
+  }
+  FitGrid fg;
+  fg.boxes = hp.boxes;
+  fg.nodes = hp.nodes;
+  fg.fft_len = hp.L;
+  fg.lo = (double)hp.lo;
+  fg.box_width = (double)hp.box_width;
+  fg.spacing = (double)hp.spacing;
+  return fg;
+}
+
+template struct FitWorkspace<float>;
+template struct FitWorkspace<double>;
+template FitGrid fit_repulsion<float>(FitWorkspace<float>&, int, const float*, int64_t, const BoxParams<float>*, float*,
+                                      double*, cudaStream_t);
+template FitGrid fit_repulsion<double>(FitWorkspace<double>&, int, const double*, int64_t, const BoxParams<double>*,
+                                       double*, double*, cudaStream_t);
+
+}  // namespace bhg

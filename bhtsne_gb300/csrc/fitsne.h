@@ -1,0 +1,34 @@
+// FIt-SNE repulsion (see fitsne.cu).
+#pragma once
+
+#include "bh.h"
+
+namespace bhg {
+
+template <class T>
+struct FitParams {
+  T lo, extent, box_width, inv_box_width, spacing;
+  int boxes, nodes, L;
+};
+
+struct FitGrid {
+  int boxes = 0, nodes = 0, fft_len = 0;
+  double lo = 0, box_width = 0, spacing = 0;
+};
+
+template <class T>
+struct FitWorkspace {
+  typedef typename std::conditional<sizeof(T) == 4, float2, double2>::type T2;
+  DevBuf params, g0, g1, h0, h1, khat, tw, zpart, done;
+  int tw_len = 0;
+  bool done_zeroed = false;
+  const T2* twiddles(int L);
+};
+
+// Repulsive forces (neg) and Z (z_out, device) at y; `box` must hold the
+// current per-axis bounds. Synchronises once to size the grid.
+template <class T>
+FitGrid fit_repulsion(FitWorkspace<T>& ws, int D, const T* y, int64_t n, const BoxParams<T>* box, T* neg, double* z_out,
+                      cudaStream_t s);
+
+}  // namespace bhg

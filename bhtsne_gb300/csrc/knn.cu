@@ -1,0 +1,402 @@
+// Exact k-nearest neighbours for dense Euclidean data, the GPU replacement of
+// the VP-tree search (src/tsne/vptree.rs:274-319 of bhtsne 0.7.10) for
+// `barnes_hut` / `fit_sne` over a Euclidean metric closure.
+//
+// Result contract (the reference's brute-force test helper,
+// src/test.rs:856-881): distance = sqrt(sum over dimensions, in order, of
+// (a - b)^2) rounded in T at every step; neighbours ordered by (distance,
+// index); the query itself excluded.
+//
+// Pipeline:
+//  1. candidates: a register-tiled FP32 pass computes |q|^2 + |c|^2 - 2 q.c
+//     for 64 queries x 128 candidates per tile and keeps, per query, the C
+//     smallest (C = 128 or 256, C > k) in a sorted list in shared memory.
+//  2. re-rank: the exact distance of every candidate is recomputed in the
+//     reference's operation order, the list is sorted by (distance, index)
+//     and the first k are kept.
+//  3. certification: a neighbour outside the candidate list has an
+//     approximate squared distance >= the list's C-th value, and the FP32
+//     error of that approximation is below (4 dim + 16) u (|q|^2 + max|x|^2).
+//     When the exact k-th squared distance is below that bound the row is
+//     provably exact; otherwise the row is recomputed by an exact brute-force
+//     warp over all points. Either way the output equals brute force.
+#include "knn.h"
+
+#include <algorithm>
+#include <cfloat>
+#include <type_traits>
+
+namespace bhg {
+
+namespace {
+
+constexpr int QB = 64;    // queries per block
+constexpr int CB = 128;   // candidates per tile
+constexpr int DK = 32;    // dimensions per candidate chunk
+constexpr int kThreads = 256;
+constexpr uint32_t SENT = 0xffffffffu;
+
+__global__ void sq_norm_kernel(const float* __restrict__ X, int64_t n, int dim, float* __restrict__ norms,
+                               unsigned* __restrict__ max_bits) {
+  const int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (i >= n) return;
+  float s = 0.f;
+  for (int d = lane; d < dim; d += 32) {
+    const float v = X[i * dim + d];
+    s = fmaf(v, v, s);
+  }
+  s = warp_sum(s);
+  if (lane == 0) {
+    norms[i] = s;
+    atomicMax(max_bits, __float_as_uint(s));
+  }
+}
+
+template <class T>
+__global__ void to_f32_kernel(const T* __restrict__ X, int64_t count, float* __restrict__ out) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = (float)X[i];
+}
+
+// Warp-cooperative insertion of (v, j) into a sorted list (v, j ascending) of
+// capacity cap holding *len entries.
+template <class V>
+__device__ __forceinline__ bool lt_pair(V a, uint32_t ai, V b, uint32_t bi) {
+  return a < b || (a == b && ai < bi);
+}
+
+template <class V>
+__device__ void warp_insert(V* lv, uint32_t* li, int* len_p, int cap, V v, uint32_t j, int lane) {
+  const int len = *len_p;
+  if (len == cap && !lt_pair(v, j, lv[cap - 1], li[cap - 1])) return;
+  int pos = 0;
+  for (int b = 0; b < len; b += 32) {
+    const int e = b + lane;
+    const bool less = e < len && lt_pair(lv[e], li[e], v, j);
+    pos += __popc(__ballot_sync(kFull, less));
+  }
+  const int top = len < cap ? len : cap - 1;  // last index to move from (exclusive bound handled below)
+  for (int b = ((top - 1) >> 5) << 5; b >= 0 && top > 0; b -= 32) {
+    const int e = b + lane;
+    V tv{};
+    uint32_t tj = 0;
+    const bool mv = e >= pos && e < top;
+    if (mv) {
+      tv = lv[e];
+      tj = li[e];
+    }
+    __syncwarp();
+    if (mv) {
+      lv[e + 1] = tv;
+      li[e + 1] = tj;
+    }
+    __syncwarp();
+    if (b == 0) break;
+  }
+  if (lane == 0) {
+    lv[pos] = v;
+    li[pos] = j;
+    *len_p = len < cap ? len + 1 : cap;
+  }
+  __syncwarp();
+}
+
+template <int C>
+struct CandSmem {
+  static constexpr int kQDimMax = C == 128 ? 256 : 128;
+};
+
+// dynamic shared layout: Qs[dim][QB] | Cs[DK][CB] | S[QB][CB+1] | lv[QB][C] | li[QB][C] | len[QB] | qn[QB]
+template <int C>
+__global__ void __launch_bounds__(kThreads, 1) knn_candidates_kernel(const float* __restrict__ X, int64_t n, int dim,
+                                                                     const float* __restrict__ norms,
+                                                                     uint32_t* __restrict__ cand, float* __restrict__ thr) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  float* Qs = reinterpret_cast<float*>(smem);
+  float* Cs = Qs + (size_t)dim * QB;
+  float* S = Cs + DK * CB;
+  float* lv = S + QB * (CB + 1);
+  uint32_t* li = reinterpret_cast<uint32_t*>(lv + QB * C);
+  int* len = reinterpret_cast<int*>(li + QB * C);
+  float* qn = reinterpret_cast<float*>(len + QB);
+
+  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+  const int tq = tid >> 4, tc = tid & 15;
+  const int64_t q0 = (int64_t)blockIdx.x * QB;
+
+  for (int e = tid; e < QB * dim; e += kThreads) {
+    const int q = e / dim, d = e % dim;
+    const int64_t qi = q0 + q;
+    Qs[d * QB + q] = qi < n ? X[qi * dim + d] : 0.f;
+  }
+  if (tid < QB) {
+    len[tid] = 0;
+    qn[tid] = (q0 + tid < n) ? norms[q0 + tid] : 0.f;
+  }
+  __syncthreads();
+
+  for (int64_t c0 = 0; c0 < n; c0 += CB) {
+    float acc[4][8];
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+      for (int b = 0; b < 8; ++b) acc[a][b] = 0.f;
+    for (int d0 = 0; d0 < dim; d0 += DK) {
+      // load Cs[dd][c] = X[c0 + c][d0 + dd]
+      for (int e = tid; e < DK * CB; e += kThreads) {
+        const int c = e / DK, dd = e % DK;
+        const int64_t j = c0 + c;
+        Cs[dd * CB + c] = (j < n && d0 + dd < dim) ? X[j * dim + d0 + dd] : 0.f;
+      }
+      __syncthreads();
+      const int dmax = min(DK, dim - d0);
+      for (int dd = 0; dd < dmax; ++dd) {
+        const float4 a4 = *reinterpret_cast<const float4*>(Qs + (d0 + dd) * QB + tq * 4);
+        const float4 b0 = *reinterpret_cast<const float4*>(Cs + dd * CB + tc * 4);
+        const float4 b1 = *reinterpret_cast<const float4*>(Cs + dd * CB + 64 + tc * 4);
+        const float av[4] = {a4.x, a4.y, a4.z, a4.w};
+        const float bv[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+#pragma unroll
+        for (int a = 0; a < 4; ++a)
+#pragma unroll
+          for (int b = 0; b < 8; ++b) acc[a][b] = fmaf(av[a], bv[b], acc[a][b]);
+      }
+      __syncthreads();
+    }
+#pragma unroll
+    for (int a = 0; a < 4; ++a) {
+      const int q = tq * 4 + a;
+#pragma unroll
+      for (int b = 0; b < 8; ++b) {
+        const int c = b < 4 ? tc * 4 + b : 64 + tc * 4 + (b - 4);
+        const int64_t j = c0 + c;
+        const float cn = j < n ? norms[j] : 0.f;
+        S[q * (CB + 1) + c] = qn[q] + cn - 2.f * acc[a][b];
+      }
+    }
+    __syncthreads();
+    for (int qq = 0; qq < QB / 8; ++qq) {
+      const int q = w * (QB / 8) + qq;
+      const int64_t qi = q0 + q;
+      if (qi >= n) continue;
+      float* qlv = lv + q * C;
+      uint32_t* qli = li + q * C;
+#pragma unroll
+      for (int part = 0; part < CB / 32; ++part) {
+        const int c = part * 32 + lane;
+        const int64_t j = c0 + c;
+        const float v = S[q * (CB + 1) + c];
+        const int L = len[q];
+        bool ok = j < n && j != qi;
+        if (ok && L == C) ok = lt_pair(v, (uint32_t)j, qlv[C - 1], qli[C - 1]);
+        unsigned mask = __ballot_sync(kFull, ok);
+        while (mask) {
+          const int src = __ffs(mask) - 1;
+          mask &= mask - 1;
+          const float vv = __shfl_sync(kFull, v, src);
+          const uint32_t jj = (uint32_t)(c0 + part * 32 + src);
+          warp_insert<float>(qlv, qli, &len[q], C, vv, jj, lane);
+        }
+      }
+    }
+    __syncthreads();
+  }
+  for (int qq = 0; qq < QB / 8; ++qq) {
+    const int q = w * (QB / 8) + qq;
+    const int64_t qi = q0 + q;
+    if (qi >= n) continue;
+    const int L = len[q];
+    for (int t = lane; t < C; t += 32) cand[qi * C + t] = t < L ? li[q * C + t] : SENT;
+    if (lane == 0) thr[qi] = L == C ? lv[q * C + C - 1] : INFINITY;
+  }
+}
+
+// Exact distance in the reference's order (sequential over dimensions, T).
+template <class T>
+__device__ __forceinline__ T exact_d2(const T* __restrict__ a, const T* __restrict__ b, int dim) {
+  T s = T(0);
+  for (int d = 0; d < dim; ++d) {
+    const T t = a[d] - b[d];
+    s = s + t * t;
+  }
+  return s;
+}
+
+// One warp per query: exact distances of the C candidates, bitonic sort by
+// (distance, index), first k out, certification.
+template <class T, int C>
+__global__ void knn_rerank_kernel(const T* __restrict__ X, int64_t n, int dim, int k, const uint32_t* __restrict__ cand,
+                                  const float* __restrict__ thr, const float* __restrict__ norms,
+                                  const unsigned* __restrict__ max_bits, uint32_t* __restrict__ out_idx,
+                                  T* __restrict__ out_dist, uint32_t* __restrict__ fail_list,
+                                  unsigned* __restrict__ fail_count) {
+  constexpr int W = 4;
+  __shared__ T sd[W][C];
+  __shared__ T sd2[W][C];
+  __shared__ uint32_t sj[W][C];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t qi = (int64_t)blockIdx.x * W + w;
+  if (qi >= n) return;
+  const T* xq = X + qi * dim;
+  for (int t = lane; t < C; t += 32) {
+    const uint32_t j = cand[qi * C + t];
+    T d2 = (T)INFINITY, d = (T)INFINITY;
+    if (j != SENT) {
+      d2 = exact_d2<T>(xq, X + (int64_t)j * dim, dim);
+      d = dsqrt(d2);
+    }
+    sd[w][t] = d;
+    sd2[w][t] = d2;
+    sj[w][t] = j;
+  }
+  __syncwarp();
+  for (int size = 2; size <= C; size <<= 1) {
+    for (int stride = size >> 1; stride > 0; stride >>= 1) {
+      for (int t = lane; t < C / 2; t += 32) {
+        const int lo = 2 * t - (t & (stride - 1));
+        const int hi = lo + stride;
+        const bool up = (lo & size) == 0;
+        const bool gt = lt_pair(sd[w][hi], sj[w][hi], sd[w][lo], sj[w][lo]);
+        if (gt == up) {
+          T a = sd[w][lo];
+          sd[w][lo] = sd[w][hi];
+          sd[w][hi] = a;
+          a = sd2[w][lo];
+          sd2[w][lo] = sd2[w][hi];
+          sd2[w][hi] = a;
+          const uint32_t b = sj[w][lo];
+          sj[w][lo] = sj[w][hi];
+          sj[w][hi] = b;
+        }
+      }
+      __syncwarp();
+    }
+  }
+  for (int t = lane; t < k; t += 32) {
+    out_idx[qi * k + t] = sj[w][t];
+    out_dist[qi * k + t] = sd[w][t];
+  }
+  if (lane == 0) {
+    const float th = thr[qi];
+    bool ok = true;
+    if (!isinf(th)) {
+      const double u = 1.0 / 16777216.0;
+      const double maxn = (double)__uint_as_float(*max_bits);
+      const double delta = (4.0 * dim + 16.0) * u * ((double)norms[qi] + maxn);
+      const double bound = ((double)th - delta) * (1.0 - (dim + 2.0) * u) - 1e-30;
+      ok = (double)sd2[w][k - 1] < bound;
+    }
+    if (!ok) fail_list[atomicAdd(fail_count, 1u)] = (uint32_t)qi;
+  }
+}
+
+// Exact brute force for the listed queries, one warp per query, list of size k
+// kept sorted in shared memory by (distance, index).
+template <class T>
+__global__ void knn_exact_kernel(const T* __restrict__ X, int64_t n, int dim, int k, const uint32_t* __restrict__ rows,
+                                 const unsigned* __restrict__ nrows_p, int64_t nrows_fixed,
+                                 uint32_t* __restrict__ out_idx, T* __restrict__ out_dist) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  constexpr int W = 4;
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  T* lv = reinterpret_cast<T*>(smem) + (size_t)w * k;
+  uint32_t* li = reinterpret_cast<uint32_t*>(reinterpret_cast<T*>(smem) + (size_t)W * k) + (size_t)w * k;
+  __shared__ int len[W];
+  const int64_t nrows = nrows_p ? (int64_t)*nrows_p : nrows_fixed;
+  const int64_t r = (int64_t)blockIdx.x * W + w;
+  if (r >= nrows) return;
+  const int64_t qi = rows ? (int64_t)rows[r] : r;
+  if (lane == 0) len[w] = 0;
+  __syncwarp();
+  const T* xq = X + qi * dim;
+  for (int64_t b = 0; b < n; b += 32) {
+    const int64_t j = b + lane;
+    T d = T(0);
+    bool ok = j < n && j != qi;
+    if (ok) d = dsqrt(exact_d2<T>(xq, X + j * dim, dim));
+    if (ok && len[w] == k) ok = lt_pair(d, (uint32_t)j, lv[k - 1], li[k - 1]);
+    unsigned mask = __ballot_sync(kFull, ok);
+    while (mask) {
+      const int src = __ffs(mask) - 1;
+      mask &= mask - 1;
+      const T dv = __shfl_sync(kFull, d, src);
+      warp_insert<T>(lv, li, &len[w], k, dv, (uint32_t)(b + src), lane);
+    }
+  }
+  for (int t = lane; t < k; t += 32) {
+    out_idx[qi * k + t] = li[t];
+    out_dist[qi * k + t] = lv[t];
+  }
+}
+
+}  // namespace
+
+template <class T>
+int64_t knn_euclidean(const T* X, int64_t n, int dim, int k, uint32_t* out_idx, T* out_dist, KnnWorkspace& ws,
+                      cudaStream_t s) {
+  if (k <= 0 || k > n - 1) throw Error(ST_EINVAL, "error: k must be in [1, n_samples - 1].");
+  const int C = k <= 96 ? 128 : (k <= 224 ? 256 : 0);
+  const int qdim_max = C == 128 ? 256 : 128;
+  const bool use_candidates = C != 0 && dim <= qdim_max && n > C;
+  unsigned* fail_count = static_cast<unsigned*>(ws.counters.ensure(64));
+  BHG_CUDA(cudaMemsetAsync(fail_count, 0, 64, s));
+  if (!use_candidates) {
+    const size_t smem = (size_t)4 * k * (sizeof(T) + sizeof(uint32_t));
+    if (smem > 48 * 1024)
+      BHG_CUDA(cudaFuncSetAttribute(knn_exact_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    knn_exact_kernel<T><<<(unsigned)ceil_div(n, 4), 128, smem, s>>>(X, n, dim, k, nullptr, nullptr, n, out_idx, out_dist);
+    BHG_LAUNCH_CHECK();
+    return n;
+  }
+  const float* Xf;
+  if constexpr (std::is_same<T, float>::value) {
+    Xf = X;
+  } else {
+    float* tmp = static_cast<float*>(ws.xf.ensure((size_t)n * dim * sizeof(float)));
+    to_f32_kernel<T><<<1024, 256, 0, s>>>(X, n * dim, tmp);
+    BHG_LAUNCH_CHECK();
+    Xf = tmp;
+  }
+  float* norms = static_cast<float*>(ws.norms.ensure((size_t)n * sizeof(float)));
+  unsigned* max_bits = fail_count + 1;
+  sq_norm_kernel<<<(unsigned)ceil_div(n * 32, 256), 256, 0, s>>>(Xf, n, dim, norms, max_bits);
+  BHG_LAUNCH_CHECK();
+  uint32_t* cand = static_cast<uint32_t*>(ws.cand.ensure((size_t)n * C * sizeof(uint32_t)));
+  float* thr = static_cast<float*>(ws.thr.ensure((size_t)n * sizeof(float)));
+  uint32_t* fails = static_cast<uint32_t*>(ws.fails.ensure((size_t)n * sizeof(uint32_t)));
+  const size_t smem = ((size_t)dim * QB + DK * CB + QB * (CB + 1) + (size_t)QB * C * 2 + 2 * QB) * 4;
+  const unsigned grid = (unsigned)ceil_div(n, QB);
+  if (C == 128) {
+    BHG_CUDA(cudaFuncSetAttribute(knn_candidates_kernel<128>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    knn_candidates_kernel<128><<<grid, kThreads, smem, s>>>(Xf, n, dim, norms, cand, thr);
+    BHG_LAUNCH_CHECK();
+    knn_rerank_kernel<T, 128><<<(unsigned)ceil_div(n, 4), 128, 0, s>>>(X, n, dim, k, cand, thr, norms, max_bits, out_idx,
+                                                                       out_dist, fails, fail_count);
+  } else {
+    BHG_CUDA(cudaFuncSetAttribute(knn_candidates_kernel<256>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    knn_candidates_kernel<256><<<grid, kThreads, smem, s>>>(Xf, n, dim, norms, cand, thr);
+    BHG_LAUNCH_CHECK();
+    knn_rerank_kernel<T, 256><<<(unsigned)ceil_div(n, 4), 128, 0, s>>>(X, n, dim, k, cand, thr, norms, max_bits, out_idx,
+                                                                       out_dist, fails, fail_count);
+  }
+  BHG_LAUNCH_CHECK();
+  unsigned nfail = 0;
+  BHG_CUDA(cudaMemcpyAsync(&nfail, fail_count, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+  BHG_CUDA(cudaStreamSynchronize(s));
+  if (nfail > 0) {
+    const size_t esmem = (size_t)4 * k * (sizeof(T) + sizeof(uint32_t));
+    if (esmem > 48 * 1024)
+      BHG_CUDA(cudaFuncSetAttribute(knn_exact_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)esmem));
+    knn_exact_kernel<T><<<(unsigned)ceil_div(nfail, 4), 128, esmem, s>>>(X, n, dim, k, fails, nullptr, nfail, out_idx,
+                                                                        out_dist);
+    BHG_LAUNCH_CHECK();
+  }
+  return (int64_t)nfail;
+}
+
+template int64_t knn_euclidean<float>(const float*, int64_t, int, int, uint32_t*, float*, KnnWorkspace&, cudaStream_t);
+template int64_t knn_euclidean<double>(const double*, int64_t, int, int, uint32_t*, double*, KnnWorkspace&,
+                                       cudaStream_t);
+
+}  // namespace bhg

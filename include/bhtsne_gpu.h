@@ -1,0 +1,164 @@
+/*
+ * bhtsne_gpu.h - C ABI of the GB300 (sm_103a) t-SNE library.
+ *
+ * This is the drop-in boundary for the fitting path of the Rust crate bhtsne
+ * 0.7.10. The reference has no FFI of its own; its public surface is the
+ * `tSNE<'data, T, U, const D>` builder in src/lib.rs. Every entry point below
+ * names the reference item it stands in for (path:line in the reference
+ * crate), so that a thin Rust wrapper can re-export the
+ * builder with the same method names, defaults and panic messages.
+ *
+ * Conventions
+ *  - Every call returns an int status: BHTSNE_OK (0) or an error code. The
+ *    reference's panics become BHTSNE_EINVAL with the reference's message
+ *    text, readable through bhtsne_tsne_last_error / bhtsne_ctx_last_error.
+ *  - All array arguments are HOST pointers owned by the caller; the library
+ *    copies in and out. Device state (affinities, embedding, gains, velocity)
+ *    lives in the handle until bhtsne_tsne_free.
+ *  - A handle computes in one scalar type fixed at creation (the reference's
+ *    T): BHTSNE_F32 or BHTSNE_F64. `const void*` / `void*` value buffers hold
+ *    that type. Neighbour indices are uint64_t (the reference's usize),
+ *    sparse columns uint32_t, sparse row offsets uint64_t.
+ *  - A context owns one CUDA stream on one device and is single-threaded;
+ *    separate contexts may be used from separate threads.
+ */
+#ifndef BHTSNE_GPU_H
+#define BHTSNE_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define BHTSNE_OK 0
+#define BHTSNE_ENOMEM 12
+#define BHTSNE_EINVAL 22
+#define BHTSNE_ETIMEDOUT 110
+#define BHTSNE_ECUDA 1001
+#define BHTSNE_EINTERNAL 1002
+
+#define BHTSNE_F32 0
+#define BHTSNE_F64 1
+
+/* Fitting routines, as recorded by the reference's `enum Fit` (src/lib.rs:99-103). */
+#define BHTSNE_METHOD_EXACT 1
+#define BHTSNE_METHOD_BARNES_HUT 2
+#define BHTSNE_METHOD_FIT_SNE 3
+
+typedef struct bhtsne_ctx bhtsne_ctx;
+typedef struct bhtsne_tsne bhtsne_tsne;
+
+/* Epoch callback: `EpochCallback` (src/lib.rs:95), invoked on the calling
+ * thread after each epoch with a host snapshot of the embedding (n * D values
+ * of the handle's type). */
+typedef void (*bhtsne_epoch_cb)(int64_t epoch, const void* embedding, void* user);
+
+/* ---- context ------------------------------------------------------------- */
+/* No reference counterpart: owns the device, stream and scratch. */
+int bhtsne_ctx_create(int device, bhtsne_ctx** out);
+int bhtsne_ctx_destroy(bhtsne_ctx* ctx);
+const char* bhtsne_ctx_last_error(const bhtsne_ctx* ctx);
+const char* bhtsne_version(void);
+
+/* ---- builder ------------------------------------------------------------- */
+/* tSNE::new (src/lib.rs:241-266): defaults lr auto, 1000 epochs, momentum
+ * 0.5 -> 0.8 at epoch 250, stop lying at 250, exaggeration 12, perplexity 20.
+ * `embed_dim` is the const generic D: 2..3 for Barnes-Hut, 1..2 for FIt-SNE,
+ * 1..3 for exact. */
+int bhtsne_tsne_new(bhtsne_ctx* ctx, int dtype, int32_t embed_dim, int64_t n_samples, bhtsne_tsne** out);
+int bhtsne_tsne_free(bhtsne_tsne* t);
+const char* bhtsne_tsne_last_error(const bhtsne_tsne* t);
+
+/* Setters: src/lib.rs:277-435. */
+int bhtsne_tsne_learning_rate(bhtsne_tsne* t, double learning_rate);        /* :277 */
+int bhtsne_tsne_epochs(bhtsne_tsne* t, int64_t epochs);                      /* :288 */
+int bhtsne_tsne_momentum(bhtsne_tsne* t, double momentum);                   /* :299 */
+int bhtsne_tsne_final_momentum(bhtsne_tsne* t, double final_momentum);       /* :310 */
+int bhtsne_tsne_momentum_switch_epoch(bhtsne_tsne* t, int64_t epoch);        /* :322 */
+int bhtsne_tsne_stop_lying_epoch(bhtsne_tsne* t, int64_t epoch);             /* :338 */
+int bhtsne_tsne_early_exaggeration(bhtsne_tsne* t, double exaggeration);     /* :352 */
+int bhtsne_tsne_perplexity(bhtsne_tsne* t, double perplexity);               /* :367 */
+int bhtsne_tsne_epoch_callback(bhtsne_tsne* t, bhtsne_epoch_cb cb, void* user); /* :415 */
+int bhtsne_tsne_initial_embedding(bhtsne_tsne* t, const void* y, int64_t len);  /* :431 */
+/* No reference counterpart: the reference's random_init (src/tsne/mod.rs:142-147)
+ * draws N(0, 1e-4) from an unseeded generator; here the draw is seeded. */
+int bhtsne_tsne_random_seed(bhtsne_tsne* t, uint64_t seed);
+
+/* Finishers. `data` is n_samples x dim, row-major, of the handle's type. */
+/* exact (src/lib.rs:489-646) with the Euclidean distance (squared = 0) or the
+ * squared Euclidean distance (squared = 1) as `distance_f`. */
+int bhtsne_tsne_exact_euclidean(bhtsne_tsne* t, const void* data, int32_t dim, int32_t squared);
+/* exact with an arbitrary `distance_f`, given as its n x n matrix (only the
+ * strict upper triangle is read, as the reference evaluates it). */
+int bhtsne_tsne_exact_distances(bhtsne_tsne* t, const void* distances);
+/* barnes_hut (src/lib.rs:701-742) with the Euclidean metric. */
+int bhtsne_tsne_barnes_hut_euclidean(bhtsne_tsne* t, double theta, const void* data, int32_t dim);
+/* barnes_hut_with_neighbors (src/lib.rs:757-772): rows x k table of
+ * Neighbor{index, distance} (src/lib.rs:108-111) split into two arrays. */
+int bhtsne_tsne_barnes_hut_with_neighbors(bhtsne_tsne* t, double theta, const uint64_t* indices,
+                                          const void* distances, int64_t rows, int64_t k);
+/* fit_sne (src/lib.rs:835-871) with the Euclidean metric. */
+int bhtsne_tsne_fit_sne_euclidean(bhtsne_tsne* t, const void* data, int32_t dim);
+/* fit_sne_with_neighbors (src/lib.rs:884-894). */
+int bhtsne_tsne_fit_sne_with_neighbors(bhtsne_tsne* t, const uint64_t* indices, const void* distances, int64_t rows,
+                                       int64_t k);
+
+/* Getters. */
+/* embedding (src/lib.rs:438-440): n * D values. */
+int bhtsne_tsne_embedding(bhtsne_tsne* t, void* out);
+/* kl_divergence (src/lib.rs:448-477). *has_value = 0 before a fit. With
+ * quirk = 1 the sparse cost reads the value array at the row index, exactly
+ * as the reference does (src/tsne/mod.rs:768-770); quirk = 0 gives the
+ * textbook sum over the CSR entries. The exact method ignores `quirk`. */
+int bhtsne_tsne_kl_divergence(bhtsne_tsne* t, int32_t quirk, double* out, int32_t* has_value);
+/* affinities (src/lib.rs:1019-1037): pristine (un-exaggerated) CSR. Pass NULL
+ * arrays to query nnz first. *has_value = 0 when no sparse graph exists. */
+int bhtsne_tsne_affinities(bhtsne_tsne* t, uint64_t* rows, uint32_t* columns, void* values, int64_t* nnz,
+                           double* perplexity, int32_t* has_value);
+/* with_affinities (src/lib.rs:1043-1051). rows has n_rows entries. */
+int bhtsne_tsne_with_affinities(bhtsne_tsne* t, const uint64_t* rows, int64_t n_rows, const uint32_t* columns,
+                                const void* values, int64_t nnz, double perplexity);
+
+/* No reference counterpart: continues the last fit for `epochs` more epochs on
+ * the device-resident state (same epoch numbering, exaggeration and momentum
+ * schedule), so that fit(E1) followed by advance(E2) equals fit(E1 + E2). */
+int bhtsne_tsne_advance(bhtsne_tsne* t, int64_t epochs);
+/* No reference counterpart: device time of the last affinity build and of the
+ * epochs run by the last finisher or advance call (CUDA events, ms). */
+int bhtsne_tsne_timings(const bhtsne_tsne* t, double* affinity_ms, double* loop_ms, int64_t* loop_epochs);
+
+/* ---- stage entry points (parity and integration seams) -------------------- */
+/* Exact kNN under the Euclidean metric, the result the VP-tree search
+ * (src/tsne/vptree.rs:274-319) returns for `barnes_hut`: per row the k nearest
+ * other rows by (distance, index). idx/dist are n x k. */
+int bhtsne_knn_euclidean(bhtsne_ctx* ctx, int dtype, const void* data, int64_t n, int32_t dim, int32_t k,
+                         uint32_t* indices, void* distances);
+/* search_beta per row (src/tsne/mod.rs:201-275): conditional P (n x k) from
+ * neighbour distances (n x k). iterations (optional, n) gets the bisection
+ * count per row. */
+int bhtsne_conditional_p(bhtsne_ctx* ctx, int dtype, const void* distances, int64_t n, int32_t k, double perplexity,
+                         void* p, int32_t* iterations);
+/* symmetrize_sparse_matrix (src/tsne/mod.rs:306-406): symmetric CSR from the
+ * kNN table (n x k columns and conditional P). Call with NULL outputs to get
+ * nnz, then with rows (n + 1), columns (nnz), values (nnz). */
+int bhtsne_symmetrize(bhtsne_ctx* ctx, int dtype, const uint32_t* columns, const void* p, int64_t n, int32_t k,
+                      uint64_t* rows_out, uint32_t* columns_out, void* values_out, int64_t* nnz);
+/* Repulsion::step (src/repulsion.rs:31-54): attractive forces `pos`,
+ * repulsive forces `neg` (n x D) and Z at a fixed embedding y, for
+ * BHTSNE_METHOD_BARNES_HUT (theta) or BHTSNE_METHOD_FIT_SNE. For
+ * BHTSNE_METHOD_EXACT, `values` is the dense n x n P, `pos` receives the
+ * exact gradient dy (src/lib.rs:596-619) and `neg` is unused. */
+int bhtsne_gradient(bhtsne_ctx* ctx, int dtype, int32_t method, int32_t embed_dim, const void* y, int64_t n,
+                    const uint64_t* rows, const uint32_t* columns, const void* values, int64_t nnz, double theta,
+                    void* pos, void* neg, double* z);
+/* gradient_descent_step + zero_mean (src/tsne/mod.rs:470-516, :534-568) on
+ * host arrays (n x D), in place. */
+int bhtsne_update(bhtsne_ctx* ctx, int dtype, int32_t embed_dim, void* y, const void* pos, const void* neg, void* uy,
+                  void* gains, int64_t n, double learning_rate, double momentum, double inverse_z);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* BHTSNE_GPU_H */

@@ -1,0 +1,70 @@
+"""First GPU parity checks: stage entry points against the oracle."""
+import numpy as np
+import pytest
+
+from conftest import blobs
+
+pytestmark = pytest.mark.gpu
+
+
+def rel_l2(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def test_knn_matches_bruteforce(gpu, oracle):
+    X, _ = blobs(1500, 50, 10, 1)
+    gi, gd = gpu.knn_euclidean(X, 90)
+    oi, od = oracle.knn(X, 90)
+    assert np.array_equal(gi, oi)
+    assert np.array_equal(gd, od)
+
+
+def test_conditional_p(gpu, oracle):
+    X, _ = blobs(1000, 20, 5, 2)
+    _, od = oracle.knn(X, 90)
+    gp, _ = gpu.conditional_p(od, 30.0)
+    op, _ = oracle.search_beta(od, 30.0)
+    assert np.max(np.abs(gp - op) / np.maximum(op, 1e-30)) < 1e-5
+
+
+def test_symmetrize_bit_exact(gpu, oracle):
+    X, _ = blobs(1000, 20, 5, 3)
+    oi, od = oracle.knn(X, 90)
+    op, _ = oracle.search_beta(od, 30.0)
+    gr, gc, gv = gpu.symmetrize(oi, op)
+    orr, oc, ov = oracle.symmetrize(oi, op)
+    assert np.array_equal(gr, orr)
+    assert np.array_equal(gc, oc)
+    assert np.array_equal(gv, ov)
+
+
+@pytest.mark.parametrize("D", [2, 3])
+def test_bh_gradient(gpu, oracle, D):
+    X, _ = blobs(2000, 20, 5, 4)
+    oi, od = oracle.knn(X, 90)
+    op, _ = oracle.search_beta(od, 30.0)
+    rows, cols, vals = oracle.symmetrize(oi, op)
+    vals = oracle.normalize(vals, 12.0)
+    rng = np.random.default_rng(5)
+    y = rng.normal(0, 3.0, size=(2000, D)).astype(np.float32)
+    pos, neg, z = gpu.gradient(gpu.METHOD_BARNES_HUT, y, rows, cols, vals, theta=0.5)
+    opos = oracle.edge_forces(y, rows, cols, vals)
+    oneg, _, oz = oracle.bh_repulsion(y, 0.5)
+    assert rel_l2(pos, opos) < 1e-5
+    assert rel_l2(neg, oneg) < 1e-4
+    assert abs(z - oz) / oz < 1e-4
+
+
+@pytest.mark.parametrize("D", [1, 2])
+def test_fit_gradient(gpu, oracle, D):
+    rng = np.random.default_rng(6)
+    y = rng.uniform(-20, 20, size=(3000, D)).astype(np.float32)
+    rows = np.zeros(3001, np.uint64)
+    cols = np.zeros(0, np.uint32)
+    vals = np.zeros(0, np.float32)
+    _, neg, z = gpu.gradient(gpu.METHOD_FIT_SNE, y, rows, cols, vals)
+    oneg, oz, _ = oracle.fit_repulsion(y)
+    assert rel_l2(neg, oneg) < 1e-4
+    assert abs(z - oz) / abs(oz) < 1e-4
