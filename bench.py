@@ -1,0 +1,330 @@
+"""t-SNE epochs/s at 1M points on one GB300 (Barnes-Hut, theta 0.5, 2-D).
+
+Workload (the 1M-point configuration): N = 1,000,000 points, input dim 128,
+float32, a 100-cluster mixture with Student-t (nu = 5) radial spread and
+centres ~ N(0, 8^2 I); perplexity 30 (k = 90); Barnes-Hut theta 0.5 into 2-D.
+A "step" is one optimisation epoch (tree build, traversal, attractive pass,
+fused update + recentre) over the full 1M-point embedding.
+
+  value  : epochs/s with the affinities and embedding resident in HBM, timed
+           with CUDA events on the library's stream (bhtsne_tsne_advance).
+  e2e    : epochs/s through the C ABI as a user calls it: with_affinities
+           (host CSR) + barnes_hut + embedding(), host<->device copies inside.
+  roofline / cpu_baseline / clocks: see the design doc.
+
+--impl reference times the CPU restatement of the reference (oracle/, C++
+with OpenMP on every host core) on the same workload: a bounded number of
+1M-point epochs. Run with --gpus N for N independent replicas (the path does
+not shard; one process per GPU under torchrun).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "t-SNE epochs/s @1M pts (Barnes-Hut theta 0.5, 2-D)"
+UNIT = "epochs/s"
+
+
+def make_workload(n, dim=128, clusters=100, seed=1003):
+    """100-cluster Student-t (nu=5) mixture, centres ~ N(0, 8^2 I), equal weights."""
+    rng = np.random.default_rng(seed)
+    centres = rng.normal(0.0, 8.0, size=(clusters, dim)).astype(np.float32)
+    lab = rng.integers(0, clusters, size=n)
+    g = rng.standard_normal(size=(n, dim), dtype=np.float32)
+    w = (rng.chisquare(5.0, size=n) / 5.0).astype(np.float32)
+    X = centres[lab] + g / np.sqrt(w)[:, None]
+    return np.ascontiguousarray(X, dtype=np.float32), lab
+
+
+def within_cluster_knn(X, lab, k):
+    """kNN restricted to each generating cluster (BLAS distances); used only to
+    give the CPU arm its affinity input. In this mixture the clusters are far
+    apart, so it coincides with the global kNN up to rounding ties."""
+    n = X.shape[0]
+    idx = np.zeros((n, k), np.uint64)
+    dist = np.zeros((n, k), np.float32)
+    for c in np.unique(lab):
+        members = np.nonzero(lab == c)[0]
+        Xc = X[members].astype(np.float32)
+        sq = (Xc * Xc).sum(1)
+        for s in range(0, len(members), 4096):
+            blk = Xc[s:s + 4096]
+            d2 = sq[s:s + 4096, None] + sq[None, :] - 2.0 * (blk @ Xc.T)
+            np.maximum(d2, 0, out=d2)
+            rows = np.arange(blk.shape[0])
+            d2[rows, rows + s] = np.inf
+            part = np.argpartition(d2, k, axis=1)[:, :k]
+            pd = np.take_along_axis(d2, part, 1)
+            order = np.argsort(pd, axis=1, kind="stable")
+            part = np.take_along_axis(part, order, 1)
+            idx[members[s:s + 4096]] = members[part]
+            dist[members[s:s + 4096]] = np.sqrt(np.take_along_axis(pd, order, 1))
+    return idx, dist
+
+
+class ClockSampler:
+    """Samples SM clocks and throttle reasons with nvidia-smi while running."""
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device=0):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return d.get("hbm_gbs"), "measured"
+    return 6800.0, "fallback"
+
+
+def dist_info():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def barrier_and_max(value, ws):
+    """Barrier + max over ranks (gloo over the host; each rank runs its own GPU)."""
+    if ws <= 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    if not dist.is_initialized():
+        dist.init_process_group("gloo")
+    t = torch.tensor([value], dtype=torch.float64)
+    dist.barrier()
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def run_ours(args):
+    import bhtsne_gb300 as bg
+    ws, rank, local = dist_info()
+    n = args.n
+    X, lab = make_workload(n, seed=args.seed)
+    ctx = bg.Context(local)
+    perp, theta = 30.0, 0.5
+    t = bg.TSNE(X, D=2, ctx=ctx).perplexity(perp).epochs(0).random_seed(42 + rank)
+    t0 = time.time()
+    t.barnes_hut(theta)  # kNN + affinities + seeding, no epochs
+    setup_s = time.time() - t0
+    tm = t.timings()
+    t.advance(args.warmup)
+    t.profile(True)
+    launches0 = ctx.lib.bhtsne_launch_count()
+    barrier_and_max(0.0, ws)
+    with ClockSampler(local) as clk:
+        t.advance(args.steps)
+    launches = ctx.lib.bhtsne_launch_count() - launches0
+    loop_ms = t.timings()["loop_ms"]
+    loop_ms = barrier_and_max(loop_ms, ws)
+    ph = t.phase_times()
+    aff = t.affinities()
+    nnz = int(aff.values.size)
+    value = ws * args.steps / (loop_ms / 1e3)
+
+    # roofline: dominant phase of the epoch
+    peak, peak_kind = measured_peaks()
+    per = {k: ph[k] / max(ph["epochs"], 1) for k in ("tree", "repulsion", "attractive", "update")}
+    dom = max(per, key=per.get)
+    D = 2
+    alg = {
+        # traversal: queries (perm + y), every node once (16 B geometry + 4 B skip), forces out
+        "repulsion": 4 * n + 4 * n * D + 20 * (2 * n - 1) + 4 * n * D,
+        # CSR attractive: row offsets, (col, val) per entry, y once, forces out
+        "attractive": 8 * (n + 1) + 8 * nnz + 4 * n * D + 4 * n * D,
+        # update + recentre: 32 N D + 8 N D (+ bbox, included in the recentre read)
+        "update": 32 * n * D + 8 * n * D,
+        # Morton + sort: y in, 8 radix passes over (u64 key, u32 idx)
+        "tree": 4 * n * D + 12 * n * 2 * 8,
+    }
+    achieved = alg[dom] / (per[dom] / 1e3) / 1e9
+    roofline = {"kernel": {"repulsion": "bh_traverse_kernel", "attractive": "attractive_kernel",
+                           "update": "update_kernel+recenter_bbox_kernel", "tree": "morton+radix sort+tree build"}[dom],
+                "bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 5), "traffic": None, "peak_source": peak_kind,
+                "algorithmic_bytes": alg[dom], "ms_per_launch": round(per[dom], 4)}
+    att_gbs = alg["attractive"] / (per["attractive"] / 1e3) / 1e9
+
+    # e2e: through the C ABI with host buffers (with_affinities -> barnes_hut -> embedding)
+    t2 = bg.TSNE(n, D=2, ctx=ctx).epochs(args.steps).random_seed(7 + rank)
+    h2d = aff.rows.nbytes + aff.columns.nbytes + aff.values.nbytes
+    barrier_and_max(0.0, ws)
+    w0 = time.perf_counter()
+    t2.with_affinities(aff)
+    t2.barnes_hut(theta)
+    emb = t2.embedding()
+    e2e_s = time.perf_counter() - w0
+    e2e_s = barrier_and_max(e2e_s, ws)
+    e2e = {"value": round(ws * args.steps / e2e_s, 3), "unit": UNIT, "h2d_bytes_per_step": h2d // args.steps,
+           "d2h_bytes_per_step": emb.nbytes // args.steps,
+           "note": "with_affinities(host CSR) + barnes_hut(epochs=steps) + embedding(); affinity "
+                   "normalisation, seeding and all copies inside the timed region"}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        cpu = cpu_baseline_sample(aff, emb.reshape(n, 2), args.cpu_epochs)
+
+    out = {
+        "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(loop_ms / args.steps, 4), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "bh2d_1M_d128", "n_points": n, "input_dim": 128, "clusters": 100,
+                   "perplexity": perp, "k": 90, "theta": theta, "embed_dim": 2, "nnz": nnz,
+                   "l2": "inputs larger than L2 (CSR P of %.2f GB)" % ((8 * nnz + 8 * n) / 1e9),
+                   "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"},
+        "e2e": e2e,
+        "roofline": roofline,
+        "roofline_attractive": {"achieved": round(att_gbs, 2), "peak": peak, "unit": "GB/s",
+                                "frac": round(att_gbs / peak, 4)},
+        "phase_ms_per_epoch": {k: round(v, 4) for k, v in per.items()},
+        "setup_s": round(setup_s, 3), "affinity_ms": round(tm["affinity_ms"], 2),
+        "gpu_launches": int(launches),
+        "clocks": clk.summary(),
+    }
+    if cpu:
+        out["cpu_baseline"] = cpu
+    if rank == 0:
+        print(json.dumps(out))
+
+
+def cpu_baseline_sample(aff, y0, epochs):
+    """The oracle (C++/OpenMP restatement) on the same CSR and a 1M-point
+    embedding for a bounded number of epochs."""
+    from oracle import pyoracle as O
+    n = y0.shape[0]
+    O.build()
+    threads = os.cpu_count() or 1
+    O.set_threads(threads)
+    t = O.TSNE(n).epochs(epochs).initial_embedding(y0)
+    t.with_affinities(aff.rows, aff.columns, aff.values, aff.perplexity)
+    dummy = np.zeros((n, 1), np.float32)
+    w0 = time.perf_counter()
+    t.barnes_hut(0.5, dummy)
+    s = time.perf_counter() - w0
+    return {"value": round(epochs / s, 4), "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{epochs} Barnes-Hut epochs at N={n} on the same CSR (oracle C++ restatement, OpenMP)"}
+
+
+def run_reference(args):
+    ws, rank, _ = dist_info()
+    if rank != 0:
+        return
+    from oracle import pyoracle as O
+    O.build()
+    threads = os.cpu_count() or 1
+    O.set_threads(threads)
+    n = args.n
+    X, lab = make_workload(n, seed=args.seed)
+    idx, dist = within_cluster_knn(X, lab, 90)
+    del X
+    t = O.TSNE(n).perplexity(30.0).epochs(0).seed(42)
+    t.barnes_hut_with_neighbors(0.5, idx, dist)
+    aff = t.affinities()
+    y = t.embedding().reshape(n, 2)
+    rows, cols, vals, perp = aff
+    # warm-up epochs, then K timed epochs, each a full 1M-point epoch
+    def run_epochs(k, y_init):
+        h = O.TSNE(n).epochs(k).initial_embedding(y_init)
+        h.with_affinities(rows, cols, vals, perp)
+        w0 = time.perf_counter()
+        h.barnes_hut(0.5, np.zeros((n, 1), np.float32))
+        return time.perf_counter() - w0, h.embedding().reshape(n, 2)
+    _, y = run_epochs(args.warmup, y)
+    s, _ = run_epochs(args.steps, y)
+    v = args.steps / s
+    out = {"metric": METRIC, "value": round(v, 4), "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": round(1e3 * s / args.steps, 2), "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "impl": "reference",
+           "config": {"workload": "bh2d_1M_d128", "n_points": n, "input_dim": 128, "perplexity": 30.0,
+                      "theta": 0.5, "embed_dim": 2, "nnz": int(vals.size)},
+           "cpu_baseline": {"value": round(v, 4), "unit": UNIT, "cores": threads, "kind": "port",
+                            "sample": f"{args.steps} timed Barnes-Hut epochs at N={n} after {args.warmup} warm-up "
+                                      "epochs; affinities from within-cluster kNN (untimed)"},
+           "e2e": {"value": round(v, 4), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--n", type=int, default=1_000_000)
+    ap.add_argument("--seed", type=int, default=1003)
+    ap.add_argument("--cpu-epochs", type=int, default=3)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        if args.steps > 30:
+            args.steps = 30  # bounded CPU sample: each step is a full 1M-point epoch
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -51,6 +51,9 @@ SIGNATURES = {
     "bhtsne_tsne_with_affinities": (C.c_int, [_vp, _u64p, _i64, _u32p, _vp, _i64, _dbl]),
     "bhtsne_tsne_advance": (C.c_int, [_vp, _i64]),
     "bhtsne_tsne_timings": (C.c_int, [_vp, _dblp, _dblp, _i64p]),
+    "bhtsne_tsne_profile": (C.c_int, [_vp, _i32]),
+    "bhtsne_tsne_phase_times": (C.c_int, [_vp, _dblp, _i64p]),
+    "bhtsne_launch_count": (C.c_int64, []),
     "bhtsne_knn_euclidean": (C.c_int, [_vp, C.c_int, _vp, _i64, _i32, _i32, _u32p, _vp]),
     "bhtsne_conditional_p": (C.c_int, [_vp, C.c_int, _vp, _i64, _i32, _dbl, _vp, _i32p]),
     "bhtsne_symmetrize": (C.c_int, [_vp, C.c_int, _u32p, _vp, _i64, _i32, _u64p, _u32p, _vp, _i64p]),

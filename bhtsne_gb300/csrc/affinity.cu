@@ -6,8 +6,7 @@
 //    metric distance; sum += min_positive; H = sum(beta p d^2)/sum + ln sum;
 //    stop when |H - ln(perplexity)| < 1e-5 or after 200 iterations; beta
 //    doubles/halves until bracketed, then bisects; finally p /= sum + eps.
-//    The two row sums are accumulated in FP64 (a warp reduction) and rounded
-//    to T before use; everything else follows the reference in T.
+//    Sums are sequential in T as in the reference (see search_beta_kernel).
 //  * symmetrize_sparse_matrix: src/tsne/mod.rs:306-406. The reference emits,
 //    for every directed kNN edge i->j, the entries (i, j) and (j, i) with value
 //    p_ij + p_ji when i and j list each other (once, from the side i < j) and
@@ -27,8 +26,23 @@ namespace bhg {
 namespace {
 
 // ---------------------------------------------------------------------------
-// search_beta: one warp per row.
+// search_beta: one warp per row. The lanes evaluate the kernel values of the
+// row in parallel and park them in the output row; lane 0 then forms both
+// sums sequentially in index order, in T, exactly as the reference folds
+// them. exp and ln are evaluated in FP64 and rounded to T, which reproduces
+// the correctly rounded single-precision libm results the reference gets on
+// the host; the bisection's 1e-5 stopping test is sensitive to last-ulp
+// differences, so this is what keeps P within 1e-5 of the reference.
 // ---------------------------------------------------------------------------
+template <class T>
+__device__ __forceinline__ T exp_rn(T x) {
+  return (T)exp((double)x);
+}
+template <class T>
+__device__ __forceinline__ T log_rn(T x) {
+  return (T)log((double)x);
+}
+
 template <class T>
 __global__ void search_beta_kernel(const T* __restrict__ dist, int64_t n, int64_t k, T perplexity,
                                    T* __restrict__ p, int32_t* __restrict__ iters) {
@@ -41,24 +55,27 @@ __global__ void search_beta_kernel(const T* __restrict__ dist, int64_t n, int64_
   T beta = T(1), min_beta = -Lim<T>::max(), max_beta = Lim<T>::max();
   const T tolerance = (T)1e-5;
   const T two = T(2);
-  const T ln_perp = dlog(perplexity);
-  T sum = T(0), beta_used = beta;
+  const T ln_perp = log_rn(perplexity);
+  T sum = T(0);
   int iteration = 0;
   while (!found && iteration < 200) {
-    double s = 0.0, e = 0.0;
     for (int64_t j = lane; j < k; j += 32) {
       const T dj = d[j];
-      const T d2 = dj * dj;
-      const T pj = dexp(-beta * d2);
-      s += (double)pj;
-      e += (double)(beta * pj * d2);
+      out[j] = exp_rn(-beta * (dj * dj));
     }
-    s = warp_sum(s);
-    e = warp_sum(e);
-    beta_used = beta;
-    sum = (T)s + Lim<T>::min_pos();
-    T entropy = (T)e;
-    entropy = entropy / sum + dlog(sum);
+    __syncwarp();
+    T s = T(0), e = T(0);
+    if (lane == 0) {
+      for (int64_t j = 0; j < k; ++j) s = s + out[j];
+      for (int64_t j = 0; j < k; ++j) {
+        const T dj = d[j];
+        e = e + beta * out[j] * (dj * dj);
+      }
+    }
+    s = __shfl_sync(kFull, s, 0);
+    e = __shfl_sync(kFull, e, 0);
+    sum = s + Lim<T>::min_pos();
+    T entropy = e / sum + log_rn(sum);
     const T diff = entropy - ln_perp;
     if (diff < tolerance && -diff < tolerance) {
       found = true;
@@ -76,12 +93,10 @@ __global__ void search_beta_kernel(const T* __restrict__ dist, int64_t n, int64_
       if (isinf(beta) && beta < T(0)) beta = -Lim<T>::max();
     }
     ++iteration;
+    __syncwarp();
   }
   const T denom = sum + Lim<T>::eps();
-  for (int64_t j = lane; j < k; j += 32) {
-    const T dj = d[j];
-    out[j] = dexp(-beta_used * (dj * dj)) / denom;
-  }
+  for (int64_t j = lane; j < k; j += 32) out[j] = out[j] / denom;
   if (iters && lane == 0) iters[row] = iteration;
 }
 

@@ -25,6 +25,10 @@
 
 using namespace bhg;
 
+namespace bhg {
+std::atomic<long long> g_launches{0};
+}
+
 struct bhtsne_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
@@ -115,6 +119,9 @@ struct bhtsne_tsne {
   // timings
   double aff_ms = 0, loop_ms = 0;
   int64_t loop_epochs = 0;
+  bool profile = false;
+  double phase_ms[BHTSNE_PHASES] = {0, 0, 0, 0};
+  int64_t phase_epochs = 0;
   std::string err;
   State<float>* sf = nullptr;
   State<double>* sd = nullptr;
@@ -320,30 +327,51 @@ void advance_impl(bhtsne_tsne* t, int64_t epochs) {
   BHG_CUDA(cudaEventRecord(e0, s));
   T* y = S.y.template as<T>();
   double* z = S.zbuf.template as<double>();
+  // Optional phase profiling: 5 events per epoch bound the 4 phases.
+  const bool prof = t->profile;
+  std::vector<cudaEvent_t> ev;
+  if (prof) {
+    ev.resize((size_t)epochs * (BHTSNE_PHASES + 1));
+    for (auto& e : ev) BHG_CUDA(cudaEventCreate(&e));
+  }
+  auto mark = [&](int64_t k, int ph) {
+    if (prof) BHG_CUDA(cudaEventRecord(ev[(size_t)k * (BHTSNE_PHASES + 1) + ph], s));
+  };
   for (int64_t k = 0; k < epochs; ++k) {
     const int64_t epoch = t->cursor;
     if (epoch == 0) launch_recenter_bbox<T>(D, y, n, nullptr, false, S.bh, bits, s);
     const T mom = (T)t->momentum;
+    mark(k, 0);
     if (t->loop_kind == BHTSNE_METHOD_BARNES_HUT) {
       bh_build<T>(S.bh, D, y, n, s);
+      mark(k, 1);
       bh_traverse<T>(S.bh, D, y, n, (T)t->loop_theta, S.neg.template as<T>(), nullptr, s);
+      mark(k, 2);
       launch_attractive<T>(D, S.rows.template as<uint64_t>(), S.cols.template as<uint32_t>(), S.vals.template as<T>(), y, n,
                            S.pos.template as<T>(), s);
+      mark(k, 3);
       launch_update<T>(D, y, S.pos.template as<T>(), S.neg.template as<T>(), S.uy.template as<T>(),
                        S.gains.template as<T>(), n, S.bh.z(), T(0), lr, mom, S.us, s);
     } else if (t->loop_kind == BHTSNE_METHOD_FIT_SNE) {
+      mark(k, 1);
       fit_repulsion<T>(S.fit, D, y, n, S.bh.params.template as<BoxParams<T>>(), S.neg.template as<T>(), z, s);
+      mark(k, 2);
       launch_attractive<T>(D, S.rows.template as<uint64_t>(), S.cols.template as<uint32_t>(), S.vals.template as<T>(), y, n,
                            S.pos.template as<T>(), s);
+      mark(k, 3);
       launch_update<T>(D, y, S.pos.template as<T>(), S.neg.template as<T>(), S.uy.template as<T>(),
                        S.gains.template as<T>(), n, z, T(0), lr, mom, S.us, s);
     } else {
+      mark(k, 1);
       launch_exact_z<T>(D, y, n, z, S.tmp, s);
       launch_exact_grad<T>(D, y, S.pdense.template as<T>(), n, z, S.pos.template as<T>(), s);
+      mark(k, 2);
+      mark(k, 3);
       launch_update<T>(D, y, S.pos.template as<T>(), nullptr, S.uy.template as<T>(), S.gains.template as<T>(), n,
                        nullptr, T(0), lr, mom, S.us, s);
     }
     launch_recenter_bbox<T>(D, y, n, S.us.mean(), true, S.bh, bits, s);
+    mark(k, 4);
     epoch_tail<T>(t, epoch, snap);
     t->cursor += 1;
   }
@@ -355,6 +383,18 @@ void advance_impl(bhtsne_tsne* t, int64_t epochs) {
   BHG_CUDA(cudaEventDestroy(e1));
   t->loop_ms = ms;
   t->loop_epochs = epochs;
+  if (prof) {
+    for (int ph = 0; ph < BHTSNE_PHASES; ++ph) t->phase_ms[ph] = 0;
+    for (int64_t k = 0; k < epochs; ++k)
+      for (int ph = 0; ph < BHTSNE_PHASES; ++ph) {
+        float pm = 0;
+        BHG_CUDA(cudaEventElapsedTime(&pm, ev[(size_t)k * (BHTSNE_PHASES + 1) + ph],
+                                      ev[(size_t)k * (BHTSNE_PHASES + 1) + ph + 1]));
+        t->phase_ms[ph] += pm;
+      }
+    for (auto& e : ev) cudaEventDestroy(e);
+    t->phase_epochs = epochs;
+  }
 }
 
 template <class T>
@@ -866,6 +906,22 @@ int bhtsne_tsne_advance(bhtsne_tsne* t, int64_t epochs) {
     DISPATCH(t, advance_impl<T>(t, epochs));
   });
 }
+
+int bhtsne_tsne_profile(bhtsne_tsne* t, int32_t enable) {
+  if (!t) return BHTSNE_EINVAL;
+  t->profile = enable != 0;
+  return BHTSNE_OK;
+}
+
+int bhtsne_tsne_phase_times(const bhtsne_tsne* t, double* ms, int64_t* epochs) {
+  if (!t) return BHTSNE_EINVAL;
+  if (ms)
+    for (int ph = 0; ph < BHTSNE_PHASES; ++ph) ms[ph] = t->phase_ms[ph];
+  if (epochs) *epochs = t->phase_epochs;
+  return BHTSNE_OK;
+}
+
+int64_t bhtsne_launch_count(void) { return (int64_t)g_launches.load(); }
 
 int bhtsne_tsne_timings(const bhtsne_tsne* t, double* affinity_ms, double* loop_ms, int64_t* loop_epochs) {
   if (!t) return BHTSNE_EINVAL;

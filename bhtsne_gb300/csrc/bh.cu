@@ -393,6 +393,7 @@ __global__ void tree_emit_kernel(const uint64_t* __restrict__ codes, int64_t n, 
     if ((c0 >> sh1) == (codes[a] >> sh1)) {
       const uint32_t m = mask[a];
       const int64_t idx = (int64_t)base[a] + __popc(m & ((1u << l) - 1u));
+      if (idx >= 2 * n) return;  // cannot happen for a well-formed build; never write out of bounds
       const double cnt = (double)(e - a);
       T com[D];
 #pragma unroll
@@ -414,6 +415,7 @@ __global__ void tree_emit_kernel(const uint64_t* __restrict__ codes, int64_t n, 
     }
     const uint32_t m = mask[s];
     const int64_t idx = (int64_t)base[s] + __popc(m);
+    if (idx >= 2 * n) return;
     const uint32_t count = (uint32_t)(e - s);
     T com[D];
     if (count == 1) {
@@ -444,6 +446,7 @@ __global__ void tree_emit_kernel(const uint64_t* __restrict__ codes, int64_t n, 
 template <class T, int D>
 __global__ void __launch_bounds__(kThreads) bh_traverse_kernel(const T* __restrict__ y, const uint32_t* __restrict__ perm,
                                                                int64_t n, TreeNodes<T, D> nodes, const uint64_t* __restrict__ n_nodes_p,
+                                                               int64_t max_nodes,
                                                                T theta_sq, T* __restrict__ neg, T* __restrict__ qout,
                                                                double* __restrict__ zpart, unsigned* __restrict__ done,
                                                                double* __restrict__ z_out) {
@@ -456,7 +459,8 @@ __global__ void __launch_bounds__(kThreads) bh_traverse_kernel(const T* __restri
     T qv[D];
 #pragma unroll
     for (int a = 0; a < D; ++a) qv[a] = y[pi * D + a];
-    const uint32_t M = (uint32_t)*n_nodes_p;
+    const uint64_t m_raw = *n_nodes_p;
+    const uint32_t M = (uint32_t)(m_raw < (uint64_t)max_nodes ? m_raw : (uint64_t)max_nodes);
     T f[D];
 #pragma unroll
     for (int a = 0; a < D; ++a) f[a] = T(0);
@@ -477,7 +481,8 @@ __global__ void __launch_bounds__(kThreads) bh_traverse_kernel(const T* __restri
         ++i;
         continue;
       }
-      i = skip;
+      // skip > i by construction; max() keeps the walk finite regardless.
+      i = skip > i ? skip : i + 1;
       if (r2 < T(0) && dist == T(0)) continue;
       const T inv = T(1) / (T(1) + dist);
       T m = mass * inv;
@@ -628,11 +633,11 @@ void bh_traverse(BhWorkspace<T>& ws, int D, const T* y, int64_t n, T theta, T* n
   const T theta_sq = theta * theta;
   const uint64_t* M = ws.base.template as<uint64_t>() + n;
   if (D == 2)
-    bh_traverse_kernel<T, 2><<<g, kThreads, 0, s>>>(y, ws.perm.template as<uint32_t>(), n, nodes_of<T, 2>(ws), M, theta_sq, neg,
+    bh_traverse_kernel<T, 2><<<g, kThreads, 0, s>>>(y, ws.perm.template as<uint32_t>(), n, nodes_of<T, 2>(ws), M, 2 * n, theta_sq, neg,
                                                     qout, ws.zpart.template as<double>(), ws.zdone.template as<unsigned>(),
                                                     ws.zval.template as<double>());
   else
-    bh_traverse_kernel<T, 3><<<g, kThreads, 0, s>>>(y, ws.perm.template as<uint32_t>(), n, nodes_of<T, 3>(ws), M, theta_sq, neg,
+    bh_traverse_kernel<T, 3><<<g, kThreads, 0, s>>>(y, ws.perm.template as<uint32_t>(), n, nodes_of<T, 3>(ws), M, 2 * n, theta_sq, neg,
                                                     qout, ws.zpart.template as<double>(), ws.zdone.template as<unsigned>(),
                                                     ws.zval.template as<double>());
   BHG_LAUNCH_CHECK();

@@ -7,6 +7,7 @@
 
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cstdint>
 #include <cstdio>
 #include <stdexcept>
@@ -42,7 +43,14 @@ struct Error : std::runtime_error {
     if (e_ != cudaSuccess) ::bhg::throw_cuda(e_, #call, __FILE__, __LINE__); \
   } while (0)
 
-#define BHG_LAUNCH_CHECK() BHG_CUDA(cudaGetLastError())
+// Every kernel launch in the library is followed by this check, which also
+// counts launches (bhtsne_launch_count).
+extern std::atomic<long long> g_launches;
+#define BHG_LAUNCH_CHECK()                                   \
+  do {                                                       \
+    ::bhg::g_launches.fetch_add(1, std::memory_order_relaxed); \
+    BHG_CUDA(cudaGetLastError());                            \
+  } while (0)
 
 inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
 

@@ -19,7 +19,10 @@
 //    wrapped lags are never read), so only rounding differs.
 //  * The kernel is real and even, so its spectrum is real: two real charge
 //    grids are packed as the real and imaginary parts of one complex grid and
-//    convolved together (D + 2 terms -> 2 complex transforms).
+//    convolved together (D + 2 terms -> 2 complex transforms). The pairs are
+//    (s, y_1) and (y_2, |y|^2 / s) with s a power of two near max |y|, so both
+//    halves of a pair have similar magnitude and neither one's rounding noise
+//    swamps the other; scaling by a power of two is exact.
 //  * 2-D transforms are row FFTs in shared memory plus tiled transposes; the
 //    spectrum stays in transposed layout, which is harmless because the
 //    kernel spectrum is symmetric in its two axes. Rows that are known to be
@@ -102,6 +105,10 @@ __global__ void fit_params_kernel(const BoxParams<T>* __restrict__ box, FitParam
   int L = 16;
   while (L < 2 * nodes - 1) L <<= 1;
   const T box_width = extent / (T)(double)boxes;
+  T m = fmax(fmax(fabs(lo), fabs(hi)), T(1));
+  int ex = 0;
+  frexp(m, &ex);
+  out->scale = ldexp(T(1), ex);
   out->lo = lo;
   out->extent = extent;
   out->box_width = box_width;
@@ -162,14 +169,14 @@ __global__ void spread_kernel(const T* __restrict__ y, int64_t n, const FitParam
     T* c0 = reinterpret_cast<T*>(g0 + flat);
     T* c1 = reinterpret_cast<T*>(g1 + flat);
     if (D == 2) {
-      atomicAdd(c0, wt * T(1));
+      atomicAdd(c0, wt * p.scale);
       atomicAdd(c0 + 1, wt * yv[0]);
       atomicAdd(c1, wt * yv[D - 1]);
-      atomicAdd(c1 + 1, wt * sq);
+      atomicAdd(c1 + 1, wt * (sq / p.scale));
     } else {
-      atomicAdd(c0, wt * T(1));
+      atomicAdd(c0, wt * p.scale);
       atomicAdd(c0 + 1, wt * yv[0]);
-      atomicAdd(c1, wt * sq);
+      atomicAdd(c1, wt * (sq / p.scale));
     }
   }
 }
@@ -323,6 +330,8 @@ __global__ void gather_kernel(const T* __restrict__ y, int64_t n, const FitParam
       phi[2] = phi[2] + wt * a1.x;
       if (D == 2) phi[3] = phi[3] + wt * a1.y;
     }
+    phi[0] = phi[0] / p.scale;
+    phi[D + 1] = phi[D + 1] * p.scale;
     const T density = phi[0];
     const T sqp = phi[D + 1];
     T norm_sq = T(0), cross = T(0);

@@ -8,6 +8,7 @@ namespace bhg {
 template <class T>
 struct FitParams {
   T lo, extent, box_width, inv_box_width, spacing;
+  T scale;  // power of two >= max |y|: balances the magnitudes of packed terms
   int boxes, nodes, L;
 };
 

@@ -237,6 +237,16 @@ class TSNE:
         return self._check(self.lib.bhtsne_tsne_with_affinities(self.handle, _ptr(rows), rows.size, _ptr(cols),
                                                                 _ptr(vals), vals.size, float(aff.perplexity)))
 
+    def profile(self, enable: bool = True):
+        """Per-phase CUDA-event timing of subsequent epochs (no reference counterpart)."""
+        return self._check(self.lib.bhtsne_tsne_profile(self.handle, 1 if enable else 0))
+
+    def phase_times(self):
+        ms = (C.c_double * 4)()
+        e = C.c_int64()
+        self.lib.bhtsne_tsne_phase_times(self.handle, ms, C.byref(e))
+        return {"tree": ms[0], "repulsion": ms[1], "attractive": ms[2], "update": ms[3], "epochs": e.value}
+
     def timings(self):
         a, lp, e = C.c_double(), C.c_double(), C.c_int64()
         self.lib.bhtsne_tsne_timings(self.handle, C.byref(a), C.byref(lp), C.byref(e))

@@ -128,6 +128,20 @@ int bhtsne_tsne_advance(bhtsne_tsne* t, int64_t epochs);
  * epochs run by the last finisher or advance call (CUDA events, ms). */
 int bhtsne_tsne_timings(const bhtsne_tsne* t, double* affinity_ms, double* loop_ms, int64_t* loop_epochs);
 
+/* No reference counterpart: per-phase device times of the epoch loop. With
+ * profiling enabled, each epoch records CUDA events on the handle's stream
+ * around the phases below; bhtsne_tsne_phase_times returns the summed ms and
+ * the number of timed epochs of the last finisher or advance call. */
+#define BHTSNE_PHASE_TREE 0       /* Morton codes, radix sort, tree build */
+#define BHTSNE_PHASE_REPULSION 1  /* BH traversal, or FIt-SNE spread/FFT/gather, or exact gradient */
+#define BHTSNE_PHASE_ATTRACTIVE 2 /* CSR attractive forces */
+#define BHTSNE_PHASE_UPDATE 3     /* fused update + recentre + bounding box */
+#define BHTSNE_PHASES 4
+int bhtsne_tsne_profile(bhtsne_tsne* t, int32_t enable);
+int bhtsne_tsne_phase_times(const bhtsne_tsne* t, double* ms, int64_t* epochs);
+/* Number of CUDA kernel launches this library has issued since it was loaded. */
+int64_t bhtsne_launch_count(void);
+
 /* ---- stage entry points (parity and integration seams) -------------------- */
 /* Exact kNN under the Euclidean metric, the result the VP-tree search
  * (src/tsne/vptree.rs:274-319) returns for `barnes_hut`: per row the k nearest
