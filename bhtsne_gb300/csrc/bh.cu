@@ -398,7 +398,7 @@ __global__ void tree_emit_kernel(const uint64_t* __restrict__ codes, int64_t n, 
       T com[D];
 #pragma unroll
       for (int q = 0; q < D; ++q) com[q] = (T)((pre[e * D + q] - pre[a * D + q]) / cnt);
-      nodes.write(idx, com, (T)(uint32_t)(e - a), prm->hw2[l], (uint32_t)base[e]);
+      nodes.write(idx, com, (T)(uint32_t)(e - a), l, (uint32_t)base[e]);
     }
   }
   if (run_start) {
@@ -433,7 +433,7 @@ __global__ void tree_emit_kernel(const uint64_t* __restrict__ codes, int64_t n, 
 #pragma unroll
       for (int q = 0; q < D; ++q) com[q] = acc[q] * inv;
     }
-    nodes.write(idx, com, (T)count, T(-1), (uint32_t)base[e]);
+    nodes.write(idx, com, (T)count, -1, (uint32_t)base[e]);
   }
 }
 
@@ -446,12 +446,16 @@ __global__ void tree_emit_kernel(const uint64_t* __restrict__ codes, int64_t n, 
 template <class T, int D>
 __global__ void __launch_bounds__(kThreads) bh_traverse_kernel(const T* __restrict__ y, const uint32_t* __restrict__ perm,
                                                                int64_t n, TreeNodes<T, D> nodes, const uint64_t* __restrict__ n_nodes_p,
-                                                               int64_t max_nodes,
+                                                               int64_t max_nodes, const BoxParams<T>* __restrict__ prm,
                                                                T theta_sq, T* __restrict__ neg, T* __restrict__ qout,
                                                                double* __restrict__ zpart, unsigned* __restrict__ done,
                                                                double* __restrict__ z_out) {
   __shared__ double sh[32];
   __shared__ bool last;
+  __shared__ T hw2s[40];
+  if (threadIdx.x < 40) hw2s[threadIdx.x] = prm->hw2[threadIdx.x];
+  __syncthreads();
+  nodes.hw2 = hw2s;
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   double qd = 0.0;
   if (t < n) {
@@ -552,11 +556,10 @@ void BhWorkspace<T>::reserve(int64_t n_, int D_) {
   base.ensure((nn + 1) * 8);
   const int64_t max_nodes = 2 * nn;
   if (D == 2) {
-    geom.ensure(max_nodes * sizeof(Quad<T>));
-    aux.ensure(max_nodes * sizeof(uint32_t));
+    geom.ensure(max_nodes * sizeof(Node2<T>));
   } else {
     geom.ensure(max_nodes * sizeof(Quad<T>));
-    aux.ensure(max_nodes * sizeof(RSkip<T>));
+    word.ensure(max_nodes * sizeof(uint32_t));
   }
   part_min.ensure(2 * 152 * 3 * sizeof(T));
   part_max.ensure(2 * 152 * 3 * sizeof(T));
@@ -575,9 +578,13 @@ void BhWorkspace<T>::reserve(int64_t n_, int D_) {
 template <class T, int D>
 static TreeNodes<T, D> nodes_of(BhWorkspace<T>& ws) {
   TreeNodes<T, D> t;
-  t.geom = ws.geom.template as<Quad<T>>();
-  if constexpr (D == 2) t.skip = ws.aux.template as<uint32_t>();
-  else t.rs = ws.aux.template as<RSkip<T>>();
+  t.hw2 = nullptr;
+  if constexpr (D == 2) {
+    t.geom = ws.geom.template as<Node2<T>>();
+  } else {
+    t.geom = ws.geom.template as<Quad<T>>();
+    t.word = ws.word.template as<uint32_t>();
+  }
   return t;
 }
 
@@ -618,6 +625,7 @@ static void bh_build_impl(BhWorkspace<T>& ws, const T* y, int64_t n, cudaStream_
 template <class T>
 void bh_build(BhWorkspace<T>& ws, int D, const T* y, int64_t n, cudaStream_t s) {
   if (n <= 0) return;
+  if (n > kMaxTreePoints) throw Error(ST_EINVAL, "error: the GPU Barnes-Hut arena holds at most 2^26 - 1 points.");
   if (D == 2) bh_build_impl<T, 2>(ws, y, n, s);
   else if (D == 3) bh_build_impl<T, 3>(ws, y, n, s);
   else throw Error(ST_EINVAL, "error: the GPU Barnes-Hut path covers D in {2, 3}.");
@@ -633,11 +641,11 @@ void bh_traverse(BhWorkspace<T>& ws, int D, const T* y, int64_t n, T theta, T* n
   const T theta_sq = theta * theta;
   const uint64_t* M = ws.base.template as<uint64_t>() + n;
   if (D == 2)
-    bh_traverse_kernel<T, 2><<<g, kThreads, 0, s>>>(y, ws.perm.template as<uint32_t>(), n, nodes_of<T, 2>(ws), M, 2 * n, theta_sq, neg,
+    bh_traverse_kernel<T, 2><<<g, kThreads, 0, s>>>(y, ws.perm.template as<uint32_t>(), n, nodes_of<T, 2>(ws), M, 2 * n, ws.params.template as<BoxParams<T>>(), theta_sq, neg,
                                                     qout, ws.zpart.template as<double>(), ws.zdone.template as<unsigned>(),
                                                     ws.zval.template as<double>());
   else
-    bh_traverse_kernel<T, 3><<<g, kThreads, 0, s>>>(y, ws.perm.template as<uint32_t>(), n, nodes_of<T, 3>(ws), M, 2 * n, theta_sq, neg,
+    bh_traverse_kernel<T, 3><<<g, kThreads, 0, s>>>(y, ws.perm.template as<uint32_t>(), n, nodes_of<T, 3>(ws), M, 2 * n, ws.params.template as<BoxParams<T>>(), theta_sq, neg,
                                                     qout, ws.zpart.template as<double>(), ws.zdone.template as<unsigned>(),
                                                     ws.zval.template as<double>());
   BHG_LAUNCH_CHECK();

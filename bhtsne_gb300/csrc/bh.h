@@ -22,66 +22,74 @@ struct alignas(16) Quad {
   T x, y, z, w;
 };
 
+// Packed level + skip word: internal nodes hold (skip << 5) | level, leaves
+// hold all ones (their skip is always index + 1 and they have no level). Five
+// bits cover the levels of D = 2 (0..31) and D = 3 (0..20); 27 bits of skip
+// bound the arena at 2^27 - 1 nodes, i.e. N < 2^26 points.
+constexpr uint32_t kLeafWord = 0xffffffffu;
+constexpr int64_t kMaxTreePoints = (1LL << 26) - 1;
+
 template <class T>
-struct RSkip {
-  T r2;
-  uint32_t skip;
+struct alignas(16) Node2 {
+  T x, y, mass;
+  typename std::conditional<sizeof(T) == 4, uint32_t, uint64_t>::type w;
 };
 
-// Node storage, depth-first preorder. D = 2: geom = {x, y, mass, r2} plus a
-// skip array. D = 3: geom = {x, y, z, mass} plus {r2, skip}. r2 < 0 marks a
-// leaf; r2 >= 0 is the half-width^2 of the node's level.
+// Node storage, depth-first preorder. D = 2: one 16-byte (f32) record
+// {x, y, mass, word}, a single load per visit. D = 3: {x, y, z, mass} plus a
+// separate word array. The squared half width of an internal node's level is
+// read from a per-launch table (BoxParams::hw2, staged in shared memory).
 template <class T, int D>
 struct TreeNodes;
 
 template <class T>
 struct TreeNodes<T, 2> {
-  Quad<T>* geom;
-  uint32_t* skip;
-  __device__ __forceinline__ void write(int64_t i, const T* c, T mass, T r2, uint32_t sk) const {
-    Quad<T> g;
+  Node2<T>* geom;
+  const T* hw2;  // shared-memory copy of BoxParams::hw2 inside the traversal
+  __device__ __forceinline__ void write(int64_t i, const T* c, T mass, int level, uint32_t sk) const {
+    Node2<T> g;
     g.x = c[0];
     g.y = c[1];
-    g.z = mass;
-    g.w = r2;
+    g.mass = mass;
+    g.w = level < 0 ? kLeafWord : ((sk << 5) | (uint32_t)level);
     geom[i] = g;
-    skip[i] = sk;
   }
   __device__ __forceinline__ void read(uint32_t i, T* c, T* mass, T* r2, uint32_t* sk) const {
-    const Quad<T> g = geom[i];
-    *sk = __ldg(skip + i);
+    const Node2<T> g = geom[i];
     c[0] = g.x;
     c[1] = g.y;
-    *mass = g.z;
-    *r2 = g.w;
+    *mass = g.mass;
+    const uint32_t w = (uint32_t)g.w;
+    const bool leaf = w == kLeafWord;
+    *r2 = leaf ? T(-1) : hw2[w & 31u];
+    *sk = leaf ? i + 1 : (w >> 5);
   }
 };
 
 template <class T>
 struct TreeNodes<T, 3> {
   Quad<T>* geom;
-  RSkip<T>* rs;
-  __device__ __forceinline__ void write(int64_t i, const T* c, T mass, T r2, uint32_t sk) const {
+  uint32_t* word;
+  const T* hw2;
+  __device__ __forceinline__ void write(int64_t i, const T* c, T mass, int level, uint32_t sk) const {
     Quad<T> g;
     g.x = c[0];
     g.y = c[1];
     g.z = c[2];
     g.w = mass;
     geom[i] = g;
-    RSkip<T> r;
-    r.r2 = r2;
-    r.skip = sk;
-    rs[i] = r;
+    word[i] = level < 0 ? kLeafWord : ((sk << 5) | (uint32_t)level);
   }
   __device__ __forceinline__ void read(uint32_t i, T* c, T* mass, T* r2, uint32_t* sk) const {
     const Quad<T> g = geom[i];
-    const RSkip<T> r = rs[i];
+    const uint32_t w = word[i];
     c[0] = g.x;
     c[1] = g.y;
     c[2] = g.z;
     *mass = g.w;
-    *r2 = r.r2;
-    *sk = r.skip;
+    const bool leaf = w == kLeafWord;
+    *r2 = leaf ? T(-1) : hw2[w & 31u];
+    *sk = leaf ? i + 1 : (w >> 5);
   }
 };
 
@@ -90,7 +98,7 @@ struct BhWorkspace {
   int64_t n = 0;
   int D = 0;
   bool zeroed = false;
-  DevBuf keys, keys_alt, perm, perm_alt, ys, pre, pre_part, mask, cnt, base, geom, aux;
+  DevBuf keys, keys_alt, perm, perm_alt, ys, pre, pre_part, mask, cnt, base, geom, word;
   DevBuf part_min, part_max, done, zdone, params, zpart, zval, sort_tmp, scan_tmp;
   void reserve(int64_t n, int D);
   const double* z() const { return static_cast<const double*>(zval.ptr); }

@@ -171,11 +171,14 @@ class TSNE:
         return self._check(self.lib.bhtsne_tsne_exact_distances(self.handle, _ptr(d)))
 
     def barnes_hut(self, theta, metric="euclidean"):
-        """barnes_hut (src/lib.rs:701-742) with the Euclidean metric."""
+        """barnes_hut (src/lib.rs:701-742) with the Euclidean metric. With
+        cached affinities (with_affinities or an earlier fit) the dataset is not
+        read, as in the reference."""
         if metric != "euclidean":
             raise L.BhtsneError(L.EINVAL, "error: other metrics enter through barnes_hut_with_neighbors.")
-        X = self._need_data()
-        return self._check(self.lib.bhtsne_tsne_barnes_hut_euclidean(self.handle, float(theta), _ptr(X), X.shape[1]))
+        X = self.data
+        return self._check(self.lib.bhtsne_tsne_barnes_hut_euclidean(
+            self.handle, float(theta), _ptr(X), 0 if X is None else X.shape[1]))
 
     def barnes_hut_with_neighbors(self, theta, neighbors):
         """barnes_hut_with_neighbors (src/lib.rs:757-772)."""
@@ -190,8 +193,8 @@ class TSNE:
         """fit_sne (src/lib.rs:835-871) with the Euclidean metric."""
         if metric != "euclidean":
             raise L.BhtsneError(L.EINVAL, "error: other metrics enter through fit_sne_with_neighbors.")
-        X = self._need_data()
-        return self._check(self.lib.bhtsne_tsne_fit_sne_euclidean(self.handle, _ptr(X), X.shape[1]))
+        X = self.data
+        return self._check(self.lib.bhtsne_tsne_fit_sne_euclidean(self.handle, _ptr(X), 0 if X is None else X.shape[1]))
 
     def fit_sne_with_neighbors(self, neighbors):
         """fit_sne_with_neighbors (src/lib.rs:884-894)."""

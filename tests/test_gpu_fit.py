@@ -1,0 +1,221 @@
+"""GPU builder behaviour against the reference's integration tests
+(src/test.rs) and against the oracle on the same inputs."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from conftest import blobs, lcg_samples
+
+pytestmark = pytest.mark.gpu
+
+KATS = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "reference_kats.json")))
+
+
+def cluster_data(k):
+    state = k["lcg_seed"]
+    vals = []
+    for c in k["centres"]:
+        for _ in range(k["n_per_cluster"] * k["dim"]):
+            state = (state * 6364136223846793005 + 1442695040888963407) & 0xFFFFFFFFFFFFFFFF
+            r = np.float32(np.float32(state >> 33) / np.float32(4294967295.0)) - np.float32(0.5)
+            vals.append(np.float32(c) + np.float32(k["noise_scale"]) * r)
+    return np.array(vals, np.float32).reshape(-1, k["dim"])
+
+
+def same_cluster_fraction(emb, labels):
+    e = emb.reshape(len(labels), -1).astype(np.float64)
+    d = ((e[:, None, :] - e[None, :, :]) ** 2).sum(-1)
+    np.fill_diagonal(d, np.inf)
+    return float(np.mean(labels == labels[d.argmin(1)]))
+
+
+def test_barnes_hut_separates_clusters(gpu):
+    k = KATS["clusters_separate_large_scale"]
+    X = cluster_data(k)
+    t = gpu.TSNE(X).perplexity(k["perplexity"]).epochs(k["epochs"])
+    t.barnes_hut(k["theta"])
+    lab = np.arange(len(X)) < k["n_per_cluster"]
+    assert same_cluster_fraction(t.embedding(), lab) > k["min_fraction"]
+
+
+def test_fit_sne_separates_clusters(gpu):
+    k = KATS["clusters_separate_large_scale"]
+    X = cluster_data(k)
+    t = gpu.TSNE(X).perplexity(k["perplexity"]).epochs(k["epochs"])
+    t.fit_sne()
+    lab = np.arange(len(X)) < k["n_per_cluster"]
+    assert same_cluster_fraction(t.embedding(), lab) > k["min_fraction"]
+
+
+@pytest.mark.parametrize("method", ["bh", "fit"])
+def test_does_not_collapse(gpu, method):
+    k = KATS["no_collapse"]
+    X = lcg_samples(k["n"], k["dim"], k["lcg_seed"])
+    t = gpu.TSNE(X).perplexity(k["perplexity"]).epochs(k["epochs"])
+    t.barnes_hut(k["theta"]) if method == "bh" else t.fit_sne()
+    e = t.embedding().reshape(-1, 2)
+    assert len({(int(round(a * 100)), int(round(b * 100))) for a, b in e}) > k["min_distinct_fraction"] * k["n"]
+
+
+def test_kl_finite_nonnegative_all_methods(gpu):
+    k = KATS["kl_finite_nonnegative"]
+    X = lcg_samples(k["n"], k["dim"], k["lcg_seed"])
+    for run in ("bh", "fit", "exact"):
+        t = gpu.TSNE(X).perplexity(k["perplexity"]).epochs(k["epochs"])
+        assert t.kl_divergence() is None
+        {"bh": lambda: t.barnes_hut(0.5), "fit": lambda: t.fit_sne(), "exact": lambda: t.exact("sqeuclidean")}[run]()
+        kl = t.kl_divergence()
+        assert kl is not None and np.isfinite(kl) and kl >= 0, run
+
+
+def test_with_neighbors_equals_metric_path(gpu, oracle):
+    k = KATS["with_neighbors_equals_metric_path"]
+    X = lcg_samples(k["n"], k["dim"], k["lcg_seed"])
+    seed = lcg_samples(k["n"], 2, k["seed_lcg"])
+    idx, dist = oracle.knn(X, int(3 * k["perplexity"]))
+    a = gpu.TSNE(X).perplexity(k["perplexity"]).epochs(k["epochs"]).initial_embedding(seed)
+    a.barnes_hut(k["theta"])
+    b = gpu.TSNE(X).perplexity(k["perplexity"]).epochs(k["epochs"]).initial_embedding(seed)
+    b.barnes_hut_with_neighbors(k["theta"], (idx, dist))
+    assert np.array_equal(a.embedding(), b.embedding())
+    c = gpu.TSNE(X).perplexity(k["perplexity"]).epochs(k["epochs"]).initial_embedding(seed)
+    c.fit_sne()
+    d = gpu.TSNE(X).perplexity(k["perplexity"]).epochs(k["epochs"]).initial_embedding(seed)
+    d.fit_sne_with_neighbors((idx, dist))
+    assert np.array_equal(c.embedding(), d.embedding())
+
+
+def test_runs_are_deterministic(gpu):
+    X, _ = blobs(600, 8, 4, 11)
+    seed = lcg_samples(600, 2, 99)
+    runs = []
+    for _ in range(2):
+        t = gpu.TSNE(X).perplexity(10).epochs(150).initial_embedding(seed)
+        t.barnes_hut(0.5)
+        runs.append(t.embedding())
+    assert np.array_equal(runs[0], runs[1])
+
+
+def test_advance_equals_longer_fit(gpu):
+    X, _ = blobs(700, 10, 5, 12)
+    seed = lcg_samples(700, 2, 5)
+    a = gpu.TSNE(X).perplexity(15).epochs(300).initial_embedding(seed)
+    a.barnes_hut(0.5)
+    b = gpu.TSNE(X).perplexity(15).epochs(120).initial_embedding(seed)
+    b.barnes_hut(0.5)
+    b.advance(180)
+    assert np.array_equal(a.embedding(), b.embedding())
+
+
+def test_epoch_callback_reports_each_epoch(gpu):
+    X = lcg_samples(60, 4, 7)
+    seen, snaps = [], []
+    t = gpu.TSNE(X).perplexity(10).epochs(100)
+    t.epoch_callback(lambda e, y: (seen.append(e), snaps.append(y)))
+    t.barnes_hut(0.5)
+    assert seen == list(range(100))
+    assert np.array_equal(snaps[-1], t.embedding())
+    seen.clear()
+    t.exact("sqeuclidean")
+    assert seen == list(range(100))
+
+
+def test_warm_start_and_seed_consumption(gpu):
+    X = lcg_samples(60, 4, 7)
+    t0 = gpu.TSNE(X).perplexity(10).epochs(300)
+    t0.barnes_hut(0.5)
+    seed = t0.embedding()
+    first = []
+    t = gpu.TSNE(X).perplexity(10).epochs(5).stop_lying_epoch(0).momentum_switch_epoch(0).initial_embedding(seed)
+    t.epoch_callback(lambda e, y: first.append(y) if e == 0 else None)
+    t.barnes_hut(0.5)
+    s = seed.reshape(-1, 2)
+    disp = np.linalg.norm(first[0].reshape(-1, 2) - s, axis=1).mean()
+    diag = np.linalg.norm(s.max(0) - s.min(0))
+    assert disp < 0.05 * diag
+    # the seed is consumed: the next fit starts from a fresh random draw
+    t.barnes_hut(0.5)
+    assert np.linalg.norm(t.embedding().reshape(-1, 2), axis=1).mean() < np.linalg.norm(s, axis=1).mean()
+
+
+def test_error_messages(gpu):
+    X = lcg_samples(80, 4, 11)
+    with pytest.raises(gpu.BhtsneError, match="theta value must be greater than 0.0"):
+        gpu.TSNE(X).perplexity(10).barnes_hut(0.0)
+    with pytest.raises(gpu.BhtsneError, match="perplexity is too large"):
+        gpu.TSNE(X[:20]).perplexity(10).barnes_hut(0.5)
+    with pytest.raises(gpu.BhtsneError, match="initial embedding has 3 values"):
+        gpu.TSNE(X).perplexity(10).epochs(1).initial_embedding([1.0, 2.0, 3.0]).barnes_hut(0.5)
+    idx = np.tile(np.arange(1, 31, dtype=np.uint64), (80, 1))
+    dist = np.ones((80, 30), np.float32)
+    idx[0, 0] = 80
+    with pytest.raises(gpu.BhtsneError, match="out of range"):
+        gpu.TSNE(80).perplexity(10).epochs(1).barnes_hut_with_neighbors(0.5, (idx, dist))
+    rows = [[gpu.Neighbor(1, 1.0)]] * 79 + [[]]
+    with pytest.raises(gpu.BhtsneError, match="same length"):
+        gpu.TSNE(80).perplexity(10).epochs(1).barnes_hut_with_neighbors(0.5, rows)
+    with pytest.raises(gpu.BhtsneError, match="rows, expected one per sample"):
+        gpu.TSNE(80).perplexity(10).epochs(1).fit_sne_with_neighbors((idx[:10], dist[:10]))
+
+
+def test_early_exaggeration_one_matches_stop_lying_zero(gpu):
+    X = lcg_samples(60, 4, 7)
+    seed = lcg_samples(60, 2, 3)
+    a = gpu.TSNE(X).perplexity(10).epochs(20).early_exaggeration(1.0).initial_embedding(seed)
+    a.exact("sqeuclidean")
+    b = gpu.TSNE(X).perplexity(10).epochs(20).stop_lying_epoch(0).initial_embedding(seed)
+    b.exact("sqeuclidean")
+    assert np.allclose(a.embedding(), b.embedding(), rtol=1e-5, atol=1e-6)
+
+
+def test_affinities_round_trip_and_cache(gpu, oracle):
+    X, _ = blobs(500, 10, 3, 21)
+    t = gpu.TSNE(X).perplexity(20).epochs(50)
+    assert t.affinities() is None
+    t.barnes_hut(0.5)
+    aff = t.affinities()
+    assert aff is not None and aff.perplexity == pytest.approx(20.0)
+    assert abs(aff.values.sum() - 1.0) < 0.05
+    # pristine form is independent of the run length (stop lying fired or not)
+    t2 = gpu.TSNE(X).perplexity(20).epochs(300)
+    t2.barnes_hut(0.5)
+    assert np.allclose(t2.affinities().values, aff.values, rtol=1e-6)
+    # matches the oracle's affinity graph entry for entry
+    o = oracle.TSNE(500).perplexity(20).epochs(0)
+    o.barnes_hut(0.5, X)
+    orows, ocols, ovals, _ = o.affinities()
+    assert np.array_equal(aff.rows, orows) and np.array_equal(aff.columns, ocols)
+    assert np.max(np.abs(aff.values - ovals) / ovals) < 1e-5
+    # injected affinities are reused in place of the neighbour search
+    seed = lcg_samples(500, 2, 4)
+    b = gpu.TSNE(X).with_affinities(aff).epochs(30).initial_embedding(seed)
+    b.barnes_hut(0.5)
+    c = gpu.TSNE(X).perplexity(20).epochs(30).initial_embedding(seed)
+    c.barnes_hut(0.5)
+    assert np.allclose(b.embedding(), c.embedding(), rtol=1e-4, atol=1e-5)
+    # a perplexity change invalidates the cache
+    d = gpu.TSNE(X).with_affinities(aff).perplexity(10).epochs(1)
+    d.barnes_hut(0.5)
+    assert d.affinities().perplexity == pytest.approx(10.0)
+
+
+def test_final_kl_within_one_percent_of_oracle(gpu, oracle):
+    """Same inputs (kNN table, seed) through the GPU and the oracle; trajectories
+    are chaotic, so the final cost is compared (reference-compatible and true KL)."""
+    X, _ = blobs(2000, 50, 10, 1001)
+    idx, dist = oracle.knn(X, 90)
+    seed = np.random.default_rng(5).normal(0, 1e-4, size=(2000, 2)).astype(np.float32)
+    for method in ("bh", "fit"):
+        g = gpu.TSNE(2000).perplexity(30).epochs(1000).initial_embedding(seed)
+        o = oracle.TSNE(2000).perplexity(30).epochs(1000).initial_embedding(seed)
+        if method == "bh":
+            g.barnes_hut_with_neighbors(0.5, (idx, dist))
+            o.barnes_hut_with_neighbors(0.5, idx.astype(np.uint64), dist)
+        else:
+            g.fit_sne_with_neighbors((idx, dist))
+            o.fit_sne_with_neighbors(idx.astype(np.uint64), dist)
+        for quirk in (True, False):
+            kg, ko = g.kl_divergence(quirk), o.kl_divergence(quirk)
+            assert abs(kg - ko) / abs(ko) < 0.01, (method, quirk, kg, ko)
