@@ -102,16 +102,20 @@ __device__ void warp_insert(V* lv, uint32_t* li, int* len_p, int cap, V v, uint3
   __syncwarp();
 }
 
-template <int C>
-struct CandSmem {
-  static constexpr int kQDimMax = C == 128 ? 256 : 128;
-};
-
+// Register-tiled distance tile: 64 queries x 128 candidates per step, 4 x 8
+// values per thread, dimensions consumed in order in chunks of 32. With
+// EXACT = false a value is |q|^2 + |c|^2 - 2 q.c (FP32 FMA, the candidate
+// pass); with EXACT = true it is the reference's distance sqrt(sum_d (q-c)^2)
+// rounded at every step (the certified fallback), and the kept list is the
+// answer. Queries are rows q0.. of X, or the rows listed in `qrows`.
+//
 // dynamic shared layout: Qs[dim][QB] | Cs[DK][CB] | S[QB][CB+1] | lv[QB][C] | li[QB][C] | len[QB] | qn[QB]
-template <int C>
-__global__ void __launch_bounds__(kThreads, 1) knn_candidates_kernel(const float* __restrict__ X, int64_t n, int dim,
-                                                                     const float* __restrict__ norms,
-                                                                     uint32_t* __restrict__ cand, float* __restrict__ thr) {
+template <int C, bool EXACT>
+__global__ void __launch_bounds__(kThreads, 1) knn_tile_kernel(const float* __restrict__ X, int64_t n, int dim,
+                                                               const float* __restrict__ norms,
+                                                               const uint32_t* __restrict__ qrows, int64_t nq, int cap,
+                                                               uint32_t* __restrict__ out_idx,
+                                                               float* __restrict__ out_val) {
   extern __shared__ __align__(16) unsigned char smem[];
   float* Qs = reinterpret_cast<float*>(smem);
   float* Cs = Qs + (size_t)dim * QB;
@@ -120,36 +124,73 @@ __global__ void __launch_bounds__(kThreads, 1) knn_candidates_kernel(const float
   uint32_t* li = reinterpret_cast<uint32_t*>(lv + QB * C);
   int* len = reinterpret_cast<int*>(li + QB * C);
   float* qn = reinterpret_cast<float*>(len + QB);
+  __shared__ int64_t qidx[QB];
 
   const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
   const int tq = tid >> 4, tc = tid & 15;
   const int64_t q0 = (int64_t)blockIdx.x * QB;
-
-  for (int e = tid; e < QB * dim; e += kThreads) {
-    const int q = e / dim, d = e % dim;
-    const int64_t qi = q0 + q;
-    Qs[d * QB + q] = qi < n ? X[qi * dim + d] : 0.f;
-  }
   if (tid < QB) {
+    const int64_t r = q0 + tid;
+    qidx[tid] = r < nq ? (qrows ? (int64_t)qrows[r] : r) : -1;
     len[tid] = 0;
-    qn[tid] = (q0 + tid < n) ? norms[q0 + tid] : 0.f;
   }
   __syncthreads();
+  for (int e = tid; e < QB * dim; e += kThreads) {
+    const int q = e / dim, d = e % dim;
+    const int64_t qi = qidx[q];
+    Qs[d * QB + q] = qi >= 0 ? X[qi * dim + d] : 0.f;
+  }
+  if (tid < QB) qn[tid] = (!EXACT && qidx[tid] >= 0) ? norms[qidx[tid]] : 0.f;
 
+  // Candidate chunk staging: thread t owns candidate c = t % CB and 4-dim
+  // groups (t / CB) * 4 + 8 g, loaded as float4 when the row allows it.
+  const bool vec4 = (dim & 3) == 0;
+  float pre[16];
+  auto load_chunk = [&](int64_t c0, int d0) {
+#pragma unroll
+    for (int g = 0; g < 4; ++g) {
+      const int c = tid % CB;
+      const int dq = (tid / CB) * 4 + 8 * g;
+      const int64_t j = c0 + c;
+      const int d = d0 + dq;
+      if (j < n && vec4 && d + 3 < dim) {
+        const float4 v = *reinterpret_cast<const float4*>(X + j * dim + d);
+        pre[4 * g + 0] = v.x;
+        pre[4 * g + 1] = v.y;
+        pre[4 * g + 2] = v.z;
+        pre[4 * g + 3] = v.w;
+      } else {
+#pragma unroll
+        for (int i = 0; i < 4; ++i) pre[4 * g + i] = (j < n && d + i < dim) ? X[j * dim + d + i] : 0.f;
+      }
+    }
+  };
+  auto store_chunk = [&]() {
+#pragma unroll
+    for (int g = 0; g < 4; ++g) {
+      const int c = tid % CB;
+      const int dq = (tid / CB) * 4 + 8 * g;
+#pragma unroll
+      for (int i = 0; i < 4; ++i) Cs[(dq + i) * CB + c] = pre[4 * g + i];
+    }
+  };
+
+  const int nchunks = (dim + DK - 1) / DK;
+  load_chunk(0, 0);
   for (int64_t c0 = 0; c0 < n; c0 += CB) {
     float acc[4][8];
 #pragma unroll
     for (int a = 0; a < 4; ++a)
 #pragma unroll
       for (int b = 0; b < 8; ++b) acc[a][b] = 0.f;
-    for (int d0 = 0; d0 < dim; d0 += DK) {
-      // load Cs[dd][c] = X[c0 + c][d0 + dd]
-      for (int e = tid; e < DK * CB; e += kThreads) {
-        const int c = e / DK, dd = e % DK;
-        const int64_t j = c0 + c;
-        Cs[dd * CB + c] = (j < n && d0 + dd < dim) ? X[j * dim + d0 + dd] : 0.f;
-      }
+    for (int ch = 0; ch < nchunks; ++ch) {
+      const int d0 = ch * DK;
       __syncthreads();
+      store_chunk();
+      __syncthreads();
+      // prefetch the next chunk (next dims, or the next candidate tile's first dims)
+      if (ch + 1 < nchunks) load_chunk(c0, d0 + DK);
+      else if (c0 + CB < n) load_chunk(c0 + CB, 0);
       const int dmax = min(DK, dim - d0);
       for (int dd = 0; dd < dmax; ++dd) {
         const float4 a4 = *reinterpret_cast<const float4*>(Qs + (d0 + dd) * QB + tq * 4);
@@ -160,9 +201,15 @@ __global__ void __launch_bounds__(kThreads, 1) knn_candidates_kernel(const float
 #pragma unroll
         for (int a = 0; a < 4; ++a)
 #pragma unroll
-          for (int b = 0; b < 8; ++b) acc[a][b] = fmaf(av[a], bv[b], acc[a][b]);
+          for (int b = 0; b < 8; ++b) {
+            if (EXACT) {
+              const float t = av[a] - bv[b];
+              acc[a][b] = __fadd_rn(acc[a][b], __fmul_rn(t, t));
+            } else {
+              acc[a][b] = fmaf(av[a], bv[b], acc[a][b]);
+            }
+          }
       }
-      __syncthreads();
     }
 #pragma unroll
     for (int a = 0; a < 4; ++a) {
@@ -170,16 +217,22 @@ __global__ void __launch_bounds__(kThreads, 1) knn_candidates_kernel(const float
 #pragma unroll
       for (int b = 0; b < 8; ++b) {
         const int c = b < 4 ? tc * 4 + b : 64 + tc * 4 + (b - 4);
-        const int64_t j = c0 + c;
-        const float cn = j < n ? norms[j] : 0.f;
-        S[q * (CB + 1) + c] = qn[q] + cn - 2.f * acc[a][b];
+        float v;
+        if (EXACT) {
+          v = sqrtf(acc[a][b]);
+        } else {
+          const int64_t j = c0 + c;
+          const float cn = j < n ? norms[j] : 0.f;
+          v = qn[q] + cn - 2.f * acc[a][b];
+        }
+        S[q * (CB + 1) + c] = v;
       }
     }
     __syncthreads();
     for (int qq = 0; qq < QB / 8; ++qq) {
       const int q = w * (QB / 8) + qq;
-      const int64_t qi = q0 + q;
-      if (qi >= n) continue;
+      const int64_t qi = qidx[q];
+      if (qi < 0) continue;
       float* qlv = lv + q * C;
       uint32_t* qli = li + q * C;
 #pragma unroll
@@ -189,26 +242,33 @@ __global__ void __launch_bounds__(kThreads, 1) knn_candidates_kernel(const float
         const float v = S[q * (CB + 1) + c];
         const int L = len[q];
         bool ok = j < n && j != qi;
-        if (ok && L == C) ok = lt_pair(v, (uint32_t)j, qlv[C - 1], qli[C - 1]);
+        if (ok && L == cap) ok = lt_pair(v, (uint32_t)j, qlv[cap - 1], qli[cap - 1]);
         unsigned mask = __ballot_sync(kFull, ok);
         while (mask) {
           const int src = __ffs(mask) - 1;
           mask &= mask - 1;
           const float vv = __shfl_sync(kFull, v, src);
           const uint32_t jj = (uint32_t)(c0 + part * 32 + src);
-          warp_insert<float>(qlv, qli, &len[q], C, vv, jj, lane);
+          warp_insert<float>(qlv, qli, &len[q], cap, vv, jj, lane);
         }
       }
     }
-    __syncthreads();
   }
+  __syncthreads();
   for (int qq = 0; qq < QB / 8; ++qq) {
     const int q = w * (QB / 8) + qq;
-    const int64_t qi = q0 + q;
-    if (qi >= n) continue;
+    const int64_t qi = qidx[q];
+    if (qi < 0) continue;
     const int L = len[q];
-    for (int t = lane; t < C; t += 32) cand[qi * C + t] = t < L ? li[q * C + t] : SENT;
-    if (lane == 0) thr[qi] = L == C ? lv[q * C + C - 1] : INFINITY;
+    if (EXACT) {
+      for (int t = lane; t < cap; t += 32) {
+        out_idx[qi * cap + t] = li[q * C + t];
+        out_val[qi * cap + t] = lv[q * C + t];
+      }
+    } else {
+      for (int t = lane; t < C; t += 32) out_idx[qi * C + t] = t < L ? li[q * C + t] : SENT;
+      if (lane == 0) out_val[qi] = L == C ? lv[q * C + C - 1] : INFINITY;
+    }
   }
 }
 
@@ -278,14 +338,20 @@ __global__ void knn_rerank_kernel(const T* __restrict__ X, int64_t n, int dim, i
     out_dist[qi * k + t] = sd[w][t];
   }
   if (lane == 0) {
+    // A point c outside the candidate list that ranked within the first k
+    // would have true |q - c|^2 <= d2k, hence |c| <= |q| + sqrt(d2k), so the
+    // FP32 error of its candidate value is at most E below; yet that value is
+    // >= th. Certified when d2k (inflated by its own rounding) + E < th.
     const float th = thr[qi];
     bool ok = true;
     if (!isinf(th)) {
       const double u = 1.0 / 16777216.0;
-      const double maxn = (double)__uint_as_float(*max_bits);
-      const double delta = (4.0 * dim + 16.0) * u * ((double)norms[qi] + maxn);
-      const double bound = ((double)th - delta) * (1.0 - (dim + 2.0) * u) - 1e-30;
-      ok = (double)sd2[w][k - 1] < bound;
+      const double g = (dim + 2.0) * u;
+      const double qn = (double)norms[qi] * (1.0 + g);
+      const double d2k = (double)sd2[w][k - 1] * (1.0 + g) * (1.0 + 16.0 * u);
+      const double r = sqrt(qn) + sqrt(d2k);
+      const double E = (4.0 * dim + 16.0) * u * (qn + r * r);
+      ok = d2k + E < (double)th;
     }
     if (!ok) fail_list[atomicAdd(fail_count, 1u)] = (uint32_t)qi;
   }
@@ -368,14 +434,14 @@ int64_t knn_euclidean(const T* X, int64_t n, int dim, int k, uint32_t* out_idx, 
   const size_t smem = ((size_t)dim * QB + DK * CB + QB * (CB + 1) + (size_t)QB * C * 2 + 2 * QB) * 4;
   const unsigned grid = (unsigned)ceil_div(n, QB);
   if (C == 128) {
-    BHG_CUDA(cudaFuncSetAttribute(knn_candidates_kernel<128>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    knn_candidates_kernel<128><<<grid, kThreads, smem, s>>>(Xf, n, dim, norms, cand, thr);
+    BHG_CUDA(cudaFuncSetAttribute(knn_tile_kernel<128, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    knn_tile_kernel<128, false><<<grid, kThreads, smem, s>>>(Xf, n, dim, norms, nullptr, n, 128, cand, thr);
     BHG_LAUNCH_CHECK();
     knn_rerank_kernel<T, 128><<<(unsigned)ceil_div(n, 4), 128, 0, s>>>(X, n, dim, k, cand, thr, norms, max_bits, out_idx,
                                                                        out_dist, fails, fail_count);
   } else {
-    BHG_CUDA(cudaFuncSetAttribute(knn_candidates_kernel<256>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    knn_candidates_kernel<256><<<grid, kThreads, smem, s>>>(Xf, n, dim, norms, cand, thr);
+    BHG_CUDA(cudaFuncSetAttribute(knn_tile_kernel<256, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    knn_tile_kernel<256, false><<<grid, kThreads, smem, s>>>(Xf, n, dim, norms, nullptr, n, 256, cand, thr);
     BHG_LAUNCH_CHECK();
     knn_rerank_kernel<T, 256><<<(unsigned)ceil_div(n, 4), 128, 0, s>>>(X, n, dim, k, cand, thr, norms, max_bits, out_idx,
                                                                        out_dist, fails, fail_count);
@@ -385,13 +451,28 @@ int64_t knn_euclidean(const T* X, int64_t n, int dim, int k, uint32_t* out_idx, 
   BHG_CUDA(cudaMemcpyAsync(&nfail, fail_count, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
   BHG_CUDA(cudaStreamSynchronize(s));
   if (nfail > 0) {
-    const size_t esmem = (size_t)4 * k * (sizeof(T) + sizeof(uint32_t));
-    if (esmem > 48 * 1024)
-      BHG_CUDA(cudaFuncSetAttribute(knn_exact_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)esmem));
-    knn_exact_kernel<T><<<(unsigned)ceil_div(nfail, 4), 128, esmem, s>>>(X, n, dim, k, fails, nullptr, nfail, out_idx,
-                                                                        out_dist);
-    BHG_LAUNCH_CHECK();
+    if constexpr (std::is_same<T, float>::value) {
+      // certified fallback: the same tiled kernel computing the reference's
+      // exact distances for the failing rows only
+      const unsigned fgrid = (unsigned)ceil_div(nfail, QB);
+      if (C == 128) {
+        BHG_CUDA(cudaFuncSetAttribute(knn_tile_kernel<128, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        knn_tile_kernel<128, true><<<fgrid, kThreads, smem, s>>>(X, n, dim, norms, fails, nfail, k, out_idx, out_dist);
+      } else {
+        BHG_CUDA(cudaFuncSetAttribute(knn_tile_kernel<256, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        knn_tile_kernel<256, true><<<fgrid, kThreads, smem, s>>>(X, n, dim, norms, fails, nfail, k, out_idx, out_dist);
+      }
+      BHG_LAUNCH_CHECK();
+    } else {
+      const size_t esmem = (size_t)4 * k * (sizeof(T) + sizeof(uint32_t));
+      if (esmem > 48 * 1024)
+        BHG_CUDA(cudaFuncSetAttribute(knn_exact_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)esmem));
+      knn_exact_kernel<T><<<(unsigned)ceil_div(nfail, 4), 128, esmem, s>>>(X, n, dim, k, fails, nullptr, nfail, out_idx,
+                                                                          out_dist);
+      BHG_LAUNCH_CHECK();
+    }
   }
+  ws.last_fallback_rows = nfail;
   return (int64_t)nfail;
 }
 

@@ -7,6 +7,7 @@ namespace bhg {
 
 struct KnnWorkspace {
   DevBuf xf, norms, cand, thr, fails, counters;
+  int64_t last_fallback_rows = 0;
   void release() {
     xf.release();
     norms.release();
