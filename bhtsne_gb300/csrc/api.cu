@@ -122,6 +122,15 @@ struct bhtsne_tsne {
   bool profile = false;
   double phase_ms[BHTSNE_PHASES] = {0, 0, 0, 0};
   int64_t phase_epochs = 0;
+  // CUDA graph of one epoch body (Barnes-Hut and exact), re-captured when the
+  // momentum changes or a new fit starts.
+  cudaGraphExec_t graph = nullptr;
+  double graph_momentum = 0;
+  int64_t graph_kernels = 0;
+  void drop_graph() {
+    if (graph) cudaGraphExecDestroy(graph);
+    graph = nullptr;
+  }
   std::string err;
   State<float>* sf = nullptr;
   State<double>* sd = nullptr;
@@ -337,10 +346,54 @@ void advance_impl(bhtsne_tsne* t, int64_t epochs) {
   auto mark = [&](int64_t k, int ph) {
     if (prof) BHG_CUDA(cudaEventRecord(ev[(size_t)k * (BHTSNE_PHASES + 1) + ph], s));
   };
+  // Graph replay of the epoch body: Barnes-Hut and exact epochs have a fixed
+  // launch sequence (the node count is read on the device), so after one
+  // eager epoch has sized every buffer the body is captured once and
+  // replayed. Off while profiling or when a callback needs per-epoch copies.
+  static const bool graphs_off = getenv("BHTSNE_NO_GRAPH") != nullptr;
+  const bool graphable = !graphs_off && !prof && !t->cb && t->loop_kind != BHTSNE_METHOD_FIT_SNE;
+  auto body = [&](T mom) {
+    if (t->loop_kind == BHTSNE_METHOD_BARNES_HUT) {
+      bh_build<T>(S.bh, D, y, n, s);
+      bh_traverse<T>(S.bh, D, y, n, (T)t->loop_theta, S.neg.template as<T>(), nullptr, s);
+      launch_attractive<T>(D, S.rows.template as<uint64_t>(), S.cols.template as<uint32_t>(), S.vals.template as<T>(), y, n,
+                           S.pos.template as<T>(), s);
+      launch_update<T>(D, y, S.pos.template as<T>(), S.neg.template as<T>(), S.uy.template as<T>(),
+                       S.gains.template as<T>(), n, S.bh.z(), T(0), lr, mom, S.us, s);
+    } else {
+      launch_exact_z<T>(D, y, n, z, S.tmp, s);
+      launch_exact_grad<T>(D, y, S.pdense.template as<T>(), n, z, S.pos.template as<T>(), s);
+      launch_update<T>(D, y, S.pos.template as<T>(), nullptr, S.uy.template as<T>(), S.gains.template as<T>(), n,
+                       nullptr, T(0), lr, mom, S.us, s);
+    }
+    launch_recenter_bbox<T>(D, y, n, S.us.mean(), true, S.bh, bits, s);
+  };
+  bool warmed = false;
   for (int64_t k = 0; k < epochs; ++k) {
     const int64_t epoch = t->cursor;
     if (epoch == 0) launch_recenter_bbox<T>(D, y, n, nullptr, false, S.bh, bits, s);
     const T mom = (T)t->momentum;
+    if (graphable && warmed) {
+      if (!t->graph || t->graph_momentum != t->momentum) {
+        t->drop_graph();
+        cudaGraph_t g;
+        const long long before = g_launches.load();
+        BHG_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed));
+        body(mom);
+        BHG_CUDA(cudaStreamEndCapture(s, &g));
+        t->graph_kernels = g_launches.load() - before;
+        g_launches.fetch_sub(t->graph_kernels);
+        BHG_CUDA(cudaGraphInstantiate(&t->graph, g, 0));
+        BHG_CUDA(cudaGraphDestroy(g));
+        t->graph_momentum = t->momentum;
+      }
+      BHG_CUDA(cudaGraphLaunch(t->graph, s));
+      g_launches.fetch_add(t->graph_kernels);
+      epoch_tail<T>(t, epoch, snap);
+      t->cursor += 1;
+      continue;
+    }
+    warmed = true;
     mark(k, 0);
     if (t->loop_kind == BHTSNE_METHOD_BARNES_HUT) {
       bh_build<T>(S.bh, D, y, n, s);
@@ -399,6 +452,7 @@ void advance_impl(bhtsne_tsne* t, int64_t epochs) {
 
 template <class T>
 void run_loop(bhtsne_tsne* t, int kind, double theta) {
+  t->drop_graph();
   t->armed = true;
   t->loop_kind = kind;
   t->loop_theta = theta;
@@ -715,6 +769,7 @@ int bhtsne_tsne_new(bhtsne_ctx* ctx, int dtype, int32_t embed_dim, int64_t n_sam
 int bhtsne_tsne_free(bhtsne_tsne* t) {
   if (!t) return BHTSNE_OK;
   cudaSetDevice(t->ctx->device);
+  t->drop_graph();
   delete t->sf;
   delete t->sd;
   delete t;

@@ -142,20 +142,14 @@ __global__ void recenter_bbox_kernel(T* __restrict__ y, int64_t n, const double*
   __syncthreads();
   if (!last) return;
   __threadfence();
+  __shared__ T shr[32];
+  T fmn[D], fmx[D];
+#pragma unroll
+  for (int a = 0; a < D; ++a) {
+    fmn[a] = block_min_parts<T>(part_min, gridDim.x, D, a, Lim<T>::max(), shr);
+    fmx[a] = block_max_parts<T>(part_max, gridDim.x, D, a, -Lim<T>::max(), shr);
+  }
   if (threadIdx.x == 0) {
-    T fmn[D], fmx[D];
-#pragma unroll
-    for (int a = 0; a < D; ++a) {
-      fmn[a] = Lim<T>::max();
-      fmx[a] = -Lim<T>::max();
-    }
-    for (unsigned b = 0; b < gridDim.x; ++b) {
-#pragma unroll
-      for (int a = 0; a < D; ++a) {
-        fmn[a] = fmin(fmn[a], ((volatile T*)part_min)[b * D + a]);
-        fmx[a] = fmax(fmx[a], ((volatile T*)part_max)[b * D + a]);
-      }
-    }
     const T scale = (T)(double)(1ULL << bits);
     T max_extent = T(0);
 #pragma unroll
@@ -507,12 +501,13 @@ __global__ void __launch_bounds__(kThreads) bh_traverse_kernel(const T* __restri
     last = atomicAdd(done, 1u) == gridDim.x - 1;
   }
   __syncthreads();
-  if (last && threadIdx.x == 0) {
+  if (last) {
     __threadfence();
-    double z = 0.0;
-    for (unsigned b = 0; b < gridDim.x; ++b) z += ((volatile double*)zpart)[b];
-    *z_out = z;
-    *done = 0;
+    const double z = block_sum_parts(zpart, gridDim.x, 1, 0, sh);
+    if (threadIdx.x == 0) {
+      *z_out = z;
+      *done = 0;
+    }
   }
 }
 

@@ -117,6 +117,48 @@ __device__ __forceinline__ double block_sum(double v, double* sh) {
   return r;
 }
 
+// Block-wide reduction of `count` per-block partials part[b * stride + off],
+// all threads of the calling block participating (call from every thread of
+// a block-uniform branch). The order is fixed, so results are deterministic.
+__device__ __forceinline__ double block_sum_parts(const double* part, unsigned count, unsigned stride, unsigned off,
+                                                  double* sh) {
+  double s = 0.0;
+  for (unsigned b = threadIdx.x; b < count; b += blockDim.x) s += ((const volatile double*)part)[b * stride + off];
+  return block_sum(s, sh);
+}
+
+template <class V>
+__device__ __forceinline__ V block_min_parts(const V* part, unsigned count, unsigned stride, unsigned off, V init,
+                                             V* sh) {
+  V s = init;
+  for (unsigned b = threadIdx.x; b < count; b += blockDim.x) s = fmin(s, ((const volatile V*)part)[b * stride + off]);
+  s = warp_min(s);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) sh[w] = s;
+  __syncthreads();
+  V r = init;
+  if (threadIdx.x == 0)
+    for (int q = 0; q < (int)((blockDim.x + 31) >> 5); ++q) r = fmin(r, sh[q]);
+  return r;
+}
+
+template <class V>
+__device__ __forceinline__ V block_max_parts(const V* part, unsigned count, unsigned stride, unsigned off, V init,
+                                             V* sh) {
+  V s = init;
+  for (unsigned b = threadIdx.x; b < count; b += blockDim.x) s = fmax(s, ((const volatile V*)part)[b * stride + off]);
+  s = warp_max(s);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) sh[w] = s;
+  __syncthreads();
+  V r = init;
+  if (threadIdx.x == 0)
+    for (int q = 0; q < (int)((blockDim.x + 31) >> 5); ++q) r = fmax(r, sh[q]);
+  return r;
+}
+
 // Rust `signum`: +1 for +0.0 and positives, -1 for -0.0 and negatives, NaN for NaN.
 template <class T>
 __device__ __forceinline__ T signum(T x) {

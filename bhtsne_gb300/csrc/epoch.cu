@@ -24,6 +24,10 @@ template <class T, int D>
 __global__ void __launch_bounds__(256) attractive_kernel(const uint64_t* __restrict__ rows, const uint32_t* __restrict__ cols,
                                                          const T* __restrict__ vals, const T* __restrict__ y, int64_t n,
                                                          T* __restrict__ pos) {
+  // One warp per row; each lane keeps up to kU entries in flight (their
+  // column, value and gathered y loaded before any arithmetic), so a warp has
+  // kU x 32 independent loads outstanding.
+  constexpr int kU = 4;
   const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (row >= n) return;
@@ -34,19 +38,33 @@ __global__ void __launch_bounds__(256) attractive_kernel(const uint64_t* __restr
     acc[a] = T(0);
   }
   const int64_t e0 = (int64_t)rows[row], e1 = (int64_t)rows[row + 1];
-  for (int64_t e = e0 + lane; e < e1; e += 32) {
-    const int64_t j = cols[e];
-    const T p = vals[e];
-    T disp[D];
-    T dist = T(0);
+  for (int64_t base = e0; base < e1; base += 32 * kU) {
+    uint32_t j[kU];
+    T p[kU];
+    T yj[kU][D];
 #pragma unroll
-    for (int a = 0; a < D; ++a) {
-      disp[a] = yi[a] - y[j * D + a];
-      dist += disp[a] * disp[a];
+    for (int u = 0; u < kU; ++u) {
+      const int64_t e = base + lane + 32 * u;
+      j[u] = e < e1 ? __ldg(cols + e) : (uint32_t)row;
+      p[u] = e < e1 ? __ldg(vals + e) : T(0);
     }
-    const T factor = p / (dist + T(1));
 #pragma unroll
-    for (int a = 0; a < D; ++a) acc[a] += factor * disp[a];
+    for (int u = 0; u < kU; ++u)
+#pragma unroll
+      for (int a = 0; a < D; ++a) yj[u][a] = y[(int64_t)j[u] * D + a];
+#pragma unroll
+    for (int u = 0; u < kU; ++u) {
+      T disp[D];
+      T dist = T(0);
+#pragma unroll
+      for (int a = 0; a < D; ++a) {
+        disp[a] = yi[a] - yj[u][a];
+        dist += disp[a] * disp[a];
+      }
+      const T factor = p[u] / (dist + T(1));
+#pragma unroll
+      for (int a = 0; a < D; ++a) acc[a] += factor * disp[a];
+    }
   }
 #pragma unroll
   for (int a = 0; a < D; ++a) acc[a] = warp_sum(acc[a]);
@@ -107,15 +125,15 @@ __global__ void __launch_bounds__(256) update_kernel(T* __restrict__ y, const T*
     last = atomicAdd(done, 1u) == gridDim.x - 1;
   }
   __syncthreads();
-  if (last && threadIdx.x == 0) {
+  if (last) {
     __threadfence();
+    __shared__ double shr[32];
 #pragma unroll
     for (int a = 0; a < D; ++a) {
-      double t = 0.0;
-      for (unsigned b = 0; b < gridDim.x; ++b) t += ((volatile double*)part)[b * D + a];
-      mean_sum[a] = t;
+      const double t = block_sum_parts(part, gridDim.x, D, a, shr);
+      if (threadIdx.x == 0) mean_sum[a] = t;
     }
-    *done = 0;
+    if (threadIdx.x == 0) *done = 0;
   }
 }
 

@@ -27,8 +27,11 @@
 //    spectrum stays in transposed layout, which is harmless because the
 //    kernel spectrum is symmetric in its two axes. Rows that are known to be
 //    zero (charges) or unused (potentials) are skipped.
-//  * The spread scatters with atomics; the gather re-derives each point's
-//    boxes and weights instead of storing them.
+//  * The spread scatters with 64-bit integer atomics on a fixed-point grid
+//    (units of 2^-fix_shift, chosen so no partial sum can overflow), so the
+//    accumulated charges do not depend on the order of the atomics and the fit
+//    is reproducible run to run like the reference's sequential spread; the
+//    gather re-derives each point's boxes and weights instead of storing them.
 #include "fitsne.h"
 
 #include <cmath>
@@ -88,7 +91,7 @@ struct Lagrange3 {
 };
 
 template <class T, int D>
-__global__ void fit_params_kernel(const BoxParams<T>* __restrict__ box, FitParams<T>* __restrict__ out) {
+__global__ void fit_params_kernel(const BoxParams<T>* __restrict__ box, int64_t n_points, FitParams<T>* __restrict__ out) {
   if (threadIdx.x != 0) return;
   T lo = box->mn[0], hi = box->mx[0];
 #pragma unroll
@@ -109,6 +112,12 @@ __global__ void fit_params_kernel(const BoxParams<T>* __restrict__ box, FitParam
   int ex = 0;
   frexp(m, &ex);
   out->scale = ldexp(T(1), ex);
+  // |charge| <= 2 scale and sum_combos |w| <= 3.5^D, so every partial sum is
+  // below 3.5^D * 2 scale * n; keep it under 2^62.
+  const double bound = pow(3.5, (double)D) * 2.0 * (double)out->scale * (double)(n_points > 0 ? n_points : 1);
+  int eb = 0;
+  frexp(bound, &eb);
+  out->fix_shift = 62 - eb;
   out->lo = lo;
   out->extent = extent;
   out->box_width = box_width;
@@ -134,14 +143,19 @@ __device__ __forceinline__ void locate(T v, const FitParams<T>& p, const Lagrang
   lb.weights(local, w);
 }
 
+__device__ __forceinline__ void fix_add(long long* a, double v, double up) {
+  atomicAdd(reinterpret_cast<unsigned long long*>(a), (unsigned long long)__double2ll_rn(v * up));
+}
+
 template <class T, int D>
 __global__ void spread_kernel(const T* __restrict__ y, int64_t n, const FitParams<T>* __restrict__ prm,
-                              typename Cx<T>::type* __restrict__ g0, typename Cx<T>::type* __restrict__ g1) {
+                              long long* __restrict__ acc) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const FitParams<T> p = *prm;
   const Lagrange3<T> lb;
   const int L = p.L;
+  const double up = ldexp(1.0, p.fix_shift);
   int box[D];
   T w[D][3];
   T yv[D];
@@ -166,18 +180,33 @@ __global__ void spread_kernel(const T* __restrict__ y, int64_t n, const FitParam
       flat = flat * L + (box[a] * 3 + k);
       wt = wt * w[a][k];
     }
-    T* c0 = reinterpret_cast<T*>(g0 + flat);
-    T* c1 = reinterpret_cast<T*>(g1 + flat);
+    long long* cell = acc + 4 * flat;
+    fix_add(cell + 0, (double)(wt * p.scale), up);
+    fix_add(cell + 1, (double)(wt * yv[0]), up);
     if (D == 2) {
-      atomicAdd(c0, wt * p.scale);
-      atomicAdd(c0 + 1, wt * yv[0]);
-      atomicAdd(c1, wt * yv[D - 1]);
-      atomicAdd(c1 + 1, wt * (sq / p.scale));
+      fix_add(cell + 2, (double)(wt * yv[D - 1]), up);
+      fix_add(cell + 3, (double)(wt * (sq / p.scale)), up);
     } else {
-      atomicAdd(c0, wt * p.scale);
-      atomicAdd(c0 + 1, wt * yv[0]);
-      atomicAdd(c1, wt * (sq / p.scale));
+      fix_add(cell + 2, (double)(wt * (sq / p.scale)), up);
     }
+  }
+}
+
+// Fixed-point charges -> the two packed complex grids (rows < charge_rows,
+// all L columns; zero where nothing was spread).
+template <class T>
+__global__ void unfix_kernel(const long long* __restrict__ acc, int64_t count, const FitParams<T>* __restrict__ prm,
+                             typename Cx<T>::type* __restrict__ g0, typename Cx<T>::type* __restrict__ g1) {
+  const double down = ldexp(1.0, -prm->fix_shift);
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < count; e += (int64_t)gridDim.x * blockDim.x) {
+    const long long* c = acc + 4 * e;
+    typename Cx<T>::type a, b;
+    a.x = (T)((double)c[0] * down);
+    a.y = (T)((double)c[1] * down);
+    b.x = (T)((double)c[2] * down);
+    b.y = (T)((double)c[3] * down);
+    g0[e] = a;
+    g1[e] = b;
   }
 }
 
@@ -351,12 +380,13 @@ __global__ void gather_kernel(const T* __restrict__ y, int64_t n, const FitParam
     last = atomicAdd(done, 1u) == gridDim.x - 1;
   }
   __syncthreads();
-  if (last && threadIdx.x == 0) {
+  if (last) {
     __threadfence();
-    double z = 0.0;
-    for (unsigned b = 0; b < gridDim.x; ++b) z += ((volatile double*)zpart)[b];
-    *z_out = z - (double)n;
-    *done = 0;
+    const double z = block_sum_parts(zpart, gridDim.x, 1, 0, sh);
+    if (threadIdx.x == 0) {
+      *z_out = z - (double)n;
+      *done = 0;
+    }
   }
 }
 
@@ -414,8 +444,8 @@ FitGrid fit_repulsion(FitWorkspace<T>& ws, int D, const T* y, int64_t n, const B
   typedef typename Cx<T>::type T2;
   ws.params.ensure(sizeof(FitParams<T>));
   FitParams<T>* dp = ws.params.template as<FitParams<T>>();
-  if (D == 1) fit_params_kernel<T, 1><<<1, 32, 0, s>>>(box, dp);
-  else fit_params_kernel<T, 2><<<1, 32, 0, s>>>(box, dp);
+  if (D == 1) fit_params_kernel<T, 1><<<1, 32, 0, s>>>(box, n, dp);
+  else fit_params_kernel<T, 2><<<1, 32, 0, s>>>(box, n, dp);
   BHG_LAUNCH_CHECK();
   FitParams<T> hp;
   BHG_CUDA(cudaMemcpyAsync(&hp, dp, sizeof(hp), cudaMemcpyDeviceToHost, s));
@@ -447,13 +477,17 @@ FitGrid fit_repulsion(FitWorkspace<T>& ws, int D, const T* y, int64_t n, const B
 
   // charges: zero the rows that receive them, spread
   const int64_t charge_rows = D == 1 ? 1 : nodes;
-  BHG_CUDA(cudaMemsetAsync(g0, 0, (size_t)charge_rows * (D == 1 ? L : L) * sizeof(T2), s));
-  BHG_CUDA(cudaMemsetAsync(g1, 0, (size_t)charge_rows * (D == 1 ? L : L) * sizeof(T2), s));
+  const int64_t charge_cells = charge_rows * L;
+  long long* acc = static_cast<long long*>(ws.acc.ensure((size_t)charge_cells * 4 * sizeof(long long)));
+  BHG_CUDA(cudaMemsetAsync(acc, 0, (size_t)charge_cells * 4 * sizeof(long long), s));
   if (n > 0) {
-    if (D == 1) spread_kernel<T, 1><<<(unsigned)ceil_div(n, 256), 256, 0, s>>>(y, n, dp, g0, g1);
-    else spread_kernel<T, 2><<<(unsigned)ceil_div(n, 256), 256, 0, s>>>(y, n, dp, g0, g1);
+    if (D == 1) spread_kernel<T, 1><<<(unsigned)ceil_div(n, 256), 256, 0, s>>>(y, n, dp, acc);
+    else spread_kernel<T, 2><<<(unsigned)ceil_div(n, 256), 256, 0, s>>>(y, n, dp, acc);
     BHG_LAUNCH_CHECK();
   }
+  unfix_kernel<T><<<(unsigned)std::min<int64_t>(ceil_div(charge_cells, 256), 4 * 152), 256, 0, s>>>(acc, charge_cells, dp,
+                                                                                                  g0, g1);
+  BHG_LAUNCH_CHECK();
 
   T2 *r0, *r1;
   if (D == 1) {

@@ -10,6 +10,7 @@ struct FitParams {
   T lo, extent, box_width, inv_box_width, spacing;
   T scale;  // power of two >= max |y|: balances the magnitudes of packed terms
   int boxes, nodes, L;
+  int fix_shift;  // charges are accumulated as integers in units of 2^-fix_shift
 };
 
 struct FitGrid {
@@ -20,7 +21,7 @@ struct FitGrid {
 template <class T>
 struct FitWorkspace {
   typedef typename std::conditional<sizeof(T) == 4, float2, double2>::type T2;
-  DevBuf params, g0, g1, h0, h1, khat, tw, zpart, done;
+  DevBuf params, g0, g1, h0, h1, khat, tw, zpart, done, acc;
   int tw_len = 0;
   bool done_zeroed = false;
   const T2* twiddles(int L);

@@ -219,3 +219,28 @@ def test_final_kl_within_one_percent_of_oracle(gpu, oracle):
         for quirk in (True, False):
             kg, ko = g.kl_divergence(quirk), o.kl_divergence(quirk)
             assert abs(kg - ko) / abs(ko) < 0.01, (method, quirk, kg, ko)
+
+
+@pytest.mark.parametrize("method", ["bh", "exact"])
+def test_graph_replay_equals_eager_epochs(gpu, method):
+    """Epoch bodies replayed from a captured CUDA graph give bit-identical
+    results to eagerly launched epochs (profiling forces eager launches)."""
+    X, _ = blobs(800, 12, 4, 31)
+    seed = lcg_samples(800, 2, 8)
+    out = []
+    for prof in (False, True):
+        t = gpu.TSNE(X).perplexity(20).epochs(300).initial_embedding(seed).profile(prof)
+        t.barnes_hut(0.5) if method == "bh" else t.exact("sqeuclidean")
+        out.append(t.embedding())
+    assert np.array_equal(out[0], out[1])
+
+
+def test_fit_sne_is_deterministic(gpu):
+    X, _ = blobs(900, 10, 4, 41)
+    seed = lcg_samples(900, 2, 9)
+    runs = []
+    for _ in range(2):
+        t = gpu.TSNE(X).perplexity(20).epochs(200).initial_embedding(seed)
+        t.fit_sne()
+        runs.append(t.embedding())
+    assert np.array_equal(runs[0], runs[1])
