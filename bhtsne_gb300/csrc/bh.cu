@@ -225,17 +225,50 @@ __global__ void prefix_reduce_kernel(const T* __restrict__ y, const uint32_t* __
   }
 }
 
+// Exclusive scan of the per-tile partials (one block, chunks of blockDim
+// carried in order; deterministic).
 template <int D>
 __global__ void prefix_partials_kernel(double* __restrict__ part, int64_t nparts) {
-  if (threadIdx.x < D) {
-    double run = 0.0;
-    for (int64_t b = 0; b < nparts; ++b) {
-      const double v = part[b * D + threadIdx.x];
-      part[b * D + threadIdx.x] = run;
-      run += v;
+  __shared__ double wsum[D][32];
+  __shared__ double carry[D], ctot[D];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (threadIdx.x < D) carry[threadIdx.x] = 0.0;
+  __syncthreads();
+  for (int64_t c0 = 0; c0 < nparts; c0 += blockDim.x) {
+    const int64_t b = c0 + threadIdx.x;
+    double v[D], x[D];
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+      v[a] = b < nparts ? part[b * D + a] : 0.0;
+      x[a] = v[a];
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const double y = __shfl_up_sync(kFull, x[a], o);
+        if (lane >= o) x[a] += y;
+      }
+      if (lane == 31) wsum[a][w] = x[a];
     }
-    part[nparts * D + threadIdx.x] = run;
+    __syncthreads();
+    if (threadIdx.x < D) {
+      double run = 0.0;
+      const int nw = blockDim.x >> 5;
+      for (int q = 0; q < nw; ++q) {
+        const double t = wsum[threadIdx.x][q];
+        wsum[threadIdx.x][q] = run;
+        run += t;
+      }
+      ctot[threadIdx.x] = run;
+    }
+    __syncthreads();
+    if (b < nparts) {
+#pragma unroll
+      for (int a = 0; a < D; ++a) part[b * D + a] = carry[a] + wsum[a][w] + (x[a] - v[a]);
+    }
+    __syncthreads();
+    if (threadIdx.x < D) carry[threadIdx.x] += ctot[threadIdx.x];
+    __syncthreads();
   }
+  if (threadIdx.x < D) part[nparts * D + threadIdx.x] = carry[threadIdx.x];
 }
 
 // Writes the Z-ordered points (T) and their exclusive FP64 prefix sums S[0..n].
@@ -597,7 +630,7 @@ static void bh_build_impl(BhWorkspace<T>& ws, const T* y, int64_t n, cudaStream_
   prefix_reduce_kernel<T, D><<<(unsigned)np, kPsThreads, 0, s>>>(y, ws.perm.template as<uint32_t>(), n,
                                                                   ws.pre_part.template as<double>());
   BHG_LAUNCH_CHECK();
-  prefix_partials_kernel<D><<<1, 32, 0, s>>>(ws.pre_part.template as<double>(), np);
+  prefix_partials_kernel<D><<<1, 1024, 0, s>>>(ws.pre_part.template as<double>(), np);
   BHG_LAUNCH_CHECK();
   prefix_apply_kernel<T, D><<<(unsigned)np, kPsThreads, 0, s>>>(y, ws.perm.template as<uint32_t>(), n,
                                                                  ws.pre_part.template as<double>(), np,
