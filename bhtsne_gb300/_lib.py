@@ -60,6 +60,7 @@ SIGNATURES = {
     "bhtsne_gradient": (C.c_int, [_vp, C.c_int, _i32, _i32, _vp, _i64, _u64p, _u32p, _vp, _i64, _dbl, _vp, _vp,
                                   _dblp]),
     "bhtsne_update": (C.c_int, [_vp, C.c_int, _i32, _vp, _vp, _vp, _vp, _vp, _i64, _dbl, _dbl, _dbl]),
+    "bhtsne_bh_repulsion_noalloc": (C.c_int, [_vp, _i64, _dbl, _vp, _vp, _vp]),
 }
 
 _lock = threading.Lock()

@@ -166,6 +166,20 @@ int bhtsne_symmetrize(bhtsne_ctx* ctx, int dtype, const uint32_t* columns, const
 int bhtsne_gradient(bhtsne_ctx* ctx, int dtype, int32_t method, int32_t embed_dim, const void* y, int64_t n,
                     const uint64_t* rows, const uint32_t* columns, const void* values, int64_t nnz, double theta,
                     void* pos, void* neg, double* z);
+/* No counterpart in the reference. Barnes-Hut repulsion at a fixed embedding
+ * for callers that cannot allocate device memory: code recording into a CUDA
+ * stream capture (cudaMalloc may not run while a capture is open), hosts that
+ * give the library a fixed device budget from their own pool, and loops where
+ * an allocation could synchronise the device. y (n x 2), neg (n x 2) and z (one
+ * double) are DEVICE pointers owned by the caller; `stream` is a cudaStream_t
+ * (NULL for the default stream). The result equals the Barnes-Hut step of
+ * bhtsne_gradient. f32 and D = 2 only, 2 <= n <= 32768 points; anything else
+ * returns BHTSNE_EINVAL. Scratch is one fixed ~3.4 MB device array per GPU,
+ * kept until the process exits and shared by all calls: calls that overlap on
+ * the GPU race, so serialise them. The first call on a device looks up the
+ * array's address for that device; make it before any stream capture. */
+int bhtsne_bh_repulsion_noalloc(const float* y, int64_t n, double theta, float* neg, double* z, void* stream);
+
 /* gradient_descent_step + zero_mean (src/tsne/mod.rs:470-516, :534-568) on
  * host arrays (n x D), in place. */
 int bhtsne_update(bhtsne_ctx* ctx, int dtype, int32_t embed_dim, void* y, const void* pos, const void* neg, void* uy,
