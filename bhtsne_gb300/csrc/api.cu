@@ -53,7 +53,15 @@ struct State {
   DevBuf pdense;
   // optimisation state
   DevBuf y, uy, gains, pos, neg, zbuf, klbuf, tmp, tmp2;
-  DevBuf kidx, kdist, kp, xin;
+  DevBuf kidx, kdist, kp, xin, yext;
+  Renumbering rn;  // locality layout of y/uy/gains (see launch_renumber)
+  // y in the caller's point order (a copy when the layout is renumbered).
+  const T* y_external(cudaStream_t s) {
+    if (!rn.active) return y.template as<T>();
+    T* out = static_cast<T*>(yext.ensure((size_t)n * D * sizeof(T)));
+    launch_unpermute<T>(D, y.template as<T>(), rn.ext.template as<uint32_t>(), n, out, s);
+    return out;
+  }
   BhWorkspace<T> bh;
   FitWorkspace<T> fit;
   UpdateScratch us;
@@ -307,7 +315,7 @@ void epoch_tail(bhtsne_tsne* t, int64_t epoch, std::vector<T>& snap) {
   if (epoch == t->momentum_switch_epoch) t->momentum = t->final_momentum;
   if (t->cb) {
     snap.resize(t->n * t->D);
-    BHG_CUDA(cudaMemcpyAsync(snap.data(), S.y.ptr, snap.size() * sizeof(T), cudaMemcpyDeviceToHost, s));
+    BHG_CUDA(cudaMemcpyAsync(snap.data(), S.y_external(s), snap.size() * sizeof(T), cudaMemcpyDeviceToHost, s));
     BHG_CUDA(cudaStreamSynchronize(s));
     t->cb(epoch, snap.data(), t->user);
   }
@@ -352,12 +360,40 @@ void advance_impl(bhtsne_tsne* t, int64_t epochs) {
   // replayed. Off while profiling or when a callback needs per-epoch copies.
   static const bool graphs_off = getenv("BHTSNE_NO_GRAPH") != nullptr;
   const bool graphable = !graphs_off && !prof && !t->cb && t->loop_kind != BHTSNE_METHOD_FIT_SNE;
+  // Locality renumbering: every kRenumberEvery epochs the sparse methods re-lay
+  // out y / uy / gains in the Morton order of the current embedding so that a
+  // row's neighbour gathers in the attractive pass stay close in memory.
+  const char* rev = getenv("BHTSNE_RENUMBER_EVERY");
+  const int64_t renumber_every = rev ? atoll(rev) : 50;
+  const bool sparse = t->loop_kind != BHTSNE_METHOD_EXACT;
+  auto attractive = [&]() {
+    launch_attractive<T>(D, S.rows.template as<uint64_t>(),
+                         S.rn.active ? S.rn.cols.template as<uint32_t>() : S.cols.template as<uint32_t>(),
+                         S.vals.template as<T>(), y, n, S.pos.template as<T>(), s,
+                         S.rn.active ? S.rn.ext.template as<uint32_t>() : nullptr);
+  };
+  auto maybe_renumber = [&](int64_t epoch) {
+    if (!sparse || renumber_every <= 0 || epoch == 0 || epoch % renumber_every != 0) return;
+    if (D < 2 || D > 3) return;
+    // the Morton order of the current y (the Barnes-Hut build computes it every
+    // epoch; the FIt-SNE loop builds it here)
+    if (t->loop_kind != BHTSNE_METHOD_BARNES_HUT) {
+      launch_recenter_bbox<T>(D, y, n, nullptr, false, S.bh, bh_bits<T>(D), s);
+      bh_build<T>(S.bh, D, y, n, s);
+    }
+    const bool was_active = S.rn.active;
+    launch_renumber<T>(D, S.bh.perm.template as<uint32_t>(), n, S.rn, y, S.uy.template as<T>(), S.gains.template as<T>(),
+                       S.pos.template as<T>(), S.neg.template as<T>(), static_cast<T*>(S.yext.ensure((size_t)n * D * sizeof(T))),
+                       S.cols.template as<uint32_t>(), S.nnz, s);
+    if (t->loop_kind != BHTSNE_METHOD_BARNES_HUT)
+      launch_recenter_bbox<T>(D, y, n, nullptr, false, S.bh, bits, s);
+    if (!was_active) t->drop_graph();  // the attractive pass now reads the slot arrays
+  };
   auto body = [&](T mom) {
     if (t->loop_kind == BHTSNE_METHOD_BARNES_HUT) {
       bh_build<T>(S.bh, D, y, n, s);
       bh_traverse<T>(S.bh, D, y, n, (T)t->loop_theta, S.neg.template as<T>(), nullptr, s);
-      launch_attractive<T>(D, S.rows.template as<uint64_t>(), S.cols.template as<uint32_t>(), S.vals.template as<T>(), y, n,
-                           S.pos.template as<T>(), s);
+      attractive();
       launch_update<T>(D, y, S.pos.template as<T>(), S.neg.template as<T>(), S.uy.template as<T>(),
                        S.gains.template as<T>(), n, S.bh.z(), T(0), lr, mom, S.us, s);
     } else {
@@ -372,6 +408,7 @@ void advance_impl(bhtsne_tsne* t, int64_t epochs) {
   for (int64_t k = 0; k < epochs; ++k) {
     const int64_t epoch = t->cursor;
     if (epoch == 0) launch_recenter_bbox<T>(D, y, n, nullptr, false, S.bh, bits, s);
+    maybe_renumber(epoch);
     const T mom = (T)t->momentum;
     if (graphable && warmed) {
       if (!t->graph || t->graph_momentum != t->momentum) {
@@ -400,8 +437,7 @@ void advance_impl(bhtsne_tsne* t, int64_t epochs) {
       mark(k, 1);
       bh_traverse<T>(S.bh, D, y, n, (T)t->loop_theta, S.neg.template as<T>(), nullptr, s);
       mark(k, 2);
-      launch_attractive<T>(D, S.rows.template as<uint64_t>(), S.cols.template as<uint32_t>(), S.vals.template as<T>(), y, n,
-                           S.pos.template as<T>(), s);
+      attractive();
       mark(k, 3);
       launch_update<T>(D, y, S.pos.template as<T>(), S.neg.template as<T>(), S.uy.template as<T>(),
                        S.gains.template as<T>(), n, S.bh.z(), T(0), lr, mom, S.us, s);
@@ -409,8 +445,7 @@ void advance_impl(bhtsne_tsne* t, int64_t epochs) {
       mark(k, 1);
       fit_repulsion<T>(S.fit, D, y, n, S.bh.params.template as<BoxParams<T>>(), S.neg.template as<T>(), z, s);
       mark(k, 2);
-      launch_attractive<T>(D, S.rows.template as<uint64_t>(), S.cols.template as<uint32_t>(), S.vals.template as<T>(), y, n,
-                           S.pos.template as<T>(), s);
+      attractive();
       mark(k, 3);
       launch_update<T>(D, y, S.pos.template as<T>(), S.neg.template as<T>(), S.uy.template as<T>(),
                        S.gains.template as<T>(), n, z, T(0), lr, mom, S.us, s);
@@ -453,6 +488,7 @@ void advance_impl(bhtsne_tsne* t, int64_t epochs) {
 template <class T>
 void run_loop(bhtsne_tsne* t, int kind, double theta) {
   t->drop_graph();
+  st<T>(t).rn.active = false;  // the fit starts from y in the caller's order
   t->armed = true;
   t->loop_kind = kind;
   t->loop_theta = theta;
@@ -646,7 +682,7 @@ bool kl(bhtsne_tsne* t, bool quirk, double* out) {
   cudaStream_t s = t->ctx->stream;
   const int64_t n = t->n;
   const int D = t->D;
-  T* y = S.y.template as<T>();
+  T* y = const_cast<T*>(S.y_external(s));
   double* z = S.klbuf.template as<double>();
   double* res = z + 1;
   if (t->fit == BHTSNE_METHOD_EXACT) {
@@ -885,7 +921,7 @@ int bhtsne_tsne_embedding(bhtsne_tsne* t, void* out) {
         // The reference returns an empty vector before a fit.
         return;
       }
-      BHG_CUDA(cudaMemcpyAsync(out, S.y.ptr, bytes, cudaMemcpyDeviceToHost, t->ctx->stream));
+      BHG_CUDA(cudaMemcpyAsync(out, S.y_external(t->ctx->stream), bytes, cudaMemcpyDeviceToHost, t->ctx->stream));
       BHG_CUDA(cudaStreamSynchronize(t->ctx->stream));
     });
   });

@@ -23,18 +23,21 @@ namespace {
 template <class T, int D>
 __global__ void __launch_bounds__(256) attractive_kernel(const uint64_t* __restrict__ rows, const uint32_t* __restrict__ cols,
                                                          const T* __restrict__ vals, const T* __restrict__ y, int64_t n,
-                                                         T* __restrict__ pos) {
-  // One warp per row; each lane keeps up to kU entries in flight (their
-  // column, value and gathered y loaded before any arithmetic), so a warp has
-  // kU x 32 independent loads outstanding.
+                                                         const uint32_t* __restrict__ row_of_slot, T* __restrict__ pos) {
+  // One warp per embedding slot; each lane keeps up to kU entries in flight
+  // (their column, value and gathered y loaded before any arithmetic), so a
+  // warp has kU x 32 independent loads outstanding. With a renumbered layout
+  // slot s holds the point of CSR row row_of_slot[s] and `cols` holds slots,
+  // so a row's gathers stay near s and neighbouring warps share lines.
   constexpr int kU = 4;
-  const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t slot = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
-  if (row >= n) return;
+  if (slot >= n) return;
+  const int64_t row = row_of_slot ? (int64_t)row_of_slot[slot] : slot;
   T yi[D], acc[D];
 #pragma unroll
   for (int a = 0; a < D; ++a) {
-    yi[a] = y[row * D + a];
+    yi[a] = y[slot * D + a];
     acc[a] = T(0);
   }
   const int64_t e0 = (int64_t)rows[row], e1 = (int64_t)rows[row + 1];
@@ -45,7 +48,7 @@ __global__ void __launch_bounds__(256) attractive_kernel(const uint64_t* __restr
 #pragma unroll
     for (int u = 0; u < kU; ++u) {
       const int64_t e = base + lane + 32 * u;
-      j[u] = e < e1 ? __ldg(cols + e) : (uint32_t)row;
+      j[u] = e < e1 ? __ldg(cols + e) : (uint32_t)slot;
       p[u] = e < e1 ? __ldg(vals + e) : T(0);
     }
 #pragma unroll
@@ -70,8 +73,59 @@ __global__ void __launch_bounds__(256) attractive_kernel(const uint64_t* __restr
   for (int a = 0; a < D; ++a) acc[a] = warp_sum(acc[a]);
   if (lane == 0) {
 #pragma unroll
-    for (int a = 0; a < D; ++a) pos[row * D + a] = acc[a];
+    for (int a = 0; a < D; ++a) pos[slot * D + a] = acc[a];
   }
+}
+
+// ---------------------------------------------------------------------------
+// Renumbering of the embedding layout (see launch_renumber).
+// ---------------------------------------------------------------------------
+template <class T, int D>
+__global__ void renumber_gather_kernel(const uint32_t* __restrict__ order, const uint32_t* __restrict__ ext_old,
+                                       int64_t n, const T* __restrict__ y, const T* __restrict__ uy,
+                                       const T* __restrict__ gains, T* __restrict__ y2, T* __restrict__ uy2,
+                                       T* __restrict__ g2, uint32_t* __restrict__ ext_new) {
+  const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  const int64_t o = order[s];
+  ext_new[s] = ext_old ? ext_old[o] : (uint32_t)o;
+#pragma unroll
+  for (int a = 0; a < D; ++a) {
+    y2[s * D + a] = y[o * D + a];
+    uy2[s * D + a] = uy[o * D + a];
+    g2[s * D + a] = gains[o * D + a];
+  }
+}
+
+__global__ void invert_kernel(const uint32_t* __restrict__ ext, int64_t n, uint32_t* __restrict__ inv) {
+  const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s < n) inv[ext[s]] = (uint32_t)s;
+}
+
+__global__ void remap_cols_kernel(const uint32_t* __restrict__ cols, int64_t nnz, const uint32_t* __restrict__ inv,
+                                  uint32_t* __restrict__ out) {
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < nnz; e += (int64_t)gridDim.x * blockDim.x)
+    out[e] = inv[cols[e]];
+}
+
+template <class T, int D>
+__global__ void unpermute_kernel(const T* __restrict__ y, const uint32_t* __restrict__ ext, int64_t n,
+                                 T* __restrict__ out) {
+  const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  const int64_t r = ext[s];
+#pragma unroll
+  for (int a = 0; a < D; ++a) out[r * D + a] = y[s * D + a];
+}
+
+template <class T, int D>
+__global__ void permute_in_kernel(const T* __restrict__ src, const uint32_t* __restrict__ ext, int64_t n,
+                                  T* __restrict__ y) {
+  const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  const int64_t r = ext[s];
+#pragma unroll
+  for (int a = 0; a < D; ++a) y[s * D + a] = src[r * D + a];
 }
 
 // Fused update over points; neg may be null (exact method: pos holds dy).
@@ -294,12 +348,51 @@ constexpr int kUpdBlocks = 2 * 152;
 
 template <class T>
 void launch_attractive(int D, const uint64_t* rows, const uint32_t* cols, const T* vals, const T* y, int64_t n, T* pos,
-                       cudaStream_t s) {
+                       cudaStream_t s, const uint32_t* row_of_slot) {
   if (n <= 0) return;
   const unsigned g = (unsigned)ceil_div(n * 32, 256);
-  if (D == 1) attractive_kernel<T, 1><<<g, 256, 0, s>>>(rows, cols, vals, y, n, pos);
-  else if (D == 2) attractive_kernel<T, 2><<<g, 256, 0, s>>>(rows, cols, vals, y, n, pos);
-  else attractive_kernel<T, 3><<<g, 256, 0, s>>>(rows, cols, vals, y, n, pos);
+  if (D == 1) attractive_kernel<T, 1><<<g, 256, 0, s>>>(rows, cols, vals, y, n, row_of_slot, pos);
+  else if (D == 2) attractive_kernel<T, 2><<<g, 256, 0, s>>>(rows, cols, vals, y, n, row_of_slot, pos);
+  else attractive_kernel<T, 3><<<g, 256, 0, s>>>(rows, cols, vals, y, n, row_of_slot, pos);
+  BHG_LAUNCH_CHECK();
+}
+
+template <class T>
+void launch_renumber(int D, const uint32_t* order, int64_t n, Renumbering& r, T* y, T* uy, T* gains, T* tmp_a, T* tmp_b,
+                     T* tmp_c, const uint32_t* cols, int64_t nnz, cudaStream_t s) {
+  const unsigned g = (unsigned)ceil_div(n, 256);
+  uint32_t* ext_new = static_cast<uint32_t*>(r.ext_alt.ensure((size_t)n * 4));
+  const uint32_t* ext_old = r.active ? r.ext.template as<uint32_t>() : nullptr;
+  if (D == 1)
+    renumber_gather_kernel<T, 1><<<g, 256, 0, s>>>(order, ext_old, n, y, uy, gains, tmp_a, tmp_b, tmp_c, ext_new);
+  else if (D == 2)
+    renumber_gather_kernel<T, 2><<<g, 256, 0, s>>>(order, ext_old, n, y, uy, gains, tmp_a, tmp_b, tmp_c, ext_new);
+  else
+    renumber_gather_kernel<T, 3><<<g, 256, 0, s>>>(order, ext_old, n, y, uy, gains, tmp_a, tmp_b, tmp_c, ext_new);
+  BHG_LAUNCH_CHECK();
+  const size_t bytes = (size_t)n * D * sizeof(T);
+  BHG_CUDA(cudaMemcpyAsync(y, tmp_a, bytes, cudaMemcpyDeviceToDevice, s));
+  BHG_CUDA(cudaMemcpyAsync(uy, tmp_b, bytes, cudaMemcpyDeviceToDevice, s));
+  BHG_CUDA(cudaMemcpyAsync(gains, tmp_c, bytes, cudaMemcpyDeviceToDevice, s));
+  r.ext.ensure((size_t)n * 4);
+  BHG_CUDA(cudaMemcpyAsync(r.ext.ptr, ext_new, (size_t)n * 4, cudaMemcpyDeviceToDevice, s));
+  uint32_t* inv = static_cast<uint32_t*>(r.inv.ensure((size_t)n * 4));
+  invert_kernel<<<g, 256, 0, s>>>(r.ext.template as<uint32_t>(), n, inv);
+  BHG_LAUNCH_CHECK();
+  uint32_t* cols_slot = static_cast<uint32_t*>(r.cols.ensure((size_t)std::max<int64_t>(nnz, 1) * 4));
+  if (nnz > 0) {
+    remap_cols_kernel<<<(unsigned)std::min<int64_t>(ceil_div(nnz, 256), 8 * 152), 256, 0, s>>>(cols, nnz, inv, cols_slot);
+    BHG_LAUNCH_CHECK();
+  }
+  r.active = true;
+}
+
+template <class T>
+void launch_unpermute(int D, const T* y, const uint32_t* ext, int64_t n, T* out, cudaStream_t s) {
+  const unsigned g = (unsigned)ceil_div(n, 256);
+  if (D == 1) unpermute_kernel<T, 1><<<g, 256, 0, s>>>(y, ext, n, out);
+  else if (D == 2) unpermute_kernel<T, 2><<<g, 256, 0, s>>>(y, ext, n, out);
+  else unpermute_kernel<T, 3><<<g, 256, 0, s>>>(y, ext, n, out);
   BHG_LAUNCH_CHECK();
 }
 
@@ -380,7 +473,10 @@ void launch_exact_kl(int D, const T* y, const T* p, int64_t n, const double* z, 
 
 #define BHG_INST(T)                                                                                                  \
   template void launch_attractive<T>(int, const uint64_t*, const uint32_t*, const T*, const T*, int64_t, T*,         \
-                                     cudaStream_t);                                                                  \
+                                     cudaStream_t, const uint32_t*);                                                 \
+  template void launch_renumber<T>(int, const uint32_t*, int64_t, Renumbering&, T*, T*, T*, T*, T*, T*,              \
+                                   const uint32_t*, int64_t, cudaStream_t);                                          \
+  template void launch_unpermute<T>(int, const T*, const uint32_t*, int64_t, T*, cudaStream_t);                      \
   template void launch_update<T>(int, T*, const T*, const T*, T*, T*, int64_t, const double*, T, T, T, UpdateScratch&,  \
                                  cudaStream_t);                                                                      \
   template void launch_kl_sparse<T>(int, const uint64_t*, const uint32_t*, const T*, const T*, int64_t,             \

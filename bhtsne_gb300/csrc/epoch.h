@@ -11,9 +11,28 @@ struct UpdateScratch {
   const double* mean() const { return static_cast<const double*>(mean_sum.ptr); }
 };
 
+// Attractive forces. With row_of_slot == nullptr slot s is CSR row s; with a
+// renumbered layout slot s holds CSR row row_of_slot[s] and `cols` are slots.
 template <class T>
 void launch_attractive(int D, const uint64_t* rows, const uint32_t* cols, const T* vals, const T* y, int64_t n, T* pos,
-                       cudaStream_t s);
+                       cudaStream_t s, const uint32_t* row_of_slot = nullptr);
+
+// Locality renumbering of the device-resident optimisation state. The points
+// are re-laid out in `order` (a permutation of the current slots, e.g. the
+// Morton order of the embedding); ext[s] is the point (CSR row) held by slot
+// s, inv its inverse, and cols the CSR columns translated to slots.
+struct Renumbering {
+  bool active = false;
+  DevBuf ext, ext_alt, inv, cols;
+};
+
+template <class T>
+void launch_renumber(int D, const uint32_t* order, int64_t n, Renumbering& r, T* y, T* uy, T* gains, T* tmp_a, T* tmp_b,
+                     T* tmp_c, const uint32_t* cols, int64_t nnz, cudaStream_t s);
+
+// out[ext[s]] = y[s]: back to the caller's point order.
+template <class T>
+void launch_unpermute(int D, const T* y, const uint32_t* ext, int64_t n, T* out, cudaStream_t s);
 
 // Fused gradient step; neg == nullptr means pos already holds the gradient.
 // The reciprocal normaliser is 1 / (T)*z, or inv_norm when z is null.

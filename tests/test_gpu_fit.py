@@ -250,3 +250,24 @@ def test_fit_sne_is_deterministic(gpu):
         t.fit_sne()
         runs.append(t.embedding())
     assert np.array_equal(runs[0], runs[1])
+
+
+@pytest.mark.parametrize("method", ["bh", "fit"])
+def test_locality_renumbering_preserves_the_fit(gpu, oracle, monkeypatch):
+    """The periodic Morton re-layout of the embedding state changes only
+    summation order: outputs stay in the caller's point order, the cost matches
+    an un-renumbered fit, and the affinities are untouched."""
+    X, lab = blobs(3000, 20, 6, 51)
+    seed = lcg_samples(3000, 2, 12)
+    res = {}
+    for every in ("0", "50"):
+        monkeypatch.setenv("BHTSNE_RENUMBER_EVERY", every)
+        t = gpu.TSNE(X).perplexity(30).epochs(400).initial_embedding(seed)
+        t.barnes_hut(0.5) if method == "bh" else t.fit_sne()
+        res[every] = (t.embedding(), t.kl_divergence(), t.affinities())
+    e0, kl0, a0 = res["0"]
+    e1, kl1, a1 = res["50"]
+    assert abs(kl1 - kl0) / kl0 < 0.01
+    assert np.array_equal(a0.columns, a1.columns) and np.array_equal(a0.values, a1.values)
+    # clusters are found in the caller's order
+    assert same_cluster_fraction(e1, lab) > 0.95
