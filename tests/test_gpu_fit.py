@@ -253,7 +253,7 @@ def test_fit_sne_is_deterministic(gpu):
 
 
 @pytest.mark.parametrize("method", ["bh", "fit"])
-def test_locality_renumbering_preserves_the_fit(gpu, oracle, monkeypatch):
+def test_locality_renumbering_preserves_the_fit(gpu, monkeypatch, method):
     """The periodic Morton re-layout of the embedding state changes only
     summation order: outputs stay in the caller's point order, the cost matches
     an un-renumbered fit, and the affinities are untouched."""
