@@ -32,54 +32,13 @@
 //    the children. Leaves are summed in T exactly like the reference so that
 //    a singleton leaf's centre is bit-identical to its point (the self test).
 #include "bh.h"
+#include "bh_dev.cuh"
 
 namespace bhg {
 
 namespace {
 
 constexpr int kThreads = 256;
-
-template <int D>
-struct MortonD;
-template <>
-struct MortonD<2> {
-  static constexpr int BITS = 32;
-  __device__ static uint64_t part(uint64_t x) {
-    x &= 0x00000000ffffffffULL;
-    x = (x | (x << 16)) & 0x0000ffff0000ffffULL;
-    x = (x | (x << 8)) & 0x00ff00ff00ff00ffULL;
-    x = (x | (x << 4)) & 0x0f0f0f0f0f0f0f0fULL;
-    x = (x | (x << 2)) & 0x3333333333333333ULL;
-    return (x | (x << 1)) & 0x5555555555555555ULL;
-  }
-  __device__ static uint64_t encode(const uint32_t* c) { return part(c[0]) | (part(c[1]) << 1); }
-};
-template <>
-struct MortonD<3> {
-  static constexpr int BITS = 21;
-  __device__ static uint64_t part(uint64_t x) {
-    x &= 0x1fffffULL;
-    x = (x | (x << 32)) & 0x001f00000000ffffULL;
-    x = (x | (x << 16)) & 0x001f0000ff0000ffULL;
-    x = (x | (x << 8)) & 0x100f00f00f00f00fULL;
-    x = (x | (x << 4)) & 0x10c30c30c30c30c3ULL;
-    return (x | (x << 2)) & 0x1249249249249249ULL;
-  }
-  __device__ static uint64_t encode(const uint32_t* c) {
-    return part(c[0]) | (part(c[1]) << 1) | (part(c[2]) << 2);
-  }
-};
-
-template <class T>
-__device__ __forceinline__ uint32_t quantize(T v, T mn, T inv_scale, uint32_t max_bucket) {
-  const T scaled = floor((v - mn) * inv_scale);
-  if (scaled > T(0)) {
-    if (!(scaled < T(18446744073709551616.0))) return max_bucket;
-    const uint64_t q = (uint64_t)scaled;
-    return q < (uint64_t)max_bucket ? (uint32_t)q : max_bucket;
-  }
-  return 0u;
-}
 
 // ---------------------------------------------------------------------------
 // Recentre (optional) + per-axis bounding box; the last block to finish
@@ -344,41 +303,6 @@ __global__ void prefix_apply_kernel(const T* __restrict__ y, const uint32_t* __r
 // ---------------------------------------------------------------------------
 // Tree build.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ int64_t lower_bound_u64(const uint64_t* __restrict__ c, int64_t lo, int64_t hi,
-                                                   uint64_t key) {
-  while (lo < hi) {
-    const int64_t mid = (lo + hi) >> 1;
-    if (c[mid] < key) lo = mid + 1;
-    else hi = mid;
-  }
-  return lo;
-}
-
-template <int D>
-__device__ __forceinline__ int boundary_level(uint64_t c0, uint64_t c1) {
-  constexpr int B = MortonD<D>::BITS;
-  const int highest = 63 - __clzll((long long)(c0 ^ c1));
-  return (B - 1) - highest / D;
-}
-
-// Range [a, e) of the depth-l Morton cell holding code c.
-template <int D>
-__device__ __forceinline__ void cell_range(const uint64_t* __restrict__ codes, int64_t n, uint64_t c, int l,
-                                           int64_t* a, int64_t* e) {
-  constexpr int B = MortonD<D>::BITS;
-  if (l == 0) {
-    *a = 0;
-    *e = n;
-    return;
-  }
-  const int shift = D * (B - l);
-  const uint64_t prefix = c >> shift;
-  *a = lower_bound_u64(codes, 0, n, prefix << shift);
-  const uint64_t limit = ~0ULL >> shift;  // largest prefix representable
-  if (prefix >= limit) *e = n;
-  else *e = lower_bound_u64(codes, *a, n, (prefix + 1) << shift);
-}
-
 template <int D>
 __global__ void tree_mark_kernel(const uint64_t* __restrict__ codes, int64_t n, uint32_t* __restrict__ mask) {
   const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -496,11 +420,22 @@ __global__ void __launch_bounds__(kThreads) bh_traverse_kernel(const T* __restri
 #pragma unroll
     for (int a = 0; a < D; ++a) f[a] = T(0);
     T q = T(0);
+    // Software-pipelined walk: both possible successors of the current node
+    // (i + 1 if it is opened, its skip target if it is summarised) are loaded
+    // before the decision, so the next visit never waits on a dependent load.
     uint32_t i = 0;
+    typename TreeNodes<T, D>::Raw cur = nodes.load(0);
     while (i < M) {
+      const uint32_t w = nodes.word(cur);
+      const bool leaf = w == kLeafWord;
+      const uint32_t sk_raw = leaf ? i + 1 : (w >> 5);
+      // skip > i by construction; max() keeps the walk finite regardless.
+      const uint32_t sk = sk_raw > i ? sk_raw : i + 1;
+      const uint32_t last = M - 1;
+      const typename TreeNodes<T, D>::Raw nxt_open = nodes.load(i + 1 < M ? i + 1 : last);
+      const typename TreeNodes<T, D>::Raw nxt_skip = leaf ? nxt_open : nodes.load(sk < M ? sk : last);
       T com[D], mass, r2;
-      uint32_t skip;
-      nodes.read(i, com, &mass, &r2, &skip);
+      nodes.decode(cur, com, &mass, &r2);
       T disp[D];
       T dist = T(0);
 #pragma unroll
@@ -509,11 +444,12 @@ __global__ void __launch_bounds__(kThreads) bh_traverse_kernel(const T* __restri
         dist += disp[a] * disp[a];
       }
       if (r2 >= theta_sq * dist) {
-        ++i;
+        i = i + 1;
+        cur = nxt_open;
         continue;
       }
-      // skip > i by construction; max() keeps the walk finite regardless.
-      i = skip > i ? skip : i + 1;
+      i = sk;
+      cur = nxt_skip;
       if (r2 < T(0) && dist == T(0)) continue;
       const T inv = T(1) / (T(1) + dist);
       T m = mass * inv;
@@ -611,7 +547,7 @@ static TreeNodes<T, D> nodes_of(BhWorkspace<T>& ws) {
     t.geom = ws.geom.template as<Node2<T>>();
   } else {
     t.geom = ws.geom.template as<Quad<T>>();
-    t.word = ws.word.template as<uint32_t>();
+    t.words = ws.word.template as<uint32_t>();
   }
   return t;
 }

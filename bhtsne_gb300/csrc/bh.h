@@ -46,6 +46,16 @@ template <class T>
 struct TreeNodes<T, 2> {
   Node2<T>* geom;
   const T* hw2;  // shared-memory copy of BoxParams::hw2 inside the traversal
+  typedef Node2<T> Raw;
+  __device__ __forceinline__ Raw load(uint32_t i) const { return geom[i]; }
+  __device__ __forceinline__ uint32_t word(const Raw& r) const { return (uint32_t)r.w; }
+  __device__ __forceinline__ void decode(const Raw& g, T* c, T* mass, T* r2) const {
+    c[0] = g.x;
+    c[1] = g.y;
+    *mass = g.mass;
+    const uint32_t w = (uint32_t)g.w;
+    *r2 = w == kLeafWord ? T(-1) : hw2[w & 31u];
+  }
   __device__ __forceinline__ void write(int64_t i, const T* c, T mass, int level, uint32_t sk) const {
     Node2<T> g;
     g.x = c[0];
@@ -69,8 +79,26 @@ struct TreeNodes<T, 2> {
 template <class T>
 struct TreeNodes<T, 3> {
   Quad<T>* geom;
-  uint32_t* word;
+  uint32_t* words;
   const T* hw2;
+  struct Raw {
+    Quad<T> g;
+    uint32_t w;
+  };
+  __device__ __forceinline__ Raw load(uint32_t i) const {
+    Raw r;
+    r.g = geom[i];
+    r.w = words[i];
+    return r;
+  }
+  __device__ __forceinline__ uint32_t word(const Raw& r) const { return r.w; }
+  __device__ __forceinline__ void decode(const Raw& r, T* c, T* mass, T* r2) const {
+    c[0] = r.g.x;
+    c[1] = r.g.y;
+    c[2] = r.g.z;
+    *mass = r.g.w;
+    *r2 = r.w == kLeafWord ? T(-1) : hw2[r.w & 31u];
+  }
   __device__ __forceinline__ void write(int64_t i, const T* c, T mass, int level, uint32_t sk) const {
     Quad<T> g;
     g.x = c[0];
@@ -78,11 +106,11 @@ struct TreeNodes<T, 3> {
     g.z = c[2];
     g.w = mass;
     geom[i] = g;
-    word[i] = level < 0 ? kLeafWord : ((sk << 5) | (uint32_t)level);
+    words[i] = level < 0 ? kLeafWord : ((sk << 5) | (uint32_t)level);
   }
   __device__ __forceinline__ void read(uint32_t i, T* c, T* mass, T* r2, uint32_t* sk) const {
     const Quad<T> g = geom[i];
-    const uint32_t w = word[i];
+    const uint32_t w = words[i];
     c[0] = g.x;
     c[1] = g.y;
     c[2] = g.z;

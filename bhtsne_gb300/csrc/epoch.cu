@@ -16,39 +16,41 @@
 //    src/tsne/mod.rs:579-618; dense symmetrisation: src/lib.rs:548-554.
 #include "epoch.h"
 
+#include <cstdlib>
+
 namespace bhg {
 
 namespace {
 
-template <class T, int D>
+// G lanes per embedding slot (32 / G slots per warp); each lane keeps kU
+// entries in flight (column, value and gathered y loaded before any
+// arithmetic). With a renumbered layout slot s holds the point of CSR row
+// row_of_slot[s] and `cols` holds slots, so a row's gathers stay near s and
+// neighbouring warps share lines.
+template <class T, int D, int G, int kU>
 __global__ void __launch_bounds__(256) attractive_kernel(const uint64_t* __restrict__ rows, const uint32_t* __restrict__ cols,
                                                          const T* __restrict__ vals, const T* __restrict__ y, int64_t n,
                                                          const uint32_t* __restrict__ row_of_slot, T* __restrict__ pos) {
-  // One warp per embedding slot; each lane keeps up to kU entries in flight
-  // (their column, value and gathered y loaded before any arithmetic), so a
-  // warp has kU x 32 independent loads outstanding. With a renumbered layout
-  // slot s holds the point of CSR row row_of_slot[s] and `cols` holds slots,
-  // so a row's gathers stay near s and neighbouring warps share lines.
-  constexpr int kU = 4;
-  const int64_t slot = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
-  if (slot >= n) return;
-  const int64_t row = row_of_slot ? (int64_t)row_of_slot[slot] : slot;
+  const int64_t slot = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / G;
+  const int lane = threadIdx.x & (G - 1);
+  const bool active = slot < n;
+  const int64_t sl = active ? slot : n - 1;
+  const int64_t row = row_of_slot ? (int64_t)row_of_slot[sl] : sl;
   T yi[D], acc[D];
 #pragma unroll
   for (int a = 0; a < D; ++a) {
-    yi[a] = y[slot * D + a];
+    yi[a] = y[sl * D + a];
     acc[a] = T(0);
   }
-  const int64_t e0 = (int64_t)rows[row], e1 = (int64_t)rows[row + 1];
-  for (int64_t base = e0; base < e1; base += 32 * kU) {
+  const int64_t e0 = (int64_t)rows[row], e1 = active ? (int64_t)rows[row + 1] : e0;
+  for (int64_t base = e0; base < e1; base += G * kU) {
     uint32_t j[kU];
     T p[kU];
     T yj[kU][D];
 #pragma unroll
     for (int u = 0; u < kU; ++u) {
-      const int64_t e = base + lane + 32 * u;
-      j[u] = e < e1 ? __ldg(cols + e) : (uint32_t)slot;
+      const int64_t e = base + lane + G * u;
+      j[u] = e < e1 ? __ldg(cols + e) : (uint32_t)sl;
       p[u] = e < e1 ? __ldg(vals + e) : T(0);
     }
 #pragma unroll
@@ -70,62 +72,14 @@ __global__ void __launch_bounds__(256) attractive_kernel(const uint64_t* __restr
     }
   }
 #pragma unroll
-  for (int a = 0; a < D; ++a) acc[a] = warp_sum(acc[a]);
-  if (lane == 0) {
+  for (int a = 0; a < D; ++a) {
+#pragma unroll
+    for (int o = G / 2; o > 0; o >>= 1) acc[a] += __shfl_xor_sync(kFull, acc[a], o, G);
+  }
+  if (active && lane == 0) {
 #pragma unroll
     for (int a = 0; a < D; ++a) pos[slot * D + a] = acc[a];
   }
-}
-
-// ---------------------------------------------------------------------------
-// Renumbering of the embedding layout (see launch_renumber).
-// ---------------------------------------------------------------------------
-template <class T, int D>
-__global__ void renumber_gather_kernel(const uint32_t* __restrict__ order, const uint32_t* __restrict__ ext_old,
-                                       int64_t n, const T* __restrict__ y, const T* __restrict__ uy,
-                                       const T* __restrict__ gains, T* __restrict__ y2, T* __restrict__ uy2,
-                                       T* __restrict__ g2, uint32_t* __restrict__ ext_new) {
-  const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= n) return;
-  const int64_t o = order[s];
-  ext_new[s] = ext_old ? ext_old[o] : (uint32_t)o;
-#pragma unroll
-  for (int a = 0; a < D; ++a) {
-    y2[s * D + a] = y[o * D + a];
-    uy2[s * D + a] = uy[o * D + a];
-    g2[s * D + a] = gains[o * D + a];
-  }
-}
-
-__global__ void invert_kernel(const uint32_t* __restrict__ ext, int64_t n, uint32_t* __restrict__ inv) {
-  const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (s < n) inv[ext[s]] = (uint32_t)s;
-}
-
-__global__ void remap_cols_kernel(const uint32_t* __restrict__ cols, int64_t nnz, const uint32_t* __restrict__ inv,
-                                  uint32_t* __restrict__ out) {
-  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < nnz; e += (int64_t)gridDim.x * blockDim.x)
-    out[e] = inv[cols[e]];
-}
-
-template <class T, int D>
-__global__ void unpermute_kernel(const T* __restrict__ y, const uint32_t* __restrict__ ext, int64_t n,
-                                 T* __restrict__ out) {
-  const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= n) return;
-  const int64_t r = ext[s];
-#pragma unroll
-  for (int a = 0; a < D; ++a) out[r * D + a] = y[s * D + a];
-}
-
-template <class T, int D>
-__global__ void permute_in_kernel(const T* __restrict__ src, const uint32_t* __restrict__ ext, int64_t n,
-                                  T* __restrict__ y) {
-  const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= n) return;
-  const int64_t r = ext[s];
-#pragma unroll
-  for (int a = 0; a < D; ++a) y[s * D + a] = src[r * D + a];
 }
 
 // Fused update over points; neg may be null (exact method: pos holds dy).
@@ -346,14 +300,36 @@ constexpr int kUpdBlocks = 2 * 152;
 
 }  // namespace
 
+template <class T, int D>
+static void launch_attractive_d(int variant, const uint64_t* rows, const uint32_t* cols, const T* vals, const T* y,
+                                int64_t n, T* pos, cudaStream_t s, const uint32_t* row_of_slot) {
+  switch (variant) {
+    case 0:
+      attractive_kernel<T, D, 32, 4><<<(unsigned)ceil_div(n * 32, 256), 256, 0, s>>>(rows, cols, vals, y, n, row_of_slot, pos);
+      break;
+    case 1:
+      attractive_kernel<T, D, 32, 8><<<(unsigned)ceil_div(n * 32, 256), 256, 0, s>>>(rows, cols, vals, y, n, row_of_slot, pos);
+      break;
+    case 2:
+      attractive_kernel<T, D, 16, 8><<<(unsigned)ceil_div(n * 16, 256), 256, 0, s>>>(rows, cols, vals, y, n, row_of_slot, pos);
+      break;
+    default:
+      attractive_kernel<T, D, 8, 8><<<(unsigned)ceil_div(n * 8, 256), 256, 0, s>>>(rows, cols, vals, y, n, row_of_slot, pos);
+      break;
+  }
+}
+
 template <class T>
 void launch_attractive(int D, const uint64_t* rows, const uint32_t* cols, const T* vals, const T* y, int64_t n, T* pos,
                        cudaStream_t s, const uint32_t* row_of_slot) {
   if (n <= 0) return;
-  const unsigned g = (unsigned)ceil_div(n * 32, 256);
-  if (D == 1) attractive_kernel<T, 1><<<g, 256, 0, s>>>(rows, cols, vals, y, n, row_of_slot, pos);
-  else if (D == 2) attractive_kernel<T, 2><<<g, 256, 0, s>>>(rows, cols, vals, y, n, row_of_slot, pos);
-  else attractive_kernel<T, 3><<<g, 256, 0, s>>>(rows, cols, vals, y, n, row_of_slot, pos);
+  static const int variant = [] {
+    const char* v = getenv("BHTSNE_ATTRACTIVE_VARIANT");
+    return v ? atoi(v) : 0;
+  }();
+  if (D == 1) launch_attractive_d<T, 1>(variant, rows, cols, vals, y, n, pos, s, row_of_slot);
+  else if (D == 2) launch_attractive_d<T, 2>(variant, rows, cols, vals, y, n, pos, s, row_of_slot);
+  else launch_attractive_d<T, 3>(variant, rows, cols, vals, y, n, pos, s, row_of_slot);
   BHG_LAUNCH_CHECK();
 }
 
