@@ -82,6 +82,47 @@ __global__ void __launch_bounds__(256) attractive_kernel(const uint64_t* __restr
   }
 }
 
+// ---------------------------------------------------------------------------
+// Renumbering of the embedding layout (see launch_renumber).
+// ---------------------------------------------------------------------------
+template <class T, int D>
+__global__ void renumber_gather_kernel(const uint32_t* __restrict__ order, const uint32_t* __restrict__ ext_old,
+                                       int64_t n, const T* __restrict__ y, const T* __restrict__ uy,
+                                       const T* __restrict__ gains, T* __restrict__ y2, T* __restrict__ uy2,
+                                       T* __restrict__ g2, uint32_t* __restrict__ ext_new) {
+  const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  const int64_t o = order[s];
+  ext_new[s] = ext_old ? ext_old[o] : (uint32_t)o;
+#pragma unroll
+  for (int a = 0; a < D; ++a) {
+    y2[s * D + a] = y[o * D + a];
+    uy2[s * D + a] = uy[o * D + a];
+    g2[s * D + a] = gains[o * D + a];
+  }
+}
+
+__global__ void invert_kernel(const uint32_t* __restrict__ ext, int64_t n, uint32_t* __restrict__ inv) {
+  const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s < n) inv[ext[s]] = (uint32_t)s;
+}
+
+__global__ void remap_cols_kernel(const uint32_t* __restrict__ cols, int64_t nnz, const uint32_t* __restrict__ inv,
+                                  uint32_t* __restrict__ out) {
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < nnz; e += (int64_t)gridDim.x * blockDim.x)
+    out[e] = inv[cols[e]];
+}
+
+template <class T, int D>
+__global__ void unpermute_kernel(const T* __restrict__ y, const uint32_t* __restrict__ ext, int64_t n,
+                                 T* __restrict__ out) {
+  const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  const int64_t r = ext[s];
+#pragma unroll
+  for (int a = 0; a < D; ++a) out[r * D + a] = y[s * D + a];
+}
+
 // Fused update over points; neg may be null (exact method: pos holds dy).
 // Accumulates sum(y_new) per axis in FP64 into mean_sum (deterministic: the
 // last block reduces the per-block partials in block order).
