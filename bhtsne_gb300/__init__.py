@@ -6,11 +6,12 @@ Python mirror of the reference's `tSNE` builder over that ABI.
 """
 from ._lib import (BhtsneError, Context, F32, F64, METHOD_BARNES_HUT, METHOD_EXACT, METHOD_FIT_SNE, SIGNATURES,
                    default_context, library_path, load)
+from .batch import Batch
 from .tsne import (Neighbor, SparseAffinities, TSNE, conditional_p, gradient, knn_euclidean, neighbors_to_arrays,
                    symmetrize, update)
 
 __all__ = [
-    "BhtsneError", "Context", "F32", "F64", "METHOD_BARNES_HUT", "METHOD_EXACT", "METHOD_FIT_SNE", "SIGNATURES",
+    "Batch", "BhtsneError", "Context", "F32", "F64", "METHOD_BARNES_HUT", "METHOD_EXACT", "METHOD_FIT_SNE", "SIGNATURES",
     "default_context", "library_path", "load", "Neighbor", "SparseAffinities", "TSNE", "conditional_p", "gradient",
     "knn_euclidean", "neighbors_to_arrays", "symmetrize", "update",
 ]

@@ -61,7 +61,35 @@ SIGNATURES = {
                                   _dblp]),
     "bhtsne_update": (C.c_int, [_vp, C.c_int, _i32, _vp, _vp, _vp, _vp, _vp, _i64, _dbl, _dbl, _dbl]),
     "bhtsne_bh_repulsion_noalloc": (C.c_int, [_vp, _i64, _dbl, _vp, _vp, _vp]),
+    "bhtsne_batch_params_default": (None, [_vp]),
+    "bhtsne_batch_new": (C.c_int, [_vp, C.c_int, _i32, _vp, C.POINTER(C.c_void_p)]),
+    "bhtsne_batch_free": (C.c_int, [_vp]),
+    "bhtsne_batch_last_error": (C.c_char_p, [_vp]),
+    "bhtsne_batch_add_euclidean": (C.c_int, [_vp, _vp, _i64, _i32, _i64p]),
+    "bhtsne_batch_add_with_neighbors": (C.c_int, [_vp, _u64p, _vp, _i64, _i64, _i64p]),
+    "bhtsne_batch_initial_embedding": (C.c_int, [_vp, _i64, _vp]),
+    "bhtsne_batch_fit": (C.c_int, [_vp]),
+    "bhtsne_batch_jobs": (C.c_int64, [_vp]),
+    "bhtsne_batch_embedding": (C.c_int, [_vp, _i64, _vp]),
+    "bhtsne_batch_kl_divergence": (C.c_int, [_vp, _i64, _i32, _dblp]),
+    "bhtsne_batch_timings": (C.c_int, [_vp, _dblp, _dblp]),
 }
+
+
+class BatchParams(C.Structure):
+    """Mirror of struct bhtsne_batch_params."""
+    _fields_ = [
+        ("perplexity", C.c_double),
+        ("epochs", C.c_int64),
+        ("learning_rate", C.c_double),
+        ("momentum", C.c_double),
+        ("final_momentum", C.c_double),
+        ("momentum_switch_epoch", C.c_int64),
+        ("stop_lying_epoch", C.c_int64),
+        ("early_exaggeration", C.c_double),
+        ("theta", C.c_double),
+        ("seed", C.c_uint64),
+    ]
 
 _lock = threading.Lock()
 _lib = None

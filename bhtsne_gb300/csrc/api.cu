@@ -22,6 +22,7 @@
 #include "epoch.h"
 #include "fitsne.h"
 #include "knn.h"
+#include "batch.h"
 
 using namespace bhg;
 
@@ -1165,6 +1166,472 @@ int bhtsne_update(bhtsne_ctx* ctx, int dtype, int32_t embed_dim, void* y, const 
       BHG_CUDA(cudaStreamSynchronize(s));
     });
   });
+}
+
+}  // extern "C"
+
+// ===========================================================================
+// Batches of independent fits.
+// ===========================================================================
+struct bhtsne_batch {
+  bhtsne_ctx* ctx = nullptr;
+  int dtype = BHTSNE_F32;
+  int D = 2;
+  bhtsne_batch_params prm;
+  std::string err;
+  void* impl = nullptr;
+};
+
+namespace {
+
+template <class T>
+struct BatchJob {
+  int64_t n = 0, nnz = 0;
+  DevBuf rows, cols, vals;
+  bool has_init = false;
+  std::vector<T> init;
+};
+
+template <class T>
+struct BatchImpl {
+  std::vector<std::unique_ptr<BatchJob<T>>> jobs;
+  int K = 0;
+  int64_t total = 0, nnz = 0;
+  std::vector<int64_t> off, nnz_off;
+  DevBuf d_off, job_of, rows, cols, vals, y, uy, gains, pos, neg, q, z, lr, mom, boxes, codes, jobkey, jobkey_alt;
+  DevBuf tmp, sumtmp, kidx, kdist, kp, xin;
+  BhWorkspace<T> ws;
+  SymWorkspace<T> sym;
+  KnnWorkspace knn;
+  bool fitted = false;
+  double aff_ms = 0, loop_ms = 0;
+  cudaGraphExec_t graph = nullptr;
+  ~BatchImpl() {
+    if (graph) cudaGraphExecDestroy(graph);
+  }
+};
+
+template <class F>
+int guard_batch(bhtsne_batch* b, F&& f) {
+  if (!b) return BHTSNE_EINVAL;
+  try {
+    BHG_CUDA(cudaSetDevice(b->ctx->device));
+    f();
+    return BHTSNE_OK;
+  } catch (const Error& e) {
+    b->err = e.what();
+    return e.code;
+  } catch (const std::exception& e) {
+    b->err = e.what();
+    return BHTSNE_EINTERNAL;
+  }
+}
+
+template <class T>
+BatchImpl<T>& bimpl(bhtsne_batch* b) {
+  return *static_cast<BatchImpl<T>*>(b->impl);
+}
+
+// Affinities of one job from a device kNN table (search_beta + symmetrize).
+template <class T>
+void batch_job_affinities(bhtsne_batch* b, BatchJob<T>& job, int64_t k) {
+  BatchImpl<T>& B = bimpl<T>(b);
+  cudaStream_t s = b->ctx->stream;
+  const int64_t n = job.n;
+  B.kp.ensure((size_t)n * k * sizeof(T));
+  const T perp = (T)b->prm.perplexity;
+  launch_search_beta<T>(B.kdist.template as<T>(), n, k, perp, B.kp.template as<T>(), nullptr, s);
+  const int64_t nnz = symmetrize<T>(B.kidx.template as<uint32_t>(), B.kp.template as<T>(), n, (int)k, B.sym, s);
+  job.rows.ensure((size_t)(n + 1) * 8);
+  job.cols.ensure((size_t)std::max<int64_t>(nnz, 1) * 4);
+  job.vals.ensure((size_t)std::max<int64_t>(nnz, 1) * sizeof(T));
+  symmetrize_finish<T>(B.sym, n, nnz, job.rows.template as<uint64_t>(), job.cols.template as<uint32_t>(),
+                       job.vals.template as<T>(), s);
+  BHG_CUDA(cudaStreamSynchronize(s));
+  job.nnz = nnz;
+}
+
+void batch_check_job(const bhtsne_batch* b, int64_t n) {
+  const double perp = b->prm.perplexity;
+  const int64_t as_usize = perp > 0 ? (int64_t)perp : 0;
+  if (n < 2 || (n - 1) < 3 * as_usize)
+    invalid("error: the provided perplexity is too large for the number of data points.\n");
+}
+
+template <class T>
+int64_t batch_add_with_neighbors(bhtsne_batch* b, const uint64_t* idx, const void* dist, int64_t n, int64_t k) {
+  BatchImpl<T>& B = bimpl<T>(b);
+  batch_check_job(b, n);
+  if (k <= 0 || !idx || !dist) invalid("error: every neighbors row must have the same length, greater than zero.");
+  std::vector<uint32_t> idx32((size_t)(n * k));
+  for (int64_t e = 0; e < n * k; ++e) {
+    if (idx[e] >= (uint64_t)n)
+      invalid("error: a neighbor index is out of range, every index must be < n_samples = " + std::to_string(n) + ".");
+    idx32[e] = (uint32_t)idx[e];
+  }
+  cudaStream_t s = b->ctx->stream;
+  auto job = std::make_unique<BatchJob<T>>();
+  job->n = n;
+  B.kidx.ensure((size_t)n * k * 4);
+  BHG_CUDA(cudaMemcpyAsync(B.kidx.ptr, idx32.data(), (size_t)n * k * 4, cudaMemcpyHostToDevice, s));
+  upload<T>(B.kdist, dist, (size_t)n * k * sizeof(T), s);
+  batch_job_affinities<T>(b, *job, k);
+  B.jobs.push_back(std::move(job));
+  B.fitted = false;
+  return (int64_t)B.jobs.size() - 1;
+}
+
+template <class T>
+int64_t batch_add_euclidean(bhtsne_batch* b, const void* data, int64_t n, int32_t dim) {
+  BatchImpl<T>& B = bimpl<T>(b);
+  batch_check_job(b, n);
+  if (!data || dim <= 0) invalid("error: data must be a non-empty n_samples x dim array.");
+  cudaStream_t s = b->ctx->stream;
+  const int64_t k = (int64_t)((T)3.0 * (T)b->prm.perplexity);
+  auto job = std::make_unique<BatchJob<T>>();
+  job->n = n;
+  upload<T>(B.xin, data, (size_t)n * dim * sizeof(T), s);
+  B.kidx.ensure((size_t)n * k * 4);
+  B.kdist.ensure((size_t)n * k * sizeof(T));
+  knn_euclidean<T>(B.xin.template as<T>(), n, dim, (int)k, B.kidx.template as<uint32_t>(), B.kdist.template as<T>(),
+                   B.knn, s);
+  batch_job_affinities<T>(b, *job, k);
+  B.jobs.push_back(std::move(job));
+  B.fitted = false;
+  return (int64_t)B.jobs.size() - 1;
+}
+
+template <class T>
+__global__ void batch_fill_kernel(T* p, int64_t n, T v) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) p[i] = v;
+}
+
+// Lockstep Barnes-Hut fit of every job (run_loop, src/lib.rs:961-1014, per job).
+template <class T>
+void batch_fit(bhtsne_batch* b) {
+  BatchImpl<T>& B = bimpl<T>(b);
+  cudaStream_t s = b->ctx->stream;
+  const int D = b->D;
+  const bhtsne_batch_params& P = b->prm;
+  if (B.jobs.empty()) invalid("error: the batch has no jobs.");
+  if (!(P.theta > 0))
+    invalid("error: theta value must be greater than 0.0.\n            A value of 0.0 corresponds to using the exact "
+            "version of the algorithm.");
+  B.K = (int)B.jobs.size();
+  B.off.assign(B.K + 1, 0);
+  B.nnz_off.assign(B.K + 1, 0);
+  for (int j = 0; j < B.K; ++j) {
+    B.off[j + 1] = B.off[j] + B.jobs[j]->n;
+    B.nnz_off[j + 1] = B.nnz_off[j] + B.jobs[j]->nnz;
+  }
+  B.total = B.off[B.K];
+  B.nnz = B.nnz_off[B.K];
+  const int64_t total = B.total;
+  cudaEvent_t e0, e1;
+  BHG_CUDA(cudaEventCreate(&e0));
+  BHG_CUDA(cudaEventCreate(&e1));
+  BHG_CUDA(cudaEventRecord(e0, s));
+  // block-diagonal CSR
+  B.rows.ensure((size_t)(total + 1) * 8);
+  B.cols.ensure((size_t)std::max<int64_t>(B.nnz, 1) * 4);
+  B.vals.ensure((size_t)std::max<int64_t>(B.nnz, 1) * sizeof(T));
+  B.job_of.ensure((size_t)total * 4);
+  for (int j = 0; j < B.K; ++j) {
+    BatchJob<T>& J = *B.jobs[j];
+    batch_append_csr(J.rows.template as<uint64_t>(), J.cols.template as<uint32_t>(), J.n, J.nnz,
+                     (uint64_t)B.nnz_off[j], (uint32_t)B.off[j], B.rows.template as<uint64_t>() + B.off[j],
+                     B.cols.template as<uint32_t>() + B.nnz_off[j], s);
+    if (J.nnz)
+      BHG_CUDA(cudaMemcpyAsync(B.vals.template as<T>() + B.nnz_off[j], J.vals.ptr, J.nnz * sizeof(T),
+                               cudaMemcpyDeviceToDevice, s));
+    // normalize_p_values per job (src/tsne/mod.rs:284-293), then stop_lying if disabled
+    double* sum = static_cast<double*>(B.sumtmp.ensure(64));
+    launch_normalize<T>(B.vals.template as<T>() + B.nnz_off[j], J.nnz, (T)P.early_exaggeration, sum, B.tmp, s);
+    if (P.stop_lying_epoch == 0)
+      launch_scale<T>(B.vals.template as<T>() + B.nnz_off[j], J.nnz, T(1) / (T)P.early_exaggeration, s);
+    batch_fill_job(B.job_of.template as<uint32_t>(), B.off[j], B.off[j + 1], (uint32_t)j, s);
+  }
+  BHG_CUDA(cudaStreamSynchronize(s));
+  for (auto& J : B.jobs) {
+    J->rows.release();
+    J->cols.release();
+    J->vals.release();
+  }
+  upload<T>(B.d_off, B.off.data(), B.off.size() * 8, s);
+  // seeds, velocity, gains, per-job learning rate and momentum
+  std::vector<T> yh((size_t)total * D);
+  std::vector<T> lrh(B.K), momh(B.K, (T)P.momentum);
+  for (int j = 0; j < B.K; ++j) {
+    BatchJob<T>& J = *B.jobs[j];
+    T* dst = yh.data() + B.off[j] * D;
+    if (J.has_init) {
+      std::copy(J.init.begin(), J.init.end(), dst);
+      J.has_init = false;
+    } else {
+      uint64_t sd = P.seed + (uint64_t)j;
+      for (int64_t e = 0; e < J.n * D; e += 2) {
+        const double u1 = ((lcg_next(sd) >> 11) + 0.5) * (1.0 / 9007199254740992.0);
+        const double u2 = ((lcg_next(sd) >> 11) + 0.5) * (1.0 / 9007199254740992.0);
+        const double r = std::sqrt(-2.0 * std::log(u1));
+        dst[e] = (T)(1e-4 * r * std::cos(2 * M_PI * u2));
+        if (e + 1 < J.n * D) dst[e + 1] = (T)(1e-4 * r * std::sin(2 * M_PI * u2));
+      }
+    }
+    if (P.learning_rate > 0) lrh[j] = (T)P.learning_rate;
+    else {
+      const T a = (T)(double)J.n / (T)P.early_exaggeration / (T)4.0;
+      lrh[j] = a > (T)50.0 ? a : (T)50.0;
+    }
+  }
+  const size_t ybytes = (size_t)total * D * sizeof(T);
+  upload<T>(B.y, yh.data(), ybytes, s);
+  B.uy.ensure(ybytes);
+  B.gains.ensure(ybytes);
+  B.pos.ensure(ybytes);
+  B.neg.ensure(ybytes);
+  B.q.ensure((size_t)total * sizeof(T));
+  BHG_CUDA(cudaMemsetAsync(B.uy.ptr, 0, ybytes, s));
+  batch_fill_kernel<T><<<256, 256, 0, s>>>(B.gains.template as<T>(), total * D, T(1));
+  BHG_LAUNCH_CHECK();
+  upload<T>(B.lr, lrh.data(), B.K * sizeof(T), s);
+  upload<T>(B.mom, momh.data(), B.K * sizeof(T), s);
+  B.z.ensure((size_t)B.K * 8);
+  B.boxes.ensure((size_t)B.K * sizeof(BoxParams<T>));
+  B.ws.reserve(total, D);
+  BHG_CUDA(cudaEventRecord(e1, s));
+  BHG_CUDA(cudaEventSynchronize(e1));
+  float ms = 0;
+  BHG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+  B.aff_ms += ms;
+
+  // epoch loop
+  const int bits = D == 2 ? 32 : 21;
+  T* y = B.y.template as<T>();
+  BoxParams<T>* boxes = B.boxes.template as<BoxParams<T>>();
+  const int64_t* off = B.d_off.template as<int64_t>();
+  auto body = [&]() {
+    batch_sort_and_build<T>(D, y, total, B.K, B.job_of.template as<uint32_t>(), off, boxes, B.ws, B.codes, B.jobkey,
+                            B.jobkey_alt, s);
+    Segs sg;
+    sg.job = B.jobkey.template as<uint64_t>();
+    sg.off = off;
+    bh_traverse<T>(B.ws, D, y, total, (T)P.theta, B.neg.template as<T>(), B.q.template as<T>(), s, sg, boxes);
+    batch_z<T>(B.q.template as<T>(), off, B.K, B.z.template as<double>(), s);
+    launch_attractive<T>(D, B.rows.template as<uint64_t>(), B.cols.template as<uint32_t>(), B.vals.template as<T>(), y,
+                         total, B.pos.template as<T>(), s);
+    batch_update<T>(D, y, B.pos.template as<T>(), B.neg.template as<T>(), B.uy.template as<T>(),
+                    B.gains.template as<T>(), total, B.job_of.template as<uint32_t>(), B.z.template as<double>(),
+                    B.lr.template as<T>(), B.mom.template as<T>(), s);
+    batch_box<T>(D, y, off, B.K, true, boxes, bits, s);
+  };
+  if (B.graph) {
+    cudaGraphExecDestroy(B.graph);
+    B.graph = nullptr;
+  }
+  int64_t graph_kernels = 0;
+  BHG_CUDA(cudaEventRecord(e0, s));
+  batch_box<T>(D, y, off, B.K, false, boxes, bits, s);
+  for (int64_t epoch = 0; epoch < P.epochs; ++epoch) {
+    if (epoch == 0) {
+      body();
+    } else {
+      if (!B.graph) {
+        cudaGraph_t g;
+        const long long before = g_launches.load();
+        BHG_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed));
+        body();
+        BHG_CUDA(cudaStreamEndCapture(s, &g));
+        graph_kernels = g_launches.load() - before;
+        g_launches.fetch_sub(graph_kernels);
+        BHG_CUDA(cudaGraphInstantiate(&B.graph, g, 0));
+        BHG_CUDA(cudaGraphDestroy(g));
+      }
+      BHG_CUDA(cudaGraphLaunch(B.graph, s));
+      g_launches.fetch_add(graph_kernels);
+    }
+    // epoch_tail (src/lib.rs:1162-1179), for every job at once
+    if (epoch == P.stop_lying_epoch && epoch != 0)
+      launch_scale<T>(B.vals.template as<T>(), B.nnz, T(1) / (T)P.early_exaggeration, s);
+    if (epoch == P.momentum_switch_epoch) {
+      batch_fill_kernel<T><<<(unsigned)std::max<int64_t>(1, ceil_div(B.K, 256)), 256, 0, s>>>(
+          B.mom.template as<T>(), B.K, (T)P.final_momentum);
+      BHG_LAUNCH_CHECK();
+    }
+  }
+  BHG_CUDA(cudaEventRecord(e1, s));
+  BHG_CUDA(cudaEventSynchronize(e1));
+  BHG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+  B.loop_ms = ms;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  B.fitted = true;
+}
+
+// KL of one job: its slice of the batch in a temporary single-fit handle.
+template <class T>
+double batch_kl(bhtsne_batch* b, int64_t j, bool quirk) {
+  BatchImpl<T>& B = bimpl<T>(b);
+  if (!B.fitted || j < 0 || j >= B.K) invalid("error: no fitted job with that index.");
+  cudaStream_t s = b->ctx->stream;
+  const int64_t n = B.off[j + 1] - B.off[j], nnz = B.nnz_off[j + 1] - B.nnz_off[j];
+  bhtsne_tsne t;
+  t.ctx = b->ctx;
+  t.dtype = b->dtype;
+  t.D = b->D;
+  t.n = n;
+  new_state<T>(&t);
+  std::unique_ptr<State<T>> hold(&st<T>(&t));
+  State<T>& S = *hold;
+  S.n = n;
+  S.D = b->D;
+  ensure_state<T>(&t);
+  S.rows.ensure((size_t)(n + 1) * 8);
+  S.cols.ensure((size_t)std::max<int64_t>(nnz, 1) * 4);
+  S.vals.ensure((size_t)std::max<int64_t>(nnz, 1) * sizeof(T));
+  batch_extract_csr(B.rows.template as<uint64_t>() + B.off[j], B.cols.template as<uint32_t>() + B.nnz_off[j], n, nnz,
+                    (uint64_t)B.nnz_off[j], (uint32_t)B.off[j], S.rows.template as<uint64_t>(),
+                    S.cols.template as<uint32_t>(), s);
+  if (nnz)
+    BHG_CUDA(cudaMemcpyAsync(S.vals.ptr, B.vals.template as<T>() + B.nnz_off[j], nnz * sizeof(T),
+                             cudaMemcpyDeviceToDevice, s));
+  S.y.ensure((size_t)n * b->D * sizeof(T));
+  BHG_CUDA(cudaMemcpyAsync(S.y.ptr, B.y.template as<T>() + B.off[j] * b->D, (size_t)n * b->D * sizeof(T),
+                           cudaMemcpyDeviceToDevice, s));
+  S.nnz = nnz;
+  S.has_sparse = true;
+  S.sparse_rows = n + 1;
+  t.fit = BHTSNE_METHOD_BARNES_HUT;
+  t.fit_theta = b->prm.theta;
+  double out = 0;
+  kl<T>(&t, quirk, &out);
+  return out;
+}
+
+}  // namespace
+
+extern "C" {
+
+void bhtsne_batch_params_default(bhtsne_batch_params* p) {
+  if (!p) return;
+  p->perplexity = 20.0;
+  p->epochs = 1000;
+  p->learning_rate = 0.0;
+  p->momentum = 0.5;
+  p->final_momentum = 0.8;
+  p->momentum_switch_epoch = 250;
+  p->stop_lying_epoch = 250;
+  p->early_exaggeration = 12.0;
+  p->theta = 0.5;
+  p->seed = 0x6268747336e65ULL;
+}
+
+int bhtsne_batch_new(bhtsne_ctx* ctx, int dtype, int32_t embed_dim, const bhtsne_batch_params* p, bhtsne_batch** out) {
+  if (!ctx || !out) return BHTSNE_EINVAL;
+  *out = nullptr;
+  if (dtype != BHTSNE_F32 && dtype != BHTSNE_F64) {
+    ctx->err = "error: dtype must be BHTSNE_F32 or BHTSNE_F64.";
+    return BHTSNE_EINVAL;
+  }
+  if (embed_dim < 2 || embed_dim > 3) {
+    ctx->err = "error: the GPU Barnes-Hut path covers D in {2, 3}.";
+    return BHTSNE_EINVAL;
+  }
+  bhtsne_batch* b = new bhtsne_batch();
+  b->ctx = ctx;
+  b->dtype = dtype;
+  b->D = embed_dim;
+  bhtsne_batch_params_default(&b->prm);
+  if (p) b->prm = *p;
+  if (dtype == BHTSNE_F32) b->impl = new BatchImpl<float>();
+  else b->impl = new BatchImpl<double>();
+  *out = b;
+  return BHTSNE_OK;
+}
+
+int bhtsne_batch_free(bhtsne_batch* b) {
+  if (!b) return BHTSNE_OK;
+  cudaSetDevice(b->ctx->device);
+  if (b->dtype == BHTSNE_F32) delete static_cast<BatchImpl<float>*>(b->impl);
+  else delete static_cast<BatchImpl<double>*>(b->impl);
+  delete b;
+  return BHTSNE_OK;
+}
+
+const char* bhtsne_batch_last_error(const bhtsne_batch* b) { return b ? b->err.c_str() : "null batch"; }
+
+int bhtsne_batch_add_euclidean(bhtsne_batch* b, const void* data, int64_t n, int32_t dim, int64_t* job) {
+  return guard_batch(b, [&] {
+    int64_t j = -1;
+    DISPATCH_DT(b->dtype, j = batch_add_euclidean<T>(b, data, n, dim));
+    if (job) *job = j;
+  });
+}
+
+int bhtsne_batch_add_with_neighbors(bhtsne_batch* b, const uint64_t* indices, const void* distances, int64_t n,
+                                    int64_t k, int64_t* job) {
+  return guard_batch(b, [&] {
+    int64_t j = -1;
+    DISPATCH_DT(b->dtype, j = batch_add_with_neighbors<T>(b, indices, distances, n, k));
+    if (job) *job = j;
+  });
+}
+
+int bhtsne_batch_initial_embedding(bhtsne_batch* b, int64_t job, const void* y) {
+  return guard_batch(b, [&] {
+    DISPATCH_DT(b->dtype, {
+      BatchImpl<T>& B = bimpl<T>(b);
+      if (job < 0 || job >= (int64_t)B.jobs.size() || !y) invalid("error: no job with that index.");
+      BatchJob<T>& J = *B.jobs[job];
+      J.init.assign((const T*)y, (const T*)y + J.n * b->D);
+      J.has_init = true;
+    });
+  });
+}
+
+int bhtsne_batch_fit(bhtsne_batch* b) {
+  return guard_batch(b, [&] { DISPATCH_DT(b->dtype, batch_fit<T>(b)); });
+}
+
+int64_t bhtsne_batch_jobs(const bhtsne_batch* b) {
+  if (!b) return -1;
+  if (b->dtype == BHTSNE_F32) return (int64_t)static_cast<BatchImpl<float>*>(b->impl)->jobs.size();
+  return (int64_t)static_cast<BatchImpl<double>*>(b->impl)->jobs.size();
+}
+
+int bhtsne_batch_embedding(bhtsne_batch* b, int64_t job, void* out) {
+  return guard_batch(b, [&] {
+    DISPATCH_DT(b->dtype, {
+      BatchImpl<T>& B = bimpl<T>(b);
+      if (!B.fitted || job < 0 || job >= B.K || !out) invalid("error: no fitted job with that index.");
+      const size_t bytes = (size_t)(B.off[job + 1] - B.off[job]) * b->D * sizeof(T);
+      BHG_CUDA(cudaMemcpyAsync(out, B.y.template as<T>() + B.off[job] * b->D, bytes, cudaMemcpyDeviceToHost,
+                               b->ctx->stream));
+      BHG_CUDA(cudaStreamSynchronize(b->ctx->stream));
+    });
+  });
+}
+
+int bhtsne_batch_kl_divergence(bhtsne_batch* b, int64_t job, int32_t quirk, double* out) {
+  return guard_batch(b, [&] {
+    double v = 0;
+    DISPATCH_DT(b->dtype, v = batch_kl<T>(b, job, quirk != 0));
+    if (out) *out = v;
+  });
+}
+
+int bhtsne_batch_timings(const bhtsne_batch* b, double* affinity_ms, double* loop_ms) {
+  if (!b) return BHTSNE_EINVAL;
+  double a = 0, l = 0;
+  if (b->dtype == BHTSNE_F32) {
+    a = static_cast<BatchImpl<float>*>(b->impl)->aff_ms;
+    l = static_cast<BatchImpl<float>*>(b->impl)->loop_ms;
+  } else {
+    a = static_cast<BatchImpl<double>*>(b->impl)->aff_ms;
+    l = static_cast<BatchImpl<double>*>(b->impl)->loop_ms;
+  }
+  if (affinity_ms) *affinity_ms = a;
+  if (loop_ms) *loop_ms = l;
+  return BHTSNE_OK;
 }
 
 }  // extern "C"

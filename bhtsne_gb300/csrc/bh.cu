@@ -303,43 +303,62 @@ __global__ void prefix_apply_kernel(const T* __restrict__ y, const uint32_t* __r
 // ---------------------------------------------------------------------------
 // Tree build.
 // ---------------------------------------------------------------------------
+__device__ __forceinline__ void seg_bounds(const Segs& sg, int64_t s, int64_t n, int64_t* lo, int64_t* hi) {
+  if (sg.job) {
+    const uint64_t j = sg.job[s];
+    *lo = sg.off[j];
+    *hi = sg.off[j + 1];
+  } else {
+    *lo = 0;
+    *hi = n;
+  }
+}
+
+__device__ __forceinline__ bool same_set(const Segs& sg, int64_t a, int64_t b) {
+  return !sg.job || sg.job[a] == sg.job[b];
+}
+
 template <int D>
-__global__ void tree_mark_kernel(const uint64_t* __restrict__ codes, int64_t n, uint32_t* __restrict__ mask) {
+__global__ void tree_mark_kernel(const uint64_t* __restrict__ codes, int64_t n, uint32_t* __restrict__ mask, Segs sg) {
   const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (s <= 0 || s >= n) return;
+  if (!same_set(sg, s - 1, s)) return;
   const uint64_t c0 = codes[s - 1], c1 = codes[s];
   if (c0 == c1) return;
   constexpr int B = MortonD<D>::BITS;
   const int l = boundary_level<D>(c0, c1);
-  int64_t a, e;
-  cell_range<D>(codes, n, c1, l, &a, &e);
+  int64_t lo, hi, a, e;
+  seg_bounds(sg, s, n, &lo, &hi);
+  cell_range_in<D>(codes, lo, hi, c1, l, &a, &e);
   const int sh1 = D * (B - l - 1);
   if ((c0 >> sh1) == (codes[a] >> sh1)) atomicOr(&mask[a], 1u << l);
 }
 
 __global__ void tree_count_kernel(const uint64_t* __restrict__ codes, int64_t n, const uint32_t* __restrict__ mask,
-                                  uint32_t* __restrict__ cnt) {
+                                  uint32_t* __restrict__ cnt, Segs sg) {
   const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= n) return;
-  const bool run_start = s == 0 || codes[s - 1] != codes[s];
+  const bool run_start = s == 0 || !same_set(sg, s - 1, s) || codes[s - 1] != codes[s];
   cnt[s] = (uint32_t)__popc(mask[s]) + (run_start ? 1u : 0u);
 }
 
 template <class T, int D>
 __global__ void tree_emit_kernel(const uint64_t* __restrict__ codes, int64_t n, const uint32_t* __restrict__ mask,
                                  const uint64_t* __restrict__ base, const T* __restrict__ ys,
-                                 const double* __restrict__ pre, const BoxParams<T>* __restrict__ prm,
-                                 TreeNodes<T, D> nodes) {
+                                 const double* __restrict__ pre, TreeNodes<T, D> nodes, Segs sg) {
   const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= n) return;
   constexpr int B = MortonD<D>::BITS;
   const uint64_t c1 = codes[s];
-  const bool run_start = s == 0 || codes[s - 1] != c1;
-  if (s > 0 && run_start) {
+  const bool set_start = s == 0 || !same_set(sg, s - 1, s);
+  const bool run_start = set_start || codes[s - 1] != c1;
+  int64_t lo, hi;
+  seg_bounds(sg, s, n, &lo, &hi);
+  if (!set_start && run_start) {
     const uint64_t c0 = codes[s - 1];
     const int l = boundary_level<D>(c0, c1);
     int64_t a, e;
-    cell_range<D>(codes, n, c1, l, &a, &e);
+    cell_range_in<D>(codes, lo, hi, c1, l, &a, &e);
     const int sh1 = D * (B - l - 1);
     if ((c0 >> sh1) == (codes[a] >> sh1)) {
       const uint32_t m = mask[a];
@@ -354,15 +373,15 @@ __global__ void tree_emit_kernel(const uint64_t* __restrict__ codes, int64_t n, 
   }
   if (run_start) {
     int64_t e = s + 1;
-    if (e < n && codes[e] == c1) {
-      // duplicate codes: find the run end
-      int64_t lo = e, hi = n;
-      while (lo < hi) {
-        const int64_t mid = (lo + hi) >> 1;
-        if (codes[mid] <= c1) lo = mid + 1;
-        else hi = mid;
+    if (e < hi && codes[e] == c1) {
+      // duplicate codes: find the run end within the set
+      int64_t a = e, b = hi;
+      while (a < b) {
+        const int64_t mid = (a + b) >> 1;
+        if (codes[mid] <= c1) a = mid + 1;
+        else b = mid;
       }
-      e = lo;
+      e = a;
     }
     const uint32_t m = mask[s];
     const int64_t idx = (int64_t)base[s] + __popc(m);
@@ -400,11 +419,13 @@ __global__ void __launch_bounds__(kThreads) bh_traverse_kernel(const T* __restri
                                                                int64_t max_nodes, const BoxParams<T>* __restrict__ prm,
                                                                T theta_sq, T* __restrict__ neg, T* __restrict__ qout,
                                                                double* __restrict__ zpart, unsigned* __restrict__ done,
-                                                               double* __restrict__ z_out) {
+                                                               double* __restrict__ z_out, Segs sg,
+                                                               const BoxParams<T>* __restrict__ boxes,
+                                                               const uint64_t* __restrict__ base) {
   __shared__ double sh[32];
   __shared__ bool last;
   __shared__ T hw2s[40];
-  if (threadIdx.x < 40) hw2s[threadIdx.x] = prm->hw2[threadIdx.x];
+  if (!sg.job && threadIdx.x < 40) hw2s[threadIdx.x] = prm->hw2[threadIdx.x];
   __syncthreads();
   nodes.hw2 = hw2s;
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -415,7 +436,16 @@ __global__ void __launch_bounds__(kThreads) bh_traverse_kernel(const T* __restri
 #pragma unroll
     for (int a = 0; a < D; ++a) qv[a] = y[pi * D + a];
     const uint64_t m_raw = *n_nodes_p;
-    const uint32_t M = (uint32_t)(m_raw < (uint64_t)max_nodes ? m_raw : (uint64_t)max_nodes);
+    uint32_t M = (uint32_t)(m_raw < (uint64_t)max_nodes ? m_raw : (uint64_t)max_nodes);
+    uint32_t root = 0;
+    if (sg.job) {
+      // this query's own tree: nodes [base[off[j]], base[off[j+1]])
+      const uint64_t j = sg.job[t];
+      root = (uint32_t)base[sg.off[j]];
+      const uint32_t end = (uint32_t)base[sg.off[j + 1]];
+      M = end < M ? end : M;
+      nodes.hw2 = boxes[j].hw2;
+    }
     T f[D];
 #pragma unroll
     for (int a = 0; a < D; ++a) f[a] = T(0);
@@ -423,17 +453,17 @@ __global__ void __launch_bounds__(kThreads) bh_traverse_kernel(const T* __restri
     // Software-pipelined walk: both possible successors of the current node
     // (i + 1 if it is opened, its skip target if it is summarised) are loaded
     // before the decision, so the next visit never waits on a dependent load.
-    uint32_t i = 0;
-    typename TreeNodes<T, D>::Raw cur = nodes.load(0);
+    uint32_t i = root;
+    typename TreeNodes<T, D>::Raw cur = nodes.load(root < M ? root : 0);
     while (i < M) {
       const uint32_t w = nodes.word(cur);
       const bool leaf = w == kLeafWord;
       const uint32_t sk_raw = leaf ? i + 1 : (w >> 5);
       // skip > i by construction; max() keeps the walk finite regardless.
       const uint32_t sk = sk_raw > i ? sk_raw : i + 1;
-      const uint32_t last = M - 1;
-      const typename TreeNodes<T, D>::Raw nxt_open = nodes.load(i + 1 < M ? i + 1 : last);
-      const typename TreeNodes<T, D>::Raw nxt_skip = leaf ? nxt_open : nodes.load(sk < M ? sk : last);
+      const uint32_t lastn = M - 1;
+      const typename TreeNodes<T, D>::Raw nxt_open = nodes.load(i + 1 < M ? i + 1 : lastn);
+      const typename TreeNodes<T, D>::Raw nxt_skip = leaf ? nxt_open : nodes.load(sk < M ? sk : lastn);
       T com[D], mass, r2;
       nodes.decode(cur, com, &mass, &r2);
       T disp[D];
@@ -553,6 +583,9 @@ static TreeNodes<T, D> nodes_of(BhWorkspace<T>& ws) {
 }
 
 template <class T, int D>
+static void build_from_sorted_impl(BhWorkspace<T>& ws, const T* y, int64_t n, const Segs& sg, cudaStream_t s);
+
+template <class T, int D>
 static void bh_build_impl(BhWorkspace<T>& ws, const T* y, int64_t n, cudaStream_t s) {
   constexpr int B = MortonD<D>::BITS;
   const unsigned g = (unsigned)ceil_div(n, kThreads);
@@ -562,6 +595,12 @@ static void bh_build_impl(BhWorkspace<T>& ws, const T* y, int64_t n, cudaStream_
   radix_sort_pairs<uint32_t>(ws.keys.template as<uint64_t>(), ws.perm.template as<uint32_t>(),
                              ws.keys_alt.template as<uint64_t>(), ws.perm_alt.template as<uint32_t>(), n, 0, D * B,
                              ws.sort_tmp, s);
+  build_from_sorted_impl<T, D>(ws, y, n, Segs(), s);
+}
+
+template <class T, int D>
+static void build_from_sorted_impl(BhWorkspace<T>& ws, const T* y, int64_t n, const Segs& sg, cudaStream_t s) {
+  const unsigned g = (unsigned)ceil_div(n, kThreads);
   const int64_t np = ceil_div(n, kPsTile);
   prefix_reduce_kernel<T, D><<<(unsigned)np, kPsThreads, 0, s>>>(y, ws.perm.template as<uint32_t>(), n,
                                                                   ws.pre_part.template as<double>());
@@ -573,16 +612,15 @@ static void bh_build_impl(BhWorkspace<T>& ws, const T* y, int64_t n, cudaStream_
                                                                  ws.ys.template as<T>(), ws.pre.template as<double>());
   BHG_LAUNCH_CHECK();
   BHG_CUDA(cudaMemsetAsync(ws.mask.ptr, 0, (size_t)n * 4, s));
-  tree_mark_kernel<D><<<g, kThreads, 0, s>>>(ws.keys.template as<uint64_t>(), n, ws.mask.template as<uint32_t>());
+  tree_mark_kernel<D><<<g, kThreads, 0, s>>>(ws.keys.template as<uint64_t>(), n, ws.mask.template as<uint32_t>(), sg);
   BHG_LAUNCH_CHECK();
   tree_count_kernel<<<g, kThreads, 0, s>>>(ws.keys.template as<uint64_t>(), n, ws.mask.template as<uint32_t>(),
-                                           ws.cnt.template as<uint32_t>());
+                                           ws.cnt.template as<uint32_t>(), sg);
   BHG_LAUNCH_CHECK();
   scan_u32_to_u64(ws.cnt.template as<uint32_t>(), ws.base.template as<uint64_t>(), n, ws.scan_tmp, s);
   tree_emit_kernel<T, D><<<g, kThreads, 0, s>>>(ws.keys.template as<uint64_t>(), n, ws.mask.template as<uint32_t>(),
                                                 ws.base.template as<uint64_t>(), ws.ys.template as<T>(),
-                                                ws.pre.template as<double>(), ws.params.template as<BoxParams<T>>(),
-                                                nodes_of<T, D>(ws));
+                                                ws.pre.template as<double>(), nodes_of<T, D>(ws), sg);
   BHG_LAUNCH_CHECK();
 }
 
@@ -596,7 +634,17 @@ void bh_build(BhWorkspace<T>& ws, int D, const T* y, int64_t n, cudaStream_t s) 
 }
 
 template <class T>
-void bh_traverse(BhWorkspace<T>& ws, int D, const T* y, int64_t n, T theta, T* neg, T* qout, cudaStream_t s) {
+void bh_build_from_sorted(BhWorkspace<T>& ws, int D, const T* y, int64_t n, const Segs& segs, cudaStream_t s) {
+  if (n <= 0) return;
+  if (n > kMaxTreePoints) throw Error(ST_EINVAL, "error: the GPU Barnes-Hut arena holds at most 2^26 - 1 points.");
+  if (D == 2) build_from_sorted_impl<T, 2>(ws, y, n, segs, s);
+  else if (D == 3) build_from_sorted_impl<T, 3>(ws, y, n, segs, s);
+  else throw Error(ST_EINVAL, "error: the GPU Barnes-Hut path covers D in {2, 3}.");
+}
+
+template <class T>
+void bh_traverse(BhWorkspace<T>& ws, int D, const T* y, int64_t n, T theta, T* neg, T* qout, cudaStream_t s,
+                 const Segs& segs, const BoxParams<T>* boxes) {
   if (n <= 0) {
     BHG_CUDA(cudaMemsetAsync(ws.zval.ptr, 0, sizeof(double), s));
     return;
@@ -607,11 +655,11 @@ void bh_traverse(BhWorkspace<T>& ws, int D, const T* y, int64_t n, T theta, T* n
   if (D == 2)
     bh_traverse_kernel<T, 2><<<g, kThreads, 0, s>>>(y, ws.perm.template as<uint32_t>(), n, nodes_of<T, 2>(ws), M, 2 * n, ws.params.template as<BoxParams<T>>(), theta_sq, neg,
                                                     qout, ws.zpart.template as<double>(), ws.zdone.template as<unsigned>(),
-                                                    ws.zval.template as<double>());
+                                                    ws.zval.template as<double>(), segs, boxes, ws.base.template as<uint64_t>());
   else
     bh_traverse_kernel<T, 3><<<g, kThreads, 0, s>>>(y, ws.perm.template as<uint32_t>(), n, nodes_of<T, 3>(ws), M, 2 * n, ws.params.template as<BoxParams<T>>(), theta_sq, neg,
                                                     qout, ws.zpart.template as<double>(), ws.zdone.template as<unsigned>(),
-                                                    ws.zval.template as<double>());
+                                                    ws.zval.template as<double>(), segs, boxes, ws.base.template as<uint64_t>());
   BHG_LAUNCH_CHECK();
 }
 
@@ -627,9 +675,12 @@ template void launch_recenter_bbox<double>(int, double*, int64_t, const double*,
                                            cudaStream_t);
 template void bh_build<float>(BhWorkspace<float>&, int, const float*, int64_t, cudaStream_t);
 template void bh_build<double>(BhWorkspace<double>&, int, const double*, int64_t, cudaStream_t);
-template void bh_traverse<float>(BhWorkspace<float>&, int, const float*, int64_t, float, float*, float*, cudaStream_t);
+template void bh_traverse<float>(BhWorkspace<float>&, int, const float*, int64_t, float, float*, float*, cudaStream_t,
+                                 const Segs&, const BoxParams<float>*);
 template void bh_traverse<double>(BhWorkspace<double>&, int, const double*, int64_t, double, double*, double*,
-                                  cudaStream_t);
+                                  cudaStream_t, const Segs&, const BoxParams<double>*);
+template void bh_build_from_sorted<float>(BhWorkspace<float>&, int, const float*, int64_t, const Segs&, cudaStream_t);
+template void bh_build_from_sorted<double>(BhWorkspace<double>&, int, const double*, int64_t, const Segs&, cudaStream_t);
 template int bh_bits<float>(int);
 template int bh_bits<double>(int);
 

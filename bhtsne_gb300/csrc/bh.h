@@ -133,6 +133,14 @@ struct BhWorkspace {
   uint64_t* node_count() const { return static_cast<uint64_t*>(base.ptr) + n; }
 };
 
+// Independent point sets laid out back to back (a batch of fits): job[s] is
+// the set of sorted position s and off[j]..off[j+1] the positions of set j.
+// Both null means one set spanning everything.
+struct Segs {
+  const uint64_t* job = nullptr;
+  const int64_t* off = nullptr;
+};
+
 // Recentres y by mean_sum/n when apply_mean, then writes BoxParams (bits = Morton
 // bits per axis for the tree's half-width table; any value for FIt-SNE).
 template <class T>
@@ -143,9 +151,17 @@ void launch_recenter_bbox(int D, T* y, int64_t n, const double* mean_sum, bool a
 template <class T>
 void bh_build(BhWorkspace<T>& ws, int D, const T* y, int64_t n, cudaStream_t s);
 
-// Repulsive forces (neg, original order), optional per-point q, and Z into ws.zval.
+// Tree build from codes already sorted into ws.keys with the point order in
+// ws.perm (one forest of independent trees when segs are given).
 template <class T>
-void bh_traverse(BhWorkspace<T>& ws, int D, const T* y, int64_t n, T theta, T* neg, T* qout, cudaStream_t s);
+void bh_build_from_sorted(BhWorkspace<T>& ws, int D, const T* y, int64_t n, const Segs& segs, cudaStream_t s);
+
+// Repulsive forces (neg, original order), optional per-point q, and Z into
+// ws.zval. With segs, each query walks only its own set's tree, whose level
+// half widths come from boxes[set].
+template <class T>
+void bh_traverse(BhWorkspace<T>& ws, int D, const T* y, int64_t n, T theta, T* neg, T* qout, cudaStream_t s,
+                 const Segs& segs = Segs(), const BoxParams<T>* boxes = nullptr);
 
 template <class T>
 int bh_bits(int D);

@@ -185,6 +185,42 @@ int bhtsne_bh_repulsion_noalloc(const float* y, int64_t n, double theta, float* 
 int bhtsne_update(bhtsne_ctx* ctx, int dtype, int32_t embed_dim, void* y, const void* pos, const void* neg, void* uy,
                   void* gains, int64_t n, double learning_rate, double momentum, double inverse_z);
 
+/* ---- batches of independent fits (no reference counterpart) --------------- */
+/* Many independent Barnes-Hut embeddings of uneven size, fitted together: every
+ * stage of an epoch (box, Morton sort, tree, traversal, Z, attractive pass,
+ * update) runs once for the whole batch. Each job follows the reference's
+ * schedule (defaults of tSNE::new, src/lib.rs:241-266) with its own learning
+ * rate max(n_j / exaggeration / 4, 50) and its own Z, mean and tree. */
+typedef struct bhtsne_batch bhtsne_batch;
+typedef struct bhtsne_batch_params {
+  double perplexity;             /* 20 */
+  int64_t epochs;                /* 1000 */
+  double learning_rate;          /* <= 0: automatic per job */
+  double momentum;               /* 0.5 */
+  double final_momentum;         /* 0.8 */
+  int64_t momentum_switch_epoch; /* 250 */
+  int64_t stop_lying_epoch;      /* 250 */
+  double early_exaggeration;     /* 12 */
+  double theta;                  /* 0.5 */
+  uint64_t seed;                 /* job j's random_init is seeded with seed + j */
+} bhtsne_batch_params;
+void bhtsne_batch_params_default(bhtsne_batch_params* p);
+int bhtsne_batch_new(bhtsne_ctx* ctx, int dtype, int32_t embed_dim, const bhtsne_batch_params* p, bhtsne_batch** out);
+int bhtsne_batch_free(bhtsne_batch* b);
+const char* bhtsne_batch_last_error(const bhtsne_batch* b);
+/* Adds a job from dense data (Euclidean kNN on the device) or from a kNN table;
+ * its affinities are built immediately. *job receives the job index. */
+int bhtsne_batch_add_euclidean(bhtsne_batch* b, const void* data, int64_t n, int32_t dim, int64_t* job);
+int bhtsne_batch_add_with_neighbors(bhtsne_batch* b, const uint64_t* indices, const void* distances, int64_t n,
+                                    int64_t k, int64_t* job);
+int bhtsne_batch_initial_embedding(bhtsne_batch* b, int64_t job, const void* y);
+/* Runs params.epochs Barnes-Hut epochs for every job. */
+int bhtsne_batch_fit(bhtsne_batch* b);
+int64_t bhtsne_batch_jobs(const bhtsne_batch* b);
+int bhtsne_batch_embedding(bhtsne_batch* b, int64_t job, void* out);
+int bhtsne_batch_kl_divergence(bhtsne_batch* b, int64_t job, int32_t quirk, double* out);
+int bhtsne_batch_timings(const bhtsne_batch* b, double* affinity_ms, double* loop_ms);
+
 #ifdef __cplusplus
 }
 #endif
