@@ -169,6 +169,9 @@ def run_ours(args):
     t.barnes_hut(theta)  # kNN + affinities + seeding, no epochs
     setup_s = time.time() - t0
     tm = t.timings()
+    # burn-in past the early-exaggeration phase (epochs 0..250), so that the
+    # timed epochs see the expanded embedding of a typical fit; untimed
+    t.advance(args.burn_in)
     t.advance(args.warmup)
     launches0 = ctx.lib.bhtsne_launch_count()
     barrier_and_max(0.0, ws)
@@ -226,6 +229,10 @@ def run_ours(args):
            "note": "with_affinities(host CSR) + barnes_hut(epochs=steps) + embedding(); affinity "
                    "normalisation, seeding and all copies inside the timed region"}
 
+    batched = None
+    if args.batch_jobs > 0:
+        batched = run_batched(args, ctx)
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         cpu = cpu_baseline_sample(aff, emb.reshape(n, 2), args.cpu_epochs)
@@ -237,6 +244,7 @@ def run_ours(args):
         "config": {"workload": "bh2d_1M_d128", "n_points": n, "input_dim": 128, "clusters": 100,
                    "perplexity": perp, "k": 90, "theta": theta, "embed_dim": 2, "nnz": nnz,
                    "l2": "inputs larger than L2 (CSR P of %.2f GB)" % ((8 * nnz + 8 * n) / 1e9),
+                   "burn_in_epochs": args.burn_in,
                    "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"},
         "e2e": e2e,
         "roofline": roofline,
@@ -247,10 +255,75 @@ def run_ours(args):
         "gpu_launches": int(launches),
         "clocks": clk.summary(),
     }
+    if batched:
+        out["batched"] = batched
     if cpu:
         out["cpu_baseline"] = cpu
     if rank == 0:
         print(json.dumps(out))
+
+
+def make_batch_workload(jobs=512, dim=32, seed=2024):
+    """Per-job N log-uniform in [500, 50000]; each job a Gaussian mixture of
+    5-20 equal-weight unit-variance components with centres ~ N(0, 10^2 I)."""
+    rng = np.random.default_rng(seed)
+    sizes = np.exp(rng.uniform(np.log(500), np.log(50000), size=jobs)).astype(int)
+    data = []
+    for n in sizes:
+        c = int(rng.integers(5, 21))
+        centres = rng.normal(0.0, 10.0, size=(c, dim)).astype(np.float32)
+        lab = rng.integers(0, c, size=n)
+        data.append(np.ascontiguousarray(centres[lab] + rng.standard_normal(size=(n, dim), dtype=np.float32)))
+    return data
+
+
+def run_batched(args, ctx):
+    """512 independent embeddings: one bhtsne_batch (segmented kNN/affinities,
+    lockstep epochs with per-job trees, one graph per epoch) against the same
+    512 run one at a time through the plain builder. Both arms start from host
+    arrays and end with every embedding back on the host."""
+    import bhtsne_gb300 as bg
+    data = make_batch_workload(args.batch_jobs)
+    E, perp, theta = args.batch_epochs, 30.0, 0.5
+    w0 = time.perf_counter()
+    b = bg.Batch(perplexity=perp, epochs=E, theta=theta, seed=11, ctx=ctx)
+    for X in data:
+        b.add(X)
+    b.fit()
+    embs = [b.embedding(j) for j in range(len(data))]
+    batched_s = time.perf_counter() - w0
+    aff_ms, loop_ms = b.timings()
+    kl_b = [b.kl_divergence(j) for j in range(len(data))]
+    del embs
+    b.close()
+    lat, kl_p = [], []
+    w0 = time.perf_counter()
+    for j, X in enumerate(data):
+        t = bg.TSNE(X, ctx=ctx).perplexity(perp).epochs(E).random_seed(11 + j)
+        t.barnes_hut(theta)
+        t.embedding()
+        lat.append(time.perf_counter() - w0)
+        kl_p.append(t.kl_divergence())
+        t.close()
+    plain_s = time.perf_counter() - w0
+    gap = np.abs(np.array(kl_b) - np.array(kl_p)) / np.abs(np.array(kl_p))
+    J = len(data)
+    return {
+        "workload": f"{J} jobs, N log-uniform [500, 50000] (total {sum(len(x) for x in data)} points), input dim 32, "
+                    f"5-20 component mixtures, perplexity {perp}, BH theta {theta}, 2-D, {E} epochs",
+        "jobs_per_s": round(J / batched_s, 3), "plain_jobs_per_s": round(J / plain_s, 3),
+        "speedup_vs_plain": round(plain_s / batched_s, 3),
+        "batched_s": round(batched_s, 3), "plain_s": round(plain_s, 3),
+        "batched_affinity_ms": round(aff_ms, 1), "batched_epoch_loop_ms": round(loop_ms, 1),
+        "latency_s": {"batched_p50": round(batched_s, 3), "batched_p99": round(batched_s, 3),
+                      "plain_p50": round(float(np.percentile(lat, 50)), 3),
+                      "plain_p99": round(float(np.percentile(lat, 99)), 3),
+                      "note": "all jobs submitted at t=0; lockstep batch returns every job at the end"},
+        "kl_gap": {"mean": round(float(gap.mean()), 5), "p99": round(float(np.percentile(gap, 99)), 5),
+                   "max": round(float(gap.max()), 5),
+                   "aggregate": round(abs(sum(kl_b) - sum(kl_p)) / abs(sum(kl_p)), 6),
+                   "within_1pct": int((gap <= 0.01).sum())},
+    }
 
 
 def cpu_baseline_sample(aff, y0, epochs):
@@ -319,7 +392,10 @@ def main():
     ap.add_argument("--n", type=int, default=1_000_000)
     ap.add_argument("--seed", type=int, default=1003)
     ap.add_argument("--cpu-epochs", type=int, default=3)
+    ap.add_argument("--burn-in", type=int, default=250, help="untimed epochs before the warm-up")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--batch-jobs", type=int, default=512, help="batched-fit comparison (0 to skip)")
+    ap.add_argument("--batch-epochs", type=int, default=500)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

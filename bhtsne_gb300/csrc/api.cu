@@ -9,6 +9,7 @@
 // for the optional per-epoch callback snapshot.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <functional>
@@ -1184,12 +1185,25 @@ struct bhtsne_batch {
 
 namespace {
 
+// Affinities of jobs prepared together: one block-diagonal CSR over their
+// rows in job order.
+template <class T>
+struct BatchGroup {
+  DevBuf rows, cols, vals;
+  std::vector<uint64_t> rows_h;  // host copy of the row offsets
+};
+
 template <class T>
 struct BatchJob {
-  int64_t n = 0, nnz = 0;
-  DevBuf rows, cols, vals;
+  int64_t n = 0;
+  int kind = 0;  // 0: dense Euclidean data, 1: kNN table
+  int32_t dim = 0;
+  int64_t k = 0;
+  DevBuf in_a, in_b;  // data, or (u32 indices, T distances) until prepared
   bool has_init = false;
   std::vector<T> init;
+  std::shared_ptr<BatchGroup<T>> group;
+  int64_t goff = 0;  // first row of this job in its group
 };
 
 template <class T>
@@ -1199,7 +1213,7 @@ struct BatchImpl {
   int64_t total = 0, nnz = 0;
   std::vector<int64_t> off, nnz_off;
   DevBuf d_off, job_of, rows, cols, vals, y, uy, gains, pos, neg, q, z, lr, mom, boxes, codes, jobkey, jobkey_alt;
-  DevBuf tmp, sumtmp, kidx, kdist, kp, xin;
+  DevBuf tmp, kidx, kdist, kp, xin, g_off, g_of, d_nnz_off;
   BhWorkspace<T> ws;
   SymWorkspace<T> sym;
   KnnWorkspace knn;
@@ -1232,25 +1246,6 @@ BatchImpl<T>& bimpl(bhtsne_batch* b) {
   return *static_cast<BatchImpl<T>*>(b->impl);
 }
 
-// Affinities of one job from a device kNN table (search_beta + symmetrize).
-template <class T>
-void batch_job_affinities(bhtsne_batch* b, BatchJob<T>& job, int64_t k) {
-  BatchImpl<T>& B = bimpl<T>(b);
-  cudaStream_t s = b->ctx->stream;
-  const int64_t n = job.n;
-  B.kp.ensure((size_t)n * k * sizeof(T));
-  const T perp = (T)b->prm.perplexity;
-  launch_search_beta<T>(B.kdist.template as<T>(), n, k, perp, B.kp.template as<T>(), nullptr, s);
-  const int64_t nnz = symmetrize<T>(B.kidx.template as<uint32_t>(), B.kp.template as<T>(), n, (int)k, B.sym, s);
-  job.rows.ensure((size_t)(n + 1) * 8);
-  job.cols.ensure((size_t)std::max<int64_t>(nnz, 1) * 4);
-  job.vals.ensure((size_t)std::max<int64_t>(nnz, 1) * sizeof(T));
-  symmetrize_finish<T>(B.sym, n, nnz, job.rows.template as<uint64_t>(), job.cols.template as<uint32_t>(),
-                       job.vals.template as<T>(), s);
-  BHG_CUDA(cudaStreamSynchronize(s));
-  job.nnz = nnz;
-}
-
 void batch_check_job(const bhtsne_batch* b, int64_t n) {
   const double perp = b->prm.perplexity;
   const int64_t as_usize = perp > 0 ? (int64_t)perp : 0;
@@ -1272,10 +1267,11 @@ int64_t batch_add_with_neighbors(bhtsne_batch* b, const uint64_t* idx, const voi
   cudaStream_t s = b->ctx->stream;
   auto job = std::make_unique<BatchJob<T>>();
   job->n = n;
-  B.kidx.ensure((size_t)n * k * 4);
-  BHG_CUDA(cudaMemcpyAsync(B.kidx.ptr, idx32.data(), (size_t)n * k * 4, cudaMemcpyHostToDevice, s));
-  upload<T>(B.kdist, dist, (size_t)n * k * sizeof(T), s);
-  batch_job_affinities<T>(b, *job, k);
+  job->kind = 1;
+  job->k = k;
+  upload<T>(job->in_a, idx32.data(), (size_t)n * k * 4, s);
+  upload<T>(job->in_b, dist, (size_t)n * k * sizeof(T), s);
+  BHG_CUDA(cudaStreamSynchronize(s));
   B.jobs.push_back(std::move(job));
   B.fitted = false;
   return (int64_t)B.jobs.size() - 1;
@@ -1287,18 +1283,90 @@ int64_t batch_add_euclidean(bhtsne_batch* b, const void* data, int64_t n, int32_
   batch_check_job(b, n);
   if (!data || dim <= 0) invalid("error: data must be a non-empty n_samples x dim array.");
   cudaStream_t s = b->ctx->stream;
-  const int64_t k = (int64_t)((T)3.0 * (T)b->prm.perplexity);
   auto job = std::make_unique<BatchJob<T>>();
   job->n = n;
-  upload<T>(B.xin, data, (size_t)n * dim * sizeof(T), s);
-  B.kidx.ensure((size_t)n * k * 4);
-  B.kdist.ensure((size_t)n * k * sizeof(T));
-  knn_euclidean<T>(B.xin.template as<T>(), n, dim, (int)k, B.kidx.template as<uint32_t>(), B.kdist.template as<T>(),
-                   B.knn, s);
-  batch_job_affinities<T>(b, *job, k);
+  job->kind = 0;
+  job->dim = dim;
+  job->k = (int64_t)((T)3.0 * (T)b->prm.perplexity);
+  upload<T>(job->in_a, data, (size_t)n * dim * sizeof(T), s);
+  BHG_CUDA(cudaStreamSynchronize(s));
   B.jobs.push_back(std::move(job));
   B.fitted = false;
   return (int64_t)B.jobs.size() - 1;
+}
+
+// Affinities of every job not yet prepared, one group per (input kind, dim or
+// k): segmented kNN over the group's concatenated rows (Euclidean jobs), then
+// search_beta and symmetrize once over the group (build_affinities,
+// src/lib.rs:1061-1127, for every job at once; the block-diagonal structure
+// keeps each job's rows, columns and values those of its own fit).
+template <class T>
+void batch_prepare(bhtsne_batch* b) {
+  BatchImpl<T>& B = bimpl<T>(b);
+  cudaStream_t s = b->ctx->stream;
+  std::vector<std::pair<std::pair<int, int64_t>, std::vector<int>>> groups;
+  for (int j = 0; j < (int)B.jobs.size(); ++j) {
+    const BatchJob<T>& J = *B.jobs[j];
+    if (J.group) continue;
+    const std::pair<int, int64_t> key(J.kind, J.kind == 0 ? (int64_t)J.dim * 4096 + J.k : J.k);
+    auto it = std::find_if(groups.begin(), groups.end(), [&](const auto& g) { return g.first == key; });
+    if (it == groups.end()) groups.push_back({key, {j}});
+    else it->second.push_back(j);
+  }
+  for (auto& gr : groups) {
+    const std::vector<int>& js = gr.second;
+    const int G = (int)js.size();
+    const BatchJob<T>& J0 = *B.jobs[js[0]];
+    const int64_t k = J0.k;
+    std::vector<int64_t> goff(G + 1, 0);
+    for (int g = 0; g < G; ++g) goff[g + 1] = goff[g] + B.jobs[js[g]]->n;
+    const int64_t tot = goff[G];
+    upload<T>(B.g_off, goff.data(), goff.size() * 8, s);
+    uint32_t* gof = static_cast<uint32_t*>(B.g_of.ensure((size_t)tot * 4));
+    for (int g = 0; g < G; ++g) batch_fill_job(gof, goff[g], goff[g + 1], (uint32_t)g, s);
+    uint32_t* kidx = static_cast<uint32_t*>(B.kidx.ensure((size_t)tot * k * 4));
+    T* kdist = static_cast<T*>(B.kdist.ensure((size_t)tot * k * sizeof(T)));
+    if (J0.kind == 0) {
+      const int dim = J0.dim;
+      T* X = static_cast<T*>(B.xin.ensure((size_t)tot * dim * sizeof(T)));
+      for (int g = 0; g < G; ++g)
+        BHG_CUDA(cudaMemcpyAsync(X + goff[g] * dim, B.jobs[js[g]]->in_a.ptr, (size_t)B.jobs[js[g]]->n * dim * sizeof(T),
+                                 cudaMemcpyDeviceToDevice, s));
+      knn_euclidean_segmented<T>(X, tot, dim, (int)k, goff, B.g_off.template as<int64_t>(), gof, kidx, kdist, B.knn, s);
+      B.xin.release();
+      B.knn.release();
+    } else {
+      for (int g = 0; g < G; ++g) {
+        const BatchJob<T>& J = *B.jobs[js[g]];
+        batch_offset_indices(J.in_a.template as<uint32_t>(), J.n * k, (uint32_t)goff[g], kidx + goff[g] * k, s);
+        BHG_CUDA(cudaMemcpyAsync(kdist + goff[g] * k, J.in_b.ptr, (size_t)J.n * k * sizeof(T), cudaMemcpyDeviceToDevice,
+                                 s));
+      }
+    }
+    B.kp.ensure((size_t)tot * k * sizeof(T));
+    launch_search_beta<T>(kdist, tot, k, (T)b->prm.perplexity, B.kp.template as<T>(), nullptr, s);
+    const int64_t nnz = symmetrize<T>(kidx, B.kp.template as<T>(), tot, (int)k, B.sym, s);
+    auto grp = std::make_shared<BatchGroup<T>>();
+    grp->rows.ensure((size_t)(tot + 1) * 8);
+    grp->cols.ensure((size_t)std::max<int64_t>(nnz, 1) * 4);
+    grp->vals.ensure((size_t)std::max<int64_t>(nnz, 1) * sizeof(T));
+    symmetrize_finish<T>(B.sym, tot, nnz, grp->rows.template as<uint64_t>(), grp->cols.template as<uint32_t>(),
+                         grp->vals.template as<T>(), s);
+    grp->rows_h.resize(tot + 1);
+    BHG_CUDA(cudaMemcpyAsync(grp->rows_h.data(), grp->rows.ptr, (size_t)(tot + 1) * 8, cudaMemcpyDeviceToHost, s));
+    BHG_CUDA(cudaStreamSynchronize(s));
+    B.sym.release();
+    for (int g = 0; g < G; ++g) {
+      BatchJob<T>& J = *B.jobs[js[g]];
+      J.group = grp;
+      J.goff = goff[g];
+      J.in_a.release();
+      J.in_b.release();
+    }
+  }
+  B.kidx.release();
+  B.kdist.release();
+  B.kp.release();
 }
 
 template <class T>
@@ -1317,46 +1385,44 @@ void batch_fit(bhtsne_batch* b) {
   if (!(P.theta > 0))
     invalid("error: theta value must be greater than 0.0.\n            A value of 0.0 corresponds to using the exact "
             "version of the algorithm.");
-  B.K = (int)B.jobs.size();
-  B.off.assign(B.K + 1, 0);
-  B.nnz_off.assign(B.K + 1, 0);
-  for (int j = 0; j < B.K; ++j) {
-    B.off[j + 1] = B.off[j] + B.jobs[j]->n;
-    B.nnz_off[j + 1] = B.nnz_off[j] + B.jobs[j]->nnz;
-  }
-  B.total = B.off[B.K];
-  B.nnz = B.nnz_off[B.K];
-  const int64_t total = B.total;
   cudaEvent_t e0, e1;
   BHG_CUDA(cudaEventCreate(&e0));
   BHG_CUDA(cudaEventCreate(&e1));
   BHG_CUDA(cudaEventRecord(e0, s));
-  // block-diagonal CSR
+  batch_prepare<T>(b);
+  B.K = (int)B.jobs.size();
+  B.off.assign(B.K + 1, 0);
+  B.nnz_off.assign(B.K + 1, 0);
+  for (int j = 0; j < B.K; ++j) {
+    const BatchJob<T>& J = *B.jobs[j];
+    B.off[j + 1] = B.off[j] + J.n;
+    B.nnz_off[j + 1] = B.nnz_off[j] + (int64_t)(J.group->rows_h[J.goff + J.n] - J.group->rows_h[J.goff]);
+  }
+  B.total = B.off[B.K];
+  B.nnz = B.nnz_off[B.K];
+  const int64_t total = B.total;
+  // block-diagonal CSR of the whole batch, rows and columns renumbered from
+  // each job's place in its group to its place in the batch
   B.rows.ensure((size_t)(total + 1) * 8);
   B.cols.ensure((size_t)std::max<int64_t>(B.nnz, 1) * 4);
   B.vals.ensure((size_t)std::max<int64_t>(B.nnz, 1) * sizeof(T));
   B.job_of.ensure((size_t)total * 4);
   for (int j = 0; j < B.K; ++j) {
-    BatchJob<T>& J = *B.jobs[j];
-    batch_append_csr(J.rows.template as<uint64_t>(), J.cols.template as<uint32_t>(), J.n, J.nnz,
-                     (uint64_t)B.nnz_off[j], (uint32_t)B.off[j], B.rows.template as<uint64_t>() + B.off[j],
-                     B.cols.template as<uint32_t>() + B.nnz_off[j], s);
-    if (J.nnz)
-      BHG_CUDA(cudaMemcpyAsync(B.vals.template as<T>() + B.nnz_off[j], J.vals.ptr, J.nnz * sizeof(T),
-                               cudaMemcpyDeviceToDevice, s));
-    // normalize_p_values per job (src/tsne/mod.rs:284-293), then stop_lying if disabled
-    double* sum = static_cast<double*>(B.sumtmp.ensure(64));
-    launch_normalize<T>(B.vals.template as<T>() + B.nnz_off[j], J.nnz, (T)P.early_exaggeration, sum, B.tmp, s);
-    if (P.stop_lying_epoch == 0)
-      launch_scale<T>(B.vals.template as<T>() + B.nnz_off[j], J.nnz, T(1) / (T)P.early_exaggeration, s);
+    const BatchJob<T>& J = *B.jobs[j];
+    const uint64_t gs = J.group->rows_h[J.goff];
+    const int64_t nnz_j = B.nnz_off[j + 1] - B.nnz_off[j];
+    batch_append_csr(J.group->rows.template as<uint64_t>() + J.goff, J.group->cols.template as<uint32_t>() + gs, J.n,
+                     nnz_j, (uint64_t)B.nnz_off[j] - gs, (uint32_t)(B.off[j] - J.goff),
+                     B.rows.template as<uint64_t>() + B.off[j], B.cols.template as<uint32_t>() + B.nnz_off[j], s);
+    if (nnz_j)
+      BHG_CUDA(cudaMemcpyAsync(B.vals.template as<T>() + B.nnz_off[j], J.group->vals.template as<T>() + gs,
+                               nnz_j * sizeof(T), cudaMemcpyDeviceToDevice, s));
     batch_fill_job(B.job_of.template as<uint32_t>(), B.off[j], B.off[j + 1], (uint32_t)j, s);
   }
-  BHG_CUDA(cudaStreamSynchronize(s));
-  for (auto& J : B.jobs) {
-    J->rows.release();
-    J->cols.release();
-    J->vals.release();
-  }
+  // normalize_p_values per job (src/tsne/mod.rs:284-293), then stop_lying if disabled
+  upload<T>(B.d_nnz_off, B.nnz_off.data(), B.nnz_off.size() * 8, s);
+  batch_normalize<T>(B.vals.template as<T>(), B.d_nnz_off.template as<int64_t>(), B.K, (T)P.early_exaggeration,
+                     P.stop_lying_epoch == 0, s);
   upload<T>(B.d_off, B.off.data(), B.off.size() * 8, s);
   // seeds, velocity, gains, per-job learning rate and momentum
   std::vector<T> yh((size_t)total * D);

@@ -197,6 +197,35 @@ __global__ void sub_cols_kernel(const uint32_t* __restrict__ cols, int64_t nnz, 
     out[e] = cols[e] - sub;
 }
 
+// normalize_p_values per job: p *= exaggeration / (sum + eps) in T, the sum in
+// FP64 over the job's slice; then p *= 1 / exaggeration when lying is off.
+template <class T>
+__global__ void batch_normalize_kernel(T* __restrict__ v, const int64_t* __restrict__ nnz_off, T exaggeration,
+                                       int unexaggerate) {
+  __shared__ double sh[32];
+  __shared__ double total;
+  const int j = blockIdx.x;
+  const int64_t lo = nnz_off[j], hi = nnz_off[j + 1];
+  double s = 0.0;
+  for (int64_t e = lo + threadIdx.x; e < hi; e += blockDim.x) s += (double)v[e];
+  s = block_sum(s, sh);
+  if (threadIdx.x == 0) total = s;
+  __syncthreads();
+  const T scale = exaggeration / ((T)total + Lim<T>::eps());
+  const T un = T(1) / exaggeration;
+  for (int64_t e = lo + threadIdx.x; e < hi; e += blockDim.x) {
+    T x = v[e] * scale;
+    if (unexaggerate) x *= un;
+    v[e] = x;
+  }
+}
+
+__global__ void offset_u32_kernel(const uint32_t* __restrict__ in, int64_t count, uint32_t add,
+                                  uint32_t* __restrict__ out) {
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < count; e += (int64_t)gridDim.x * blockDim.x)
+    out[e] = in[e] + add;
+}
+
 __global__ void fill_job_kernel(uint32_t* __restrict__ job_of, int64_t lo, int64_t hi, uint32_t j) {
   const int64_t i = lo + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < hi) job_of[i] = j;
@@ -291,6 +320,19 @@ void batch_extract_csr(const uint64_t* rows, const uint32_t* cols, int64_t n, in
   }
 }
 
+template <class T>
+void batch_normalize(T* vals, const int64_t* nnz_off, int K, T exaggeration, bool unexaggerate, cudaStream_t s) {
+  if (K <= 0) return;
+  batch_normalize_kernel<T><<<K, 512, 0, s>>>(vals, nnz_off, exaggeration, unexaggerate ? 1 : 0);
+  BHG_LAUNCH_CHECK();
+}
+
+void batch_offset_indices(const uint32_t* in, int64_t count, uint32_t add, uint32_t* out, cudaStream_t s) {
+  if (count <= 0) return;
+  offset_u32_kernel<<<(unsigned)std::min<int64_t>(ceil_div(count, 256), 8 * 152), 256, 0, s>>>(in, count, add, out);
+  BHG_LAUNCH_CHECK();
+}
+
 void batch_fill_job(uint32_t* job_of, int64_t lo, int64_t hi, uint32_t j, cudaStream_t s) {
   if (hi <= lo) return;
   fill_job_kernel<<<(unsigned)ceil_div(hi - lo, 256), 256, 0, s>>>(job_of, lo, hi, j);
@@ -303,6 +345,7 @@ void batch_fill_job(uint32_t* job_of, int64_t lo, int64_t hi, uint32_t j, cudaSt
                                         const BoxParams<T>*, BhWorkspace<T>&, DevBuf&, DevBuf&, DevBuf&,             \
                                         cudaStream_t);                                                               \
   template void batch_z<T>(const T*, const int64_t*, int, double*, cudaStream_t);                                    \
+  template void batch_normalize<T>(T*, const int64_t*, int, T, bool, cudaStream_t);                                  \
   template void batch_update<T>(int, T*, const T*, const T*, T*, T*, int64_t, const uint32_t*, const double*,        \
                                 const T*, const T*, cudaStream_t);
 BHG_INST(float)

@@ -32,6 +32,11 @@ void batch_append_csr(const uint64_t* rows, const uint32_t* cols, int64_t n, int
                       uint32_t col_add, uint64_t* rows_out, uint32_t* cols_out, cudaStream_t s);
 void batch_extract_csr(const uint64_t* rows, const uint32_t* cols, int64_t n, int64_t nnz, uint64_t row_sub,
                        uint32_t col_sub, uint64_t* rows_out, uint32_t* cols_out, cudaStream_t s);
+// normalize_p_values of every job (job j's values are nnz_off[j]..nnz_off[j+1]).
+template <class T>
+void batch_normalize(T* vals, const int64_t* nnz_off, int K, T exaggeration, bool unexaggerate, cudaStream_t s);
+// out[e] = in[e] + add (kNN indices moved to a job's place in a group).
+void batch_offset_indices(const uint32_t* in, int64_t count, uint32_t add, uint32_t* out, cudaStream_t s);
 void batch_fill_job(uint32_t* job_of, int64_t lo, int64_t hi, uint32_t j, cudaStream_t s);
 
 }  // namespace bhg

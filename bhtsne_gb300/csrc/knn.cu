@@ -110,12 +110,20 @@ __device__ void warp_insert(V* lv, uint32_t* li, int* len_p, int cap, V v, uint3
 // answer. Queries are rows q0.. of X, or the rows listed in `qrows`.
 //
 // dynamic shared layout: Qs[dim][QB] | Cs[DK][CB] | S[QB][CB+1] | lv[QB][C] | li[QB][C] | len[QB] | qn[QB]
+//
+// Segmented form (blk_q0 != nullptr, candidate pass only): X holds many
+// independent point sets back to back, set j owning rows seg_off[j]..
+// seg_off[j+1]; block b takes the queries blk_q0[b].. of set blk_job[b] and
+// scans that set's rows only. Indices stay global.
 template <int C, bool EXACT>
 __global__ void __launch_bounds__(kThreads, 1) knn_tile_kernel(const float* __restrict__ X, int64_t n, int dim,
                                                                const float* __restrict__ norms,
                                                                const uint32_t* __restrict__ qrows, int64_t nq, int cap,
                                                                uint32_t* __restrict__ out_idx,
-                                                               float* __restrict__ out_val) {
+                                                               float* __restrict__ out_val,
+                                                               const int64_t* __restrict__ blk_q0 = nullptr,
+                                                               const int32_t* __restrict__ blk_job = nullptr,
+                                                               const int64_t* __restrict__ seg_off = nullptr) {
   extern __shared__ __align__(16) unsigned char smem[];
   float* Qs = reinterpret_cast<float*>(smem);
   float* Cs = Qs + (size_t)dim * QB;
@@ -128,10 +136,17 @@ __global__ void __launch_bounds__(kThreads, 1) knn_tile_kernel(const float* __re
 
   const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
   const int tq = tid >> 4, tc = tid & 15;
-  const int64_t q0 = (int64_t)blockIdx.x * QB;
+  int64_t q0 = (int64_t)blockIdx.x * QB, lo = 0, hi = n;
+  if (blk_q0) {
+    const int jb = blk_job[blockIdx.x];
+    q0 = blk_q0[blockIdx.x];
+    lo = seg_off[jb];
+    hi = seg_off[jb + 1];
+  }
   if (tid < QB) {
     const int64_t r = q0 + tid;
-    qidx[tid] = r < nq ? (qrows ? (int64_t)qrows[r] : r) : -1;
+    if (blk_q0) qidx[tid] = r < hi ? r : -1;
+    else qidx[tid] = r < nq ? (qrows ? (int64_t)qrows[r] : r) : -1;
     len[tid] = 0;
   }
   __syncthreads();
@@ -153,7 +168,7 @@ __global__ void __launch_bounds__(kThreads, 1) knn_tile_kernel(const float* __re
       const int dq = (tid / CB) * 4 + 8 * g;
       const int64_t j = c0 + c;
       const int d = d0 + dq;
-      if (j < n && vec4 && d + 3 < dim) {
+      if (j < hi && vec4 && d + 3 < dim) {
         const float4 v = *reinterpret_cast<const float4*>(X + j * dim + d);
         pre[4 * g + 0] = v.x;
         pre[4 * g + 1] = v.y;
@@ -161,7 +176,7 @@ __global__ void __launch_bounds__(kThreads, 1) knn_tile_kernel(const float* __re
         pre[4 * g + 3] = v.w;
       } else {
 #pragma unroll
-        for (int i = 0; i < 4; ++i) pre[4 * g + i] = (j < n && d + i < dim) ? X[j * dim + d + i] : 0.f;
+        for (int i = 0; i < 4; ++i) pre[4 * g + i] = (j < hi && d + i < dim) ? X[j * dim + d + i] : 0.f;
       }
     }
   };
@@ -176,8 +191,8 @@ __global__ void __launch_bounds__(kThreads, 1) knn_tile_kernel(const float* __re
   };
 
   const int nchunks = (dim + DK - 1) / DK;
-  load_chunk(0, 0);
-  for (int64_t c0 = 0; c0 < n; c0 += CB) {
+  load_chunk(lo, 0);
+  for (int64_t c0 = lo; c0 < hi; c0 += CB) {
     float acc[4][8];
 #pragma unroll
     for (int a = 0; a < 4; ++a)
@@ -190,7 +205,7 @@ __global__ void __launch_bounds__(kThreads, 1) knn_tile_kernel(const float* __re
       __syncthreads();
       // prefetch the next chunk (next dims, or the next candidate tile's first dims)
       if (ch + 1 < nchunks) load_chunk(c0, d0 + DK);
-      else if (c0 + CB < n) load_chunk(c0 + CB, 0);
+      else if (c0 + CB < hi) load_chunk(c0 + CB, 0);
       const int dmax = min(DK, dim - d0);
       for (int dd = 0; dd < dmax; ++dd) {
         const float4 a4 = *reinterpret_cast<const float4*>(Qs + (d0 + dd) * QB + tq * 4);
@@ -222,7 +237,7 @@ __global__ void __launch_bounds__(kThreads, 1) knn_tile_kernel(const float* __re
           v = sqrtf(acc[a][b]);
         } else {
           const int64_t j = c0 + c;
-          const float cn = j < n ? norms[j] : 0.f;
+          const float cn = j < hi ? norms[j] : 0.f;
           v = qn[q] + cn - 2.f * acc[a][b];
         }
         S[q * (CB + 1) + c] = v;
@@ -241,7 +256,7 @@ __global__ void __launch_bounds__(kThreads, 1) knn_tile_kernel(const float* __re
         const int64_t j = c0 + c;
         const float v = S[q * (CB + 1) + c];
         const int L = len[q];
-        bool ok = j < n && j != qi;
+        bool ok = j < hi && j != qi;
         if (ok && L == cap) ok = lt_pair(v, (uint32_t)j, qlv[cap - 1], qli[cap - 1]);
         unsigned mask = __ballot_sync(kFull, ok);
         while (mask) {
@@ -359,10 +374,13 @@ __global__ void knn_rerank_kernel(const T* __restrict__ X, int64_t n, int dim, i
 
 // Exact brute force for the listed queries, one warp per query, list of size k
 // kept sorted in shared memory by (distance, index).
+// With seg_off, a query of set j = seg_of[qi] scans rows seg_off[j]..seg_off[j+1] only.
 template <class T>
 __global__ void knn_exact_kernel(const T* __restrict__ X, int64_t n, int dim, int k, const uint32_t* __restrict__ rows,
                                  const unsigned* __restrict__ nrows_p, int64_t nrows_fixed,
-                                 uint32_t* __restrict__ out_idx, T* __restrict__ out_dist) {
+                                 uint32_t* __restrict__ out_idx, T* __restrict__ out_dist,
+                                 const int64_t* __restrict__ seg_off = nullptr,
+                                 const uint32_t* __restrict__ seg_of = nullptr) {
   extern __shared__ __align__(16) unsigned char smem[];
   constexpr int W = 4;
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -376,10 +394,15 @@ __global__ void knn_exact_kernel(const T* __restrict__ X, int64_t n, int dim, in
   if (lane == 0) len[w] = 0;
   __syncwarp();
   const T* xq = X + qi * dim;
-  for (int64_t b = 0; b < n; b += 32) {
+  int64_t lo = 0, hi = n;
+  if (seg_off) {
+    lo = seg_off[seg_of[qi]];
+    hi = seg_off[seg_of[qi] + 1];
+  }
+  for (int64_t b = lo; b < hi; b += 32) {
     const int64_t j = b + lane;
     T d = T(0);
-    bool ok = j < n && j != qi;
+    bool ok = j < hi && j != qi;
     if (ok) d = dsqrt(exact_d2<T>(xq, X + j * dim, dim));
     if (ok && len[w] == k) ok = lt_pair(d, (uint32_t)j, lv[k - 1], li[k - 1]);
     unsigned mask = __ballot_sync(kFull, ok);
@@ -476,8 +499,93 @@ int64_t knn_euclidean(const T* X, int64_t n, int dim, int k, uint32_t* out_idx, 
   return (int64_t)nfail;
 }
 
+template <class T>
+int64_t knn_euclidean_segmented(const T* X, int64_t total, int dim, int k, const std::vector<int64_t>& off,
+                                const int64_t* d_off, const uint32_t* d_seg_of, uint32_t* out_idx, T* out_dist,
+                                KnnWorkspace& ws, cudaStream_t s) {
+  const int K = (int)off.size() - 1;
+  for (int j = 0; j < K; ++j)
+    if (k <= 0 || k > off[j + 1] - off[j] - 1) throw Error(ST_EINVAL, "error: k must be in [1, n_samples - 1].");
+  const int C = k <= 96 ? 128 : (k <= 224 ? 256 : 0);
+  const int qdim_max = C == 128 ? 256 : 128;
+  if (C == 0 || dim > qdim_max)
+    throw Error(ST_EINVAL, "error: the segmented kNN covers k <= 224 and dim <= " + std::to_string(qdim_max) + ".");
+  unsigned* fail_count = static_cast<unsigned*>(ws.counters.ensure(64));
+  BHG_CUDA(cudaMemsetAsync(fail_count, 0, 64, s));
+  const float* Xf;
+  if constexpr (std::is_same<T, float>::value) {
+    Xf = X;
+  } else {
+    float* tmp = static_cast<float*>(ws.xf.ensure((size_t)total * dim * sizeof(float)));
+    to_f32_kernel<T><<<1024, 256, 0, s>>>(X, total * dim, tmp);
+    BHG_LAUNCH_CHECK();
+    Xf = tmp;
+  }
+  float* norms = static_cast<float*>(ws.norms.ensure((size_t)total * sizeof(float)));
+  unsigned* max_bits = fail_count + 1;
+  sq_norm_kernel<<<(unsigned)ceil_div(total * 32, 256), 256, 0, s>>>(Xf, total, dim, norms, max_bits);
+  BHG_LAUNCH_CHECK();
+  // block table, largest sets first (each of their blocks scans the most candidates)
+  std::vector<int> order(K);
+  for (int j = 0; j < K; ++j) order[j] = j;
+  std::stable_sort(order.begin(), order.end(),
+                   [&](int a, int b) { return off[a + 1] - off[a] > off[b + 1] - off[b]; });
+  std::vector<int64_t> q0;
+  std::vector<int32_t> bj;
+  for (int j : order)
+    for (int64_t q = off[j]; q < off[j + 1]; q += QB) {
+      q0.push_back(q);
+      bj.push_back(j);
+    }
+  const int64_t nblk = (int64_t)q0.size();
+  int64_t* d_q0 = static_cast<int64_t*>(ws.blk.ensure((size_t)nblk * (8 + 4)));
+  int32_t* d_bj = reinterpret_cast<int32_t*>(d_q0 + nblk);
+  BHG_CUDA(cudaMemcpyAsync(d_q0, q0.data(), (size_t)nblk * 8, cudaMemcpyHostToDevice, s));
+  BHG_CUDA(cudaMemcpyAsync(d_bj, bj.data(), (size_t)nblk * 4, cudaMemcpyHostToDevice, s));
+  uint32_t* cand = static_cast<uint32_t*>(ws.cand.ensure((size_t)total * C * sizeof(uint32_t)));
+  float* thr = static_cast<float*>(ws.thr.ensure((size_t)total * sizeof(float)));
+  uint32_t* fails = static_cast<uint32_t*>(ws.fails.ensure((size_t)total * sizeof(uint32_t)));
+  const size_t smem = ((size_t)dim * QB + DK * CB + QB * (CB + 1) + (size_t)QB * C * 2 + 2 * QB) * 4;
+  if (C == 128) {
+    BHG_CUDA(cudaFuncSetAttribute(knn_tile_kernel<128, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    knn_tile_kernel<128, false><<<(unsigned)nblk, kThreads, smem, s>>>(Xf, total, dim, norms, nullptr, total, 128, cand,
+                                                                      thr, d_q0, d_bj, d_off);
+    BHG_LAUNCH_CHECK();
+    knn_rerank_kernel<T, 128><<<(unsigned)ceil_div(total, 4), 128, 0, s>>>(X, total, dim, k, cand, thr, norms, max_bits,
+                                                                           out_idx, out_dist, fails, fail_count);
+  } else {
+    BHG_CUDA(cudaFuncSetAttribute(knn_tile_kernel<256, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    knn_tile_kernel<256, false><<<(unsigned)nblk, kThreads, smem, s>>>(Xf, total, dim, norms, nullptr, total, 256, cand,
+                                                                      thr, d_q0, d_bj, d_off);
+    BHG_LAUNCH_CHECK();
+    knn_rerank_kernel<T, 256><<<(unsigned)ceil_div(total, 4), 128, 0, s>>>(X, total, dim, k, cand, thr, norms, max_bits,
+                                                                           out_idx, out_dist, fails, fail_count);
+  }
+  BHG_LAUNCH_CHECK();
+  unsigned nfail = 0;
+  BHG_CUDA(cudaMemcpyAsync(&nfail, fail_count, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+  BHG_CUDA(cudaStreamSynchronize(s));
+  if (nfail > 0) {
+    const size_t esmem = (size_t)4 * k * (sizeof(T) + sizeof(uint32_t));
+    if (esmem > 48 * 1024)
+      BHG_CUDA(cudaFuncSetAttribute(knn_exact_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)esmem));
+    knn_exact_kernel<T><<<(unsigned)ceil_div(nfail, 4), 128, esmem, s>>>(X, total, dim, k, fails, nullptr, nfail, out_idx,
+                                                                        out_dist, d_off, d_seg_of);
+    BHG_LAUNCH_CHECK();
+  }
+  ws.last_fallback_rows = nfail;
+  return (int64_t)nfail;
+}
+
 template int64_t knn_euclidean<float>(const float*, int64_t, int, int, uint32_t*, float*, KnnWorkspace&, cudaStream_t);
 template int64_t knn_euclidean<double>(const double*, int64_t, int, int, uint32_t*, double*, KnnWorkspace&,
                                        cudaStream_t);
+
+template int64_t knn_euclidean_segmented<float>(const float*, int64_t, int, int, const std::vector<int64_t>&,
+                                                 const int64_t*, const uint32_t*, uint32_t*, float*, KnnWorkspace&,
+                                                 cudaStream_t);
+template int64_t knn_euclidean_segmented<double>(const double*, int64_t, int, int, const std::vector<int64_t>&,
+                                                  const int64_t*, const uint32_t*, uint32_t*, double*, KnnWorkspace&,
+                                                  cudaStream_t);
 
 }  // namespace bhg

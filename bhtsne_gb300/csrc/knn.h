@@ -1,12 +1,14 @@
 // Exact Euclidean kNN (see knn.cu).
 #pragma once
 
+#include <vector>
+
 #include "internal.h"
 
 namespace bhg {
 
 struct KnnWorkspace {
-  DevBuf xf, norms, cand, thr, fails, counters;
+  DevBuf xf, norms, cand, thr, fails, counters, blk;
   int64_t last_fallback_rows = 0;
   void release() {
     xf.release();
@@ -14,6 +16,7 @@ struct KnnWorkspace {
     cand.release();
     thr.release();
     fails.release();
+    blk.release();
   }
 };
 
@@ -23,5 +26,14 @@ struct KnnWorkspace {
 template <class T>
 int64_t knn_euclidean(const T* X, int64_t n, int dim, int k, uint32_t* out_idx, T* out_dist, KnnWorkspace& ws,
                       cudaStream_t s);
+
+// The same over many independent point sets stored back to back (set j owns
+// rows off[j]..off[j+1]; seg_of[row] is the set of a row, off is also given on
+// the device as d_off): every row gets its k nearest rows of its own set, as
+// global row indices. All sets share dim and k.
+template <class T>
+int64_t knn_euclidean_segmented(const T* X, int64_t total, int dim, int k, const std::vector<int64_t>& off,
+                                const int64_t* d_off, const uint32_t* d_seg_of, uint32_t* out_idx, T* out_dist,
+                                KnnWorkspace& ws, cudaStream_t s);
 
 }  // namespace bhg

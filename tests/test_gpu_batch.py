@@ -130,3 +130,32 @@ def test_batch_errors(gpu):
         t.fit()
     with pytest.raises(gpu.BhtsneError, match="no fitted job"):
         t.embedding(0)
+
+
+def test_mixed_inputs_in_one_batch(gpu, oracle):
+    """Euclidean jobs and kNN-table jobs (of another k) are prepared as separate
+    groups and fitted together; a job given as data and the same job given as
+    its kNN table end identical."""
+    X, _ = blobs(800, 20, 4, 31)
+    Z, _ = blobs(400, 20, 3, 32)
+    idx, dist = oracle.knn(X, 30)
+    idx2, dist2 = oracle.knn(Z, 45)
+    y = np.random.default_rng(4).normal(0, 1e-4, size=(800, 2)).astype(np.float32)
+    b = gpu.Batch(perplexity=10.0, epochs=80)
+    a0 = b.add(X)
+    a1 = b.add_with_neighbors((idx, dist))
+    a2 = b.add_with_neighbors((idx2, dist2))
+    a3 = b.add(Z)
+    b.initial_embedding(a0, y)
+    b.initial_embedding(a1, y)
+    b.fit()
+    assert np.array_equal(b.embedding(a0), b.embedding(a1))
+    for j in (a2, a3):
+        assert np.all(np.isfinite(b.embedding(j)))
+    # a second fit of the same batch restarts from fresh seeds and matches the first
+    first = [b.embedding(j) for j in range(4)]
+    b.initial_embedding(a0, y)
+    b.initial_embedding(a1, y)
+    b.fit()
+    for j in range(4):
+        assert np.array_equal(first[j], b.embedding(j))
