@@ -312,6 +312,7 @@ void epoch_tail(bhtsne_tsne* t, int64_t epoch, std::vector<T>& snap) {
     const T scale = T(1) / (T)t->early_exaggeration;
     if (t->loop_kind == BHTSNE_METHOD_EXACT) launch_scale<T>(S.pdense.template as<T>(), t->n * t->n, scale, s);
     else launch_scale<T>(S.vals.template as<T>(), S.nnz, scale, s);
+    if (S.rn.active && t->loop_kind != BHTSNE_METHOD_EXACT) launch_scale<T>(S.rn.vals.template as<T>(), S.nnz, scale, s);
     t->stop_lying_fired = true;
   }
   if (epoch == t->momentum_switch_epoch) t->momentum = t->final_momentum;
@@ -369,10 +370,12 @@ void advance_impl(bhtsne_tsne* t, int64_t epochs) {
   const int64_t renumber_every = rev ? atoll(rev) : 50;
   const bool sparse = t->loop_kind != BHTSNE_METHOD_EXACT;
   auto attractive = [&]() {
-    launch_attractive<T>(D, S.rows.template as<uint64_t>(),
-                         S.rn.active ? S.rn.cols.template as<uint32_t>() : S.cols.template as<uint32_t>(),
-                         S.vals.template as<T>(), y, n, S.pos.template as<T>(), s,
-                         S.rn.active ? S.rn.ext.template as<uint32_t>() : nullptr);
+    if (S.rn.active)
+      launch_attractive<T>(D, S.rn.rows.template as<uint64_t>(), S.rn.cols.template as<uint32_t>(),
+                           S.rn.vals.template as<T>(), y, n, S.pos.template as<T>(), s);
+    else
+      launch_attractive<T>(D, S.rows.template as<uint64_t>(), S.cols.template as<uint32_t>(), S.vals.template as<T>(), y,
+                           n, S.pos.template as<T>(), s);
   };
   auto maybe_renumber = [&](int64_t epoch) {
     if (!sparse || renumber_every <= 0 || epoch == 0 || epoch % renumber_every != 0) return;
@@ -386,7 +389,7 @@ void advance_impl(bhtsne_tsne* t, int64_t epochs) {
     const bool was_active = S.rn.active;
     launch_renumber<T>(D, S.bh.perm.template as<uint32_t>(), n, S.rn, y, S.uy.template as<T>(), S.gains.template as<T>(),
                        S.pos.template as<T>(), S.neg.template as<T>(), static_cast<T*>(S.yext.ensure((size_t)n * D * sizeof(T))),
-                       S.cols.template as<uint32_t>(), S.nnz, s);
+                       S.rows.template as<uint64_t>(), S.cols.template as<uint32_t>(), S.vals.template as<T>(), S.nnz, s);
     if (t->loop_kind != BHTSNE_METHOD_BARNES_HUT)
       launch_recenter_bbox<T>(D, y, n, nullptr, false, S.bh, bits, s);
     if (!was_active) t->drop_graph();  // the attractive pass now reads the slot arrays

@@ -16,7 +16,9 @@
 //    src/tsne/mod.rs:579-618; dense symmetrisation: src/lib.rs:548-554.
 #include "epoch.h"
 
+#include <cstdint>
 #include <cstdlib>
+#include <type_traits>
 
 namespace bhg {
 
@@ -27,7 +29,24 @@ namespace {
 // arithmetic). With a renumbered layout slot s holds the point of CSR row
 // row_of_slot[s] and `cols` holds slots, so a row's gathers stay near s and
 // neighbouring warps share lines.
-template <class T, int D, int G, int kU>
+// y[j] as one 2-wide load when D = 2 and y is aligned for it (VEC), else per axis.
+template <class T, int D, bool VEC>
+__device__ __forceinline__ void load_point(const T* __restrict__ y, int64_t j, T (&v)[D]) {
+  if constexpr (VEC && D == 2 && std::is_same<T, float>::value) {
+    const float2 t = __ldg(reinterpret_cast<const float2*>(y) + j);
+    v[0] = t.x;
+    v[1] = t.y;
+  } else if constexpr (VEC && D == 2 && std::is_same<T, double>::value) {
+    const double2 t = __ldg(reinterpret_cast<const double2*>(y) + j);
+    v[0] = t.x;
+    v[1] = t.y;
+  } else {
+#pragma unroll
+    for (int a = 0; a < D; ++a) v[a] = y[j * D + a];
+  }
+}
+
+template <class T, int D, int G, int kU, bool VEC>
 __global__ void __launch_bounds__(256) attractive_kernel(const uint64_t* __restrict__ rows, const uint32_t* __restrict__ cols,
                                                          const T* __restrict__ vals, const T* __restrict__ y, int64_t n,
                                                          const uint32_t* __restrict__ row_of_slot, T* __restrict__ pos) {
@@ -54,9 +73,7 @@ __global__ void __launch_bounds__(256) attractive_kernel(const uint64_t* __restr
       p[u] = e < e1 ? __ldg(vals + e) : T(0);
     }
 #pragma unroll
-    for (int u = 0; u < kU; ++u)
-#pragma unroll
-      for (int a = 0; a < D; ++a) yj[u][a] = y[(int64_t)j[u] * D + a];
+    for (int u = 0; u < kU; ++u) load_point<T, D, VEC>(y, (int64_t)j[u], yj[u]);
 #pragma unroll
     for (int u = 0; u < kU; ++u) {
       T disp[D];
@@ -107,10 +124,74 @@ __global__ void invert_kernel(const uint32_t* __restrict__ ext, int64_t n, uint3
   if (s < n) inv[ext[s]] = (uint32_t)s;
 }
 
-__global__ void remap_cols_kernel(const uint32_t* __restrict__ cols, int64_t nnz, const uint32_t* __restrict__ inv,
-                                  uint32_t* __restrict__ out) {
-  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < nnz; e += (int64_t)gridDim.x * blockDim.x)
-    out[e] = inv[cols[e]];
+__global__ void slot_len_kernel(const uint64_t* __restrict__ rows, const uint32_t* __restrict__ row_of_slot, int64_t n,
+                                uint32_t* __restrict__ len) {
+  const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  const int64_t r = row_of_slot[s];
+  len[s] = (uint32_t)(rows[r + 1] - rows[r]);
+}
+
+// One warp per slot: the CSR row of row_of_slot[s] moved to slot order with
+// its columns mapped to slots and sorted by slot (bitonic in shared memory),
+// so that a warp's neighbour gathers fall on few cache lines. Columns within
+// a row are distinct, so the order is unique. Rows longer than kSlotSortMax
+// keep their order (only locality is lost).
+constexpr int kSlotSortMax = 1024;
+constexpr int kSlotWarps = 4;
+
+template <class T>
+__global__ void __launch_bounds__(kSlotWarps * 32) slot_rows_kernel(
+    const uint64_t* __restrict__ rows, const uint32_t* __restrict__ cols, const T* __restrict__ vals,
+    const uint32_t* __restrict__ row_of_slot, const uint32_t* __restrict__ inv, int64_t n,
+    const uint64_t* __restrict__ rows_s, uint32_t* __restrict__ cols_s, T* __restrict__ vals_s) {
+  __shared__ uint32_t sk[kSlotWarps][kSlotSortMax];
+  __shared__ T sv[kSlotWarps][kSlotSortMax];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t nwarps = (int64_t)gridDim.x * kSlotWarps;
+  for (int64_t slot = (int64_t)blockIdx.x * kSlotWarps + w; slot < n; slot += nwarps) {
+    const int64_t r = row_of_slot[slot];
+    const int64_t e0 = (int64_t)rows[r];
+    const int64_t L = (int64_t)(rows[r + 1] - rows[r]);
+    const int64_t o = (int64_t)rows_s[slot];
+    if (L > kSlotSortMax || L <= 1) {
+      for (int64_t t = lane; t < L; t += 32) {
+        cols_s[o + t] = inv[cols[e0 + t]];
+        vals_s[o + t] = vals[e0 + t];
+      }
+      continue;
+    }
+    int P = 32;
+    while (P < L) P <<= 1;
+    for (int t = lane; t < P; t += 32) {
+      sk[w][t] = t < L ? inv[cols[e0 + t]] : 0xffffffffu;
+      sv[w][t] = t < L ? vals[e0 + t] : T(0);
+    }
+    __syncwarp();
+    for (int size = 2; size <= P; size <<= 1) {
+      for (int stride = size >> 1; stride > 0; stride >>= 1) {
+        for (int t = lane; t < P / 2; t += 32) {
+          const int lo = 2 * t - (t & (stride - 1));
+          const int hi = lo + stride;
+          const bool up = (lo & size) == 0;
+          const uint32_t a = sk[w][lo], b = sk[w][hi];
+          if ((a > b) == up) {
+            sk[w][lo] = b;
+            sk[w][hi] = a;
+            const T va = sv[w][lo];
+            sv[w][lo] = sv[w][hi];
+            sv[w][hi] = va;
+          }
+        }
+        __syncwarp();
+      }
+    }
+    for (int t = lane; t < L; t += 32) {
+      cols_s[o + t] = sk[w][t];
+      vals_s[o + t] = sv[w][t];
+    }
+    __syncwarp();
+  }
 }
 
 template <class T, int D>
@@ -341,23 +422,31 @@ constexpr int kUpdBlocks = 2 * 152;
 
 }  // namespace
 
+template <class T, int D, bool VEC>
+static void launch_attractive_v(int variant, const uint64_t* rows, const uint32_t* cols, const T* vals, const T* y,
+                                int64_t n, T* pos, cudaStream_t s, const uint32_t* row_of_slot) {
+  switch (variant) {
+    case 1:
+      attractive_kernel<T, D, 32, 8, VEC>
+          <<<(unsigned)ceil_div(n * 32, 256), 256, 0, s>>>(rows, cols, vals, y, n, row_of_slot, pos);
+      break;
+    case 2:
+      attractive_kernel<T, D, 16, 8, VEC>
+          <<<(unsigned)ceil_div(n * 16, 256), 256, 0, s>>>(rows, cols, vals, y, n, row_of_slot, pos);
+      break;
+    default:
+      attractive_kernel<T, D, 32, 4, VEC>
+          <<<(unsigned)ceil_div(n * 32, 256), 256, 0, s>>>(rows, cols, vals, y, n, row_of_slot, pos);
+      break;
+  }
+}
+
 template <class T, int D>
 static void launch_attractive_d(int variant, const uint64_t* rows, const uint32_t* cols, const T* vals, const T* y,
                                 int64_t n, T* pos, cudaStream_t s, const uint32_t* row_of_slot) {
-  switch (variant) {
-    case 0:
-      attractive_kernel<T, D, 32, 4><<<(unsigned)ceil_div(n * 32, 256), 256, 0, s>>>(rows, cols, vals, y, n, row_of_slot, pos);
-      break;
-    case 1:
-      attractive_kernel<T, D, 32, 8><<<(unsigned)ceil_div(n * 32, 256), 256, 0, s>>>(rows, cols, vals, y, n, row_of_slot, pos);
-      break;
-    case 2:
-      attractive_kernel<T, D, 16, 8><<<(unsigned)ceil_div(n * 16, 256), 256, 0, s>>>(rows, cols, vals, y, n, row_of_slot, pos);
-      break;
-    default:
-      attractive_kernel<T, D, 8, 8><<<(unsigned)ceil_div(n * 8, 256), 256, 0, s>>>(rows, cols, vals, y, n, row_of_slot, pos);
-      break;
-  }
+  const bool vec = D == 2 && (reinterpret_cast<uintptr_t>(y) % (2 * sizeof(T))) == 0;
+  if (vec) launch_attractive_v<T, D, true>(variant, rows, cols, vals, y, n, pos, s, row_of_slot);
+  else launch_attractive_v<T, D, false>(variant, rows, cols, vals, y, n, pos, s, row_of_slot);
 }
 
 template <class T>
@@ -376,7 +465,7 @@ void launch_attractive(int D, const uint64_t* rows, const uint32_t* cols, const 
 
 template <class T>
 void launch_renumber(int D, const uint32_t* order, int64_t n, Renumbering& r, T* y, T* uy, T* gains, T* tmp_a, T* tmp_b,
-                     T* tmp_c, const uint32_t* cols, int64_t nnz, cudaStream_t s) {
+                     T* tmp_c, const uint64_t* rows, const uint32_t* cols, const T* vals, int64_t nnz, cudaStream_t s) {
   const unsigned g = (unsigned)ceil_div(n, 256);
   uint32_t* ext_new = static_cast<uint32_t*>(r.ext_alt.ensure((size_t)n * 4));
   const uint32_t* ext_old = r.active ? r.ext.template as<uint32_t>() : nullptr;
@@ -396,9 +485,17 @@ void launch_renumber(int D, const uint32_t* order, int64_t n, Renumbering& r, T*
   uint32_t* inv = static_cast<uint32_t*>(r.inv.ensure((size_t)n * 4));
   invert_kernel<<<g, 256, 0, s>>>(r.ext.template as<uint32_t>(), n, inv);
   BHG_LAUNCH_CHECK();
-  uint32_t* cols_slot = static_cast<uint32_t*>(r.cols.ensure((size_t)std::max<int64_t>(nnz, 1) * 4));
+  // CSR in slot order with slot columns, sorted within each row
+  uint32_t* len = static_cast<uint32_t*>(r.len.ensure((size_t)n * 4));
+  slot_len_kernel<<<g, 256, 0, s>>>(rows, r.ext.template as<uint32_t>(), n, len);
+  BHG_LAUNCH_CHECK();
+  uint64_t* rows_s = static_cast<uint64_t*>(r.rows.ensure((size_t)(n + 1) * 8));
+  scan_u32_to_u64(len, rows_s, n, r.scan_tmp, s);
+  uint32_t* cols_s = static_cast<uint32_t*>(r.cols.ensure((size_t)std::max<int64_t>(nnz, 1) * 4));
+  T* vals_s = static_cast<T*>(r.vals.ensure((size_t)std::max<int64_t>(nnz, 1) * sizeof(T)));
   if (nnz > 0) {
-    remap_cols_kernel<<<(unsigned)std::min<int64_t>(ceil_div(nnz, 256), 8 * 152), 256, 0, s>>>(cols, nnz, inv, cols_slot);
+    slot_rows_kernel<T><<<(unsigned)std::min<int64_t>(ceil_div(n, kSlotWarps), 16 * 152), kSlotWarps * 32, 0, s>>>(
+        rows, cols, vals, r.ext.template as<uint32_t>(), inv, n, rows_s, cols_s, vals_s);
     BHG_LAUNCH_CHECK();
   }
   r.active = true;
@@ -492,7 +589,7 @@ void launch_exact_kl(int D, const T* y, const T* p, int64_t n, const double* z, 
   template void launch_attractive<T>(int, const uint64_t*, const uint32_t*, const T*, const T*, int64_t, T*,         \
                                      cudaStream_t, const uint32_t*);                                                 \
   template void launch_renumber<T>(int, const uint32_t*, int64_t, Renumbering&, T*, T*, T*, T*, T*, T*,              \
-                                   const uint32_t*, int64_t, cudaStream_t);                                          \
+                                   const uint64_t*, const uint32_t*, const T*, int64_t, cudaStream_t);               \
   template void launch_unpermute<T>(int, const T*, const uint32_t*, int64_t, T*, cudaStream_t);                      \
   template void launch_update<T>(int, T*, const T*, const T*, T*, T*, int64_t, const double*, T, T, T, UpdateScratch&,  \
                                  cudaStream_t);                                                                      \

@@ -21,14 +21,17 @@ void launch_attractive(int D, const uint64_t* rows, const uint32_t* cols, const 
 // are re-laid out in `order` (a permutation of the current slots, e.g. the
 // Morton order of the embedding); ext[s] is the point (CSR row) held by slot
 // s, inv its inverse, and cols the CSR columns translated to slots.
+// Locality layout of the embedding state: slot s holds the point ext[s]
+// (inv is the inverse map). rows/cols/vals are P in slot order: row s is the
+// CSR row of ext[s] with columns as slots, sorted within the row.
 struct Renumbering {
   bool active = false;
-  DevBuf ext, ext_alt, inv, cols;
+  DevBuf ext, ext_alt, inv, rows, cols, vals, len, scan_tmp;
 };
 
 template <class T>
 void launch_renumber(int D, const uint32_t* order, int64_t n, Renumbering& r, T* y, T* uy, T* gains, T* tmp_a, T* tmp_b,
-                     T* tmp_c, const uint32_t* cols, int64_t nnz, cudaStream_t s);
+                     T* tmp_c, const uint64_t* rows, const uint32_t* cols, const T* vals, int64_t nnz, cudaStream_t s);
 
 // out[ext[s]] = y[s]: back to the caller's point order.
 template <class T>

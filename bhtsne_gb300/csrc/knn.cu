@@ -287,6 +287,209 @@ __global__ void __launch_bounds__(kThreads, 1) knn_tile_kernel(const float* __re
   }
 }
 
+// Candidate pass with buffered selection (C = kSelC, dim <= kSelDimMax).
+// Distances as in knn_tile_kernel (same FP32 values, so the same candidate
+// list and threshold); only the selection differs. Per query, a buffer of 2C
+// (value, index) pairs in shared memory holds the C best so far (sorted, from
+// the last merge) followed by unsorted appends that beat the current C-th
+// best. Appends cost one ballot per 32 candidates; when the next 32 could
+// overflow the buffer, the owning warp bitonic-sorts it by (value, index) and
+// keeps the first C. Every rejected candidate is no better than a C-th best
+// of its time, hence no better than the final C-th: the list and threshold
+// equal those of one sorted insertion per candidate.
+constexpr int kSelC = 128;
+constexpr int kSelDimMax = 128;
+
+__device__ __forceinline__ void sel_merge(float* bv, uint32_t* bi, int& c, float& tv, uint32_t& ti, int lane) {
+  constexpr int B = 2 * kSelC;
+  for (int t = c + lane; t < B; t += 32) {
+    bv[t] = INFINITY;
+    bi[t] = SENT;
+  }
+  __syncwarp();
+  for (int size = 2; size <= B; size <<= 1) {
+    for (int stride = size >> 1; stride > 0; stride >>= 1) {
+      for (int t = lane; t < B / 2; t += 32) {
+        const int lo = 2 * t - (t & (stride - 1));
+        const int hi = lo + stride;
+        const bool up = (lo & size) == 0;
+        const float a = bv[lo], b = bv[hi];
+        const uint32_t ia = bi[lo], ib = bi[hi];
+        if (lt_pair(b, ib, a, ia) == up) {
+          bv[lo] = b;
+          bv[hi] = a;
+          bi[lo] = ib;
+          bi[hi] = ia;
+        }
+      }
+      __syncwarp();
+    }
+  }
+  c = c < kSelC ? c : kSelC;
+  if (c == kSelC) {
+    tv = bv[kSelC - 1];
+    ti = bi[kSelC - 1];
+  }
+}
+
+// dynamic shared layout: Qs[dim][QB] | Cs[DK][CB] | S[QB][CB+1] | bv[QB][2C] | bi[QB][2C]
+__global__ void __launch_bounds__(kThreads, 1) knn_cand_kernel(const float* __restrict__ X, int64_t n, int dim,
+                                                               const float* __restrict__ norms,
+                                                               uint32_t* __restrict__ out_idx,
+                                                               float* __restrict__ out_thr,
+                                                               const int64_t* __restrict__ blk_q0,
+                                                               const int32_t* __restrict__ blk_job,
+                                                               const int64_t* __restrict__ seg_off) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  float* Qs = reinterpret_cast<float*>(smem);
+  float* Cs = Qs + (size_t)dim * QB;
+  float* S = Cs + DK * CB;
+  float* bv = S + QB * (CB + 1);
+  uint32_t* bi = reinterpret_cast<uint32_t*>(bv + QB * 2 * kSelC);
+  __shared__ int64_t qidx[QB];
+  __shared__ float qn[QB];
+  constexpr int QW = QB / 8;  // queries per warp in the selection
+
+  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+  const int tq = tid >> 4, tc = tid & 15;
+  int64_t q0 = (int64_t)blockIdx.x * QB, lo = 0, hi = n;
+  if (blk_q0) {
+    const int jb = blk_job[blockIdx.x];
+    q0 = blk_q0[blockIdx.x];
+    lo = seg_off[jb];
+    hi = seg_off[jb + 1];
+  }
+  if (tid < QB) {
+    const int64_t r = q0 + tid;
+    qidx[tid] = r < hi ? r : -1;
+    qn[tid] = r < hi ? norms[r] : 0.f;
+  }
+  __syncthreads();
+  for (int e = tid; e < QB * dim; e += kThreads) {
+    const int q = e / dim, d = e % dim;
+    const int64_t qi = qidx[q];
+    Qs[d * QB + q] = qi >= 0 ? X[qi * dim + d] : 0.f;
+  }
+
+  const bool vec4 = (dim & 3) == 0;
+  float pre[16];
+  auto load_chunk = [&](int64_t c0, int d0) {
+#pragma unroll
+    for (int g = 0; g < 4; ++g) {
+      const int c = tid % CB;
+      const int dq = (tid / CB) * 4 + 8 * g;
+      const int64_t j = c0 + c;
+      const int d = d0 + dq;
+      if (j < hi && vec4 && d + 3 < dim) {
+        const float4 v = *reinterpret_cast<const float4*>(X + j * dim + d);
+        pre[4 * g + 0] = v.x;
+        pre[4 * g + 1] = v.y;
+        pre[4 * g + 2] = v.z;
+        pre[4 * g + 3] = v.w;
+      } else {
+#pragma unroll
+        for (int i = 0; i < 4; ++i) pre[4 * g + i] = (j < hi && d + i < dim) ? X[j * dim + d + i] : 0.f;
+      }
+    }
+  };
+  auto store_chunk = [&]() {
+#pragma unroll
+    for (int g = 0; g < 4; ++g) {
+      const int c = tid % CB;
+      const int dq = (tid / CB) * 4 + 8 * g;
+#pragma unroll
+      for (int i = 0; i < 4; ++i) Cs[(dq + i) * CB + c] = pre[4 * g + i];
+    }
+  };
+
+  int cnt[QW];
+  float tv[QW];
+  uint32_t ti[QW];
+#pragma unroll
+  for (int qq = 0; qq < QW; ++qq) {
+    cnt[qq] = 0;
+    tv[qq] = INFINITY;
+    ti[qq] = SENT;
+  }
+
+  const int nchunks = (dim + DK - 1) / DK;
+  load_chunk(lo, 0);
+  for (int64_t c0 = lo; c0 < hi; c0 += CB) {
+    float acc[4][8];
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+      for (int b = 0; b < 8; ++b) acc[a][b] = 0.f;
+    for (int ch = 0; ch < nchunks; ++ch) {
+      const int d0 = ch * DK;
+      __syncthreads();
+      store_chunk();
+      __syncthreads();
+      if (ch + 1 < nchunks) load_chunk(c0, d0 + DK);
+      else if (c0 + CB < hi) load_chunk(c0 + CB, 0);
+      const int dmax = min(DK, dim - d0);
+      for (int dd = 0; dd < dmax; ++dd) {
+        const float4 a4 = *reinterpret_cast<const float4*>(Qs + (d0 + dd) * QB + tq * 4);
+        const float4 b0 = *reinterpret_cast<const float4*>(Cs + dd * CB + tc * 4);
+        const float4 b1 = *reinterpret_cast<const float4*>(Cs + dd * CB + 64 + tc * 4);
+        const float av[4] = {a4.x, a4.y, a4.z, a4.w};
+        const float bv8[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+#pragma unroll
+        for (int a = 0; a < 4; ++a)
+#pragma unroll
+          for (int b = 0; b < 8; ++b) acc[a][b] = fmaf(av[a], bv8[b], acc[a][b]);
+      }
+    }
+#pragma unroll
+    for (int a = 0; a < 4; ++a) {
+      const int q = tq * 4 + a;
+#pragma unroll
+      for (int b = 0; b < 8; ++b) {
+        const int c = b < 4 ? tc * 4 + b : 64 + tc * 4 + (b - 4);
+        const int64_t j = c0 + c;
+        const float cn = j < hi ? norms[j] : 0.f;
+        S[q * (CB + 1) + c] = qn[q] + cn - 2.f * acc[a][b];
+      }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int qq = 0; qq < QW; ++qq) {
+      const int q = w * QW + qq;
+      const int64_t qi = qidx[q];
+      if (qi < 0) continue;
+      float* qbv = bv + (size_t)q * 2 * kSelC;
+      uint32_t* qbi = bi + (size_t)q * 2 * kSelC;
+#pragma unroll
+      for (int part = 0; part < CB / 32; ++part) {
+        if (cnt[qq] > 2 * kSelC - 32) sel_merge(qbv, qbi, cnt[qq], tv[qq], ti[qq], lane);
+        const int c = part * 32 + lane;
+        const int64_t j = c0 + c;
+        const float v = S[q * (CB + 1) + c];
+        const bool ok = j < hi && j != qi && lt_pair(v, (uint32_t)j, tv[qq], ti[qq]);
+        const unsigned m = __ballot_sync(kFull, ok);
+        if (ok) {
+          const int at = cnt[qq] + __popc(m & ((1u << lane) - 1u));
+          qbv[at] = v;
+          qbi[at] = (uint32_t)j;
+        }
+        cnt[qq] += __popc(m);
+      }
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int qq = 0; qq < QW; ++qq) {
+    const int q = w * QW + qq;
+    const int64_t qi = qidx[q];
+    if (qi < 0) continue;
+    float* qbv = bv + (size_t)q * 2 * kSelC;
+    uint32_t* qbi = bi + (size_t)q * 2 * kSelC;
+    sel_merge(qbv, qbi, cnt[qq], tv[qq], ti[qq], lane);
+    for (int t = lane; t < kSelC; t += 32) out_idx[qi * kSelC + t] = t < cnt[qq] ? qbi[t] : SENT;
+    if (lane == 0) out_thr[qi] = cnt[qq] == kSelC ? qbv[kSelC - 1] : INFINITY;
+  }
+}
+
 // Exact distance in the reference's order (sequential over dimensions, T).
 template <class T>
 __device__ __forceinline__ T exact_d2(const T* __restrict__ a, const T* __restrict__ b, int dim) {
@@ -419,6 +622,10 @@ __global__ void knn_exact_kernel(const T* __restrict__ X, int64_t n, int dim, in
   }
 }
 
+size_t sel_smem_bytes(int dim) {
+  return ((size_t)dim * QB + DK * CB + QB * (CB + 1)) * 4 + (size_t)QB * 2 * kSelC * 8;
+}
+
 }  // namespace
 
 template <class T>
@@ -456,7 +663,14 @@ int64_t knn_euclidean(const T* X, int64_t n, int dim, int k, uint32_t* out_idx, 
   uint32_t* fails = static_cast<uint32_t*>(ws.fails.ensure((size_t)n * sizeof(uint32_t)));
   const size_t smem = ((size_t)dim * QB + DK * CB + QB * (CB + 1) + (size_t)QB * C * 2 + 2 * QB) * 4;
   const unsigned grid = (unsigned)ceil_div(n, QB);
-  if (C == 128) {
+  if (C == 128 && dim <= kSelDimMax) {
+    const size_t ssmem = sel_smem_bytes(dim);
+    BHG_CUDA(cudaFuncSetAttribute(knn_cand_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ssmem));
+    knn_cand_kernel<<<grid, kThreads, ssmem, s>>>(Xf, n, dim, norms, cand, thr, nullptr, nullptr, nullptr);
+    BHG_LAUNCH_CHECK();
+    knn_rerank_kernel<T, 128><<<(unsigned)ceil_div(n, 4), 128, 0, s>>>(X, n, dim, k, cand, thr, norms, max_bits, out_idx,
+                                                                       out_dist, fails, fail_count);
+  } else if (C == 128) {
     BHG_CUDA(cudaFuncSetAttribute(knn_tile_kernel<128, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     knn_tile_kernel<128, false><<<grid, kThreads, smem, s>>>(Xf, n, dim, norms, nullptr, n, 128, cand, thr);
     BHG_LAUNCH_CHECK();
@@ -546,7 +760,14 @@ int64_t knn_euclidean_segmented(const T* X, int64_t total, int dim, int k, const
   float* thr = static_cast<float*>(ws.thr.ensure((size_t)total * sizeof(float)));
   uint32_t* fails = static_cast<uint32_t*>(ws.fails.ensure((size_t)total * sizeof(uint32_t)));
   const size_t smem = ((size_t)dim * QB + DK * CB + QB * (CB + 1) + (size_t)QB * C * 2 + 2 * QB) * 4;
-  if (C == 128) {
+  if (C == 128 && dim <= kSelDimMax) {
+    const size_t ssmem = sel_smem_bytes(dim);
+    BHG_CUDA(cudaFuncSetAttribute(knn_cand_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ssmem));
+    knn_cand_kernel<<<(unsigned)nblk, kThreads, ssmem, s>>>(Xf, total, dim, norms, cand, thr, d_q0, d_bj, d_off);
+    BHG_LAUNCH_CHECK();
+    knn_rerank_kernel<T, 128><<<(unsigned)ceil_div(total, 4), 128, 0, s>>>(X, total, dim, k, cand, thr, norms, max_bits,
+                                                                           out_idx, out_dist, fails, fail_count);
+  } else if (C == 128) {
     BHG_CUDA(cudaFuncSetAttribute(knn_tile_kernel<128, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     knn_tile_kernel<128, false><<<(unsigned)nblk, kThreads, smem, s>>>(Xf, total, dim, norms, nullptr, total, 128, cand,
                                                                       thr, d_q0, d_bj, d_off);
