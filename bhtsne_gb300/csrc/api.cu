@@ -785,8 +785,8 @@ int bhtsne_tsne_new(bhtsne_ctx* ctx, int dtype, int32_t embed_dim, int64_t n_sam
     ctx->err = "error: dtype must be BHTSNE_F32 or BHTSNE_F64.";
     return BHTSNE_EINVAL;
   }
-  if (embed_dim < 1 || embed_dim > 3) {
-    ctx->err = "error: the embedding dimension must be 1, 2 or 3.";
+  if (embed_dim < 1 || embed_dim > 7) {
+    ctx->err = "error: the embedding dimension must be in 1..7.";
     return BHTSNE_EINVAL;
   }
   if (n_samples < 0 || n_samples > 0x7fffffffLL) {
@@ -891,14 +891,14 @@ int bhtsne_tsne_exact_distances(bhtsne_tsne* t, const void* distances) {
 }
 int bhtsne_tsne_barnes_hut_euclidean(bhtsne_tsne* t, double theta, const void* data, int32_t dim) {
   return guard(t, [&] {
-    if (t->D < 2 || t->D > 3) invalid("error: the GPU Barnes-Hut path covers D in {2, 3}.");
+    if (t->D < 2 || t->D > 7) invalid("error: Barnes-Hut covers D in 2..7.");
     DISPATCH(t, fit_euclidean<T>(t, BHTSNE_METHOD_BARNES_HUT, tcast(t, theta), data, dim));
   });
 }
 int bhtsne_tsne_barnes_hut_with_neighbors(bhtsne_tsne* t, double theta, const uint64_t* indices, const void* distances,
                                           int64_t rows, int64_t k) {
   return guard(t, [&] {
-    if (t->D < 2 || t->D > 3) invalid("error: the GPU Barnes-Hut path covers D in {2, 3}.");
+    if (t->D < 2 || t->D > 7) invalid("error: Barnes-Hut covers D in 2..7.");
     DISPATCH(t, fit_with_neighbors<T>(t, BHTSNE_METHOD_BARNES_HUT, tcast(t, theta), indices, distances, rows, k));
   });
 }
@@ -1096,7 +1096,7 @@ int bhtsne_gradient(bhtsne_ctx* ctx, int dtype, int32_t method, int32_t embed_di
                     void* pos, void* neg, double* z) {
   return guard_ctx(ctx, [&] {
     if (!y || n < 1 || !pos) invalid("error: invalid gradient arguments.");
-    if (embed_dim < 1 || embed_dim > 3) invalid("error: the embedding dimension must be 1, 2 or 3.");
+    if (embed_dim < 1 || embed_dim > 7) invalid("error: the embedding dimension must be in 1..7.");
     DISPATCH_DT(dtype, {
       cudaStream_t s = ctx->stream;
       const int D = embed_dim;
@@ -1118,7 +1118,7 @@ int bhtsne_gradient(bhtsne_ctx* ctx, int dtype, int32_t method, int32_t embed_di
         upload<T>(vd, values, (size_t)std::max<int64_t>(nnz, 0) * sizeof(T), s);
         bh.reserve(n, D);
         if (method == BHTSNE_METHOD_BARNES_HUT) {
-          if (D < 2) invalid("error: the GPU Barnes-Hut path covers D in {2, 3}.");
+          if (D < 2) invalid("error: Barnes-Hut covers D in 2..7.");
           if (!(theta > 0)) invalid("error: theta value must be greater than 0.0.");
           launch_recenter_bbox<T>(D, yd.as<T>(), n, nullptr, false, bh, bh_bits<T>(D), s);
           bh_build<T>(bh, D, yd.as<T>(), n, s);
@@ -1147,7 +1147,7 @@ int bhtsne_update(bhtsne_ctx* ctx, int dtype, int32_t embed_dim, void* y, const 
                   void* gains, int64_t n, double learning_rate, double momentum, double inverse_z) {
   return guard_ctx(ctx, [&] {
     if (!y || !pos || !uy || !gains || n < 1) invalid("error: invalid update arguments.");
-    if (embed_dim < 1 || embed_dim > 3) invalid("error: the embedding dimension must be 1, 2 or 3.");
+    if (embed_dim < 1 || embed_dim > 7) invalid("error: the embedding dimension must be in 1..7.");
     DISPATCH_DT(dtype, {
       cudaStream_t s = ctx->stream;
       const int D = embed_dim;
@@ -1602,7 +1602,7 @@ int bhtsne_batch_new(bhtsne_ctx* ctx, int dtype, int32_t embed_dim, const bhtsne
     return BHTSNE_EINVAL;
   }
   if (embed_dim < 2 || embed_dim > 3) {
-    ctx->err = "error: the GPU Barnes-Hut path covers D in {2, 3}.";
+    ctx->err = "error: the batched Barnes-Hut path covers D in {2, 3}.";
     return BHTSNE_EINVAL;
   }
   bhtsne_batch* b = new bhtsne_batch();

@@ -96,7 +96,7 @@ __global__ void batch_box_kernel(T* __restrict__ y, const int64_t* __restrict__ 
       out->inv_scale[a] = ext > T(0) ? scale / ext : T(0);
       max_extent = fmax(max_extent, ext);
     }
-    for (int a = D; a < 3; ++a) {
+    for (int a = D; a < 8; ++a) {
       out->mn[a] = T(0);
       out->mx[a] = T(0);
       out->inv_scale[a] = T(0);

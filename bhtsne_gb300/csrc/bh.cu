@@ -119,7 +119,7 @@ __global__ void recenter_bbox_kernel(T* __restrict__ y, int64_t n, const double*
       out->inv_scale[a] = ext > T(0) ? scale / ext : T(0);
       max_extent = fmax(max_extent, ext);
     }
-    for (int a = D; a < 3; ++a) {
+    for (int a = D; a < 8; ++a) {
       out->mn[a] = T(0);
       out->mx[a] = T(0);
       out->inv_scale[a] = T(0);
@@ -133,9 +133,13 @@ __global__ void recenter_bbox_kernel(T* __restrict__ y, int64_t n, const double*
   }
 }
 
+// Morton codes of the points in index order. 64-bit codes go to keys; 128-bit
+// codes (D >= 5) are split into lo (also copied to keys, the first sort key)
+// and hi.
 template <class T, int D>
 __global__ void morton_kernel(const T* __restrict__ y, int64_t n, const BoxParams<T>* __restrict__ prm,
-                              uint64_t* __restrict__ keys, uint32_t* __restrict__ idx) {
+                              uint64_t* __restrict__ keys, uint32_t* __restrict__ idx, uint64_t* __restrict__ lo_out,
+                              uint64_t* __restrict__ hi_out) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   constexpr int B = MortonD<D>::BITS;
@@ -143,8 +147,30 @@ __global__ void morton_kernel(const T* __restrict__ y, int64_t n, const BoxParam
   uint32_t q[D];
 #pragma unroll
   for (int a = 0; a < D; ++a) q[a] = quantize<T>(y[i * D + a], prm->mn[a], prm->inv_scale[a], max_bucket);
-  keys[i] = MortonD<D>::encode(q);
+  const typename MortonD<D>::Code c = MortonD<D>::encode(q);
+  if constexpr (sizeof(c) == 8) {
+    keys[i] = (uint64_t)c;
+  } else {
+    keys[i] = (uint64_t)c;
+    lo_out[i] = (uint64_t)c;
+    hi_out[i] = (uint64_t)(c >> 64);
+  }
   idx[i] = (uint32_t)i;
+}
+
+__global__ void gather_u64_kernel(const uint32_t* __restrict__ perm, const uint64_t* __restrict__ src, int64_t n,
+                                  uint64_t* __restrict__ out) {
+  const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s < n) out[s] = src[perm[s]];
+}
+
+__global__ void compose_wide_kernel(const uint32_t* __restrict__ perm, const uint64_t* __restrict__ lo,
+                                    const uint64_t* __restrict__ hi, int64_t n, u128* __restrict__ out) {
+  const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s < n) {
+    const uint32_t p = perm[s];
+    out[s] = ((u128)hi[p] << 64) | (u128)lo[p];
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -319,11 +345,13 @@ __device__ __forceinline__ bool same_set(const Segs& sg, int64_t a, int64_t b) {
 }
 
 template <int D>
-__global__ void tree_mark_kernel(const uint64_t* __restrict__ codes, int64_t n, uint32_t* __restrict__ mask, Segs sg) {
+__global__ void tree_mark_kernel(const typename MortonD<D>::Code* __restrict__ codes, int64_t n,
+                                 uint32_t* __restrict__ mask, Segs sg) {
+  typedef typename MortonD<D>::Code Code;
   const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (s <= 0 || s >= n) return;
   if (!same_set(sg, s - 1, s)) return;
-  const uint64_t c0 = codes[s - 1], c1 = codes[s];
+  const Code c0 = codes[s - 1], c1 = codes[s];
   if (c0 == c1) return;
   constexpr int B = MortonD<D>::BITS;
   const int l = boundary_level<D>(c0, c1);
@@ -334,7 +362,8 @@ __global__ void tree_mark_kernel(const uint64_t* __restrict__ codes, int64_t n, 
   if ((c0 >> sh1) == (codes[a] >> sh1)) atomicOr(&mask[a], 1u << l);
 }
 
-__global__ void tree_count_kernel(const uint64_t* __restrict__ codes, int64_t n, const uint32_t* __restrict__ mask,
+template <class Code>
+__global__ void tree_count_kernel(const Code* __restrict__ codes, int64_t n, const uint32_t* __restrict__ mask,
                                   uint32_t* __restrict__ cnt, Segs sg) {
   const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= n) return;
@@ -343,19 +372,21 @@ __global__ void tree_count_kernel(const uint64_t* __restrict__ codes, int64_t n,
 }
 
 template <class T, int D>
-__global__ void tree_emit_kernel(const uint64_t* __restrict__ codes, int64_t n, const uint32_t* __restrict__ mask,
-                                 const uint64_t* __restrict__ base, const T* __restrict__ ys,
-                                 const double* __restrict__ pre, TreeNodes<T, D> nodes, Segs sg) {
+__global__ void tree_emit_kernel(const typename MortonD<D>::Code* __restrict__ codes, int64_t n,
+                                 const uint32_t* __restrict__ mask, const uint64_t* __restrict__ base,
+                                 const T* __restrict__ ys, const double* __restrict__ pre, TreeNodes<T, D> nodes,
+                                 Segs sg) {
+  typedef typename MortonD<D>::Code Code;
   const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= n) return;
   constexpr int B = MortonD<D>::BITS;
-  const uint64_t c1 = codes[s];
+  const Code c1 = codes[s];
   const bool set_start = s == 0 || !same_set(sg, s - 1, s);
   const bool run_start = set_start || codes[s - 1] != c1;
   int64_t lo, hi;
   seg_bounds(sg, s, n, &lo, &hi);
   if (!set_start && run_start) {
-    const uint64_t c0 = codes[s - 1];
+    const Code c0 = codes[s - 1];
     const int l = boundary_level<D>(c0, c1);
     int64_t a, e;
     cell_range_in<D>(codes, lo, hi, c1, l, &a, &e);
@@ -521,15 +552,12 @@ void launch_recenter_bbox(int D, T* y, int64_t n, const double* mean_sum, bool a
   const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(n, kThreads), 2 * 152));
   T* pmin = ws.part_min.template as<T>();
   T* pmax = ws.part_max.template as<T>();
-  if (D == 1)
-    recenter_bbox_kernel<T, 1><<<grid, kThreads, 0, s>>>(y, n, mean_sum, apply_mean ? 1 : 0, pmin, pmax,
-                                                         ws.done.template as<unsigned>(), ws.params.template as<BoxParams<T>>(), bits);
-  else if (D == 2)
-    recenter_bbox_kernel<T, 2><<<grid, kThreads, 0, s>>>(y, n, mean_sum, apply_mean ? 1 : 0, pmin, pmax,
-                                                         ws.done.template as<unsigned>(), ws.params.template as<BoxParams<T>>(), bits);
-  else
-    recenter_bbox_kernel<T, 3><<<grid, kThreads, 0, s>>>(y, n, mean_sum, apply_mean ? 1 : 0, pmin, pmax,
-                                                         ws.done.template as<unsigned>(), ws.params.template as<BoxParams<T>>(), bits);
+  with_dim<1, 7>(D, "error: the embedding dimension must be in 1..7.", [&](auto dc) {
+    constexpr int DD = decltype(dc)::value;
+    recenter_bbox_kernel<T, DD><<<grid, kThreads, 0, s>>>(y, n, mean_sum, apply_mean ? 1 : 0, pmin, pmax,
+                                                          ws.done.template as<unsigned>(),
+                                                          ws.params.template as<BoxParams<T>>(), bits);
+  });
   BHG_LAUNCH_CHECK();
 }
 
@@ -551,12 +579,20 @@ void BhWorkspace<T>::reserve(int64_t n_, int D_) {
   const int64_t max_nodes = 2 * nn;
   if (D == 2) {
     geom.ensure(max_nodes * sizeof(Node2<T>));
-  } else {
+  } else if (D == 3) {
     geom.ensure(max_nodes * sizeof(Quad<T>));
     word.ensure(max_nodes * sizeof(uint32_t));
+  } else {
+    geom.ensure(max_nodes * sizeof(Oct<T>));
+    word.ensure(max_nodes * sizeof(uint32_t));
   }
-  part_min.ensure(2 * 152 * 3 * sizeof(T));
-  part_max.ensure(2 * 152 * 3 * sizeof(T));
+  if (D >= 5) {
+    wide.ensure(nn * 16);
+    lo_orig.ensure(nn * 8);
+    hi_orig.ensure(nn * 8);
+  }
+  part_min.ensure(2 * 152 * 8 * sizeof(T));
+  part_max.ensure(2 * 152 * 8 * sizeof(T));
   done.ensure(64);
   zdone.ensure(64);
   params.ensure(sizeof(BoxParams<T>));
@@ -575,11 +611,20 @@ static TreeNodes<T, D> nodes_of(BhWorkspace<T>& ws) {
   t.hw2 = nullptr;
   if constexpr (D == 2) {
     t.geom = ws.geom.template as<Node2<T>>();
-  } else {
+  } else if constexpr (D == 3) {
     t.geom = ws.geom.template as<Quad<T>>();
+    t.words = ws.word.template as<uint32_t>();
+  } else {
+    t.geom = ws.geom.template as<Oct<T>>();
     t.words = ws.word.template as<uint32_t>();
   }
   return t;
+}
+
+// Sorted codes as the tree kernels read them.
+template <class T, int D>
+static const typename MortonD<D>::Code* sorted_codes(BhWorkspace<T>& ws) {
+  return static_cast<const typename MortonD<D>::Code*>(D >= 5 ? ws.wide.ptr : ws.keys.ptr);
 }
 
 template <class T, int D>
@@ -589,12 +634,29 @@ template <class T, int D>
 static void bh_build_impl(BhWorkspace<T>& ws, const T* y, int64_t n, cudaStream_t s) {
   constexpr int B = MortonD<D>::BITS;
   const unsigned g = (unsigned)ceil_div(n, kThreads);
+  uint64_t* lo = D >= 5 ? ws.lo_orig.template as<uint64_t>() : nullptr;
+  uint64_t* hi = D >= 5 ? ws.hi_orig.template as<uint64_t>() : nullptr;
   morton_kernel<T, D><<<g, kThreads, 0, s>>>(y, n, ws.params.template as<BoxParams<T>>(), ws.keys.template as<uint64_t>(),
-                                             ws.perm.template as<uint32_t>());
+                                             ws.perm.template as<uint32_t>(), lo, hi);
   BHG_LAUNCH_CHECK();
-  radix_sort_pairs<uint32_t>(ws.keys.template as<uint64_t>(), ws.perm.template as<uint32_t>(),
-                             ws.keys_alt.template as<uint64_t>(), ws.perm_alt.template as<uint32_t>(), n, 0, D * B,
-                             ws.sort_tmp, s);
+  if constexpr (D * B <= 64) {
+    radix_sort_pairs<uint32_t>(ws.keys.template as<uint64_t>(), ws.perm.template as<uint32_t>(),
+                               ws.keys_alt.template as<uint64_t>(), ws.perm_alt.template as<uint32_t>(), n, 0, D * B,
+                               ws.sort_tmp, s);
+  } else {
+    // 128-bit codes: stable LSD sort on the low word, then on the high word
+    radix_sort_pairs<uint32_t>(ws.keys.template as<uint64_t>(), ws.perm.template as<uint32_t>(),
+                               ws.keys_alt.template as<uint64_t>(), ws.perm_alt.template as<uint32_t>(), n, 0, 64,
+                               ws.sort_tmp, s);
+    gather_u64_kernel<<<g, kThreads, 0, s>>>(ws.perm.template as<uint32_t>(), hi, n, ws.keys.template as<uint64_t>());
+    BHG_LAUNCH_CHECK();
+    radix_sort_pairs<uint32_t>(ws.keys.template as<uint64_t>(), ws.perm.template as<uint32_t>(),
+                               ws.keys_alt.template as<uint64_t>(), ws.perm_alt.template as<uint32_t>(), n, 0,
+                               D * B - 64, ws.sort_tmp, s);
+    compose_wide_kernel<<<g, kThreads, 0, s>>>(ws.perm.template as<uint32_t>(), lo, hi, n,
+                                               ws.wide.template as<u128>());
+    BHG_LAUNCH_CHECK();
+  }
   build_from_sorted_impl<T, D>(ws, y, n, Segs(), s);
 }
 
@@ -612,13 +674,13 @@ static void build_from_sorted_impl(BhWorkspace<T>& ws, const T* y, int64_t n, co
                                                                  ws.ys.template as<T>(), ws.pre.template as<double>());
   BHG_LAUNCH_CHECK();
   BHG_CUDA(cudaMemsetAsync(ws.mask.ptr, 0, (size_t)n * 4, s));
-  tree_mark_kernel<D><<<g, kThreads, 0, s>>>(ws.keys.template as<uint64_t>(), n, ws.mask.template as<uint32_t>(), sg);
+  const typename MortonD<D>::Code* codes = sorted_codes<T, D>(ws);
+  tree_mark_kernel<D><<<g, kThreads, 0, s>>>(codes, n, ws.mask.template as<uint32_t>(), sg);
   BHG_LAUNCH_CHECK();
-  tree_count_kernel<<<g, kThreads, 0, s>>>(ws.keys.template as<uint64_t>(), n, ws.mask.template as<uint32_t>(),
-                                           ws.cnt.template as<uint32_t>(), sg);
+  tree_count_kernel<<<g, kThreads, 0, s>>>(codes, n, ws.mask.template as<uint32_t>(), ws.cnt.template as<uint32_t>(), sg);
   BHG_LAUNCH_CHECK();
   scan_u32_to_u64(ws.cnt.template as<uint32_t>(), ws.base.template as<uint64_t>(), n, ws.scan_tmp, s);
-  tree_emit_kernel<T, D><<<g, kThreads, 0, s>>>(ws.keys.template as<uint64_t>(), n, ws.mask.template as<uint32_t>(),
+  tree_emit_kernel<T, D><<<g, kThreads, 0, s>>>(codes, n, ws.mask.template as<uint32_t>(),
                                                 ws.base.template as<uint64_t>(), ws.ys.template as<T>(),
                                                 ws.pre.template as<double>(), nodes_of<T, D>(ws), sg);
   BHG_LAUNCH_CHECK();
@@ -628,9 +690,9 @@ template <class T>
 void bh_build(BhWorkspace<T>& ws, int D, const T* y, int64_t n, cudaStream_t s) {
   if (n <= 0) return;
   if (n > kMaxTreePoints) throw Error(ST_EINVAL, "error: the GPU Barnes-Hut arena holds at most 2^26 - 1 points.");
-  if (D == 2) bh_build_impl<T, 2>(ws, y, n, s);
-  else if (D == 3) bh_build_impl<T, 3>(ws, y, n, s);
-  else throw Error(ST_EINVAL, "error: the GPU Barnes-Hut path covers D in {2, 3}.");
+  with_dim<2, 7>(D, "error: Barnes-Hut covers D in 2..7.", [&](auto dc) {
+    bh_build_impl<T, decltype(dc)::value>(ws, y, n, s);
+  });
 }
 
 template <class T>
@@ -639,7 +701,7 @@ void bh_build_from_sorted(BhWorkspace<T>& ws, int D, const T* y, int64_t n, cons
   if (n > kMaxTreePoints) throw Error(ST_EINVAL, "error: the GPU Barnes-Hut arena holds at most 2^26 - 1 points.");
   if (D == 2) build_from_sorted_impl<T, 2>(ws, y, n, segs, s);
   else if (D == 3) build_from_sorted_impl<T, 3>(ws, y, n, segs, s);
-  else throw Error(ST_EINVAL, "error: the GPU Barnes-Hut path covers D in {2, 3}.");
+  else throw Error(ST_EINVAL, "error: the batched Barnes-Hut path covers D in {2, 3}.");
 }
 
 template <class T>
@@ -652,20 +714,21 @@ void bh_traverse(BhWorkspace<T>& ws, int D, const T* y, int64_t n, T theta, T* n
   const unsigned g = (unsigned)ceil_div(n, kThreads);
   const T theta_sq = theta * theta;
   const uint64_t* M = ws.base.template as<uint64_t>() + n;
-  if (D == 2)
-    bh_traverse_kernel<T, 2><<<g, kThreads, 0, s>>>(y, ws.perm.template as<uint32_t>(), n, nodes_of<T, 2>(ws), M, 2 * n, ws.params.template as<BoxParams<T>>(), theta_sq, neg,
-                                                    qout, ws.zpart.template as<double>(), ws.zdone.template as<unsigned>(),
-                                                    ws.zval.template as<double>(), segs, boxes, ws.base.template as<uint64_t>());
-  else
-    bh_traverse_kernel<T, 3><<<g, kThreads, 0, s>>>(y, ws.perm.template as<uint32_t>(), n, nodes_of<T, 3>(ws), M, 2 * n, ws.params.template as<BoxParams<T>>(), theta_sq, neg,
-                                                    qout, ws.zpart.template as<double>(), ws.zdone.template as<unsigned>(),
-                                                    ws.zval.template as<double>(), segs, boxes, ws.base.template as<uint64_t>());
+  with_dim<2, 7>(D, "error: Barnes-Hut covers D in 2..7.", [&](auto dc) {
+    constexpr int DD = decltype(dc)::value;
+    bh_traverse_kernel<T, DD><<<g, kThreads, 0, s>>>(
+        y, ws.perm.template as<uint32_t>(), n, nodes_of<T, DD>(ws), M, 2 * n, ws.params.template as<BoxParams<T>>(),
+        theta_sq, neg, qout, ws.zpart.template as<double>(), ws.zdone.template as<unsigned>(),
+        ws.zval.template as<double>(), segs, boxes, ws.base.template as<uint64_t>());
+  });
   BHG_LAUNCH_CHECK();
 }
 
 template <class T>
 int bh_bits(int D) {
-  return D == 2 ? MortonD<2>::BITS : MortonD<3>::BITS;
+  int b = 0;
+  with_dim<2, 7>(D, "error: Barnes-Hut covers D in 2..7.", [&](auto dc) { b = MortonD<decltype(dc)::value>::BITS; });
+  return b;
 }
 
 template struct BhWorkspace<float>;

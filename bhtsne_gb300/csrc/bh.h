@@ -10,9 +10,9 @@ namespace bhg {
 // Per-epoch box parameters, written on the device by the bounding-box kernel.
 template <class T>
 struct BoxParams {
-  T mn[3];
-  T mx[3];
-  T inv_scale[3];
+  T mn[8];
+  T mx[8];
+  T inv_scale[8];
   T max_extent;
   T hw2[40];  // squared half width per level, src/tsne/arena.rs:167-174
 };
@@ -24,8 +24,8 @@ struct alignas(16) Quad {
 
 // Packed level + skip word: internal nodes hold (skip << 5) | level, leaves
 // hold all ones (their skip is always index + 1 and they have no level). Five
-// bits cover the levels of D = 2 (0..31) and D = 3 (0..20); 27 bits of skip
-// bound the arena at 2^27 - 1 nodes, i.e. N < 2^26 points.
+// bits cover every level (at most 31, for D = 2); 27 bits of skip bound the
+// arena at 2^27 - 1 nodes, i.e. N < 2^26 points.
 constexpr uint32_t kLeafWord = 0xffffffffu;
 constexpr int64_t kMaxTreePoints = (1LL << 26) - 1;
 
@@ -37,10 +37,45 @@ struct alignas(16) Node2 {
 
 // Node storage, depth-first preorder. D = 2: one 16-byte (f32) record
 // {x, y, mass, word}, a single load per visit. D = 3: {x, y, z, mass} plus a
-// separate word array. The squared half width of an internal node's level is
-// read from a per-launch table (BoxParams::hw2, staged in shared memory).
+// separate word array. D = 4..7: {centre[D], mass} padded to 8 values plus a
+// word array. The squared half width of an internal node's level is read from
+// a per-launch table (BoxParams::hw2, staged in shared memory).
+template <class T>
+struct alignas(8 * sizeof(T)) Oct {
+  T v[8];
+};
+
 template <class T, int D>
-struct TreeNodes;
+struct TreeNodes {
+  static_assert(D >= 4 && D <= 7, "generic node layout is for D = 4..7");
+  Oct<T>* geom;
+  uint32_t* words;
+  const T* hw2;
+  struct Raw {
+    Oct<T> g;
+    uint32_t w;
+  };
+  __device__ __forceinline__ Raw load(uint32_t i) const {
+    Raw r;
+    r.g = geom[i];
+    r.w = words[i];
+    return r;
+  }
+  __device__ __forceinline__ uint32_t word(const Raw& r) const { return r.w; }
+  __device__ __forceinline__ void decode(const Raw& r, T* c, T* mass, T* r2) const {
+#pragma unroll
+    for (int a = 0; a < D; ++a) c[a] = r.g.v[a];
+    *mass = r.g.v[D];
+    *r2 = r.w == kLeafWord ? T(-1) : hw2[r.w & 31u];
+  }
+  __device__ __forceinline__ void write(int64_t i, const T* c, T mass, int level, uint32_t sk) const {
+    Oct<T> g;
+#pragma unroll
+    for (int a = 0; a < 8; ++a) g.v[a] = a < D ? c[a < D ? a : 0] : (a == D ? mass : T(0));
+    geom[i] = g;
+    words[i] = level < 0 ? kLeafWord : ((sk << 5) | (uint32_t)level);
+  }
+};
 
 template <class T>
 struct TreeNodes<T, 2> {
@@ -127,6 +162,7 @@ struct BhWorkspace {
   int D = 0;
   bool zeroed = false;
   DevBuf keys, keys_alt, perm, perm_alt, ys, pre, pre_part, mask, cnt, base, geom, word;
+  DevBuf wide, lo_orig, hi_orig;  // 128-bit codes (D >= 5): sorted codes and the unsorted halves
   DevBuf part_min, part_max, done, zdone, params, zpart, zval, sort_tmp, scan_tmp;
   void reserve(int64_t n, int D);
   const double* z() const { return static_cast<const double*>(zval.ptr); }

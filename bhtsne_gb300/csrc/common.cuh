@@ -12,6 +12,7 @@
 #include <cstdio>
 #include <stdexcept>
 #include <string>
+#include <type_traits>
 
 namespace bhg {
 
@@ -160,6 +161,23 @@ __device__ __forceinline__ V block_max_parts(const V* part, unsigned count, unsi
 }
 
 // Rust `signum`: +1 for +0.0 and positives, -1 for -0.0 and negatives, NaN for NaN.
+// Calls f(std::integral_constant<int, D>()) for a runtime D in [lo, hi]
+// (lo >= 1, hi <= 7); throws EINVAL with msg otherwise.
+template <int lo, int hi, class F>
+inline void with_dim(int D, const char* msg, F&& f) {
+  if (D < lo || D > hi) throw Error(ST_EINVAL, msg);
+  switch (D) {
+    case 1: if constexpr (lo <= 1 && 1 <= hi) f(std::integral_constant<int, 1>()); break;
+    case 2: if constexpr (lo <= 2 && 2 <= hi) f(std::integral_constant<int, 2>()); break;
+    case 3: if constexpr (lo <= 3 && 3 <= hi) f(std::integral_constant<int, 3>()); break;
+    case 4: if constexpr (lo <= 4 && 4 <= hi) f(std::integral_constant<int, 4>()); break;
+    case 5: if constexpr (lo <= 5 && 5 <= hi) f(std::integral_constant<int, 5>()); break;
+    case 6: if constexpr (lo <= 6 && 6 <= hi) f(std::integral_constant<int, 6>()); break;
+    case 7: if constexpr (lo <= 7 && 7 <= hi) f(std::integral_constant<int, 7>()); break;
+    default: throw Error(ST_EINVAL, msg);
+  }
+}
+
 template <class T>
 __device__ __forceinline__ T signum(T x) {
   return isnan(x) ? x : copysign(T(1), x);

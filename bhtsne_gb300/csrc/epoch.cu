@@ -457,9 +457,10 @@ void launch_attractive(int D, const uint64_t* rows, const uint32_t* cols, const 
     const char* v = getenv("BHTSNE_ATTRACTIVE_VARIANT");
     return v ? atoi(v) : 0;
   }();
-  if (D == 1) launch_attractive_d<T, 1>(variant, rows, cols, vals, y, n, pos, s, row_of_slot);
-  else if (D == 2) launch_attractive_d<T, 2>(variant, rows, cols, vals, y, n, pos, s, row_of_slot);
-  else launch_attractive_d<T, 3>(variant, rows, cols, vals, y, n, pos, s, row_of_slot);
+  with_dim<1, 7>(D, "error: the embedding dimension must be in 1..7.", [&](auto dc) {
+    constexpr int DD = decltype(dc)::value;
+    launch_attractive_d<T, DD>(variant, rows, cols, vals, y, n, pos, s, row_of_slot);
+  });
   BHG_LAUNCH_CHECK();
 }
 
@@ -469,12 +470,10 @@ void launch_renumber(int D, const uint32_t* order, int64_t n, Renumbering& r, T*
   const unsigned g = (unsigned)ceil_div(n, 256);
   uint32_t* ext_new = static_cast<uint32_t*>(r.ext_alt.ensure((size_t)n * 4));
   const uint32_t* ext_old = r.active ? r.ext.template as<uint32_t>() : nullptr;
-  if (D == 1)
-    renumber_gather_kernel<T, 1><<<g, 256, 0, s>>>(order, ext_old, n, y, uy, gains, tmp_a, tmp_b, tmp_c, ext_new);
-  else if (D == 2)
-    renumber_gather_kernel<T, 2><<<g, 256, 0, s>>>(order, ext_old, n, y, uy, gains, tmp_a, tmp_b, tmp_c, ext_new);
-  else
-    renumber_gather_kernel<T, 3><<<g, 256, 0, s>>>(order, ext_old, n, y, uy, gains, tmp_a, tmp_b, tmp_c, ext_new);
+  with_dim<1, 7>(D, "error: the embedding dimension must be in 1..7.", [&](auto dc) {
+    constexpr int DD = decltype(dc)::value;
+    renumber_gather_kernel<T, DD><<<g, 256, 0, s>>>(order, ext_old, n, y, uy, gains, tmp_a, tmp_b, tmp_c, ext_new);
+  });
   BHG_LAUNCH_CHECK();
   const size_t bytes = (size_t)n * D * sizeof(T);
   BHG_CUDA(cudaMemcpyAsync(y, tmp_a, bytes, cudaMemcpyDeviceToDevice, s));
@@ -504,26 +503,28 @@ void launch_renumber(int D, const uint32_t* order, int64_t n, Renumbering& r, T*
 template <class T>
 void launch_unpermute(int D, const T* y, const uint32_t* ext, int64_t n, T* out, cudaStream_t s) {
   const unsigned g = (unsigned)ceil_div(n, 256);
-  if (D == 1) unpermute_kernel<T, 1><<<g, 256, 0, s>>>(y, ext, n, out);
-  else if (D == 2) unpermute_kernel<T, 2><<<g, 256, 0, s>>>(y, ext, n, out);
-  else unpermute_kernel<T, 3><<<g, 256, 0, s>>>(y, ext, n, out);
+  with_dim<1, 7>(D, "error: the embedding dimension must be in 1..7.", [&](auto dc) {
+    constexpr int DD = decltype(dc)::value;
+    unpermute_kernel<T, DD><<<g, 256, 0, s>>>(y, ext, n, out);
+  });
   BHG_LAUNCH_CHECK();
 }
 
 template <class T>
 void launch_update(int D, T* y, const T* pos, const T* neg, T* uy, T* gains, int64_t n, const double* z, T inv_norm,
                    T lr, T momentum, UpdateScratch& us, cudaStream_t s) {
-  double* part = static_cast<double*>(us.part.ensure(kUpdBlocks * 3 * sizeof(double)));
+  double* part = static_cast<double*>(us.part.ensure(kUpdBlocks * 8 * sizeof(double)));
   unsigned* done = static_cast<unsigned*>(us.done.ensure(64));
   if (!us.zeroed) {
     BHG_CUDA(cudaMemset(done, 0, 64));
     us.zeroed = true;
   }
-  double* mean_sum = static_cast<double*>(us.mean_sum.ensure(3 * sizeof(double)));
+  double* mean_sum = static_cast<double*>(us.mean_sum.ensure(8 * sizeof(double)));
   const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(n, 256), kUpdBlocks));
-  if (D == 1) update_kernel<T, 1><<<grid, 256, 0, s>>>(y, pos, neg, uy, gains, n, z, inv_norm, lr, momentum, part, done, mean_sum);
-  else if (D == 2) update_kernel<T, 2><<<grid, 256, 0, s>>>(y, pos, neg, uy, gains, n, z, inv_norm, lr, momentum, part, done, mean_sum);
-  else update_kernel<T, 3><<<grid, 256, 0, s>>>(y, pos, neg, uy, gains, n, z, inv_norm, lr, momentum, part, done, mean_sum);
+  with_dim<1, 7>(D, "error: the embedding dimension must be in 1..7.", [&](auto dc) {
+    constexpr int DD = decltype(dc)::value;
+    update_kernel<T, DD><<<grid, 256, 0, s>>>(y, pos, neg, uy, gains, n, z, inv_norm, lr, momentum, part, done, mean_sum);
+  });
   BHG_LAUNCH_CHECK();
 }
 
@@ -532,9 +533,10 @@ void launch_kl_sparse(int D, const uint64_t* rows, const uint32_t* cols, const T
                       const double* z, bool quirk, double* out, DevBuf& tmp, cudaStream_t s) {
   const int blocks = 2 * 152;
   double* part = static_cast<double*>(tmp.ensure(blocks * sizeof(double)));
-  if (D == 1) kl_sparse_kernel<T, 1><<<blocks, 256, 0, s>>>(rows, cols, vals, y, n, z, quirk ? 1 : 0, part);
-  else if (D == 2) kl_sparse_kernel<T, 2><<<blocks, 256, 0, s>>>(rows, cols, vals, y, n, z, quirk ? 1 : 0, part);
-  else kl_sparse_kernel<T, 3><<<blocks, 256, 0, s>>>(rows, cols, vals, y, n, z, quirk ? 1 : 0, part);
+  with_dim<1, 7>(D, "error: the embedding dimension must be in 1..7.", [&](auto dc) {
+    constexpr int DD = decltype(dc)::value;
+    kl_sparse_kernel<T, DD><<<blocks, 256, 0, s>>>(rows, cols, vals, y, n, z, quirk ? 1 : 0, part);
+  });
   BHG_LAUNCH_CHECK();
   reduce_parts_kernel<<<1, 32, 0, s>>>(part, blocks, out);
   BHG_LAUNCH_CHECK();
@@ -557,9 +559,10 @@ void launch_dense_symmetrize(T* p, int64_t n, cudaStream_t s) {
 template <class T>
 void launch_exact_z(int D, const T* y, int64_t n, double* z, DevBuf& tmp, cudaStream_t s) {
   double* part = static_cast<double*>(tmp.ensure(n * sizeof(double)));
-  if (D == 1) exact_z_kernel<T, 1><<<(unsigned)n, 256, 0, s>>>(y, n, part);
-  else if (D == 2) exact_z_kernel<T, 2><<<(unsigned)n, 256, 0, s>>>(y, n, part);
-  else exact_z_kernel<T, 3><<<(unsigned)n, 256, 0, s>>>(y, n, part);
+  with_dim<1, 7>(D, "error: the embedding dimension must be in 1..7.", [&](auto dc) {
+    constexpr int DD = decltype(dc)::value;
+    exact_z_kernel<T, DD><<<(unsigned)n, 256, 0, s>>>(y, n, part);
+  });
   BHG_LAUNCH_CHECK();
   reduce_parts_kernel<<<1, 32, 0, s>>>(part, (int)n, z);
   BHG_LAUNCH_CHECK();
@@ -567,9 +570,10 @@ void launch_exact_z(int D, const T* y, int64_t n, double* z, DevBuf& tmp, cudaSt
 
 template <class T>
 void launch_exact_grad(int D, const T* y, const T* p, int64_t n, const double* z, T* dy, cudaStream_t s) {
-  if (D == 1) exact_grad_kernel<T, 1><<<(unsigned)n, 256, 0, s>>>(y, p, n, z, dy);
-  else if (D == 2) exact_grad_kernel<T, 2><<<(unsigned)n, 256, 0, s>>>(y, p, n, z, dy);
-  else exact_grad_kernel<T, 3><<<(unsigned)n, 256, 0, s>>>(y, p, n, z, dy);
+  with_dim<1, 7>(D, "error: the embedding dimension must be in 1..7.", [&](auto dc) {
+    constexpr int DD = decltype(dc)::value;
+    exact_grad_kernel<T, DD><<<(unsigned)n, 256, 0, s>>>(y, p, n, z, dy);
+  });
   BHG_LAUNCH_CHECK();
 }
 
@@ -577,9 +581,10 @@ template <class T>
 void launch_exact_kl(int D, const T* y, const T* p, int64_t n, const double* z, double* out, DevBuf& tmp,
                      cudaStream_t s) {
   double* part = static_cast<double*>(tmp.ensure(n * sizeof(double)));
-  if (D == 1) exact_kl_kernel<T, 1><<<(unsigned)n, 256, 0, s>>>(y, p, n, z, part);
-  else if (D == 2) exact_kl_kernel<T, 2><<<(unsigned)n, 256, 0, s>>>(y, p, n, z, part);
-  else exact_kl_kernel<T, 3><<<(unsigned)n, 256, 0, s>>>(y, p, n, z, part);
+  with_dim<1, 7>(D, "error: the embedding dimension must be in 1..7.", [&](auto dc) {
+    constexpr int DD = decltype(dc)::value;
+    exact_kl_kernel<T, DD><<<(unsigned)n, 256, 0, s>>>(y, p, n, z, part);
+  });
   BHG_LAUNCH_CHECK();
   reduce_parts_kernel<<<1, 32, 0, s>>>(part, (int)n, out);
   BHG_LAUNCH_CHECK();

@@ -64,8 +64,8 @@ const char* bhtsne_version(void);
 /* ---- builder ------------------------------------------------------------- */
 /* tSNE::new (src/lib.rs:241-266): defaults lr auto, 1000 epochs, momentum
  * 0.5 -> 0.8 at epoch 250, stop lying at 250, exaggeration 12, perplexity 20.
- * `embed_dim` is the const generic D: 2..3 for Barnes-Hut, 1..2 for FIt-SNE,
- * 1..3 for exact. */
+ * `embed_dim` is the const generic D: 2..7 for Barnes-Hut (the reference's
+ * Morton<D> bound), 1..2 for FIt-SNE, 1..7 for exact. */
 int bhtsne_tsne_new(bhtsne_ctx* ctx, int dtype, int32_t embed_dim, int64_t n_samples, bhtsne_tsne** out);
 int bhtsne_tsne_free(bhtsne_tsne* t);
 const char* bhtsne_tsne_last_error(const bhtsne_tsne* t);

@@ -35,6 +35,7 @@
 #include <limits>
 #include <numeric>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #ifdef _OPENMP
@@ -281,20 +282,82 @@ static inline uint64_t part1by2(uint64_t x) {
   return (x | (x << 2)) & 0x1249249249249249ULL;
 }
 
+// Codecs of src/tsne/morton/d2.rs-d7.rs: bits per axis 32, 21, 16, 25, 21,
+// 18 for D = 2..7; u64 words up to D = 4, u128 beyond. Bit b of axis a is
+// code bit b * D + a.
+typedef unsigned __int128 u128;
+
+template <class C, int D, uint32_t B>
+static C interleave(const uint32_t* c) {
+  C code = 0;
+  for (uint32_t b = 0; b < B; ++b)
+    for (int a = 0; a < D; ++a) code |= (C)((c[a] >> b) & 1u) << (b * D + a);
+  return code;
+}
+
 template <int D>
 struct MortonSpec;
 template <>
 struct MortonSpec<2> {
   static constexpr uint32_t BITS = 32;
+  typedef uint64_t Code;
   static uint64_t encode(const uint32_t* c) { return part1by1(c[0]) | (part1by1(c[1]) << 1); }
 };
 template <>
 struct MortonSpec<3> {
   static constexpr uint32_t BITS = 21;
+  typedef uint64_t Code;
   static uint64_t encode(const uint32_t* c) {
     return part1by2(c[0]) | (part1by2(c[1]) << 1) | (part1by2(c[2]) << 2);
   }
 };
+template <>
+struct MortonSpec<4> {
+  static constexpr uint32_t BITS = 16;
+  typedef uint64_t Code;
+  static Code encode(const uint32_t* c) { return interleave<Code, 4, 16>(c); }
+};
+template <>
+struct MortonSpec<5> {
+  static constexpr uint32_t BITS = 25;
+  typedef u128 Code;
+  static Code encode(const uint32_t* c) { return interleave<Code, 5, 25>(c); }
+};
+template <>
+struct MortonSpec<6> {
+  static constexpr uint32_t BITS = 21;
+  typedef u128 Code;
+  static Code encode(const uint32_t* c) { return interleave<Code, 6, 21>(c); }
+};
+template <>
+struct MortonSpec<7> {
+  static constexpr uint32_t BITS = 18;
+  typedef u128 Code;
+  static Code encode(const uint32_t* c) { return interleave<Code, 7, 18>(c); }
+};
+
+static inline uint32_t msb_position(uint64_t x) { return 63u - (uint32_t)__builtin_clzll(x); }
+static inline uint32_t msb_position(u128 x) {
+  const uint64_t hi = (uint64_t)(x >> 64);
+  return hi ? 64u + msb_position(hi) : msb_position((uint64_t)x);
+}
+
+// Calls f(std::integral_constant<int, D>()) for D in [lo, hi]; false otherwise.
+template <int lo, int hi, class F>
+static bool with_d(int D, F&& f) {
+  bool ok = true;
+  switch (D) {
+    case 1: if constexpr (lo <= 1 && 1 <= hi) f(std::integral_constant<int, 1>()); else ok = false; break;
+    case 2: if constexpr (lo <= 2 && 2 <= hi) f(std::integral_constant<int, 2>()); else ok = false; break;
+    case 3: if constexpr (lo <= 3 && 3 <= hi) f(std::integral_constant<int, 3>()); else ok = false; break;
+    case 4: if constexpr (lo <= 4 && 4 <= hi) f(std::integral_constant<int, 4>()); else ok = false; break;
+    case 5: if constexpr (lo <= 5 && 5 <= hi) f(std::integral_constant<int, 5>()); else ok = false; break;
+    case 6: if constexpr (lo <= 6 && 6 <= hi) f(std::integral_constant<int, 6>()); else ok = false; break;
+    case 7: if constexpr (lo <= 7 && 7 <= hi) f(std::integral_constant<int, 7>()); else ok = false; break;
+    default: ok = false;
+  }
+  return ok;
+}
 
 template <class T>
 static inline uint32_t quantize_axis(T v, T mn, T inv_scale, uint32_t max_bucket) {
@@ -330,7 +393,8 @@ template <class T, int D>
 struct Arena {
   std::vector<Node<T, D>> nodes;
   std::vector<std::pair<uint32_t, uint32_t>> ranges;
-  std::vector<std::pair<uint64_t, uint32_t>> sorted;
+  typedef typename MortonSpec<D>::Code Code;
+  std::vector<std::pair<Code, uint32_t>> sorted;
   std::vector<T> level_half_width_sq;
 
   void rebuild(const T* y, int64_t n) {
@@ -384,7 +448,7 @@ struct Arena {
     root.level = (uint8_t)bits;
     nodes.push_back(root);
     ranges.push_back({0u, (uint32_t)n});
-    const uint64_t mask = (1ULL << D) - 1;
+    const Code mask = ((Code)1 << D) - 1;
     size_t node = 0;
     while (node < nodes.size()) {
       uint32_t start = ranges[node].first, end = ranges[node].second;
@@ -392,8 +456,8 @@ struct Arena {
         node += 1;
         continue;
       }
-      uint64_t x = sorted[start].first ^ sorted[end - 1].first;
-      uint32_t highest = 63u - (uint32_t)__builtin_clzll(x);
+      const Code x = sorted[start].first ^ sorted[end - 1].first;
+      uint32_t highest = msb_position(x);
       uint32_t level = (bits - 1) - highest / D;
       uint32_t shift = D * (bits - 1 - level);
       nodes[node].level = (uint8_t)level;
@@ -401,7 +465,7 @@ struct Arena {
       uint32_t child_count = 0;
       uint32_t cs = start;
       while (cs < end) {
-        uint64_t group = (sorted[cs].first >> shift) & mask;
+        const Code group = (sorted[cs].first >> shift) & mask;
         uint32_t ce = cs + 1;
         while (ce < end && ((sorted[ce].first >> shift) & mask) == group) ce += 1;
         Node<T, D> c{};
@@ -1088,9 +1152,10 @@ struct TSNE {
 
   int dispatch_loop(int kind, T theta) {
     if (kind == FIT_BH) {
-      if (D == 2) return run_loop<2>(kind, theta);
-      if (D == 3) return run_loop<3>(kind, theta);
-      return fail("error: the oracle's Barnes-Hut path covers D in {2, 3}.");
+      int rc = 0;
+      if (!with_d<2, 7>(D, [&](auto dc) { rc = run_loop<decltype(dc)::value>(kind, theta); }))
+        return fail("error: Barnes-Hut covers D in 2..7.");
+      return rc;
     }
     if (D == 1) return run_loop<1>(kind, theta);
     if (D == 2) return run_loop<2>(kind, theta);
@@ -1234,29 +1299,25 @@ struct TSNE {
   bool kl(bool quirk, T* out) {
     if (fit == FIT_NONE) return false;
     if (fit == FIT_EXACT) {
-      if (D == 1) *out = exact_kl<T, 1>(p_values.data(), y.data(), n);
-      else if (D == 2) *out = exact_kl<T, 2>(p_values.data(), y.data(), n);
-      else *out = exact_kl<T, 3>(p_values.data(), y.data(), n);
+      with_d<1, 7>(D, [&](auto dc) { *out = exact_kl<T, decltype(dc)::value>(p_values.data(), y.data(), n); });
       return true;
     }
     T z;
     std::vector<T> neg(n * D), qs(n);
     if (fit == FIT_BH) {
-      if (D == 2) {
-        Arena<T, 2> a;
-        z = bh_repulsion<T, 2>(a, y.data(), n, fit_theta, neg.data(), qs.data());
-      } else {
-        Arena<T, 3> a;
-        z = bh_repulsion<T, 3>(a, y.data(), n, fit_theta, neg.data(), qs.data());
-      }
+      with_d<2, 7>(D, [&](auto dc) {
+        constexpr int DD = decltype(dc)::value;
+        Arena<T, DD> a;
+        z = bh_repulsion<T, DD>(a, y.data(), n, fit_theta, neg.data(), qs.data());
+      });
     } else {
       if (D == 1) z = fit_repulsion<T, 1>(y.data(), n, neg.data(), nullptr);
       else z = fit_repulsion<T, 2>(y.data(), n, neg.data(), nullptr);
     }
     T inv = T(1) / z;
-    if (D == 1) *out = sparse_kl<T, 1>(p_rows.data(), p_columns.data(), p_values.data(), y.data(), n, inv, quirk);
-    else if (D == 2) *out = sparse_kl<T, 2>(p_rows.data(), p_columns.data(), p_values.data(), y.data(), n, inv, quirk);
-    else *out = sparse_kl<T, 3>(p_rows.data(), p_columns.data(), p_values.data(), y.data(), n, inv, quirk);
+    with_d<1, 7>(D, [&](auto dc) {
+      *out = sparse_kl<T, decltype(dc)::value>(p_rows.data(), p_columns.data(), p_values.data(), y.data(), n, inv, quirk);
+    });
     return true;
   }
 };
@@ -1339,10 +1400,10 @@ void orc_normalize(int dtype, void* vals, int64_t nnz, double exaggeration) {
 int orc_edge_forces(int dtype, int32_t D, const void* y, int64_t n, const uint64_t* rows,
                     const uint32_t* cols, const void* vals, void* pos) {
   ORC_T(dtype, {
-    if (D == 1) edge_forces<T, 1>((const T*)y, n, rows, cols, (const T*)vals, (T*)pos);
-    else if (D == 2) edge_forces<T, 2>((const T*)y, n, rows, cols, (const T*)vals, (T*)pos);
-    else if (D == 3) edge_forces<T, 3>((const T*)y, n, rows, cols, (const T*)vals, (T*)pos);
-    else return 22;
+    if (!with_d<1, 7>(D, [&](auto dc) {
+          edge_forces<T, decltype(dc)::value>((const T*)y, n, rows, cols, (const T*)vals, (T*)pos);
+        }))
+      return 22;
   });
   return 0;
 }
@@ -1351,16 +1412,13 @@ int orc_edge_forces(int dtype, int32_t D, const void* y, int64_t n, const uint64
 int orc_bh_repulsion(int dtype, int32_t D, const void* y, int64_t n, double theta, void* neg,
                      void* q_sums, double* z_out) {
   ORC_T(dtype, {
-    T z;
-    if (D == 2) {
-      Arena<T, 2> a;
-      z = bh_repulsion<T, 2>(a, (const T*)y, n, (T)theta, (T*)neg, (T*)q_sums);
-    } else if (D == 3) {
-      Arena<T, 3> a;
-      z = bh_repulsion<T, 3>(a, (const T*)y, n, (T)theta, (T*)neg, (T*)q_sums);
-    } else {
+    T z = T(0);
+    if (!with_d<2, 7>(D, [&](auto dc) {
+          constexpr int DD = decltype(dc)::value;
+          Arena<T, DD> a;
+          z = bh_repulsion<T, DD>(a, (const T*)y, n, (T)theta, (T*)neg, (T*)q_sums);
+        }))
       return 22;
-    }
     *z_out = (double)z;
   });
   return 0;
@@ -1385,15 +1443,12 @@ int64_t orc_bh_tree(int dtype, int32_t D, const void* y, int64_t n, void* com, u
         if (range_end) range_end[v] = a.ranges[v].second;
       }
     };
-    if (D == 2) {
-      Arena<T, 2> a;
+    with_d<2, 7>(D, [&](auto dc) {
+      constexpr int DD = decltype(dc)::value;
+      Arena<T, DD> a;
       a.rebuild((const T*)y, n);
-      dump(a, 2);
-    } else if (D == 3) {
-      Arena<T, 3> a;
-      a.rebuild((const T*)y, n);
-      dump(a, 3);
-    }
+      dump(a, DD);
+    });
   });
   return nn;
 }
@@ -1435,11 +1490,21 @@ double orc_sparse_kl(int dtype, int32_t D, const uint64_t* rows, const uint32_t*
                      const void* vals, const void* y, int64_t n, double inv_q_sum, int quirk) {
   double out = 0;
   ORC_T(dtype, {
-    if (D == 1) out = sparse_kl<T, 1>(rows, cols, (const T*)vals, (const T*)y, n, (T)inv_q_sum, quirk != 0);
-    else if (D == 2) out = sparse_kl<T, 2>(rows, cols, (const T*)vals, (const T*)y, n, (T)inv_q_sum, quirk != 0);
-    else out = sparse_kl<T, 3>(rows, cols, (const T*)vals, (const T*)y, n, (T)inv_q_sum, quirk != 0);
+    with_d<1, 7>(D, [&](auto dc) {
+      out = sparse_kl<T, decltype(dc)::value>(rows, cols, (const T*)vals, (const T*)y, n, (T)inv_q_sum, quirk != 0);
+    });
   });
   return out;
+}
+
+// Morton code of D coordinates (D = 2..7) as two 64-bit halves.
+int orc_morton(int32_t D, const uint32_t* c, uint64_t* lo, uint64_t* hi) {
+  bool ok = with_d<2, 7>(D, [&](auto dc) {
+    const auto code = MortonSpec<decltype(dc)::value>::encode(c);
+    *lo = (uint64_t)code;
+    *hi = (uint64_t)((u128)code >> 64);
+  });
+  return ok ? 0 : 22;
 }
 
 uint64_t orc_morton2(uint32_t a, uint32_t b) {

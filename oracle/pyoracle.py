@@ -56,6 +56,7 @@ def lib():
             "orc_gradient_step": (None, [C.c_int, vp, vp, vp, vp, vp, i64, dbl, dbl, dbl]),
             "orc_zero_mean": (None, [C.c_int, vp, i64, i32]),
             "orc_sparse_kl": (dbl, [C.c_int, i32, u64p, u32p, vp, vp, i64, dbl, C.c_int]),
+            "orc_morton": (C.c_int, [i32, vp, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
             "orc_morton2": (C.c_uint64, [C.c_uint32, C.c_uint32]),
             "orc_morton3": (C.c_uint64, [C.c_uint32, C.c_uint32, C.c_uint32]),
             "orc_quantize_f32": (C.c_uint32, [C.c_float, C.c_float, C.c_float, C.c_uint32]),
@@ -210,6 +211,15 @@ def sparse_kl(rows, cols, vals, y, inv_q_sum, quirk=True):
     n, D = y.shape
     return lib().orc_sparse_kl(_dt(y), D, _p(rows), _p(cols), _p(vals), _p(y), n, float(inv_q_sum),
                                1 if quirk else 0)
+
+
+def morton(coords):
+    """Morton code of D = len(coords) quantised coordinates (D = 2..7) as an int."""
+    c = np.ascontiguousarray(coords, dtype=np.uint32)
+    lo, hi = C.c_uint64(), C.c_uint64()
+    rc = lib().orc_morton(len(c), _p(c), C.byref(lo), C.byref(hi))
+    assert rc == 0
+    return (hi.value << 64) | lo.value
 
 
 def morton2(a, b):

@@ -271,3 +271,20 @@ def test_locality_renumbering_preserves_the_fit(gpu, monkeypatch, method):
     assert np.array_equal(a0.columns, a1.columns) and np.array_equal(a0.values, a1.values)
     # clusters are found in the caller's order
     assert same_cluster_fraction(e1, lab) > 0.95
+
+
+@pytest.mark.parametrize("D", [4, 5, 7])
+def test_wide_barnes_hut_fit_matches_oracle(gpu, oracle, D):
+    """Barnes-Hut into D = 4..7 (128-bit Morton codes from D = 5): same
+    kNN table and seed through the GPU and the oracle, final KL within 1 %."""
+    X, _ = blobs(1500, 30, 6, 900 + D)
+    idx, dist = oracle.knn(X, 45)
+    seed = np.random.default_rng(D).normal(0, 1e-4, size=(1500, D)).astype(np.float32)
+    g = gpu.TSNE(1500, D=D).perplexity(15).epochs(400).initial_embedding(seed)
+    g.barnes_hut_with_neighbors(0.5, (idx, dist))
+    o = oracle.TSNE(1500, D=D).perplexity(15).epochs(400).initial_embedding(seed)
+    o.barnes_hut_with_neighbors(0.5, idx.astype(np.uint64), dist)
+    assert np.all(np.isfinite(g.embedding()))
+    for quirk in (True, False):
+        kg, ko = g.kl_divergence(quirk), o.kl_divergence(quirk)
+        assert abs(kg - ko) / abs(ko) < 0.01, (D, quirk, kg, ko)

@@ -40,7 +40,7 @@ def test_symmetrize_bit_exact(gpu, oracle):
     assert np.array_equal(gv, ov)
 
 
-@pytest.mark.parametrize("D", [2, 3])
+@pytest.mark.parametrize("D", [2, 3, 4, 5, 6, 7])
 def test_bh_gradient(gpu, oracle, D):
     X, _ = blobs(2000, 20, 5, 4)
     oi, od = oracle.knn(X, 90)

@@ -282,3 +282,38 @@ def test_symmetrize_properties(oracle):
     assert abs(vals.sum() - n) / n < 1e-5  # each conditional row sums to ~1, halved twice over
     norm = oracle.normalize(vals, 1.0)
     assert abs(norm.sum() - 1.0) < 0.05
+
+
+@pytest.mark.parametrize("D,bits", [(4, 16), (5, 25), (6, 21), (7, 18)])
+def test_morton_wide_codecs(oracle, D, bits):
+    """src/tsne/morton/d4.rs-d7.rs: bit b of axis a at code bit b * D + a
+    (d5.rs-d7.rs spread through nibble tables into a u128; d4.rs by masks)."""
+    rng = np.random.default_rng(40 + D)
+    for _ in range(100):
+        c = [int(v) for v in rng.integers(0, 2 ** bits, size=D)]
+        code = oracle.morton(c)
+        assert code < (1 << (D * bits))
+        for a in range(D):
+            assert sum(((code >> (b * D + a)) & 1) << b for b in range(bits)) == c[a]
+    # the top bit of the last axis is the code's most significant bit
+    top = [0] * D
+    top[-1] = 1 << (bits - 1)
+    assert oracle.morton(top) == 1 << (D * bits - 1)
+
+
+@pytest.mark.parametrize("D", [4, 5, 6, 7])
+def test_oracle_wide_arena_matches_exact_repulsion(oracle, D):
+    """The D = 4..7 arena conserves points and, with a tiny theta, its
+    repulsion equals the exact sum over all other points."""
+    rng = np.random.default_rng(70 + D)
+    y = rng.normal(0, 2.0, size=(600, D)).astype(np.float64)
+    t = oracle.bh_tree(y)
+    leaves = t["first_child"] == 0xFFFFFFFF
+    assert t["count"][0] == 600 and t["count"][leaves].sum() == 600
+    neg, q, z = oracle.bh_repulsion(y, 1e-6)
+    d = y[:, None, :] - y[None, :, :]
+    w = 1.0 / (1.0 + (d ** 2).sum(-1))
+    np.fill_diagonal(w, 0.0)
+    ref_neg = ((w ** 2)[:, :, None] * d).sum(1)
+    assert abs(z - w.sum()) / w.sum() < 1e-12
+    assert np.max(np.abs(neg - ref_neg)) < 1e-12 * max(1.0, np.abs(ref_neg).max())
