@@ -7,11 +7,12 @@ Python mirror of the reference's `tSNE` builder over that ABI.
 from ._lib import (BhtsneError, Context, F32, F64, METHOD_BARNES_HUT, METHOD_EXACT, METHOD_FIT_SNE, SIGNATURES,
                    default_context, library_path, load)
 from .batch import Batch
+from .serve import Server
 from .tsne import (Neighbor, SparseAffinities, TSNE, conditional_p, gradient, knn_euclidean, neighbors_to_arrays,
                    symmetrize, update)
 
 __all__ = [
-    "Batch", "BhtsneError", "Context", "F32", "F64", "METHOD_BARNES_HUT", "METHOD_EXACT", "METHOD_FIT_SNE", "SIGNATURES",
+    "Batch", "BhtsneError", "Server", "Context", "F32", "F64", "METHOD_BARNES_HUT", "METHOD_EXACT", "METHOD_FIT_SNE", "SIGNATURES",
     "default_context", "library_path", "load", "Neighbor", "SparseAffinities", "TSNE", "conditional_p", "gradient",
     "knn_euclidean", "neighbors_to_arrays", "symmetrize", "update",
 ]

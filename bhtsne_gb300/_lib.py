@@ -73,7 +73,42 @@ SIGNATURES = {
     "bhtsne_batch_embedding": (C.c_int, [_vp, _i64, _vp]),
     "bhtsne_batch_kl_divergence": (C.c_int, [_vp, _i64, _i32, _dblp]),
     "bhtsne_batch_timings": (C.c_int, [_vp, _dblp, _dblp]),
+    "bhtsne_server_params_default": (None, [_vp]),
+    "bhtsne_server_new": (C.c_int, [_vp, C.c_int, _i32, _vp, C.POINTER(C.c_void_p)]),
+    "bhtsne_server_free": (C.c_int, [_vp]),
+    "bhtsne_server_last_error": (C.c_char_p, [_vp]),
+    "bhtsne_server_submit": (C.c_int, [_vp, _vp, _i64p]),
+    "bhtsne_server_poll": (C.c_int, [_vp, _i64, _i32p]),
+    "bhtsne_server_wait": (C.c_int, [_vp, _i64, _dbl]),
+    "bhtsne_server_result": (C.c_int, [_vp, _i64, _vp, _dblp, _dblp]),
+    "bhtsne_server_stats": (C.c_int, [_vp, _i64p, _i64p, _i64p, _dblp]),
 }
+
+JOB_QUEUED, JOB_RUNNING, JOB_DONE, JOB_FAILED = 0, 1, 2, 3
+
+
+class ServerParams(C.Structure):
+    """Mirror of struct bhtsne_server_params."""
+    _fields_ = [
+        ("perplexity", C.c_double),
+        ("theta", C.c_double),
+        ("hbm_budget_bytes", C.c_int64),
+        ("round_epochs", C.c_int32),
+        ("fit_workers", C.c_int32),
+    ]
+
+
+class Request(C.Structure):
+    """Mirror of struct bhtsne_request."""
+    _fields_ = [
+        ("data", C.c_void_p),
+        ("n", C.c_int64),
+        ("dim", C.c_int32),
+        ("method", C.c_int32),
+        ("epochs", C.c_int64),
+        ("seed", C.c_uint64),
+        ("want_kl", C.c_int32),
+    ]
 
 
 class BatchParams(C.Structure):

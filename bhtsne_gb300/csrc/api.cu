@@ -37,6 +37,10 @@ struct bhtsne_ctx {
   std::string err;
 };
 
+namespace bhg {
+int ctx_device(const bhtsne_ctx* ctx) { return ctx->device; }
+}
+
 namespace {
 
 const char* kVersion = "bhtsne-gb300 0.1.0 (restates bhtsne 0.7.10)";
@@ -1188,14 +1192,6 @@ struct bhtsne_batch {
 
 namespace {
 
-// Affinities of jobs prepared together: one block-diagonal CSR over their
-// rows in job order.
-template <class T>
-struct BatchGroup {
-  DevBuf rows, cols, vals;
-  std::vector<uint64_t> rows_h;  // host copy of the row offsets
-};
-
 template <class T>
 struct BatchJob {
   int64_t n = 0;
@@ -1205,7 +1201,7 @@ struct BatchJob {
   DevBuf in_a, in_b;  // data, or (u32 indices, T distances) until prepared
   bool has_init = false;
   std::vector<T> init;
-  std::shared_ptr<BatchGroup<T>> group;
+  std::shared_ptr<GroupCsr<T>> group;
   int64_t goff = 0;  // first row of this job in its group
 };
 
@@ -1216,10 +1212,10 @@ struct BatchImpl {
   int64_t total = 0, nnz = 0;
   std::vector<int64_t> off, nnz_off;
   DevBuf d_off, job_of, rows, cols, vals, y, uy, gains, pos, neg, q, z, lr, mom, boxes, codes, jobkey, jobkey_alt;
-  DevBuf tmp, kidx, kdist, kp, xin, g_off, g_of, d_nnz_off;
+  DevBuf tmp, d_nnz_off;
   BhWorkspace<T> ws;
-  SymWorkspace<T> sym;
-  KnnWorkspace knn;
+  SegTiles tiles;
+  AffinityScratch<T> aff;
   bool fitted = false;
   double aff_ms = 0, loop_ms = 0;
   cudaGraphExec_t graph = nullptr;
@@ -1321,44 +1317,28 @@ void batch_prepare(bhtsne_batch* b) {
     const int G = (int)js.size();
     const BatchJob<T>& J0 = *B.jobs[js[0]];
     const int64_t k = J0.k;
-    std::vector<int64_t> goff(G + 1, 0);
-    for (int g = 0; g < G; ++g) goff[g + 1] = goff[g] + B.jobs[js[g]]->n;
+    std::vector<int64_t> goff(G + 1, 0), ns(G);
+    for (int g = 0; g < G; ++g) {
+      ns[g] = B.jobs[js[g]]->n;
+      goff[g + 1] = goff[g] + ns[g];
+    }
     const int64_t tot = goff[G];
-    upload<T>(B.g_off, goff.data(), goff.size() * 8, s);
-    uint32_t* gof = static_cast<uint32_t*>(B.g_of.ensure((size_t)tot * 4));
-    for (int g = 0; g < G; ++g) batch_fill_job(gof, goff[g], goff[g + 1], (uint32_t)g, s);
-    uint32_t* kidx = static_cast<uint32_t*>(B.kidx.ensure((size_t)tot * k * 4));
-    T* kdist = static_cast<T*>(B.kdist.ensure((size_t)tot * k * sizeof(T)));
+    auto grp = std::make_shared<GroupCsr<T>>();
     if (J0.kind == 0) {
-      const int dim = J0.dim;
-      T* X = static_cast<T*>(B.xin.ensure((size_t)tot * dim * sizeof(T)));
-      for (int g = 0; g < G; ++g)
-        BHG_CUDA(cudaMemcpyAsync(X + goff[g] * dim, B.jobs[js[g]]->in_a.ptr, (size_t)B.jobs[js[g]]->n * dim * sizeof(T),
-                                 cudaMemcpyDeviceToDevice, s));
-      knn_euclidean_segmented<T>(X, tot, dim, (int)k, goff, B.g_off.template as<int64_t>(), gof, kidx, kdist, B.knn, s);
-      B.xin.release();
-      B.knn.release();
+      std::vector<const T*> X(G);
+      for (int g = 0; g < G; ++g) X[g] = B.jobs[js[g]]->in_a.template as<T>();
+      group_affinities_euclidean<T>(X, ns, J0.dim, k, (T)b->prm.perplexity, *grp, B.aff, s);
     } else {
+      uint32_t* kidx = static_cast<uint32_t*>(B.aff.kidx.ensure((size_t)tot * k * 4));
+      T* kdist = static_cast<T*>(B.aff.kdist.ensure((size_t)tot * k * sizeof(T)));
       for (int g = 0; g < G; ++g) {
         const BatchJob<T>& J = *B.jobs[js[g]];
         batch_offset_indices(J.in_a.template as<uint32_t>(), J.n * k, (uint32_t)goff[g], kidx + goff[g] * k, s);
         BHG_CUDA(cudaMemcpyAsync(kdist + goff[g] * k, J.in_b.ptr, (size_t)J.n * k * sizeof(T), cudaMemcpyDeviceToDevice,
                                  s));
       }
+      group_affinities_from_knn<T>(tot, k, (T)b->prm.perplexity, *grp, B.aff, s);
     }
-    B.kp.ensure((size_t)tot * k * sizeof(T));
-    launch_search_beta<T>(kdist, tot, k, (T)b->prm.perplexity, B.kp.template as<T>(), nullptr, s);
-    const int64_t nnz = symmetrize<T>(kidx, B.kp.template as<T>(), tot, (int)k, B.sym, s);
-    auto grp = std::make_shared<BatchGroup<T>>();
-    grp->rows.ensure((size_t)(tot + 1) * 8);
-    grp->cols.ensure((size_t)std::max<int64_t>(nnz, 1) * 4);
-    grp->vals.ensure((size_t)std::max<int64_t>(nnz, 1) * sizeof(T));
-    symmetrize_finish<T>(B.sym, tot, nnz, grp->rows.template as<uint64_t>(), grp->cols.template as<uint32_t>(),
-                         grp->vals.template as<T>(), s);
-    grp->rows_h.resize(tot + 1);
-    BHG_CUDA(cudaMemcpyAsync(grp->rows_h.data(), grp->rows.ptr, (size_t)(tot + 1) * 8, cudaMemcpyDeviceToHost, s));
-    BHG_CUDA(cudaStreamSynchronize(s));
-    B.sym.release();
     for (int g = 0; g < G; ++g) {
       BatchJob<T>& J = *B.jobs[js[g]];
       J.group = grp;
@@ -1367,9 +1347,7 @@ void batch_prepare(bhtsne_batch* b) {
       J.in_b.release();
     }
   }
-  B.kidx.release();
-  B.kdist.release();
-  B.kp.release();
+  B.aff.release();
 }
 
 template <class T>
@@ -1427,6 +1405,7 @@ void batch_fit(bhtsne_batch* b) {
   batch_normalize<T>(B.vals.template as<T>(), B.d_nnz_off.template as<int64_t>(), B.K, (T)P.early_exaggeration,
                      P.stop_lying_epoch == 0, s);
   upload<T>(B.d_off, B.off.data(), B.off.size() * 8, s);
+  B.tiles.build(B.off, s);
   // seeds, velocity, gains, per-job learning rate and momentum
   std::vector<T> yh((size_t)total * D);
   std::vector<T> lrh(B.K), momh(B.K, (T)P.momentum);
@@ -1480,7 +1459,7 @@ void batch_fit(bhtsne_batch* b) {
   const int64_t* off = B.d_off.template as<int64_t>();
   auto body = [&]() {
     batch_sort_and_build<T>(D, y, total, B.K, B.job_of.template as<uint32_t>(), off, boxes, B.ws, B.codes, B.jobkey,
-                            B.jobkey_alt, s);
+                            B.jobkey_alt, B.tiles, s);
     Segs sg;
     sg.job = B.jobkey.template as<uint64_t>();
     sg.off = off;

@@ -26,13 +26,14 @@ namespace {
 
 template <class T, int D>
 __global__ void batch_box_kernel(T* __restrict__ y, const int64_t* __restrict__ off, int apply_mean,
-                                 BoxParams<T>* __restrict__ boxes, int bits) {
+                                 BoxParams<T>* __restrict__ boxes, int bits, const uint8_t* __restrict__ active) {
   __shared__ double sh[32];
   __shared__ T shr[32];
   __shared__ double means[D];
   const int j = blockIdx.x;
   const int64_t lo = off[j], hi = off[j + 1];
   const int64_t n = hi - lo;
+  if (active && !active[j]) apply_mean = 0;
   T mean[D];
 #pragma unroll
   for (int a = 0; a < D; ++a) mean[a] = T(0);
@@ -153,10 +154,12 @@ template <class T, int D>
 __global__ void batch_update_kernel(T* __restrict__ y, const T* __restrict__ pos, const T* __restrict__ neg,
                                     T* __restrict__ uy, T* __restrict__ gains, int64_t total,
                                     const uint32_t* __restrict__ job_of, const double* __restrict__ z,
-                                    const T* __restrict__ lr, const T* __restrict__ momentum) {
+                                    const T* __restrict__ lr, const T* __restrict__ momentum,
+                                    const uint8_t* __restrict__ active) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= total) return;
   const uint32_t j = job_of[i];
+  if (active && !active[j]) return;
   const T inv_norm = T(1) / (T)z[j];
   const T l = lr[j], mom = momentum[j];
   const T inc = (T)0.2, dec = (T)0.8, floor_ = (T)0.01;
@@ -240,17 +243,18 @@ int bits_for(int64_t v) {
 }  // namespace
 
 template <class T>
-void batch_box(int D, T* y, const int64_t* off, int K, bool apply_mean, BoxParams<T>* boxes, int bits, cudaStream_t s) {
+void batch_box(int D, T* y, const int64_t* off, int K, bool apply_mean, BoxParams<T>* boxes, int bits, cudaStream_t s,
+               const uint8_t* active) {
   if (K <= 0) return;
-  if (D == 2) batch_box_kernel<T, 2><<<K, 256, 0, s>>>(y, off, apply_mean ? 1 : 0, boxes, bits);
-  else batch_box_kernel<T, 3><<<K, 256, 0, s>>>(y, off, apply_mean ? 1 : 0, boxes, bits);
+  if (D == 2) batch_box_kernel<T, 2><<<K, 256, 0, s>>>(y, off, apply_mean ? 1 : 0, boxes, bits, active);
+  else batch_box_kernel<T, 3><<<K, 256, 0, s>>>(y, off, apply_mean ? 1 : 0, boxes, bits, active);
   BHG_LAUNCH_CHECK();
 }
 
 template <class T>
 void batch_sort_and_build(int D, const T* y, int64_t total, int K, const uint32_t* job_of, const int64_t* off,
                           const BoxParams<T>* boxes, BhWorkspace<T>& ws, DevBuf& codes, DevBuf& jobkey,
-                          DevBuf& jobkey_alt, cudaStream_t s) {
+                          DevBuf& jobkey_alt, const SegTiles& tiles, cudaStream_t s) {
   const unsigned g = (unsigned)ceil_div(total, 256);
   uint64_t* cd = static_cast<uint64_t*>(codes.ensure((size_t)total * 8));
   uint64_t* jk = static_cast<uint64_t*>(jobkey.ensure((size_t)total * 8));
@@ -279,6 +283,7 @@ void batch_sort_and_build(int D, const T* y, int64_t total, int K, const uint32_
   Segs sg;
   sg.job = jk;
   sg.off = off;
+  tiles.fill(sg);
   bh_build_from_sorted<T>(ws, D, y, total, sg, s);
 }
 
@@ -291,10 +296,12 @@ void batch_z(const T* q, const int64_t* off, int K, double* z, cudaStream_t s) {
 
 template <class T>
 void batch_update(int D, T* y, const T* pos, const T* neg, T* uy, T* gains, int64_t total, const uint32_t* job_of,
-                  const double* z, const T* lr, const T* momentum, cudaStream_t s) {
+                  const double* z, const T* lr, const T* momentum, cudaStream_t s, const uint8_t* active) {
   const unsigned g = (unsigned)ceil_div(total, 256);
-  if (D == 2) batch_update_kernel<T, 2><<<g, 256, 0, s>>>(y, pos, neg, uy, gains, total, job_of, z, lr, momentum);
-  else batch_update_kernel<T, 3><<<g, 256, 0, s>>>(y, pos, neg, uy, gains, total, job_of, z, lr, momentum);
+  if (D == 2)
+    batch_update_kernel<T, 2><<<g, 256, 0, s>>>(y, pos, neg, uy, gains, total, job_of, z, lr, momentum, active);
+  else
+    batch_update_kernel<T, 3><<<g, 256, 0, s>>>(y, pos, neg, uy, gains, total, job_of, z, lr, momentum, active);
   BHG_LAUNCH_CHECK();
 }
 
@@ -339,16 +346,69 @@ void batch_fill_job(uint32_t* job_of, int64_t lo, int64_t hi, uint32_t j, cudaSt
   BHG_LAUNCH_CHECK();
 }
 
+template <class T>
+void group_affinities_from_knn(int64_t tot, int64_t k, T perplexity, GroupCsr<T>& out, AffinityScratch<T>& ws,
+                               cudaStream_t s) {
+  uint32_t* kidx = ws.kidx.template as<uint32_t>();
+  T* kdist = ws.kdist.template as<T>();
+  ws.kp.ensure((size_t)tot * k * sizeof(T));
+  launch_search_beta<T>(kdist, tot, k, perplexity, ws.kp.template as<T>(), nullptr, s);
+  const int64_t nnz = symmetrize<T>(kidx, ws.kp.template as<T>(), tot, (int)k, ws.sym, s);
+  out.rows.ensure((size_t)(tot + 1) * 8);
+  out.cols.ensure((size_t)std::max<int64_t>(nnz, 1) * 4);
+  out.vals.ensure((size_t)std::max<int64_t>(nnz, 1) * sizeof(T));
+  symmetrize_finish<T>(ws.sym, tot, nnz, out.rows.template as<uint64_t>(), out.cols.template as<uint32_t>(),
+                       out.vals.template as<T>(), s);
+  out.rows_h.resize(tot + 1);
+  BHG_CUDA(cudaMemcpyAsync(out.rows_h.data(), out.rows.ptr, (size_t)(tot + 1) * 8, cudaMemcpyDeviceToHost, s));
+  BHG_CUDA(cudaStreamSynchronize(s));
+  out.nnz = nnz;
+  ws.sym.release();
+  ws.kp.release();
+}
+
+template <class T>
+void group_affinities_euclidean(const std::vector<const T*>& X, const std::vector<int64_t>& n, int dim, int64_t k,
+                                T perplexity, GroupCsr<T>& out, AffinityScratch<T>& ws, cudaStream_t s) {
+  const int G = (int)n.size();
+  std::vector<int64_t> goff(G + 1, 0);
+  for (int g = 0; g < G; ++g) goff[g + 1] = goff[g] + n[g];
+  const int64_t tot = goff[G];
+  int64_t* d_off = static_cast<int64_t*>(ws.g_off.ensure(goff.size() * 8));
+  BHG_CUDA(cudaMemcpyAsync(d_off, goff.data(), goff.size() * 8, cudaMemcpyHostToDevice, s));
+  uint32_t* gof = static_cast<uint32_t*>(ws.g_of.ensure((size_t)tot * 4));
+  for (int g = 0; g < G; ++g) batch_fill_job(gof, goff[g], goff[g + 1], (uint32_t)g, s);
+  T* Xs = static_cast<T*>(ws.xin.ensure((size_t)tot * dim * sizeof(T)));
+  for (int g = 0; g < G; ++g)
+    BHG_CUDA(cudaMemcpyAsync(Xs + goff[g] * dim, X[g], (size_t)n[g] * dim * sizeof(T), cudaMemcpyDeviceToDevice, s));
+  uint32_t* kidx = static_cast<uint32_t*>(ws.kidx.ensure((size_t)tot * k * 4));
+  T* kdist = static_cast<T*>(ws.kdist.ensure((size_t)tot * k * sizeof(T)));
+  knn_euclidean_segmented<T>(Xs, tot, dim, (int)k, goff, d_off, gof, kidx, kdist, ws.knn, s);
+  ws.xin.release();
+  ws.knn.release();
+  group_affinities_from_knn<T>(tot, k, perplexity, out, ws, s);
+}
+
 #define BHG_INST(T)                                                                                                  \
-  template void batch_box<T>(int, T*, const int64_t*, int, bool, BoxParams<T>*, int, cudaStream_t);                 \
+  template void batch_box<T>(int, T*, const int64_t*, int, bool, BoxParams<T>*, int, cudaStream_t, const uint8_t*); \
   template void batch_sort_and_build<T>(int, const T*, int64_t, int, const uint32_t*, const int64_t*,               \
                                         const BoxParams<T>*, BhWorkspace<T>&, DevBuf&, DevBuf&, DevBuf&,             \
-                                        cudaStream_t);                                                               \
+                                        const SegTiles&, cudaStream_t);                                              \
   template void batch_z<T>(const T*, const int64_t*, int, double*, cudaStream_t);                                    \
   template void batch_normalize<T>(T*, const int64_t*, int, T, bool, cudaStream_t);                                  \
   template void batch_update<T>(int, T*, const T*, const T*, T*, T*, int64_t, const uint32_t*, const double*,        \
-                                const T*, const T*, cudaStream_t);
+                                const T*, const T*, cudaStream_t, const uint8_t*);
 BHG_INST(float)
 BHG_INST(double)
+template void group_affinities_from_knn<float>(int64_t, int64_t, float, GroupCsr<float>&, AffinityScratch<float>&,
+                                               cudaStream_t);
+template void group_affinities_from_knn<double>(int64_t, int64_t, double, GroupCsr<double>&, AffinityScratch<double>&,
+                                                cudaStream_t);
+template void group_affinities_euclidean<float>(const std::vector<const float*>&, const std::vector<int64_t>&, int,
+                                                int64_t, float, GroupCsr<float>&, AffinityScratch<float>&,
+                                                cudaStream_t);
+template void group_affinities_euclidean<double>(const std::vector<const double*>&, const std::vector<int64_t>&, int,
+                                                 int64_t, double, GroupCsr<double>&, AffinityScratch<double>&,
+                                                 cudaStream_t);
 
 }  // namespace bhg

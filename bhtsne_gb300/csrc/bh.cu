@@ -326,6 +326,135 @@ __global__ void prefix_apply_kernel(const T* __restrict__ y, const uint32_t* __r
   }
 }
 
+// Job-relative prefix sums for a batch of independent sets: every tile
+// starts at its set's first position and a set's carry starts at zero, so the
+// sums (and the centres of mass taken from them) are those of the set alone.
+// pre holds n_j + 1 entries per set j: position p of set j is entry p + j.
+template <class T, int D>
+__global__ void seg_prefix_reduce_kernel(const T* __restrict__ y, const uint32_t* __restrict__ perm,
+                                         const int64_t* __restrict__ tile_start, const int64_t* __restrict__ tile_end,
+                                         double* __restrict__ part) {
+  __shared__ double sh[D][kPsThreads / 32];
+  const int64_t base = tile_start[blockIdx.x], lim = tile_end[blockIdx.x];
+  double s[D];
+#pragma unroll
+  for (int a = 0; a < D; ++a) s[a] = 0.0;
+  for (int i = 0; i < kPsItems; ++i) {
+    const int64_t p = base + (int64_t)i * kPsThreads + threadIdx.x;
+    if (p < lim) {
+      const int64_t src = perm[p];
+#pragma unroll
+      for (int a = 0; a < D; ++a) s[a] += (double)y[src * D + a];
+    }
+  }
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int a = 0; a < D; ++a) {
+    double v = warp_sum(s[a]);
+    if (lane == 0) sh[a][w] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < D) {
+    double t = 0.0;
+    for (int q = 0; q < kPsThreads / 32; ++q) t += sh[threadIdx.x][q];
+    part[blockIdx.x * D + threadIdx.x] = t;
+  }
+}
+
+// One thread per set: exclusive scan of its tile sums; set totals to tot.
+template <int D>
+__global__ void seg_prefix_partials_kernel(double* __restrict__ part, const int32_t* __restrict__ job_tile, int K,
+                                           double* __restrict__ tot) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= K) return;
+  double carry[D];
+#pragma unroll
+  for (int a = 0; a < D; ++a) carry[a] = 0.0;
+  for (int b = job_tile[j]; b < job_tile[j + 1]; ++b) {
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+      const double v = part[b * D + a];
+      part[b * D + a] = carry[a];
+      carry[a] += v;
+    }
+  }
+#pragma unroll
+  for (int a = 0; a < D; ++a) tot[j * D + a] = carry[a];
+}
+
+template <class T, int D>
+__global__ void seg_prefix_apply_kernel(const T* __restrict__ y, const uint32_t* __restrict__ perm,
+                                        const int64_t* __restrict__ tile_start, const int64_t* __restrict__ tile_end,
+                                        const int32_t* __restrict__ tile_job, const int32_t* __restrict__ job_tile,
+                                        const double* __restrict__ part, const double* __restrict__ tot,
+                                        T* __restrict__ ys, double* __restrict__ pre) {
+  __shared__ double sh[D][kPsThreads / 32];
+  const int64_t lim = tile_end[blockIdx.x];
+  const int64_t base = tile_start[blockIdx.x] + (int64_t)threadIdx.x * kPsItems;
+  const int64_t jj = tile_job[blockIdx.x];
+  double v[kPsItems][D];
+  double s[D];
+#pragma unroll
+  for (int a = 0; a < D; ++a) s[a] = 0.0;
+#pragma unroll
+  for (int i = 0; i < kPsItems; ++i) {
+    const int64_t p = base + i;
+    if (p < lim) {
+      const int64_t src = perm[p];
+#pragma unroll
+      for (int a = 0; a < D; ++a) {
+        const T t = y[src * D + a];
+        ys[p * D + a] = t;
+        v[i][a] = (double)t;
+        s[a] += v[i][a];
+      }
+    } else {
+#pragma unroll
+      for (int a = 0; a < D; ++a) v[i][a] = 0.0;
+    }
+  }
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  double x[D];
+#pragma unroll
+  for (int a = 0; a < D; ++a) {
+    x[a] = s[a];
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const double t = __shfl_up_sync(kFull, x[a], o);
+      if (lane >= o) x[a] += t;
+    }
+    if (lane == 31) sh[a][w] = x[a];
+  }
+  __syncthreads();
+  if (threadIdx.x < D) {
+    double run = 0.0;
+    for (int q = 0; q < kPsThreads / 32; ++q) {
+      const double t = sh[threadIdx.x][q];
+      sh[threadIdx.x][q] = run;
+      run += t;
+    }
+  }
+  __syncthreads();
+  double run[D];
+#pragma unroll
+  for (int a = 0; a < D; ++a) run[a] = x[a] - s[a] + sh[a][w] + part[blockIdx.x * D + a];
+#pragma unroll
+  for (int i = 0; i < kPsItems; ++i) {
+    const int64_t p = base + i;
+    if (p < lim) {
+#pragma unroll
+      for (int a = 0; a < D; ++a) {
+        pre[(p + jj) * D + a] = run[a];
+        run[a] += v[i][a];
+      }
+    }
+  }
+  if (threadIdx.x == 0 && (int64_t)blockIdx.x == (int64_t)job_tile[jj + 1] - 1) {
+#pragma unroll
+    for (int a = 0; a < D; ++a) pre[(lim + jj) * D + a] = tot[jj * D + a];
+  }
+}
+
 // ---------------------------------------------------------------------------
 // Tree build.
 // ---------------------------------------------------------------------------
@@ -396,9 +525,10 @@ __global__ void tree_emit_kernel(const typename MortonD<D>::Code* __restrict__ c
       const int64_t idx = (int64_t)base[a] + __popc(m & ((1u << l) - 1u));
       if (idx >= 2 * n) return;  // cannot happen for a well-formed build; never write out of bounds
       const double cnt = (double)(e - a);
+      const int64_t jj = sg.tile_job ? (int64_t)sg.job[s] : 0;  // job-relative prefix layout
       T com[D];
 #pragma unroll
-      for (int q = 0; q < D; ++q) com[q] = (T)((pre[e * D + q] - pre[a * D + q]) / cnt);
+      for (int q = 0; q < D; ++q) com[q] = (T)((pre[(e + jj) * D + q] - pre[(a + jj) * D + q]) / cnt);
       nodes.write(idx, com, (T)(uint32_t)(e - a), l, (uint32_t)base[e]);
     }
   }
@@ -663,16 +793,32 @@ static void bh_build_impl(BhWorkspace<T>& ws, const T* y, int64_t n, cudaStream_
 template <class T, int D>
 static void build_from_sorted_impl(BhWorkspace<T>& ws, const T* y, int64_t n, const Segs& sg, cudaStream_t s) {
   const unsigned g = (unsigned)ceil_div(n, kThreads);
-  const int64_t np = ceil_div(n, kPsTile);
-  prefix_reduce_kernel<T, D><<<(unsigned)np, kPsThreads, 0, s>>>(y, ws.perm.template as<uint32_t>(), n,
-                                                                  ws.pre_part.template as<double>());
-  BHG_LAUNCH_CHECK();
-  prefix_partials_kernel<D><<<1, 1024, 0, s>>>(ws.pre_part.template as<double>(), np);
-  BHG_LAUNCH_CHECK();
-  prefix_apply_kernel<T, D><<<(unsigned)np, kPsThreads, 0, s>>>(y, ws.perm.template as<uint32_t>(), n,
-                                                                 ws.pre_part.template as<double>(), np,
-                                                                 ws.ys.template as<T>(), ws.pre.template as<double>());
-  BHG_LAUNCH_CHECK();
+  if (sg.tile_job) {
+    const int64_t nt = sg.ntiles;
+    double* part = static_cast<double*>(ws.pre_part.ensure((size_t)(nt + 1) * D * sizeof(double)));
+    double* tot = static_cast<double*>(ws.seg_tot.ensure((size_t)std::max(sg.K, 1) * D * sizeof(double)));
+    double* pre = static_cast<double*>(ws.pre.ensure((size_t)(n + sg.K) * D * sizeof(double)));
+    seg_prefix_reduce_kernel<T, D><<<(unsigned)nt, kPsThreads, 0, s>>>(y, ws.perm.template as<uint32_t>(),
+                                                                        sg.tile_start, sg.tile_end, part);
+    BHG_LAUNCH_CHECK();
+    seg_prefix_partials_kernel<D><<<(unsigned)ceil_div(sg.K, 128), 128, 0, s>>>(part, sg.job_tile, sg.K, tot);
+    BHG_LAUNCH_CHECK();
+    seg_prefix_apply_kernel<T, D><<<(unsigned)nt, kPsThreads, 0, s>>>(
+        y, ws.perm.template as<uint32_t>(), sg.tile_start, sg.tile_end, sg.tile_job, sg.job_tile, part, tot,
+        ws.ys.template as<T>(), pre);
+    BHG_LAUNCH_CHECK();
+  } else {
+    const int64_t np = ceil_div(n, kPsTile);
+    prefix_reduce_kernel<T, D><<<(unsigned)np, kPsThreads, 0, s>>>(y, ws.perm.template as<uint32_t>(), n,
+                                                                    ws.pre_part.template as<double>());
+    BHG_LAUNCH_CHECK();
+    prefix_partials_kernel<D><<<1, 1024, 0, s>>>(ws.pre_part.template as<double>(), np);
+    BHG_LAUNCH_CHECK();
+    prefix_apply_kernel<T, D><<<(unsigned)np, kPsThreads, 0, s>>>(y, ws.perm.template as<uint32_t>(), n,
+                                                                   ws.pre_part.template as<double>(), np,
+                                                                   ws.ys.template as<T>(), ws.pre.template as<double>());
+    BHG_LAUNCH_CHECK();
+  }
   BHG_CUDA(cudaMemsetAsync(ws.mask.ptr, 0, (size_t)n * 4, s));
   const typename MortonD<D>::Code* codes = sorted_codes<T, D>(ws);
   tree_mark_kernel<D><<<g, kThreads, 0, s>>>(codes, n, ws.mask.template as<uint32_t>(), sg);
@@ -729,6 +875,42 @@ int bh_bits(int D) {
   int b = 0;
   with_dim<2, 7>(D, "error: Barnes-Hut covers D in 2..7.", [&](auto dc) { b = MortonD<decltype(dc)::value>::BITS; });
   return b;
+}
+
+void SegTiles::build(const std::vector<int64_t>& off, cudaStream_t s) {
+  K = (int)off.size() - 1;
+  std::vector<int64_t> st, en;
+  std::vector<int32_t> tj, jt(K + 1, 0);
+  for (int j = 0; j < K; ++j) {
+    jt[j] = (int32_t)st.size();
+    for (int64_t p = off[j]; p < off[j + 1]; p += kPsTile) {
+      st.push_back(p);
+      en.push_back(std::min<int64_t>(p + kPsTile, off[j + 1]));
+      tj.push_back(j);
+    }
+  }
+  jt[K] = (int32_t)st.size();
+  ntiles = (int64_t)st.size();
+  const size_t a = ((size_t)ntiles * 8 + 255) / 256 * 256;
+  const size_t b = ((size_t)ntiles * 4 + 255) / 256 * 256;
+  char* base = static_cast<char*>(buf.ensure(2 * a + b + (size_t)(K + 1) * 4 + 256));
+  BHG_CUDA(cudaMemcpyAsync(base, st.data(), (size_t)ntiles * 8, cudaMemcpyHostToDevice, s));
+  BHG_CUDA(cudaMemcpyAsync(base + a, en.data(), (size_t)ntiles * 8, cudaMemcpyHostToDevice, s));
+  BHG_CUDA(cudaMemcpyAsync(base + 2 * a, tj.data(), (size_t)ntiles * 4, cudaMemcpyHostToDevice, s));
+  BHG_CUDA(cudaMemcpyAsync(base + 2 * a + b, jt.data(), (size_t)(K + 1) * 4, cudaMemcpyHostToDevice, s));
+  BHG_CUDA(cudaStreamSynchronize(s));
+}
+
+void SegTiles::fill(Segs& sg) const {
+  const size_t a = ((size_t)ntiles * 8 + 255) / 256 * 256;
+  const size_t b = ((size_t)ntiles * 4 + 255) / 256 * 256;
+  char* base = static_cast<char*>(buf.ptr);
+  sg.tile_start = reinterpret_cast<const int64_t*>(base);
+  sg.tile_end = reinterpret_cast<const int64_t*>(base + a);
+  sg.tile_job = reinterpret_cast<const int32_t*>(base + 2 * a);
+  sg.job_tile = reinterpret_cast<const int32_t*>(base + 2 * a + b);
+  sg.ntiles = ntiles;
+  sg.K = K;
 }
 
 template struct BhWorkspace<float>;

@@ -163,6 +163,7 @@ struct BhWorkspace {
   bool zeroed = false;
   DevBuf keys, keys_alt, perm, perm_alt, ys, pre, pre_part, mask, cnt, base, geom, word;
   DevBuf wide, lo_orig, hi_orig;  // 128-bit codes (D >= 5): sorted codes and the unsorted halves
+  DevBuf seg_tot;                 // per-set coordinate sums (job-relative prefix sums)
   DevBuf part_min, part_max, done, zdone, params, zpart, zval, sort_tmp, scan_tmp;
   void reserve(int64_t n, int D);
   const double* z() const { return static_cast<const double*>(zval.ptr); }
@@ -171,10 +172,29 @@ struct BhWorkspace {
 
 // Independent point sets laid out back to back (a batch of fits): job[s] is
 // the set of sorted position s and off[j]..off[j+1] the positions of set j.
-// Both null means one set spanning everything.
+// Both null means one set spanning everything. The tile table cuts every set
+// into prefix-sum tiles that start at the set's first position (tile t spans
+// tile_start[t]..tile_end[t] of set tile_job[t]; set j owns tiles
+// job_tile[j]..job_tile[j+1]), so each set's centres of mass are summed
+// exactly as if it were alone (see SegTiles).
 struct Segs {
   const uint64_t* job = nullptr;
   const int64_t* off = nullptr;
+  const int64_t* tile_start = nullptr;
+  const int64_t* tile_end = nullptr;
+  const int32_t* tile_job = nullptr;
+  const int32_t* job_tile = nullptr;
+  int64_t ntiles = 0;
+  int K = 0;
+};
+
+// Device tile table for Segs, built on the host from the set offsets.
+struct SegTiles {
+  DevBuf buf;
+  int64_t ntiles = 0;
+  int K = 0;
+  void build(const std::vector<int64_t>& off, cudaStream_t s);
+  void fill(Segs& sg) const;
 };
 
 // Recentres y by mean_sum/n when apply_mean, then writes BoxParams (bits = Morton

@@ -35,6 +35,14 @@ struct DevBuf {
   }
   template <class V>
   V* as() const { return static_cast<V*>(ptr); }
+  void swap(DevBuf& o) {
+    void* p = ptr;
+    size_t b = bytes;
+    ptr = o.ptr;
+    bytes = o.bytes;
+    o.ptr = p;
+    o.bytes = b;
+  }
 };
 
 // ---- scan ---------------------------------------------------------------------

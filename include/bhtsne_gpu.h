@@ -221,6 +221,54 @@ int bhtsne_batch_embedding(bhtsne_batch* b, int64_t job, void* out);
 int bhtsne_batch_kl_divergence(bhtsne_batch* b, int64_t job, int32_t quirk, double* out);
 int bhtsne_batch_timings(const bhtsne_batch* b, double* affinity_ms, double* loop_ms);
 
+/* ---- serving: continuous batching of embedding requests ----------------
+ * No reference counterpart (the reference fits one embedding per builder).
+ * Requests are queued, admitted in order while their estimated device
+ * footprint fits the byte budget, and fitted concurrently: Barnes-Hut
+ * requests join one running batch (all in-flight jobs stepped together, each
+ * with its own epoch count; jobs enter and leave every round_epochs epochs),
+ * FIt-SNE requests run on fit_workers extra streams. Every request uses the
+ * reference's defaults (early exaggeration 12 until epoch 250, momentum 0.5
+ * then 0.8, learning rate max(n / 12 / 4, 50)) and the server's perplexity and
+ * theta. A server owns host threads; its calls are thread-safe. */
+typedef struct bhtsne_server bhtsne_server;
+typedef struct bhtsne_server_params {
+  double perplexity;        /* 30 (k = 3 * perplexity <= 224) */
+  double theta;             /* 0.5, for Barnes-Hut requests */
+  int64_t hbm_budget_bytes; /* admission budget; <= 0: 90% of the free device memory at creation */
+  int32_t round_epochs;     /* epochs between batch changes (25) */
+  int32_t fit_workers;      /* streams for FIt-SNE requests (2) */
+} bhtsne_server_params;
+typedef struct bhtsne_request {
+  const void* data; /* n x dim row-major in the server's dtype; copied by submit */
+  int64_t n;
+  int32_t dim;
+  int32_t method; /* BHTSNE_METHOD_BARNES_HUT or BHTSNE_METHOD_FIT_SNE */
+  int64_t epochs;
+  uint64_t seed;   /* random_init seed of this request */
+  int32_t want_kl; /* nonzero: compute the reference-compatible KL of the result */
+} bhtsne_request;
+#define BHTSNE_JOB_QUEUED 0
+#define BHTSNE_JOB_RUNNING 1
+#define BHTSNE_JOB_DONE 2
+#define BHTSNE_JOB_FAILED 3
+void bhtsne_server_params_default(bhtsne_server_params* p);
+/* embed_dim 2 or 3 (FIt-SNE requests need 2). */
+int bhtsne_server_new(bhtsne_ctx* ctx, int dtype, int32_t embed_dim, const bhtsne_server_params* p,
+                      bhtsne_server** out);
+/* Stops the threads after the current round; unfinished requests fail. */
+int bhtsne_server_free(bhtsne_server* s);
+const char* bhtsne_server_last_error(const bhtsne_server* s);
+int bhtsne_server_submit(bhtsne_server* s, const bhtsne_request* r, int64_t* id);
+int bhtsne_server_poll(bhtsne_server* s, int64_t id, int32_t* state);
+/* timeout_s < 0 waits without limit; BHTSNE_ETIMEDOUT when it runs out. */
+int bhtsne_server_wait(bhtsne_server* s, int64_t id, double timeout_s);
+/* Copies the n x embed_dim embedding (and KL, submit-to-done latency) of a
+ * finished request and forgets it; a failed request returns its error. */
+int bhtsne_server_result(bhtsne_server* s, int64_t id, void* embedding, double* kl, double* latency_ms);
+int bhtsne_server_stats(bhtsne_server* s, int64_t* done, int64_t* in_flight, int64_t* peak_bytes,
+                        double* mean_batch_points);
+
 #ifdef __cplusplus
 }
 #endif
