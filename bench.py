@@ -232,6 +232,9 @@ def run_ours(args):
     batched = None
     if args.batch_jobs > 0:
         batched = run_batched(args, ctx)
+    serving = None
+    if args.serve_requests > 0:
+        serving = run_serving(args, ctx)
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -257,6 +260,8 @@ def run_ours(args):
     }
     if batched:
         out["batched"] = batched
+    if serving:
+        out["serving"] = serving
     if cpu:
         out["cpu_baseline"] = cpu
     if rank == 0:
@@ -323,6 +328,82 @@ def run_batched(args, ctx):
                    "max": round(float(gap.max()), 5),
                    "aggregate": round(abs(sum(kl_b) - sum(kl_p)) / abs(sum(kl_p)), 6),
                    "within_1pct": int((gap <= 0.01).sum())},
+    }
+
+
+def make_serving_workload(requests, seed=2025):
+    """Requests with N log-uniform in [1000, 300000], input dim 50, each a
+    10-component Gaussian mixture (centres ~ N(0, 10^2 I), unit variance);
+    method Barnes-Hut or FIt-SNE with probability 1/2."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(requests):
+        n = int(np.exp(rng.uniform(np.log(1000), np.log(300000))))
+        centres = rng.normal(0.0, 10.0, size=(10, 50)).astype(np.float32)
+        lab = rng.integers(0, 10, size=n)
+        X = np.ascontiguousarray(centres[lab] + rng.standard_normal(size=(n, 50), dtype=np.float32))
+        method = "bh" if rng.random() < 0.5 else "fit"
+        out.append((X, method, 1000 + i))
+    return out
+
+
+def run_serving(args, ctx):
+    """The request stream through bhtsne_server (continuous batching) against
+    the same stream served one request at a time by the plain builder. Both
+    arms see the same Poisson arrivals; latency = completion - arrival."""
+    import bhtsne_gb300 as bg
+    reqs = make_serving_workload(args.serve_requests)
+    E = args.serve_epochs
+    rng = np.random.default_rng(77)
+    arrivals = np.cumsum(rng.exponential(1.0 / args.serve_rate, size=len(reqs)))
+    sv = bg.Server(ctx=ctx, perplexity=30.0, theta=0.5, fit_workers=args.serve_fit_workers)
+    ids = [None] * len(reqs)
+    w0 = time.perf_counter()
+    for i, (X, method, seed) in enumerate(reqs):
+        delay = arrivals[i] - (time.perf_counter() - w0)
+        if delay > 0:
+            time.sleep(delay)
+        ids[i] = sv.submit(X, method, epochs=E, seed=seed, want_kl=True)
+    lat_s, kl_s = [], []
+    for i in ids:
+        sv.wait(i)
+        _, kl, lat = sv.result(i)
+        lat_s.append(lat / 1e3)
+        kl_s.append(kl)
+    served_s = time.perf_counter() - w0
+    st = sv.stats()
+    sv.close()
+    # plain arm: one request at a time, in arrival order
+    lat_p, kl_p = [], []
+    w0 = time.perf_counter()
+    for i, (X, method, seed) in enumerate(reqs):
+        now = time.perf_counter() - w0
+        if now < arrivals[i]:
+            time.sleep(arrivals[i] - now)
+        t = bg.TSNE(X, ctx=ctx).perplexity(30.0).epochs(E).random_seed(seed)
+        t.barnes_hut(0.5) if method == "bh" else t.fit_sne()
+        t.embedding()
+        kl_p.append(t.kl_divergence())
+        t.close()
+        lat_p.append(time.perf_counter() - w0 - arrivals[i])
+    plain_s = time.perf_counter() - w0
+    gap = np.abs(np.array(kl_s) - np.array(kl_p)) / np.abs(np.array(kl_p))
+    J = len(reqs)
+    return {
+        "workload": f"{J} requests, N log-uniform [1000, 300000] (total {sum(len(r[0]) for r in reqs)} points), "
+                    f"input dim 50, 10-component mixtures, Barnes-Hut theta 0.5 / FIt-SNE 50:50 "
+                    f"({sum(r[1] == 'bh' for r in reqs)} BH), perplexity 30, 2-D, {E} epochs, Poisson arrivals "
+                    f"at {args.serve_rate}/s",
+        "jobs_per_s": round(J / served_s, 3), "plain_jobs_per_s": round(J / plain_s, 3),
+        "speedup_vs_plain": round(plain_s / served_s, 3),
+        "latency_s": {"p50": round(float(np.percentile(lat_s, 50)), 3), "p99": round(float(np.percentile(lat_s, 99)), 3),
+                      "plain_p50": round(float(np.percentile(lat_p, 50)), 3),
+                      "plain_p99": round(float(np.percentile(lat_p, 99)), 3)},
+        "peak_admitted_bytes": st["peak_bytes"], "mean_batch_points": round(st["mean_batch_points"], 1),
+        "fit_workers": args.serve_fit_workers,
+        "server_busy_s": {k: round(st[k], 3) for k in ("round_s", "repack_s", "prepare_s", "fit_worker_s")},
+        "kl_gap": {"mean": round(float(gap.mean()), 5), "p99": round(float(np.percentile(gap, 99)), 5),
+                   "max": round(float(gap.max()), 5), "within_1pct": int((gap <= 0.01).sum())},
     }
 
 
@@ -396,6 +477,10 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--batch-jobs", type=int, default=512, help="batched-fit comparison (0 to skip)")
     ap.add_argument("--batch-epochs", type=int, default=500)
+    ap.add_argument("--serve-requests", type=int, default=48, help="serving comparison (0 to skip)")
+    ap.add_argument("--serve-epochs", type=int, default=750)
+    ap.add_argument("--serve-rate", type=float, default=8.0, help="Poisson arrivals per second")
+    ap.add_argument("--serve-fit-workers", type=int, default=8, help="server streams for FIt-SNE requests")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

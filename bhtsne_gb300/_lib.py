@@ -82,6 +82,7 @@ SIGNATURES = {
     "bhtsne_server_wait": (C.c_int, [_vp, _i64, _dbl]),
     "bhtsne_server_result": (C.c_int, [_vp, _i64, _vp, _dblp, _dblp]),
     "bhtsne_server_stats": (C.c_int, [_vp, _i64p, _i64p, _i64p, _dblp]),
+    "bhtsne_server_timings": (C.c_int, [_vp, _dblp, _dblp, _dblp, _dblp]),
 }
 
 JOB_QUEUED, JOB_RUNNING, JOB_DONE, JOB_FAILED = 0, 1, 2, 3

@@ -680,6 +680,7 @@ template <class T>
 void launch_recenter_bbox(int D, T* y, int64_t n, const double* mean_sum, bool apply_mean, BhWorkspace<T>& ws,
                           int bits, cudaStream_t s) {
   const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(n, kThreads), 2 * 152));
+  ws.zero_counters(s);
   T* pmin = ws.part_min.template as<T>();
   T* pmax = ws.part_max.template as<T>();
   with_dim<1, 7>(D, "error: the embedding dimension must be in 1..7.", [&](auto dc) {
@@ -728,11 +729,7 @@ void BhWorkspace<T>::reserve(int64_t n_, int D_) {
   params.ensure(sizeof(BoxParams<T>));
   zpart.ensure((ceil_div(nn, kThreads) + 1) * sizeof(double));
   zval.ensure(sizeof(double));
-  if (!zeroed) {
-    BHG_CUDA(cudaMemset(done.ptr, 0, 64));
-    BHG_CUDA(cudaMemset(zdone.ptr, 0, 64));
-    zeroed = true;
-  }
+
 }
 
 template <class T, int D>
@@ -857,6 +854,7 @@ void bh_traverse(BhWorkspace<T>& ws, int D, const T* y, int64_t n, T theta, T* n
     BHG_CUDA(cudaMemsetAsync(ws.zval.ptr, 0, sizeof(double), s));
     return;
   }
+  ws.zero_counters(s);
   const unsigned g = (unsigned)ceil_div(n, kThreads);
   const T theta_sq = theta * theta;
   const uint64_t* M = ws.base.template as<uint64_t>() + n;
@@ -911,6 +909,17 @@ void SegTiles::fill(Segs& sg) const {
   sg.job_tile = reinterpret_cast<const int32_t*>(base + 2 * a + b);
   sg.ntiles = ntiles;
   sg.K = K;
+}
+
+// The last-block counters start at zero once; every kernel that uses one
+// leaves it at zero. Zeroed on the caller's stream (a plain cudaMemset runs on
+// the legacy stream, which does not order against non-blocking streams).
+template <class T>
+void BhWorkspace<T>::zero_counters(cudaStream_t s) {
+  if (zeroed) return;
+  BHG_CUDA(cudaMemsetAsync(done.ptr, 0, 64, s));
+  BHG_CUDA(cudaMemsetAsync(zdone.ptr, 0, 64, s));
+  zeroed = true;
 }
 
 template struct BhWorkspace<float>;

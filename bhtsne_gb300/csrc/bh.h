@@ -166,6 +166,7 @@ struct BhWorkspace {
   DevBuf seg_tot;                 // per-set coordinate sums (job-relative prefix sums)
   DevBuf part_min, part_max, done, zdone, params, zpart, zval, sort_tmp, scan_tmp;
   void reserve(int64_t n, int D);
+  void zero_counters(cudaStream_t s);
   const double* z() const { return static_cast<const double*>(zval.ptr); }
   uint64_t* node_count() const { return static_cast<uint64_t*>(base.ptr) + n; }
 };

@@ -516,7 +516,7 @@ void launch_update(int D, T* y, const T* pos, const T* neg, T* uy, T* gains, int
   double* part = static_cast<double*>(us.part.ensure(kUpdBlocks * 8 * sizeof(double)));
   unsigned* done = static_cast<unsigned*>(us.done.ensure(64));
   if (!us.zeroed) {
-    BHG_CUDA(cudaMemset(done, 0, 64));
+    BHG_CUDA(cudaMemsetAsync(done, 0, 64, s));
     us.zeroed = true;
   }
   double* mean_sum = static_cast<double*>(us.mean_sum.ensure(8 * sizeof(double)));

@@ -399,7 +399,7 @@ int ilog2(int L) {
 }  // namespace
 
 template <class T>
-const typename FitWorkspace<T>::T2* FitWorkspace<T>::twiddles(int L) {
+const typename FitWorkspace<T>::T2* FitWorkspace<T>::twiddles(int L, cudaStream_t s) {
   if (tw_len != L) {
     std::vector<T2> h(L / 2 > 0 ? L / 2 : 1);
     for (int k = 0; k < L / 2; ++k) {
@@ -408,7 +408,10 @@ const typename FitWorkspace<T>::T2* FitWorkspace<T>::twiddles(int L) {
       h[k].y = (T)std::sin(ang);
     }
     tw.ensure(h.size() * sizeof(T2));
-    BHG_CUDA(cudaMemcpy(tw.ptr, h.data(), h.size() * sizeof(T2), cudaMemcpyHostToDevice));
+    // on the stream of the FFTs that read it (the legacy stream would not
+    // order against a non-blocking one); the pageable source is staged
+    // before the call returns
+    BHG_CUDA(cudaMemcpyAsync(tw.ptr, h.data(), h.size() * sizeof(T2), cudaMemcpyHostToDevice, s));
     tw_len = L;
   }
   return tw.template as<T2>();
@@ -425,7 +428,7 @@ static void fft_rows(FitWorkspace<T>& ws, typename Cx<T>::type* data, int L, int
     BHG_CUDA(cudaFuncSetAttribute(fft_rows_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     attr_set[sizeof(T) == 8] = true;
   }
-  fft_rows_kernel<T><<<rows, threads, smem, s>>>(data, L, ilog2(L), stride, ws.twiddles(L), inverse ? 1 : 0);
+  fft_rows_kernel<T><<<rows, threads, smem, s>>>(data, L, ilog2(L), stride, ws.twiddles(L, s), inverse ? 1 : 0);
   BHG_LAUNCH_CHECK();
 }
 
@@ -523,7 +526,7 @@ FitGrid fit_repulsion(FitWorkspace<T>& ws, int D, const T* y, int64_t n, const B
   ws.zpart.ensure((ceil_div(std::max<int64_t>(n, 1), 256) + 1) * sizeof(double));
   if (!ws.done_zeroed) {
     ws.done.ensure(64);
-    BHG_CUDA(cudaMemset(ws.done.ptr, 0, 64));
+    BHG_CUDA(cudaMemsetAsync(ws.done.ptr, 0, 64, s));
     ws.done_zeroed = true;
   }
   if (n > 0) {

@@ -24,7 +24,7 @@ struct FitWorkspace {
   DevBuf params, g0, g1, h0, h1, khat, tw, zpart, done, acc;
   int tw_len = 0;
   bool done_zeroed = false;
-  const T2* twiddles(int L);
+  const T2* twiddles(int L, cudaStream_t s);
 };
 
 // Repulsive forces (neg) and Z (z_out, device) at y; `box` must hold the

@@ -100,7 +100,7 @@ struct bhtsne_server {
   bhtsne_server_params prm{};
   int64_t budget = 0;
   std::mutex m;
-  std::condition_variable cv_bh, cv_fit, cv_done;
+  std::condition_variable cv_bh, cv_run, cv_fit, cv_done;
   std::deque<Request*> queue;
   std::map<int64_t, std::unique_ptr<Request>> reqs;
   std::deque<Request*> bh_pending, fit_pending;
@@ -108,6 +108,7 @@ struct bhtsne_server {
   int64_t used = 0, peak = 0, done = 0, in_flight = 0;
   double batch_points_sum = 0;
   int64_t batch_epochs = 0;
+  double t_round = 0, t_repack = 0, t_prepare = 0, t_fit = 0;  // host seconds per executor
   bool stop = false;
   std::string err;
   std::vector<std::thread> threads;
@@ -162,21 +163,32 @@ struct BhEngine {
   std::vector<std::unique_ptr<Slot<T>>> slots;
   int64_t total = 0, nnz = 0;
   DevBuf d_off, job_of, rows, cols, vals, y, uy, gains, y2, uy2, g2, pos, neg, q, z, lr, mom, active, boxes;
-  DevBuf codes, jobkey, jobkey_alt, tmp, sumtmp, klbuf, kltmp, ykl, upload_y;
+  DevBuf codes, jobkey, jobkey_alt, klbuf, kltmp, ykl;
   BhWorkspace<T> ws, kws;
   SegTiles tiles;
-  AffinityScratch<T> aff;
+  // affinity preparation runs on its own thread and stream, overlapping the
+  // batch's epochs; prepared jobs wait in `ready` for the next repack
+  cudaStream_t ps = nullptr;
+  AffinityScratch<T> paff;
+  DevBuf psum, ptmp;
+  std::vector<std::unique_ptr<Slot<T>>> ready;
   cudaGraphExec_t graph = nullptr;
   int64_t graph_kernels = 0;
 
   explicit BhEngine(bhtsne_server* server) : sv(server) {
     BHG_CUDA(cudaSetDevice(sv->device));
-    BHG_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    // the batch's epochs outrank affinity preparation (long kNN launches), so
+    // freed SMs go to the running jobs first
+    int lo = 0, hi = 0;
+    BHG_CUDA(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+    BHG_CUDA(cudaStreamCreateWithPriority(&s, cudaStreamNonBlocking, hi));
+    BHG_CUDA(cudaStreamCreateWithPriority(&ps, cudaStreamNonBlocking, lo));
   }
   ~BhEngine() {
     cudaSetDevice(sv->device);
     if (graph) cudaGraphExecDestroy(graph);
     if (s) cudaStreamDestroy(s);
+    if (ps) cudaStreamDestroy(ps);
   }
 
   // Embedding (and KL) of a finished job, then it leaves the batch.
@@ -209,6 +221,10 @@ struct BhEngine {
   // Affinities of newly admitted requests (grouped by input dim), their P
   // normalised and exaggerated (normalize_p_values, src/tsne/mod.rs:284-293).
   std::vector<std::unique_ptr<Slot<T>>> prepare(const std::vector<Request*>& fresh) {
+    cudaStream_t s = ps;
+    DevBuf& sumtmp = psum;
+    DevBuf& tmp = ptmp;
+    AffinityScratch<T>& aff = paff;
     std::vector<std::unique_ptr<Slot<T>>> out;
     std::map<int32_t, std::vector<Request*>> by_dim;
     for (Request* r : fresh) by_dim[r->dim].push_back(r);
@@ -474,33 +490,57 @@ struct BhEngine {
     }
   }
 
-  void loop() {
+  // Preparer thread: affinities of admitted requests, handed to the batch.
+  void prepare_loop() {
     BHG_CUDA(cudaSetDevice(sv->device));
     for (;;) {
       std::vector<Request*> fresh;
-      bool have_work = false;
       {
         std::unique_lock<std::mutex> lk(sv->m);
-        sv->cv_bh.wait(lk, [&] { return sv->stop || !sv->bh_pending.empty() || !slots.empty(); });
+        sv->cv_bh.wait(lk, [&] { return sv->stop || !sv->bh_pending.empty(); });
         if (sv->stop) break;
         fresh.assign(sv->bh_pending.begin(), sv->bh_pending.end());
         sv->bh_pending.clear();
       }
+      std::vector<std::unique_ptr<Slot<T>>> prepared;
+      const double t0 = now_s();
+      try {
+        prepared = prepare(fresh);
+      } catch (const std::exception& ex) {
+        for (Request* r : fresh) sv->finish(r, ex.what());
+        continue;
+      }
+      std::lock_guard<std::mutex> lk(sv->m);
+      sv->t_prepare += now_s() - t0;
+      for (auto& p : prepared) ready.push_back(std::move(p));
+      sv->cv_run.notify_all();
+    }
+  }
+
+  // Batch thread: repack when jobs arrive or leave, then a round of epochs.
+  void loop() {
+    BHG_CUDA(cudaSetDevice(sv->device));
+    for (;;) {
+      std::vector<std::unique_ptr<Slot<T>>> fresh;
+      bool have_work = false;
+      {
+        std::unique_lock<std::mutex> lk(sv->m);
+        sv->cv_run.wait(lk, [&] { return sv->stop || !ready.empty() || !slots.empty(); });
+        if (sv->stop) break;
+        for (auto& p : ready) fresh.push_back(std::move(p));
+        ready.clear();
+      }
       try {
         bool need_repack = !fresh.empty();
         for (auto& sl : slots) need_repack = need_repack || !sl->active;
-        if (need_repack) {
-          std::vector<std::unique_ptr<Slot<T>>> prepared;
-          try {
-            prepared = prepare(fresh);
-          } catch (const std::exception& ex) {
-            for (Request* r : fresh) sv->finish(r, ex.what());
-            prepared.clear();
-          }
-          repack(std::move(prepared));
-        }
+        const double t0 = now_s();
+        if (need_repack) repack(std::move(fresh));
+        const double t1 = now_s();
         for (auto& sl : slots) have_work = have_work || sl->active;
         if (have_work) round();
+        std::lock_guard<std::mutex> lk(sv->m);
+        sv->t_repack += t1 - t0;
+        sv->t_round += now_s() - t1;
       } catch (const std::exception& ex) {
         fail_all(ex.what());
       }
@@ -549,8 +589,11 @@ void fit_worker(bhtsne_server* sv) {
       r = sv->fit_pending.front();
       sv->fit_pending.pop_front();
     }
+    const double t0 = now_s();
     if (rc != BHTSNE_OK) sv->finish(r, "error: a FIt-SNE worker could not create its context.");
     else run_fit_request<T>(sv, wctx, r);
+    std::lock_guard<std::mutex> lk(sv->m);
+    sv->t_fit += now_s() - t0;
   }
   if (wctx) bhtsne_ctx_destroy(wctx);
 }
@@ -560,6 +603,7 @@ void start(bhtsne_server* sv) {
   auto* eng = new BhEngine<T>(sv);
   sv->engine = eng;
   sv->threads.emplace_back([eng] { eng->loop(); });
+  sv->threads.emplace_back([eng] { eng->prepare_loop(); });
   for (int w = 0; w < sv->prm.fit_workers; ++w) sv->threads.emplace_back([sv] { fit_worker<T>(sv); });
 }
 
@@ -620,6 +664,7 @@ int bhtsne_server_free(bhtsne_server* sv) {
     sv->queue.clear();
   }
   sv->cv_bh.notify_all();
+  sv->cv_run.notify_all();
   sv->cv_fit.notify_all();
   for (auto& t : sv->threads) t.join();
   if (sv->dtype == BHTSNE_F32) delete static_cast<BhEngine<float>*>(sv->engine);
@@ -724,6 +769,16 @@ int bhtsne_server_result(bhtsne_server* sv, int64_t id, void* embedding, double*
   if (kl) *kl = r->kl;
   if (latency_ms) *latency_ms = 1e3 * (r->t_done - r->t_submit);
   sv->reqs.erase(it);
+  return BHTSNE_OK;
+}
+
+int bhtsne_server_timings(bhtsne_server* sv, double* round_s, double* repack_s, double* prepare_s, double* fit_s) {
+  if (!sv) return BHTSNE_EINVAL;
+  std::lock_guard<std::mutex> lk(sv->m);
+  if (round_s) *round_s = sv->t_round;
+  if (repack_s) *repack_s = sv->t_repack;
+  if (prepare_s) *prepare_s = sv->t_prepare;
+  if (fit_s) *fit_s = sv->t_fit;
   return BHTSNE_OK;
 }
 

@@ -96,4 +96,7 @@ class Server:
     def stats(self):
         d, f, p, m = C.c_int64(), C.c_int64(), C.c_int64(), C.c_double()
         self._check(self.lib.bhtsne_server_stats(self.handle, C.byref(d), C.byref(f), C.byref(p), C.byref(m)))
-        return {"done": d.value, "in_flight": f.value, "peak_bytes": p.value, "mean_batch_points": m.value}
+        a, b, c, e = C.c_double(), C.c_double(), C.c_double(), C.c_double()
+        self._check(self.lib.bhtsne_server_timings(self.handle, C.byref(a), C.byref(b), C.byref(c), C.byref(e)))
+        return {"done": d.value, "in_flight": f.value, "peak_bytes": p.value, "mean_batch_points": m.value,
+                "round_s": a.value, "repack_s": b.value, "prepare_s": c.value, "fit_worker_s": e.value}

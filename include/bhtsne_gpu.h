@@ -268,6 +268,9 @@ int bhtsne_server_wait(bhtsne_server* s, int64_t id, double timeout_s);
 int bhtsne_server_result(bhtsne_server* s, int64_t id, void* embedding, double* kl, double* latency_ms);
 int bhtsne_server_stats(bhtsne_server* s, int64_t* done, int64_t* in_flight, int64_t* peak_bytes,
                         double* mean_batch_points);
+/* Host seconds spent so far: Barnes-Hut rounds, repacks, affinity preparation,
+ * FIt-SNE requests (summed over workers). */
+int bhtsne_server_timings(bhtsne_server* s, double* round_s, double* repack_s, double* prepare_s, double* fit_s);
 
 #ifdef __cplusplus
 }
