@@ -24,6 +24,7 @@
 
 #include <algorithm>
 #include <cfloat>
+#include <cstdlib>
 #include <type_traits>
 
 namespace bhg {
@@ -508,7 +509,7 @@ __global__ void knn_rerank_kernel(const T* __restrict__ X, int64_t n, int dim, i
                                   const float* __restrict__ thr, const float* __restrict__ norms,
                                   const unsigned* __restrict__ max_bits, uint32_t* __restrict__ out_idx,
                                   T* __restrict__ out_dist, uint32_t* __restrict__ fail_list,
-                                  unsigned* __restrict__ fail_count) {
+                                  unsigned* __restrict__ fail_count, double ecoef) {
   constexpr int W = 4;
   __shared__ T sd[W][C];
   __shared__ T sd2[W][C];
@@ -568,7 +569,7 @@ __global__ void knn_rerank_kernel(const T* __restrict__ X, int64_t n, int dim, i
       const double qn = (double)norms[qi] * (1.0 + g);
       const double d2k = (double)sd2[w][k - 1] * (1.0 + g) * (1.0 + 16.0 * u);
       const double r = sqrt(qn) + sqrt(d2k);
-      const double E = (4.0 * dim + 16.0) * u * (qn + r * r);
+      const double E = ecoef * (qn + r * r);
       ok = d2k + E < (double)th;
     }
     if (!ok) fail_list[atomicAdd(fail_count, 1u)] = (uint32_t)qi;
@@ -622,6 +623,13 @@ __global__ void knn_exact_kernel(const T* __restrict__ X, int64_t n, int dim, in
   }
 }
 
+// The candidate pass runs on the tensor cores unless BHTSNE_KNN_SIMT is set
+// (the FP32 CUDA-core kernels, kept for comparison).
+bool use_tensor_cores() {
+  static const bool simt = getenv("BHTSNE_KNN_SIMT") != nullptr;
+  return !simt;
+}
+
 size_t sel_smem_bytes(int dim) {
   return ((size_t)dim * QB + DK * CB + QB * (CB + 1)) * 4 + (size_t)QB * 2 * kSelC * 8;
 }
@@ -663,25 +671,31 @@ int64_t knn_euclidean(const T* X, int64_t n, int dim, int k, uint32_t* out_idx, 
   uint32_t* fails = static_cast<uint32_t*>(ws.fails.ensure((size_t)n * sizeof(uint32_t)));
   const size_t smem = ((size_t)dim * QB + DK * CB + QB * (CB + 1) + (size_t)QB * C * 2 + 2 * QB) * 4;
   const unsigned grid = (unsigned)ceil_div(n, QB);
-  if (C == 128 && dim <= kSelDimMax) {
+  const double simt_coef = (4.0 * dim + 16.0) / 16777216.0;
+  if (C == 128 && use_tensor_cores()) {
+    knn_tc_candidates(Xf, n, dim, norms, nullptr, nullptr, nullptr, ceil_div(n, 128), cand, thr, ws.tc, s);
+    knn_rerank_kernel<T, 128><<<(unsigned)ceil_div(n, 4), 128, 0, s>>>(X, n, dim, k, cand, thr, norms, max_bits, out_idx,
+                                                                       out_dist, fails, fail_count,
+                                                                       knn_tc_error_coef(dim));
+  } else if (C == 128 && dim <= kSelDimMax) {
     const size_t ssmem = sel_smem_bytes(dim);
     BHG_CUDA(cudaFuncSetAttribute(knn_cand_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ssmem));
     knn_cand_kernel<<<grid, kThreads, ssmem, s>>>(Xf, n, dim, norms, cand, thr, nullptr, nullptr, nullptr);
     BHG_LAUNCH_CHECK();
     knn_rerank_kernel<T, 128><<<(unsigned)ceil_div(n, 4), 128, 0, s>>>(X, n, dim, k, cand, thr, norms, max_bits, out_idx,
-                                                                       out_dist, fails, fail_count);
+                                                                       out_dist, fails, fail_count, simt_coef);
   } else if (C == 128) {
     BHG_CUDA(cudaFuncSetAttribute(knn_tile_kernel<128, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     knn_tile_kernel<128, false><<<grid, kThreads, smem, s>>>(Xf, n, dim, norms, nullptr, n, 128, cand, thr);
     BHG_LAUNCH_CHECK();
     knn_rerank_kernel<T, 128><<<(unsigned)ceil_div(n, 4), 128, 0, s>>>(X, n, dim, k, cand, thr, norms, max_bits, out_idx,
-                                                                       out_dist, fails, fail_count);
+                                                                       out_dist, fails, fail_count, simt_coef);
   } else {
     BHG_CUDA(cudaFuncSetAttribute(knn_tile_kernel<256, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     knn_tile_kernel<256, false><<<grid, kThreads, smem, s>>>(Xf, n, dim, norms, nullptr, n, 256, cand, thr);
     BHG_LAUNCH_CHECK();
     knn_rerank_kernel<T, 256><<<(unsigned)ceil_div(n, 4), 128, 0, s>>>(X, n, dim, k, cand, thr, norms, max_bits, out_idx,
-                                                                       out_dist, fails, fail_count);
+                                                                       out_dist, fails, fail_count, simt_coef);
   }
   BHG_LAUNCH_CHECK();
   unsigned nfail = 0;
@@ -760,27 +774,46 @@ int64_t knn_euclidean_segmented(const T* X, int64_t total, int dim, int k, const
   float* thr = static_cast<float*>(ws.thr.ensure((size_t)total * sizeof(float)));
   uint32_t* fails = static_cast<uint32_t*>(ws.fails.ensure((size_t)total * sizeof(uint32_t)));
   const size_t smem = ((size_t)dim * QB + DK * CB + QB * (CB + 1) + (size_t)QB * C * 2 + 2 * QB) * 4;
-  if (C == 128 && dim <= kSelDimMax) {
+  const double simt_coef = (4.0 * dim + 16.0) / 16777216.0;
+  if (C == 128 && use_tensor_cores()) {
+    // 128-query blocks per set, largest sets first
+    std::vector<int64_t> tq0;
+    std::vector<int32_t> tbj;
+    for (int j : order)
+      for (int64_t q = off[j]; q < off[j + 1]; q += 128) {
+        tq0.push_back(q);
+        tbj.push_back(j);
+      }
+    const int64_t tn = (int64_t)tq0.size();
+    int64_t* t_q0 = static_cast<int64_t*>(ws.tc_blk.ensure((size_t)tn * (8 + 4)));
+    int32_t* t_bj = reinterpret_cast<int32_t*>(t_q0 + tn);
+    BHG_CUDA(cudaMemcpyAsync(t_q0, tq0.data(), (size_t)tn * 8, cudaMemcpyHostToDevice, s));
+    BHG_CUDA(cudaMemcpyAsync(t_bj, tbj.data(), (size_t)tn * 4, cudaMemcpyHostToDevice, s));
+    knn_tc_candidates(Xf, total, dim, norms, t_q0, t_bj, d_off, tn, cand, thr, ws.tc, s);
+    knn_rerank_kernel<T, 128><<<(unsigned)ceil_div(total, 4), 128, 0, s>>>(X, total, dim, k, cand, thr, norms, max_bits,
+                                                                           out_idx, out_dist, fails, fail_count,
+                                                                           knn_tc_error_coef(dim));
+  } else if (C == 128 && dim <= kSelDimMax) {
     const size_t ssmem = sel_smem_bytes(dim);
     BHG_CUDA(cudaFuncSetAttribute(knn_cand_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ssmem));
     knn_cand_kernel<<<(unsigned)nblk, kThreads, ssmem, s>>>(Xf, total, dim, norms, cand, thr, d_q0, d_bj, d_off);
     BHG_LAUNCH_CHECK();
     knn_rerank_kernel<T, 128><<<(unsigned)ceil_div(total, 4), 128, 0, s>>>(X, total, dim, k, cand, thr, norms, max_bits,
-                                                                           out_idx, out_dist, fails, fail_count);
+                                                                           out_idx, out_dist, fails, fail_count, simt_coef);
   } else if (C == 128) {
     BHG_CUDA(cudaFuncSetAttribute(knn_tile_kernel<128, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     knn_tile_kernel<128, false><<<(unsigned)nblk, kThreads, smem, s>>>(Xf, total, dim, norms, nullptr, total, 128, cand,
                                                                       thr, d_q0, d_bj, d_off);
     BHG_LAUNCH_CHECK();
     knn_rerank_kernel<T, 128><<<(unsigned)ceil_div(total, 4), 128, 0, s>>>(X, total, dim, k, cand, thr, norms, max_bits,
-                                                                           out_idx, out_dist, fails, fail_count);
+                                                                           out_idx, out_dist, fails, fail_count, simt_coef);
   } else {
     BHG_CUDA(cudaFuncSetAttribute(knn_tile_kernel<256, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     knn_tile_kernel<256, false><<<(unsigned)nblk, kThreads, smem, s>>>(Xf, total, dim, norms, nullptr, total, 256, cand,
                                                                       thr, d_q0, d_bj, d_off);
     BHG_LAUNCH_CHECK();
     knn_rerank_kernel<T, 256><<<(unsigned)ceil_div(total, 4), 128, 0, s>>>(X, total, dim, k, cand, thr, norms, max_bits,
-                                                                           out_idx, out_dist, fails, fail_count);
+                                                                           out_idx, out_dist, fails, fail_count, simt_coef);
   }
   BHG_LAUNCH_CHECK();
   unsigned nfail = 0;

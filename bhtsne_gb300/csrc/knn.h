@@ -4,11 +4,13 @@
 #include <vector>
 
 #include "internal.h"
+#include "knn_tc.h"
 
 namespace bhg {
 
 struct KnnWorkspace {
-  DevBuf xf, norms, cand, thr, fails, counters, blk;
+  DevBuf xf, norms, cand, thr, fails, counters, blk, tc_blk;
+  KnnTcScratch tc;
   int64_t last_fallback_rows = 0;
   void release() {
     xf.release();
@@ -17,6 +19,8 @@ struct KnnWorkspace {
     thr.release();
     fails.release();
     blk.release();
+    tc_blk.release();
+    tc.release();
   }
 };
 

@@ -1,0 +1,32 @@
+// Tensor-core candidate pass of the exact kNN (see knn_tc.cu).
+#pragma once
+
+#include <cmath>
+
+#include "internal.h"
+
+namespace bhg {
+
+struct KnnTcScratch {
+  DevBuf xhi, err;  // xhi: rows padded to a multiple of 16 dimensions when needed
+  void release() { xhi.release(); }
+};
+
+// Per query of X (n x dim, FP32): the indices of its 128 candidates with the
+// smallest |q|^2 + |c|^2 - 2 q.c (3xTF32 tensor-core dot products), sorted by
+// (value, index), into cand[q * 128 ..], and the 128-th value into thr[q]
+// (INFINITY when fewer candidates exist). Blocks of 128 queries; with a block
+// table (blk_q0, blk_job, seg_off) block b takes queries blk_q0[b].. of set
+// blk_job[b] and scans only that set's rows. Synchronises the stream.
+void knn_tc_candidates(const float* X, int64_t n, int dim, const float* norms, const int64_t* blk_q0,
+                       const int32_t* blk_job, const int64_t* seg_off, int64_t nblocks, uint32_t* cand, float* thr,
+                       KnnTcScratch& ws, cudaStream_t s);
+
+// Error coefficient of the tensor-core candidate values: |v - d^2| <= coef *
+// (|q|^2 + r^2) for candidates within radius r of the origin.
+inline double knn_tc_error_coef(int dim) {
+  const int dim_pad = (dim + 15) / 16 * 16;
+  return 2.0 * (std::ldexp(1.0, -19) + (3.0 * dim_pad + 8.0) * std::ldexp(1.0, -23) + (dim + 8.0) * std::ldexp(1.0, -24));
+}
+
+}  // namespace bhg

@@ -21,6 +21,24 @@ def test_knn_matches_bruteforce(gpu, oracle):
     assert np.array_equal(gd, od)
 
 
+@pytest.mark.parametrize("n,dim,k,spread", [(9000, 100, 90, 10.0), (6000, 17, 30, 3.0), (3000, 300, 60, 1.0),
+                                             (700, 8, 20, 0.0)])
+def test_knn_tensor_core_pass_is_exact(gpu, oracle, n, dim, k, spread):
+    """The tensor-core candidate pass (3xTF32) with the exact re-rank and the
+    certificate: neighbour lists and distances equal brute force, including
+    dims that are not multiples of the 32-dimension chunk, tight clusters
+    (spread 1), and exact ties (spread 0: every point duplicated)."""
+    if spread > 0:
+        X, _ = blobs(n, dim, 8, 40 + dim, spread=spread)
+    else:
+        base, _ = blobs(n // 2, dim, 3, 77)
+        X = np.concatenate([base, base])
+    gi, gd = gpu.knn_euclidean(X, k)
+    oi, od = oracle.knn(X, k)
+    assert np.array_equal(gi, oi)
+    assert np.array_equal(gd, od)
+
+
 def test_conditional_p(gpu, oracle):
     X, _ = blobs(1000, 20, 5, 2)
     _, od = oracle.knn(X, 90)
