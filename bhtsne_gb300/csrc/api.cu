@@ -39,7 +39,23 @@ struct bhtsne_ctx {
 
 namespace bhg {
 int ctx_device(const bhtsne_ctx* ctx) { return ctx->device; }
+
+// A context whose stream has the given priority (lower numbers run first);
+// used by the server for its FIt-SNE workers.
+int ctx_create_with_priority(int device, int priority, bhtsne_ctx** out) {
+  if (!out) return BHTSNE_EINVAL;
+  *out = nullptr;
+  bhtsne_ctx* c = new bhtsne_ctx();
+  c->device = device;
+  if (cudaSetDevice(device) != cudaSuccess ||
+      cudaStreamCreateWithPriority(&c->stream, cudaStreamNonBlocking, priority) != cudaSuccess) {
+    delete c;
+    return BHTSNE_ECUDA;
+  }
+  *out = c;
+  return BHTSNE_OK;
 }
+}  // namespace bhg
 
 namespace {
 

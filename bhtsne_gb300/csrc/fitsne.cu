@@ -143,52 +143,91 @@ __device__ __forceinline__ void locate(T v, const FitParams<T>& p, const Lagrang
   lb.weights(local, w);
 }
 
-__device__ __forceinline__ void fix_add(long long* a, double v, double up) {
-  atomicAdd(reinterpret_cast<unsigned long long*>(a), (unsigned long long)__double2ll_rn(v * up));
-}
-
+// Charges of one point in fixed point: 3^D nodes x (D + 2) values. Integer
+// sums are exact and order-free, so the grid does not depend on how the adds
+// are grouped.
 template <class T, int D>
 __global__ void spread_kernel(const T* __restrict__ y, int64_t n, const FitParams<T>* __restrict__ prm,
                               long long* __restrict__ acc) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
+  const int lane = threadIdx.x & 31;
+  const bool valid = i < n;
   const FitParams<T> p = *prm;
   const Lagrange3<T> lb;
   const int L = p.L;
   const double up = ldexp(1.0, p.fix_shift);
+  constexpr int combos = D == 1 ? 3 : 9;
+  constexpr int NV = D + 2;
   int box[D];
   T w[D][3];
   T yv[D];
 #pragma unroll
   for (int a = 0; a < D; ++a) {
-    yv[a] = y[i * D + a];
+    yv[a] = valid ? y[i * D + a] : T(0);
     locate<T>(yv[a], p, lb, &box[a], w[a]);
   }
   T sq = T(0);
 #pragma unroll
   for (int a = 0; a < D; ++a) sq = sq + yv[a] * yv[a];
-  constexpr int combos = D == 1 ? 3 : 9;
+  long long v[combos][NV];
 #pragma unroll
   for (int c = 0; c < combos; ++c) {
     int rem = c;
-    int64_t flat = 0;
     T wt = T(1);
 #pragma unroll
     for (int a = 0; a < D; ++a) {
       const int k = rem % 3;
       rem /= 3;
-      flat = flat * L + (box[a] * 3 + k);
       wt = wt * w[a][k];
     }
-    long long* cell = acc + 4 * flat;
-    fix_add(cell + 0, (double)(wt * p.scale), up);
-    fix_add(cell + 1, (double)(wt * yv[0]), up);
-    if (D == 2) {
-      fix_add(cell + 2, (double)(wt * yv[D - 1]), up);
-      fix_add(cell + 3, (double)(wt * (sq / p.scale)), up);
-    } else {
-      fix_add(cell + 2, (double)(wt * (sq / p.scale)), up);
+    v[c][0] = __double2ll_rn((double)(wt * p.scale) * up);
+    v[c][1] = __double2ll_rn((double)(wt * yv[0]) * up);
+    if (D == 2) v[c][D] = __double2ll_rn((double)(wt * yv[D - 1]) * up);
+    v[c][NV - 1] = __double2ll_rn((double)(wt * (sq / p.scale)) * up);
+    if (!valid) {
+#pragma unroll
+      for (int q = 0; q < NV; ++q) v[c][q] = 0;
     }
+  }
+  // Points are mostly in Z-order (the layout is renumbered by Morton order),
+  // so runs of lanes share a box and so all 3^D target cells: sum each run in
+  // registers (segmented reduction to the run's first lane) and let that lane
+  // alone issue the atomics. A warp with many runs adds directly.
+  long long key = valid ? (long long)box[0] : -1 - (long long)lane;
+  if (D == 2 && valid) key = key * 4096 + box[D - 1];
+  const long long prev = __shfl_up_sync(0xffffffffu, key, 1);
+  const bool head = lane == 0 || prev != key;
+  const unsigned heads = __ballot_sync(0xffffffffu, head);
+  const bool combine = __popc(heads) <= 16;
+  if (combine) {
+    const int run = __popc(heads & ((2u << lane) - 1u));
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+      const int orun = __shfl_down_sync(0xffffffffu, run, off);
+      const bool take = lane + off < 32 && orun == run;
+#pragma unroll
+      for (int c = 0; c < combos; ++c)
+#pragma unroll
+        for (int q = 0; q < NV; ++q) {
+          const long long o = __shfl_down_sync(0xffffffffu, v[c][q], off);
+          if (take) v[c][q] += o;
+        }
+    }
+  }
+  if (!valid || (combine && !head)) return;
+#pragma unroll
+  for (int c = 0; c < combos; ++c) {
+    int rem = c;
+    int64_t flat = 0;
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+      const int k = rem % 3;
+      rem /= 3;
+      flat = flat * L + (box[a] * 3 + k);
+    }
+    unsigned long long* cell = reinterpret_cast<unsigned long long*>(acc + 4 * flat);
+#pragma unroll
+    for (int q = 0; q < NV; ++q) atomicAdd(cell + q, (unsigned long long)v[c][q]);
   }
 }
 

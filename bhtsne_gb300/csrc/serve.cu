@@ -41,6 +41,7 @@
 
 namespace bhg {
 int ctx_device(const bhtsne_ctx* ctx);
+int ctx_create_with_priority(int device, int priority, bhtsne_ctx** out);
 }
 
 using namespace bhg;
@@ -177,11 +178,13 @@ struct BhEngine {
 
   explicit BhEngine(bhtsne_server* server) : sv(server) {
     BHG_CUDA(cudaSetDevice(sv->device));
-    // the batch's epochs outrank affinity preparation (long kNN launches), so
-    // freed SMs go to the running jobs first
+    // stream priorities: FIt-SNE workers (small, host-synchronised epochs)
+    // first, then the batch's epochs, then affinity preparation (long kNN
+    // launches), so freed SMs go to the latency-bound work first
     int lo = 0, hi = 0;
     BHG_CUDA(cudaDeviceGetStreamPriorityRange(&lo, &hi));
-    BHG_CUDA(cudaStreamCreateWithPriority(&s, cudaStreamNonBlocking, hi));
+    const int mid = lo + (hi - lo) / 2;
+    BHG_CUDA(cudaStreamCreateWithPriority(&s, cudaStreamNonBlocking, mid == hi ? lo : mid));
     BHG_CUDA(cudaStreamCreateWithPriority(&ps, cudaStreamNonBlocking, lo));
   }
   ~BhEngine() {
@@ -579,7 +582,9 @@ void run_fit_request(bhtsne_server* sv, bhtsne_ctx* wctx, Request* r) {
 template <class T>
 void fit_worker(bhtsne_server* sv) {
   bhtsne_ctx* wctx = nullptr;
-  const int rc = bhtsne_ctx_create(sv->device, &wctx);
+  int lo = 0, hi = 0;
+  cudaDeviceGetStreamPriorityRange(&lo, &hi);
+  const int rc = ctx_create_with_priority(sv->device, hi, &wctx);
   for (;;) {
     Request* r = nullptr;
     {
