@@ -479,7 +479,7 @@ def main():
     ap.add_argument("--batch-epochs", type=int, default=500)
     ap.add_argument("--serve-requests", type=int, default=48, help="serving comparison (0 to skip)")
     ap.add_argument("--serve-epochs", type=int, default=750)
-    ap.add_argument("--serve-rate", type=float, default=8.0, help="Poisson arrivals per second")
+    ap.add_argument("--serve-rate", type=float, default=64.0, help="Poisson arrivals per second")
     ap.add_argument("--serve-fit-workers", type=int, default=8, help="server streams for FIt-SNE requests")
     args = ap.parse_args()
     if args.warmup < 3:

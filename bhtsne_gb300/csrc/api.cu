@@ -14,6 +14,7 @@
 #include <cstring>
 #include <functional>
 #include <memory>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -29,7 +30,21 @@ using namespace bhg;
 
 namespace bhg {
 std::atomic<long long> g_launches{0};
+thread_local cudaStream_t g_alloc_stream = nullptr;
+
+void keep_pool_cached(int device) {
+  static std::mutex m;
+  static bool done[128] = {};
+  std::lock_guard<std::mutex> lk(m);
+  if (device < 0 || device >= 128 || done[device]) return;
+  cudaMemPool_t pool;
+  if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+    uint64_t keep = UINT64_MAX;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+  }
+  done[device] = true;
 }
+}  // namespace bhg
 
 struct bhtsne_ctx {
   int device = 0;
@@ -52,6 +67,7 @@ int ctx_create_with_priority(int device, int priority, bhtsne_ctx** out) {
     delete c;
     return BHTSNE_ECUDA;
   }
+  keep_pool_cached(device);
   *out = c;
   return BHTSNE_OK;
 }
@@ -75,7 +91,7 @@ struct State {
   DevBuf pdense;
   // optimisation state
   DevBuf y, uy, gains, pos, neg, zbuf, klbuf, tmp, tmp2;
-  DevBuf kidx, kdist, kp, xin, yext;
+  DevBuf kidx, kdist, kp, xin, yext, ckpt;
   Renumbering rn;  // locality layout of y/uy/gains (see launch_renumber)
   // y in the caller's point order (a copy when the layout is renumbered).
   const T* y_external(cudaStream_t s) {
@@ -175,6 +191,7 @@ double tcast(const bhtsne_tsne* t, double v) { return t->dtype == BHTSNE_F32 ? (
 template <class F>
 int guard_ctx(bhtsne_ctx* ctx, F&& f) {
   if (!ctx) return BHTSNE_EINVAL;
+  AllocStreamScope scope(ctx->stream);
   try {
     BHG_CUDA(cudaSetDevice(ctx->device));
     f();
@@ -192,6 +209,7 @@ int guard_ctx(bhtsne_ctx* ctx, F&& f) {
 template <class F>
 int guard(bhtsne_tsne* t, F&& f) {
   if (!t) return BHTSNE_EINVAL;
+  AllocStreamScope scope(t->ctx->stream);
   try {
     BHG_CUDA(cudaSetDevice(t->ctx->device));
     f();
@@ -383,6 +401,7 @@ void advance_impl(bhtsne_tsne* t, int64_t epochs) {
   // replayed. Off while profiling or when a callback needs per-epoch copies.
   static const bool graphs_off = getenv("BHTSNE_NO_GRAPH") != nullptr;
   const bool graphable = !graphs_off && !prof && !t->cb && t->loop_kind != BHTSNE_METHOD_FIT_SNE;
+  const bool graphable_fit = !graphs_off && !prof && !t->cb && t->loop_kind == BHTSNE_METHOD_FIT_SNE;
   // Locality renumbering: every kRenumberEvery epochs the sparse methods re-lay
   // out y / uy / gains in the Morton order of the current embedding so that a
   // row's neighbour gathers in the attractive pass stay close in memory.
@@ -414,6 +433,13 @@ void advance_impl(bhtsne_tsne* t, int64_t epochs) {
       launch_recenter_bbox<T>(D, y, n, nullptr, false, S.bh, bits, s);
     if (!was_active) t->drop_graph();  // the attractive pass now reads the slot arrays
   };
+  auto fit_body = [&](T mom) {
+    fit_repulsion_cap<T>(S.fit, D, y, n, S.bh.params.template as<BoxParams<T>>(), S.neg.template as<T>(), z, s);
+    attractive();
+    launch_update<T>(D, y, S.pos.template as<T>(), S.neg.template as<T>(), S.uy.template as<T>(),
+                     S.gains.template as<T>(), n, z, T(0), lr, mom, S.us, s);
+    launch_recenter_bbox<T>(D, y, n, S.us.mean(), true, S.bh, bits, s);
+  };
   auto body = [&](T mom) {
     if (t->loop_kind == BHTSNE_METHOD_BARNES_HUT) {
       bh_build<T>(S.bh, D, y, n, s);
@@ -429,8 +455,99 @@ void advance_impl(bhtsne_tsne* t, int64_t epochs) {
     }
     launch_recenter_bbox<T>(D, y, n, S.us.mean(), true, S.bh, bits, s);
   };
+  // FIt-SNE without a host synchronisation per epoch: the grid sizes are read
+  // on the device within a reserved transform capacity, so the epoch body is
+  // a graph too. Epochs run in chunks (up to 25, ending before a renumbering
+  // and at an epoch whose tail changes P or the momentum); after a chunk one
+  // synchronisation checks the capacity flag. If the embedding outgrew the
+  // capacity, the chunk's starting state is restored, the capacity doubled
+  // and the chunk repeated, so results never depend on the capacity.
+  if (graphable_fit && epochs > 0) {
+    FitWorkspace<T>& fw = S.fit;
+    const size_t ybytes = (size_t)n * D * sizeof(T);
+    T* ck = static_cast<T*>(S.ckpt.ensure(3 * ybytes));
+    int64_t k = 0;
+    bool eager_next = true;
+    while (k < epochs) {
+      const int64_t epoch = t->cursor;
+      if (epoch == 0) launch_recenter_bbox<T>(D, y, n, nullptr, false, S.bh, bits, s);
+      maybe_renumber(epoch);
+      int64_t len = std::min<int64_t>(25, epochs - k);
+      for (int64_t i = 0; i < len; ++i) {
+        const int64_t e = epoch + i;
+        if (i > 0 && renumber_every > 0 && e % renumber_every == 0) {
+          len = i;
+          break;
+        }
+        if ((e == t->stop_lying_epoch && e != 0) || e == t->momentum_switch_epoch) {
+          len = i + 1;
+          break;
+        }
+      }
+      if (fw.cap_L == 0) {
+        const int need = fit_needed_length<T>(fw, D, n, S.bh.params.template as<BoxParams<T>>(), s);
+        int cap = 64;
+        while (cap < 2 * need) cap <<= 1;
+        fw.reserve(D, n, cap);
+        t->drop_graph();
+        eager_next = true;
+      }
+      BHG_CUDA(cudaMemcpyAsync(ck, y, ybytes, cudaMemcpyDeviceToDevice, s));
+      BHG_CUDA(cudaMemcpyAsync(ck + (size_t)n * D, S.uy.ptr, ybytes, cudaMemcpyDeviceToDevice, s));
+      BHG_CUDA(cudaMemcpyAsync(ck + 2 * (size_t)n * D, S.gains.ptr, ybytes, cudaMemcpyDeviceToDevice, s));
+      BHG_CUDA(cudaMemsetAsync(fw.flag.ptr, 0, sizeof(int), s));
+      const T mom = (T)t->momentum;
+      for (int64_t i = 0; i < len; ++i) {
+        if (eager_next) {
+          fit_body(mom);
+          eager_next = false;
+          continue;
+        }
+        if (!t->graph || t->graph_momentum != t->momentum) {
+          t->drop_graph();
+          cudaGraph_t g;
+          const long long before = g_launches.load();
+          BHG_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed));
+          fit_body(mom);
+          BHG_CUDA(cudaStreamEndCapture(s, &g));
+          t->graph_kernels = g_launches.load() - before;
+          g_launches.fetch_sub(t->graph_kernels);
+          BHG_CUDA(cudaGraphInstantiate(&t->graph, g, 0));
+          BHG_CUDA(cudaGraphDestroy(g));
+          t->graph_momentum = t->momentum;
+        }
+        BHG_CUDA(cudaGraphLaunch(t->graph, s));
+        g_launches.fetch_add(t->graph_kernels);
+      }
+      int over = 0;
+      FitParams<T> hp;
+      BHG_CUDA(cudaMemcpyAsync(&over, fw.flag.ptr, sizeof(int), cudaMemcpyDeviceToHost, s));
+      BHG_CUDA(cudaMemcpyAsync(&hp, fw.params.ptr, sizeof(hp), cudaMemcpyDeviceToHost, s));
+      BHG_CUDA(cudaStreamSynchronize(s));
+      if (over) {
+        BHG_CUDA(cudaMemcpyAsync(y, ck, ybytes, cudaMemcpyDeviceToDevice, s));
+        BHG_CUDA(cudaMemcpyAsync(S.uy.ptr, ck + (size_t)n * D, ybytes, cudaMemcpyDeviceToDevice, s));
+        BHG_CUDA(cudaMemcpyAsync(S.gains.ptr, ck + 2 * (size_t)n * D, ybytes, cudaMemcpyDeviceToDevice, s));
+        launch_recenter_bbox<T>(D, y, n, nullptr, false, S.bh, bits, s);
+        fw.reserve(D, n, 2 * fw.cap_L);
+        t->drop_graph();
+        eager_next = true;
+        continue;
+      }
+      for (int64_t i = 0; i < len; ++i) epoch_tail<T>(t, epoch + i, snap);
+      t->cursor += len;
+      k += len;
+      if (2 * hp.need_L > fw.cap_L) {
+        int cap = fw.cap_L;
+        while (cap < 2 * hp.need_L) cap <<= 1;
+        fw.reserve(D, n, cap);
+        t->drop_graph();
+        eager_next = true;
+      }
+    }
+  }
   bool warmed = false;
-  for (int64_t k = 0; k < epochs; ++k) {
+  for (int64_t k = graphable_fit ? epochs : 0; k < epochs; ++k) {
     const int64_t epoch = t->cursor;
     if (epoch == 0) launch_recenter_bbox<T>(D, y, n, nullptr, false, S.bh, bits, s);
     maybe_renumber(epoch);
@@ -784,6 +901,7 @@ int bhtsne_ctx_create(int device, bhtsne_ctx** out) {
     delete c;
     return BHTSNE_ECUDA;
   }
+  keep_pool_cached(device);
   *out = c;
   return BHTSNE_OK;
 }
@@ -1243,6 +1361,7 @@ struct BatchImpl {
 template <class F>
 int guard_batch(bhtsne_batch* b, F&& f) {
   if (!b) return BHTSNE_EINVAL;
+  AllocStreamScope scope(b->ctx->stream);
   try {
     BHG_CUDA(cudaSetDevice(b->ctx->device));
     f();

@@ -46,22 +46,25 @@ __device__ __forceinline__ void load_point(const T* __restrict__ y, int64_t j, T
   }
 }
 
-template <class T, int D, int G, int kU, bool VEC>
+// One warp per row (slot); consecutive warps take consecutive slots, so the
+// rows in flight are a contiguous window of P and their sorted slot columns
+// gather nearby y[j].
+template <class T, int D, int kU, bool VEC>
 __global__ void __launch_bounds__(256) attractive_kernel(const uint64_t* __restrict__ rows, const uint32_t* __restrict__ cols,
                                                          const T* __restrict__ vals, const T* __restrict__ y, int64_t n,
                                                          const uint32_t* __restrict__ row_of_slot, T* __restrict__ pos) {
+  constexpr int G = 32;
   const int64_t slot = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / G;
   const int lane = threadIdx.x & (G - 1);
-  const bool active = slot < n;
-  const int64_t sl = active ? slot : n - 1;
-  const int64_t row = row_of_slot ? (int64_t)row_of_slot[sl] : sl;
+  if (slot >= n) return;
+  const int64_t row = row_of_slot ? (int64_t)row_of_slot[slot] : slot;
   T yi[D], acc[D];
 #pragma unroll
   for (int a = 0; a < D; ++a) {
-    yi[a] = y[sl * D + a];
+    yi[a] = y[slot * D + a];
     acc[a] = T(0);
   }
-  const int64_t e0 = (int64_t)rows[row], e1 = active ? (int64_t)rows[row + 1] : e0;
+  const int64_t e0 = (int64_t)rows[row], e1 = (int64_t)rows[row + 1];
   for (int64_t base = e0; base < e1; base += G * kU) {
     uint32_t j[kU];
     T p[kU];
@@ -69,7 +72,7 @@ __global__ void __launch_bounds__(256) attractive_kernel(const uint64_t* __restr
 #pragma unroll
     for (int u = 0; u < kU; ++u) {
       const int64_t e = base + lane + G * u;
-      j[u] = e < e1 ? __ldg(cols + e) : (uint32_t)sl;
+      j[u] = e < e1 ? __ldg(cols + e) : (uint32_t)slot;
       p[u] = e < e1 ? __ldg(vals + e) : T(0);
     }
 #pragma unroll
@@ -91,9 +94,9 @@ __global__ void __launch_bounds__(256) attractive_kernel(const uint64_t* __restr
 #pragma unroll
   for (int a = 0; a < D; ++a) {
 #pragma unroll
-    for (int o = G / 2; o > 0; o >>= 1) acc[a] += __shfl_xor_sync(kFull, acc[a], o, G);
+    for (int o = G / 2; o > 0; o >>= 1) acc[a] += __shfl_xor_sync(kFull, acc[a], o);
   }
-  if (active && lane == 0) {
+  if (lane == 0) {
 #pragma unroll
     for (int a = 0; a < D; ++a) pos[slot * D + a] = acc[a];
   }
@@ -422,44 +425,22 @@ constexpr int kUpdBlocks = 2 * 152;
 
 }  // namespace
 
-template <class T, int D, bool VEC>
-static void launch_attractive_v(int variant, const uint64_t* rows, const uint32_t* cols, const T* vals, const T* y,
-                                int64_t n, T* pos, cudaStream_t s, const uint32_t* row_of_slot) {
-  switch (variant) {
-    case 1:
-      attractive_kernel<T, D, 32, 8, VEC>
-          <<<(unsigned)ceil_div(n * 32, 256), 256, 0, s>>>(rows, cols, vals, y, n, row_of_slot, pos);
-      break;
-    case 2:
-      attractive_kernel<T, D, 16, 8, VEC>
-          <<<(unsigned)ceil_div(n * 16, 256), 256, 0, s>>>(rows, cols, vals, y, n, row_of_slot, pos);
-      break;
-    default:
-      attractive_kernel<T, D, 32, 4, VEC>
-          <<<(unsigned)ceil_div(n * 32, 256), 256, 0, s>>>(rows, cols, vals, y, n, row_of_slot, pos);
-      break;
-  }
-}
-
 template <class T, int D>
-static void launch_attractive_d(int variant, const uint64_t* rows, const uint32_t* cols, const T* vals, const T* y,
-                                int64_t n, T* pos, cudaStream_t s, const uint32_t* row_of_slot) {
+static void launch_attractive_d(const uint64_t* rows, const uint32_t* cols, const T* vals, const T* y, int64_t n, T* pos,
+                                cudaStream_t s, const uint32_t* row_of_slot) {
   const bool vec = D == 2 && (reinterpret_cast<uintptr_t>(y) % (2 * sizeof(T))) == 0;
-  if (vec) launch_attractive_v<T, D, true>(variant, rows, cols, vals, y, n, pos, s, row_of_slot);
-  else launch_attractive_v<T, D, false>(variant, rows, cols, vals, y, n, pos, s, row_of_slot);
+  const unsigned grid = (unsigned)ceil_div(n, 8);
+  if (vec) attractive_kernel<T, D, 4, true><<<grid, 256, 0, s>>>(rows, cols, vals, y, n, row_of_slot, pos);
+  else attractive_kernel<T, D, 4, false><<<grid, 256, 0, s>>>(rows, cols, vals, y, n, row_of_slot, pos);
 }
 
 template <class T>
 void launch_attractive(int D, const uint64_t* rows, const uint32_t* cols, const T* vals, const T* y, int64_t n, T* pos,
                        cudaStream_t s, const uint32_t* row_of_slot) {
   if (n <= 0) return;
-  static const int variant = [] {
-    const char* v = getenv("BHTSNE_ATTRACTIVE_VARIANT");
-    return v ? atoi(v) : 0;
-  }();
   with_dim<1, 7>(D, "error: the embedding dimension must be in 1..7.", [&](auto dc) {
     constexpr int DD = decltype(dc)::value;
-    launch_attractive_d<T, DD>(variant, rows, cols, vals, y, n, pos, s, row_of_slot);
+    launch_attractive_d<T, DD>(rows, cols, vals, y, n, pos, s, row_of_slot);
   });
   BHG_LAUNCH_CHECK();
 }

@@ -90,8 +90,13 @@ struct Lagrange3 {
   }
 };
 
+// Grid parameters of the current embedding. With cap_L > 0 the grid must fit
+// a cap_L transform: when it does not, out->need_L records the length needed,
+// *overflow is raised and the box count is cut so every later kernel stays
+// inside the capacity (that epoch's result is discarded by the caller).
 template <class T, int D>
-__global__ void fit_params_kernel(const BoxParams<T>* __restrict__ box, int64_t n_points, FitParams<T>* __restrict__ out) {
+__global__ void fit_params_kernel(const BoxParams<T>* __restrict__ box, int64_t n_points, FitParams<T>* __restrict__ out,
+                                  int cap_L, int* __restrict__ overflow) {
   if (threadIdx.x != 0) return;
   T lo = box->mn[0], hi = box->mx[0];
 #pragma unroll
@@ -104,9 +109,16 @@ __global__ void fit_params_kernel(const BoxParams<T>* __restrict__ box, int64_t 
   int64_t boxes = 0;
   if (scaled > T(0)) boxes = scaled >= T(9.0e18) ? INT64_MAX : (int64_t)scaled;
   boxes = boxes < 10 ? 10 : (boxes > 1000 ? 1000 : boxes);
-  const int nodes = (int)boxes * 3;
+  int nodes = (int)boxes * 3;
   int L = 16;
   while (L < 2 * nodes - 1) L <<= 1;
+  out->need_L = L;
+  if (cap_L > 0 && L > cap_L) {
+    *overflow = 1;
+    boxes = cap_L / 6 > 1 ? cap_L / 6 : 1;
+    nodes = (int)boxes * 3;
+    L = cap_L;
+  }
   const T box_width = extent / (T)(double)boxes;
   T m = fmax(fmax(fabs(lo), fabs(hi)), T(1));
   int ex = 0;
@@ -231,12 +243,21 @@ __global__ void spread_kernel(const T* __restrict__ y, int64_t n, const FitParam
   }
 }
 
+// Zeroes the accumulator cells the spread can reach (device-side size).
+template <class T, int D>
+__global__ void zero_acc_kernel(long long* __restrict__ acc, const FitParams<T>* __restrict__ prm) {
+  const int64_t count = 4 * (D == 1 ? (int64_t)prm->L : (int64_t)prm->nodes * prm->L);
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < count; e += (int64_t)gridDim.x * blockDim.x)
+    acc[e] = 0;
+}
+
 // Fixed-point charges -> the two packed complex grids (rows < charge_rows,
 // all L columns; zero where nothing was spread).
-template <class T>
-__global__ void unfix_kernel(const long long* __restrict__ acc, int64_t count, const FitParams<T>* __restrict__ prm,
+template <class T, int D>
+__global__ void unfix_kernel(const long long* __restrict__ acc, const FitParams<T>* __restrict__ prm,
                              typename Cx<T>::type* __restrict__ g0, typename Cx<T>::type* __restrict__ g1) {
   const double down = ldexp(1.0, -prm->fix_shift);
+  const int64_t count = D == 1 ? (int64_t)prm->L : (int64_t)prm->nodes * prm->L;
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < count; e += (int64_t)gridDim.x * blockDim.x) {
     const long long* c = acc + 4 * e;
     typename Cx<T>::type a, b;
@@ -275,9 +296,10 @@ __global__ void kernel_grid_kernel(const FitParams<T>* __restrict__ prm, typenam
 }
 
 template <class T>
-__global__ void take_real_scaled_kernel(const typename Cx<T>::type* __restrict__ g, int64_t total,
-                                        const FitParams<T>* __restrict__ prm, int D, T* __restrict__ khat) {
+__global__ void take_real_scaled_kernel(const typename Cx<T>::type* __restrict__ g, const FitParams<T>* __restrict__ prm,
+                                        int D, T* __restrict__ khat) {
   const int L = prm->L;
+  const int64_t total = D == 1 ? (int64_t)L : (int64_t)L * L;
   const T inv_total = T(1) / (T)(D == 1 ? (double)L : (double)L * (double)L);
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x)
     khat[e] = g[e].x * inv_total;
@@ -285,7 +307,8 @@ __global__ void take_real_scaled_kernel(const typename Cx<T>::type* __restrict__
 
 template <class T>
 __global__ void multiply_kernel(typename Cx<T>::type* __restrict__ a, typename Cx<T>::type* __restrict__ b,
-                                const T* __restrict__ khat, int64_t total) {
+                                const T* __restrict__ khat, const FitParams<T>* __restrict__ prm, int D) {
+  const int64_t total = D == 1 ? (int64_t)prm->L : (int64_t)prm->L * prm->L;
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
     const T k = khat[e];
     typename Cx<T>::type u = a[e], v = b[e];
@@ -298,14 +321,22 @@ __global__ void multiply_kernel(typename Cx<T>::type* __restrict__ a, typename C
   }
 }
 
-// Radix-2 FFT of `rows` rows of length L held in shared memory.
+// Radix-2 FFT of rows of length L (from the parameters) held in shared
+// memory, row b at data + b L; rows: 0 -> L rows, 1 -> `nodes` rows, 2 -> one
+// row. tw holds the twiddles of a cap_L transform (L divides cap_L).
 template <class T>
-__global__ void fft_rows_kernel(typename Cx<T>::type* __restrict__ data, int L, int log2L, int64_t stride,
-                                const typename Cx<T>::type* __restrict__ tw, int inverse) {
+__global__ void fft_rows_kernel(typename Cx<T>::type* __restrict__ data, const FitParams<T>* __restrict__ prm,
+                                int rows_sel, const typename Cx<T>::type* __restrict__ tw, int cap_L, int inverse) {
   typedef typename Cx<T>::type T2;
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int L = prm->L;
+  const int rows = rows_sel == 0 ? L : (rows_sel == 1 ? prm->nodes : 1);
+  if ((int)blockIdx.x >= rows) return;
+  int log2L = 0;
+  while ((1 << log2L) < L) ++log2L;
+  const int tws = cap_L / L;
   T2* s = reinterpret_cast<T2*>(smem_raw);
-  T2* d = data + (int64_t)blockIdx.x * stride;
+  T2* d = data + (int64_t)blockIdx.x * L;
   for (int i = threadIdx.x; i < L; i += blockDim.x) s[__brev((unsigned)i) >> (32 - log2L)] = d[i];
   __syncthreads();
   for (int lg = 1; lg <= log2L; ++lg) {
@@ -315,7 +346,7 @@ __global__ void fft_rows_kernel(typename Cx<T>::type* __restrict__ data, int L, 
       const int pos = b & (half - 1);
       const int i = ((b >> (lg - 1)) << lg) + pos;
       const int j = i + half;
-      T2 w = tw[pos * tstep];
+      T2 w = tw[pos * tstep * tws];
       if (inverse) w.y = -w.y;
       const T2 u = s[i];
       const T2 v = cmul(s[j], w);
@@ -333,13 +364,20 @@ __global__ void fft_rows_kernel(typename Cx<T>::type* __restrict__ data, int L, 
 }
 
 // out[c][r] = in[r][c] for r < rows_in (zero for rows_in <= r < out_cols),
-// c < cols; out row length ld_out.
+// c < cols; rows of length L in and out. Sizes from the parameters: sel 0 ->
+// L, 1 -> nodes. Blocks past the current sizes exit.
 template <class T>
-__global__ void transpose_kernel(const typename Cx<T>::type* __restrict__ in, int rows_in, int cols, int64_t ld_in,
-                                 typename Cx<T>::type* __restrict__ out, int out_cols, int64_t ld_out) {
+__global__ void transpose_kernel(const typename Cx<T>::type* __restrict__ in, const FitParams<T>* __restrict__ prm,
+                                 int rows_sel, int cols_sel, typename Cx<T>::type* __restrict__ out) {
   typedef typename Cx<T>::type T2;
   __shared__ T2 tile[32][33];
+  const int L = prm->L;
+  const int rows_in = rows_sel == 0 ? L : prm->nodes;
+  const int cols = cols_sel == 0 ? L : prm->nodes;
+  const int out_cols = L;
+  const int64_t ld_in = L, ld_out = L;
   const int c0 = blockIdx.x * 32, r0 = blockIdx.y * 32;
+  if (c0 >= cols || r0 >= out_cols) return;
   for (int k = threadIdx.y; k < 32; k += blockDim.y) {
     const int r = r0 + k, c = c0 + threadIdx.x;
     T2 v;
@@ -429,11 +467,6 @@ __global__ void gather_kernel(const T* __restrict__ y, int64_t n, const FitParam
   }
 }
 
-int ilog2(int L) {
-  int r = 0;
-  while ((1 << r) < L) ++r;
-  return r;
-}
 
 }  // namespace
 
@@ -457,49 +490,74 @@ const typename FitWorkspace<T>::T2* FitWorkspace<T>::twiddles(int L, cudaStream_
 }
 
 template <class T>
-static void fft_rows(FitWorkspace<T>& ws, typename Cx<T>::type* data, int L, int rows, int64_t stride, bool inverse,
-                     cudaStream_t s) {
-  if (rows <= 0) return;
-  const int threads = std::min(512, std::max(32, L / 2));
-  const size_t smem = (size_t)L * sizeof(typename Cx<T>::type);
-  static bool attr_set[2] = {false, false};
-  if (smem > 48 * 1024 && !attr_set[sizeof(T) == 8]) {
-    BHG_CUDA(cudaFuncSetAttribute(fft_rows_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-    attr_set[sizeof(T) == 8] = true;
-  }
-  fft_rows_kernel<T><<<rows, threads, smem, s>>>(data, L, ilog2(L), stride, ws.twiddles(L, s), inverse ? 1 : 0);
+static void fft_rows(FitWorkspace<T>& ws, typename Cx<T>::type* data, const FitParams<T>* dp, int rows_sel, int cap_L,
+                     bool inverse, cudaStream_t s) {
+  const int threads = std::min(512, std::max(32, cap_L / 2));
+  const size_t smem = (size_t)cap_L * sizeof(typename Cx<T>::type);
+  const int grid = rows_sel == 2 ? 1 : cap_L;
+  fft_rows_kernel<T><<<grid, threads, smem, s>>>(data, dp, rows_sel, ws.twiddles(cap_L, s), cap_L, inverse ? 1 : 0);
   BHG_LAUNCH_CHECK();
 }
 
 template <class T>
-static void transpose(const typename Cx<T>::type* in, int rows_in, int cols, int64_t ld_in, typename Cx<T>::type* out,
-                      int out_cols, int64_t ld_out, cudaStream_t s) {
+static void transpose(const typename Cx<T>::type* in, const FitParams<T>* dp, int rows_sel, int cols_sel,
+                      typename Cx<T>::type* out, int cap_L, cudaStream_t s) {
   dim3 b(32, 8);
-  dim3 g((unsigned)ceil_div(cols, 32), (unsigned)ceil_div(out_cols, 32));
-  transpose_kernel<T><<<g, b, 0, s>>>(in, rows_in, cols, ld_in, out, out_cols, ld_out);
+  dim3 g((unsigned)ceil_div(cap_L, 32), (unsigned)ceil_div(cap_L, 32));
+  transpose_kernel<T><<<g, b, 0, s>>>(in, dp, rows_sel, cols_sel, out);
   BHG_LAUNCH_CHECK();
 }
 
 template <class T>
-FitGrid fit_repulsion(FitWorkspace<T>& ws, int D, const T* y, int64_t n, const BoxParams<T>* box, T* neg, double* z_out,
-                      cudaStream_t s) {
-  typedef typename Cx<T>::type T2;
+void FitWorkspace<T>::reserve(int D, int64_t n, int cap) {
+  typedef typename Cx<T>::type C2;
+  const int64_t total = D == 1 ? (int64_t)cap : (int64_t)cap * cap;
+  params.ensure(sizeof(FitParams<T>));
+  g0.ensure(total * sizeof(C2));
+  g1.ensure(total * sizeof(C2));
+  h0.ensure(total * sizeof(C2));
+  h1.ensure(total * sizeof(C2));
+  khat.ensure(total * sizeof(T));
+  // the spread reaches rows < nodes <= cap / 2 of an L <= cap grid
+  const int64_t cells = D == 1 ? (int64_t)cap : (int64_t)(cap / 2 + 1) * cap;
+  acc.ensure((size_t)cells * 4 * sizeof(long long));
+  zpart.ensure((ceil_div(std::max<int64_t>(n, 1), 256) + 1) * sizeof(double));
+  flag.ensure(64);
+  done.ensure(64);
+  if ((size_t)cap * sizeof(C2) > 48 * 1024)  // set outside any stream capture
+    BHG_CUDA(cudaFuncSetAttribute(fft_rows_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+  cap_L = cap;
+}
+
+template <class T>
+int fit_needed_length(FitWorkspace<T>& ws, int D, int64_t n, const BoxParams<T>* box, cudaStream_t s) {
   ws.params.ensure(sizeof(FitParams<T>));
   FitParams<T>* dp = ws.params.template as<FitParams<T>>();
-  if (D == 1) fit_params_kernel<T, 1><<<1, 32, 0, s>>>(box, n, dp);
-  else fit_params_kernel<T, 2><<<1, 32, 0, s>>>(box, n, dp);
+  if (D == 1) fit_params_kernel<T, 1><<<1, 32, 0, s>>>(box, n, dp, 0, nullptr);
+  else fit_params_kernel<T, 2><<<1, 32, 0, s>>>(box, n, dp, 0, nullptr);
   BHG_LAUNCH_CHECK();
   FitParams<T> hp;
   BHG_CUDA(cudaMemcpyAsync(&hp, dp, sizeof(hp), cudaMemcpyDeviceToHost, s));
   BHG_CUDA(cudaStreamSynchronize(s));
-  const int L = hp.L, nodes = hp.nodes;
-  const int64_t total = D == 1 ? (int64_t)L : (int64_t)L * L;
-  T2* g0 = static_cast<T2*>(ws.g0.ensure(total * sizeof(T2)));
-  T2* g1 = static_cast<T2*>(ws.g1.ensure(total * sizeof(T2)));
-  T2* h0 = static_cast<T2*>(ws.h0.ensure(total * sizeof(T2)));
-  T2* h1 = static_cast<T2*>(ws.h1.ensure(total * sizeof(T2)));
-  T* khat = static_cast<T*>(ws.khat.ensure(total * sizeof(T)));
-  const int eb = (int)std::min<int64_t>(ceil_div(total, 256), 4 * 152);
+  return hp.L;
+}
+
+template <class T>
+void fit_repulsion_cap(FitWorkspace<T>& ws, int D, const T* y, int64_t n, const BoxParams<T>* box, T* neg,
+                       double* z_out, cudaStream_t s) {
+  typedef typename Cx<T>::type T2;
+  const int cap = ws.cap_L;
+  FitParams<T>* dp = ws.params.template as<FitParams<T>>();
+  if (D == 1) fit_params_kernel<T, 1><<<1, 32, 0, s>>>(box, n, dp, cap, ws.flag.template as<int>());
+  else fit_params_kernel<T, 2><<<1, 32, 0, s>>>(box, n, dp, cap, ws.flag.template as<int>());
+  BHG_LAUNCH_CHECK();
+  T2* g0 = ws.g0.template as<T2>();
+  T2* g1 = ws.g1.template as<T2>();
+  T2* h0 = ws.h0.template as<T2>();
+  T2* h1 = ws.h1.template as<T2>();
+  T* khat = ws.khat.template as<T>();
+  const int64_t cap_total = D == 1 ? (int64_t)cap : (int64_t)cap * cap;
+  const int eb = (int)std::min<int64_t>(ceil_div(cap_total, 256), 4 * 152);
 
   // kernel spectrum (real, pre-scaled by 1/L^D); symmetric in its axes, so it
   // serves the transposed spectrum layout unchanged.
@@ -507,64 +565,64 @@ FitGrid fit_repulsion(FitWorkspace<T>& ws, int D, const T* y, int64_t n, const B
   else kernel_grid_kernel<T, 2><<<eb, 256, 0, s>>>(dp, g0);
   BHG_LAUNCH_CHECK();
   if (D == 1) {
-    fft_rows<T>(ws, g0, L, 1, L, false, s);
-    take_real_scaled_kernel<T><<<eb, 256, 0, s>>>(g0, total, dp, D, khat);
+    fft_rows<T>(ws, g0, dp, 2, cap, false, s);
+    take_real_scaled_kernel<T><<<eb, 256, 0, s>>>(g0, dp, D, khat);
   } else {
-    fft_rows<T>(ws, g0, L, L, L, false, s);
-    transpose<T>(g0, L, L, L, h0, L, L, s);
-    fft_rows<T>(ws, h0, L, L, L, false, s);
-    take_real_scaled_kernel<T><<<eb, 256, 0, s>>>(h0, total, dp, D, khat);
+    fft_rows<T>(ws, g0, dp, 0, cap, false, s);
+    transpose<T>(g0, dp, 0, 0, h0, cap, s);
+    fft_rows<T>(ws, h0, dp, 0, cap, false, s);
+    take_real_scaled_kernel<T><<<eb, 256, 0, s>>>(h0, dp, D, khat);
   }
   BHG_LAUNCH_CHECK();
 
   // charges: zero the rows that receive them, spread
-  const int64_t charge_rows = D == 1 ? 1 : nodes;
-  const int64_t charge_cells = charge_rows * L;
-  long long* acc = static_cast<long long*>(ws.acc.ensure((size_t)charge_cells * 4 * sizeof(long long)));
-  BHG_CUDA(cudaMemsetAsync(acc, 0, (size_t)charge_cells * 4 * sizeof(long long), s));
+  long long* acc = ws.acc.template as<long long>();
+  const int64_t cap_cells = D == 1 ? (int64_t)cap : (int64_t)(cap / 2 + 1) * cap;
+  const unsigned cb = (unsigned)std::min<int64_t>(ceil_div(cap_cells, 256), 4 * 152);
+  if (D == 1) zero_acc_kernel<T, 1><<<cb, 256, 0, s>>>(acc, dp);
+  else zero_acc_kernel<T, 2><<<cb, 256, 0, s>>>(acc, dp);
+  BHG_LAUNCH_CHECK();
   if (n > 0) {
     if (D == 1) spread_kernel<T, 1><<<(unsigned)ceil_div(n, 256), 256, 0, s>>>(y, n, dp, acc);
     else spread_kernel<T, 2><<<(unsigned)ceil_div(n, 256), 256, 0, s>>>(y, n, dp, acc);
     BHG_LAUNCH_CHECK();
   }
-  unfix_kernel<T><<<(unsigned)std::min<int64_t>(ceil_div(charge_cells, 256), 4 * 152), 256, 0, s>>>(acc, charge_cells, dp,
-                                                                                                  g0, g1);
+  if (D == 1) unfix_kernel<T, 1><<<cb, 256, 0, s>>>(acc, dp, g0, g1);
+  else unfix_kernel<T, 2><<<cb, 256, 0, s>>>(acc, dp, g0, g1);
   BHG_LAUNCH_CHECK();
 
   T2 *r0, *r1;
   if (D == 1) {
-    fft_rows<T>(ws, g0, L, 1, L, false, s);
-    fft_rows<T>(ws, g1, L, 1, L, false, s);
-    multiply_kernel<T><<<eb, 256, 0, s>>>(g0, g1, khat, total);
+    fft_rows<T>(ws, g0, dp, 2, cap, false, s);
+    fft_rows<T>(ws, g1, dp, 2, cap, false, s);
+    multiply_kernel<T><<<eb, 256, 0, s>>>(g0, g1, khat, dp, D);
     BHG_LAUNCH_CHECK();
-    fft_rows<T>(ws, g0, L, 1, L, true, s);
-    fft_rows<T>(ws, g1, L, 1, L, true, s);
+    fft_rows<T>(ws, g0, dp, 2, cap, true, s);
+    fft_rows<T>(ws, g1, dp, 2, cap, true, s);
     r0 = g0;
     r1 = g1;
   } else {
     // forward: rows n0 < nodes, transpose to [k1][n0], rows over n0
-    fft_rows<T>(ws, g0, L, nodes, L, false, s);
-    fft_rows<T>(ws, g1, L, nodes, L, false, s);
-    transpose<T>(g0, nodes, L, L, h0, L, L, s);
-    transpose<T>(g1, nodes, L, L, h1, L, L, s);
-    fft_rows<T>(ws, h0, L, L, L, false, s);
-    fft_rows<T>(ws, h1, L, L, L, false, s);
-    multiply_kernel<T><<<eb, 256, 0, s>>>(h0, h1, khat, total);
+    fft_rows<T>(ws, g0, dp, 1, cap, false, s);
+    fft_rows<T>(ws, g1, dp, 1, cap, false, s);
+    transpose<T>(g0, dp, 1, 0, h0, cap, s);
+    transpose<T>(g1, dp, 1, 0, h1, cap, s);
+    fft_rows<T>(ws, h0, dp, 0, cap, false, s);
+    fft_rows<T>(ws, h1, dp, 0, cap, false, s);
+    multiply_kernel<T><<<eb, 256, 0, s>>>(h0, h1, khat, dp, D);
     BHG_LAUNCH_CHECK();
     // inverse: rows over k0, transpose back (rows n0 < nodes only), rows over k1
-    fft_rows<T>(ws, h0, L, L, L, true, s);
-    fft_rows<T>(ws, h1, L, L, L, true, s);
-    transpose<T>(h0, L, nodes, L, g0, L, L, s);
-    transpose<T>(h1, L, nodes, L, g1, L, L, s);
-    fft_rows<T>(ws, g0, L, nodes, L, true, s);
-    fft_rows<T>(ws, g1, L, nodes, L, true, s);
+    fft_rows<T>(ws, h0, dp, 0, cap, true, s);
+    fft_rows<T>(ws, h1, dp, 0, cap, true, s);
+    transpose<T>(h0, dp, 0, 1, g0, cap, s);
+    transpose<T>(h1, dp, 0, 1, g1, cap, s);
+    fft_rows<T>(ws, g0, dp, 1, cap, true, s);
+    fft_rows<T>(ws, g1, dp, 1, cap, true, s);
     r0 = g0;
     r1 = g1;
   }
 
-  ws.zpart.ensure((ceil_div(std::max<int64_t>(n, 1), 256) + 1) * sizeof(double));
   if (!ws.done_zeroed) {
-    ws.done.ensure(64);
     BHG_CUDA(cudaMemsetAsync(ws.done.ptr, 0, 64, s));
     ws.done_zeroed = true;
   }
@@ -580,6 +638,18 @@ FitGrid fit_repulsion(FitWorkspace<T>& ws, int D, const T* y, int64_t n, const B
   } else {
     BHG_CUDA(cudaMemsetAsync(z_out, 0, sizeof(double), s));
   }
+}
+
+template <class T>
+FitGrid fit_repulsion(FitWorkspace<T>& ws, int D, const T* y, int64_t n, const BoxParams<T>* box, T* neg, double* z_out,
+                      cudaStream_t s) {
+  const int L = fit_needed_length<T>(ws, D, n, box, s);
+  if (ws.cap_L < L) ws.reserve(D, n, L);
+  else ws.reserve(D, n, ws.cap_L);
+  fit_repulsion_cap<T>(ws, D, y, n, box, neg, z_out, s);
+  FitParams<T> hp;
+  BHG_CUDA(cudaMemcpyAsync(&hp, ws.params.ptr, sizeof(hp), cudaMemcpyDeviceToHost, s));
+  BHG_CUDA(cudaStreamSynchronize(s));
   FitGrid fg;
   fg.boxes = hp.boxes;
   fg.nodes = hp.nodes;
@@ -596,5 +666,11 @@ template FitGrid fit_repulsion<float>(FitWorkspace<float>&, int, const float*, i
                                       double*, cudaStream_t);
 template FitGrid fit_repulsion<double>(FitWorkspace<double>&, int, const double*, int64_t, const BoxParams<double>*,
                                        double*, double*, cudaStream_t);
+template void fit_repulsion_cap<float>(FitWorkspace<float>&, int, const float*, int64_t, const BoxParams<float>*,
+                                       float*, double*, cudaStream_t);
+template void fit_repulsion_cap<double>(FitWorkspace<double>&, int, const double*, int64_t, const BoxParams<double>*,
+                                        double*, double*, cudaStream_t);
+template int fit_needed_length<float>(FitWorkspace<float>&, int, int64_t, const BoxParams<float>*, cudaStream_t);
+template int fit_needed_length<double>(FitWorkspace<double>&, int, int64_t, const BoxParams<double>*, cudaStream_t);
 
 }  // namespace bhg

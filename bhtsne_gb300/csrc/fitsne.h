@@ -10,6 +10,7 @@ struct FitParams {
   T lo, extent, box_width, inv_box_width, spacing;
   T scale;  // power of two >= max |y|: balances the magnitudes of packed terms
   int boxes, nodes, L;
+  int need_L;     // transform length the embedding needs (L unless the capacity was too small)
   int fix_shift;  // charges are accumulated as integers in units of 2^-fix_shift
 };
 
@@ -21,10 +22,13 @@ struct FitGrid {
 template <class T>
 struct FitWorkspace {
   typedef typename std::conditional<sizeof(T) == 4, float2, double2>::type T2;
-  DevBuf params, g0, g1, h0, h1, khat, tw, zpart, done, acc;
+  DevBuf params, g0, g1, h0, h1, khat, tw, zpart, done, acc, flag;
   int tw_len = 0;
+  int cap_L = 0;  // transform length the buffers hold
   bool done_zeroed = false;
   const T2* twiddles(int L, cudaStream_t s);
+  // Buffers for transforms up to cap (a power of two) at n points.
+  void reserve(int D, int64_t n, int cap);
 };
 
 // Repulsive forces (neg) and Z (z_out, device) at y; `box` must hold the
@@ -32,5 +36,18 @@ struct FitWorkspace {
 template <class T>
 FitGrid fit_repulsion(FitWorkspace<T>& ws, int D, const T* y, int64_t n, const BoxParams<T>* box, T* neg, double* z_out,
                       cudaStream_t s);
+
+// The same without a host synchronisation (graph-capturable): every size is
+// read on the device from the current parameters, within the reserved
+// capacity ws.cap_L. If the embedding needs a longer transform, the flag
+// ws.flag (int) is raised and the result is not valid; the caller grows the
+// capacity (fit_needed_length) and repeats the step.
+template <class T>
+void fit_repulsion_cap(FitWorkspace<T>& ws, int D, const T* y, int64_t n, const BoxParams<T>* box, T* neg,
+                       double* z_out, cudaStream_t s);
+
+// Transform length the current embedding needs (synchronises).
+template <class T>
+int fit_needed_length(FitWorkspace<T>& ws, int D, int64_t n, const BoxParams<T>* box, cudaStream_t s);
 
 }  // namespace bhg

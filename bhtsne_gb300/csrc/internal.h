@@ -12,24 +12,55 @@
 namespace bhg {
 
 // ---- device buffers ---------------------------------------------------------
-// A grow-only device allocation owned by a context or a fit workspace.
+// Stream that orders the DevBuf allocations and frees of the calling thread.
+// The API entry points and the server's threads set it to the stream their
+// work runs on; allocations then come from the device's stream-ordered pool
+// (cudaMallocAsync / cudaFreeAsync), so freeing a buffer never waits for the
+// rest of the device, as a plain cudaFree does. Without a scope, plain
+// cudaMalloc / cudaFree.
+extern thread_local cudaStream_t g_alloc_stream;
+
+struct AllocStreamScope {
+  cudaStream_t prev;
+  explicit AllocStreamScope(cudaStream_t s) : prev(g_alloc_stream) { g_alloc_stream = s; }
+  ~AllocStreamScope() { g_alloc_stream = prev; }
+  AllocStreamScope(const AllocStreamScope&) = delete;
+  AllocStreamScope& operator=(const AllocStreamScope&) = delete;
+};
+
+// A grow-only device allocation owned by a context or a fit workspace. A
+// buffer allocated on a stream is freed on that stream (after its work), so
+// it must be used on that stream, or on another one only after synchronising.
 struct DevBuf {
   void* ptr = nullptr;
   size_t bytes = 0;
+  cudaStream_t stream = nullptr;
+  bool async = false;
   DevBuf() = default;
   DevBuf(const DevBuf&) = delete;
   DevBuf& operator=(const DevBuf&) = delete;
   ~DevBuf() { release(); }
   void release() {
-    if (ptr) cudaFree(ptr);
+    if (ptr) {
+      if (async) cudaFreeAsync(ptr, stream);
+      else cudaFree(ptr);
+    }
     ptr = nullptr;
     bytes = 0;
+    async = false;
+    stream = nullptr;
   }
   void* ensure(size_t want) {
     if (want <= bytes && ptr) return ptr;
     release();
     size_t b = want < 256 ? 256 : want;
-    BHG_CUDA(cudaMalloc(&ptr, b));
+    if (g_alloc_stream) {
+      BHG_CUDA(cudaMallocAsync(&ptr, b, g_alloc_stream));
+      stream = g_alloc_stream;
+      async = true;
+    } else {
+      BHG_CUDA(cudaMalloc(&ptr, b));
+    }
     bytes = b;
     return ptr;
   }
@@ -38,12 +69,22 @@ struct DevBuf {
   void swap(DevBuf& o) {
     void* p = ptr;
     size_t b = bytes;
+    cudaStream_t st = stream;
+    bool as_ = async;
     ptr = o.ptr;
     bytes = o.bytes;
+    stream = o.stream;
+    async = o.async;
     o.ptr = p;
     o.bytes = b;
+    o.stream = st;
+    o.async = as_;
   }
 };
+
+// Keeps the freed memory of the device's default pool cached (no release
+// back to the driver at synchronisations), once per device.
+void keep_pool_cached(int device);
 
 // ---- scan ---------------------------------------------------------------------
 // Exclusive prefix sum of n values (u32 in, u64 out); out has n+1 entries, out[n]

@@ -157,10 +157,21 @@ struct bhtsne_server {
 
 namespace {
 
+// Streams of the engine; declared first so that they outlive every buffer
+// that is freed on them.
+struct EngineStreams {
+  cudaStream_t s = nullptr, ps = nullptr;
+  ~EngineStreams() {
+    if (s) cudaStreamSynchronize(s), cudaStreamDestroy(s);
+    if (ps) cudaStreamSynchronize(ps), cudaStreamDestroy(ps);
+  }
+};
+
 template <class T>
 struct BhEngine {
+  EngineStreams streams;
   bhtsne_server* sv;
-  cudaStream_t s = nullptr;
+  cudaStream_t& s = streams.s;
   std::vector<std::unique_ptr<Slot<T>>> slots;
   int64_t total = 0, nnz = 0;
   DevBuf d_off, job_of, rows, cols, vals, y, uy, gains, y2, uy2, g2, pos, neg, q, z, lr, mom, active, boxes;
@@ -169,7 +180,7 @@ struct BhEngine {
   SegTiles tiles;
   // affinity preparation runs on its own thread and stream, overlapping the
   // batch's epochs; prepared jobs wait in `ready` for the next repack
-  cudaStream_t ps = nullptr;
+  cudaStream_t& ps = streams.ps;
   AffinityScratch<T> paff;
   DevBuf psum, ptmp;
   std::vector<std::unique_ptr<Slot<T>>> ready;
@@ -190,8 +201,6 @@ struct BhEngine {
   ~BhEngine() {
     cudaSetDevice(sv->device);
     if (graph) cudaGraphExecDestroy(graph);
-    if (s) cudaStreamDestroy(s);
-    if (ps) cudaStreamDestroy(ps);
   }
 
   // Embedding (and KL) of a finished job, then it leaves the batch.
@@ -496,6 +505,7 @@ struct BhEngine {
   // Preparer thread: affinities of admitted requests, handed to the batch.
   void prepare_loop() {
     BHG_CUDA(cudaSetDevice(sv->device));
+    AllocStreamScope scope(ps);
     for (;;) {
       std::vector<Request*> fresh;
       {
@@ -523,6 +533,7 @@ struct BhEngine {
   // Batch thread: repack when jobs arrive or leave, then a round of epochs.
   void loop() {
     BHG_CUDA(cudaSetDevice(sv->device));
+    AllocStreamScope scope(s);
     for (;;) {
       std::vector<std::unique_ptr<Slot<T>>> fresh;
       bool have_work = false;
