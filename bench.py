@@ -10,7 +10,12 @@ fused update + recentre) over the full 1M-point embedding.
            with CUDA events on the library's stream (bhtsne_tsne_advance).
   e2e    : epochs/s through the C ABI as a user calls it: with_affinities
            (host CSR) + barnes_hut + embedding(), host<->device copies inside.
-  roofline / cpu_baseline / clocks: see the design doc.
+  roofline: the dominant epoch phase's algorithmic bytes per launch over its
+           live CUDA-event time, against the measured HBM copy peak.
+  cpu_baseline: the oracle (C++/OpenMP restatement) on a few 1M-point epochs.
+  clocks : nvidia-smi samples taken during the timed epochs.
+  batched / serving: the 512-job batch and the request stream against the
+           same work run one job at a time through the builder.
 
 --impl reference times the CPU restatement of the reference (oracle/, C++
 with OpenMP on every host core) on the same workload: a bounded number of
@@ -206,11 +211,15 @@ def run_ours(args):
         "tree": 4 * n * D + 12 * n * 2 * 8,
     }
     achieved = alg[dom] / (per[dom] / 1e3) / 1e9
+    # DRAM bytes (read + write) per launch from one ncu capture of the same
+    # kernel at N = 300,000 (429.7 MB for 52.5M CSR entries), scaled by this
+    # run's entries; null for the other phases
+    traffic = {"attractive": int(429.7e6 * nnz / 52.5e6)}
     interactions = None
     roofline = {"kernel": {"repulsion": "bh_traverse_kernel", "attractive": "attractive_kernel",
                            "update": "update_kernel+recenter_bbox_kernel", "tree": "morton+radix sort+tree build"}[dom],
                 "bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
-                "frac": round(achieved / peak, 5), "traffic": None, "peak_source": peak_kind,
+                "frac": round(achieved / peak, 5), "traffic": traffic.get(dom), "peak_source": peak_kind,
                 "algorithmic_bytes": alg[dom], "ms_per_launch": round(per[dom], 4)}
     att_gbs = alg["attractive"] / (per["attractive"] / 1e3) / 1e9
 
@@ -464,6 +473,19 @@ def run_reference(args):
     print(json.dumps(out))
 
 
+def run_knn_only(args):
+    """The affinity build's kNN alone on the 1M workload's distribution at --n
+    points (k = 90): a 2,000-row warm-up call, then all rows, timed on the host."""
+    import bhtsne_gb300 as bg
+    X, _ = make_workload(args.n, seed=args.seed)
+    bg.knn_euclidean(X[:2000], 90)
+    w0 = time.perf_counter()
+    bg.knn_euclidean(X, 90)
+    el = time.perf_counter() - w0
+    print(json.dumps({"metric": "exact kNN seconds (k = 90)", "value": round(el, 4), "unit": "s",
+                      "higher_is_better": False, "config": {"n_points": args.n, "input_dim": 128, "k": 90}}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -481,7 +503,11 @@ def main():
     ap.add_argument("--serve-epochs", type=int, default=750)
     ap.add_argument("--serve-rate", type=float, default=64.0, help="Poisson arrivals per second")
     ap.add_argument("--serve-fit-workers", type=int, default=8, help="server streams for FIt-SNE requests")
+    ap.add_argument("--knn-only", action="store_true", help="time only the kNN of the workload at --n points")
     args = ap.parse_args()
+    if args.knn_only:
+        run_knn_only(args)
+        return
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":

@@ -5,8 +5,8 @@
  * 0.7.10. The reference has no FFI of its own; its public surface is the
  * `tSNE<'data, T, U, const D>` builder in src/lib.rs. Every entry point below
  * names the reference item it stands in for (path:line in the reference
- * crate), so that a thin Rust wrapper can re-export the
- * builder with the same method names, defaults and panic messages.
+ * crate), so that a thin Rust wrapper can re-export the builder with the
+ * same method names, defaults and panic messages.
  *
  * Conventions
  *  - Every call returns an int status: BHTSNE_OK (0) or an error code. The
