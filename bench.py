@@ -216,7 +216,7 @@ def run_ours(args):
     # run's entries; null for the other phases
     traffic = {"attractive": int(429.7e6 * nnz / 52.5e6)}
     interactions = None
-    roofline = {"kernel": {"repulsion": "bh_traverse_kernel", "attractive": "attractive_kernel",
+    roofline = {"kernel": {"repulsion": "bh_traverse_kernel", "attractive": "attractive_task_kernel+attractive_fixup_kernel",
                            "update": "update_kernel+recenter_bbox_kernel", "tree": "morton+radix sort+tree build"}[dom],
                 "bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 5), "traffic": traffic.get(dom), "peak_source": peak_kind,

@@ -93,6 +93,8 @@ struct State {
   DevBuf y, uy, gains, pos, neg, zbuf, klbuf, tmp, tmp2;
   DevBuf kidx, kdist, kp, xin, yext, ckpt;
   Renumbering rn;  // locality layout of y/uy/gains (see launch_renumber)
+  AttrTasks at;    // attractive-pass tasks of the current CSR layout
+  uint64_t layout_gen = 0;
   // y in the caller's point order (a copy when the layout is renumbered).
   const T* y_external(cudaStream_t s) {
     if (!rn.active) return y.template as<T>();
@@ -408,13 +410,20 @@ void advance_impl(bhtsne_tsne* t, int64_t epochs) {
   const char* rev = getenv("BHTSNE_RENUMBER_EVERY");
   const int64_t renumber_every = rev ? atoll(rev) : 50;
   const bool sparse = t->loop_kind != BHTSNE_METHOD_EXACT;
+  // Tasks of the current CSR layout, rebuilt (outside any capture) when the
+  // layout changes: at a fit's start and at each renumbering.
+  auto ensure_tasks = [&]() {
+    if (!sparse || S.at.gen == S.layout_gen) return;
+    build_attr_tasks<T>(S.at, D, (S.rn.active ? S.rn.rows : S.rows).template as<uint64_t>(), n, s);
+    S.at.gen = S.layout_gen;
+  };
   auto attractive = [&]() {
     if (S.rn.active)
-      launch_attractive<T>(D, S.rn.rows.template as<uint64_t>(), S.rn.cols.template as<uint32_t>(),
-                           S.rn.vals.template as<T>(), y, n, S.pos.template as<T>(), s);
+      launch_attractive_tasks<T>(S.at, S.rn.cols.template as<uint32_t>(), S.rn.vals.template as<T>(), y,
+                                 S.pos.template as<T>(), s);
     else
-      launch_attractive<T>(D, S.rows.template as<uint64_t>(), S.cols.template as<uint32_t>(), S.vals.template as<T>(), y,
-                           n, S.pos.template as<T>(), s);
+      launch_attractive_tasks<T>(S.at, S.cols.template as<uint32_t>(), S.vals.template as<T>(), y,
+                                 S.pos.template as<T>(), s);
   };
   auto maybe_renumber = [&](int64_t epoch) {
     if (!sparse || renumber_every <= 0 || epoch == 0 || epoch % renumber_every != 0) return;
@@ -431,8 +440,11 @@ void advance_impl(bhtsne_tsne* t, int64_t epochs) {
                        S.rows.template as<uint64_t>(), S.cols.template as<uint32_t>(), S.vals.template as<T>(), S.nnz, s);
     if (t->loop_kind != BHTSNE_METHOD_BARNES_HUT)
       launch_recenter_bbox<T>(D, y, n, nullptr, false, S.bh, bits, s);
+    ++S.layout_gen;
+    ensure_tasks();
     if (!was_active) t->drop_graph();  // the attractive pass now reads the slot arrays
   };
+  ensure_tasks();
   auto fit_body = [&](T mom) {
     fit_repulsion_cap<T>(S.fit, D, y, n, S.bh.params.template as<BoxParams<T>>(), S.neg.template as<T>(), z, s);
     attractive();
@@ -631,6 +643,7 @@ template <class T>
 void run_loop(bhtsne_tsne* t, int kind, double theta) {
   t->drop_graph();
   st<T>(t).rn.active = false;  // the fit starts from y in the caller's order
+  ++st<T>(t).layout_gen;
   t->armed = true;
   t->loop_kind = kind;
   t->loop_theta = theta;

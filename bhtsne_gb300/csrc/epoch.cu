@@ -103,6 +103,115 @@ __global__ void __launch_bounds__(256) attractive_kernel(const uint64_t* __restr
 }
 
 // ---------------------------------------------------------------------------
+// Attractive forces over bounded tasks (see AttrTasks). A task is at most
+// kAttrTaskLen = 4 x 32 entries: each lane issues its four column/value loads
+// (streaming, so that L1 keeps the gathered y lines) and four gathers at once.
+// ---------------------------------------------------------------------------
+struct AttrTask {
+  uint64_t begin;  // first CSR entry
+  uint32_t slot;
+  uint32_t len;    // entries; bit 31: the row has several tasks (write a partial)
+};
+
+constexpr uint32_t kPartialBit = 0x80000000u;
+
+template <class T, int D, bool VEC>
+__global__ void __launch_bounds__(256) attractive_task_kernel(const AttrTask* __restrict__ tasks, int64_t ntasks,
+                                                              const uint32_t* __restrict__ cols,
+                                                              const T* __restrict__ vals, const T* __restrict__ y,
+                                                              T* __restrict__ pos, T* __restrict__ part) {
+  constexpr int kU = kAttrTaskLen / 32;
+  const int64_t t = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (t >= ntasks) return;  // uniform per warp
+  const AttrTask tk = tasks[t];
+  const int len = (int)(tk.len & ~kPartialBit);
+  const int64_t slot = tk.slot;
+  T yi[D], acc[D];
+#pragma unroll
+  for (int a = 0; a < D; ++a) {
+    yi[a] = y[slot * D + a];
+    acc[a] = T(0);
+  }
+  uint32_t j[kU];
+  T p[kU];
+  T yj[kU][D];
+#pragma unroll
+  for (int u = 0; u < kU; ++u) {
+    const int e = lane + 32 * u;
+    j[u] = e < len ? __ldcs(cols + tk.begin + e) : (uint32_t)slot;
+    p[u] = e < len ? __ldcs(vals + tk.begin + e) : T(0);
+  }
+#pragma unroll
+  for (int u = 0; u < kU; ++u) load_point<T, D, VEC>(y, (int64_t)j[u], yj[u]);
+#pragma unroll
+  for (int u = 0; u < kU; ++u) {
+    T disp[D];
+    T dist = T(0);
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+      disp[a] = yi[a] - yj[u][a];
+      dist += disp[a] * disp[a];
+    }
+    const T factor = p[u] / (dist + T(1));
+#pragma unroll
+    for (int a = 0; a < D; ++a) acc[a] += factor * disp[a];
+  }
+#pragma unroll
+  for (int a = 0; a < D; ++a) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc[a] += __shfl_xor_sync(kFull, acc[a], o);
+  }
+  if (lane == 0) {
+    T* out = (tk.len & kPartialBit) ? part + t * D : pos + slot * D;
+#pragma unroll
+    for (int a = 0; a < D; ++a) out[a] = acc[a];
+  }
+}
+
+// Rows of several tasks: the partial sums in task order.
+template <class T, int D>
+__global__ void attractive_fixup_kernel(const uint32_t* __restrict__ longs, int64_t nlong,
+                                        const uint64_t* __restrict__ off, const T* __restrict__ part,
+                                        T* __restrict__ pos) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nlong) return;
+  const int64_t slot = longs[i];
+  T acc[D];
+#pragma unroll
+  for (int a = 0; a < D; ++a) acc[a] = T(0);
+  for (uint64_t t = off[slot]; t < off[slot + 1]; ++t) {
+#pragma unroll
+    for (int a = 0; a < D; ++a) acc[a] += part[t * D + a];
+  }
+#pragma unroll
+  for (int a = 0; a < D; ++a) pos[slot * D + a] = acc[a];
+}
+
+__global__ void task_count_kernel(const uint64_t* __restrict__ rows, int64_t n, uint32_t* __restrict__ cnt) {
+  const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  const uint64_t len = rows[s + 1] - rows[s];
+  cnt[s] = len <= (uint64_t)kAttrTaskLen ? 1u : (uint32_t)((len + kAttrTaskLen - 1) / kAttrTaskLen);
+}
+
+__global__ void task_fill_kernel(const uint64_t* __restrict__ rows, int64_t n, const uint64_t* __restrict__ off,
+                                 AttrTask* __restrict__ tasks, uint32_t* __restrict__ longs,
+                                 unsigned long long* __restrict__ nlong) {
+  const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  const uint64_t r0 = rows[s], len = rows[s + 1] - r0;
+  const uint64_t t0 = off[s], c = off[s + 1] - t0;
+  const uint32_t flag = c > 1 ? kPartialBit : 0u;
+  for (uint64_t q = 0; q < c; ++q) {
+    const uint64_t b = q * kAttrTaskLen;
+    const uint64_t l = len - b < (uint64_t)kAttrTaskLen ? len - b : (uint64_t)kAttrTaskLen;
+    tasks[t0 + q] = AttrTask{r0 + b, (uint32_t)s, (uint32_t)l | flag};
+  }
+  if (c > 1) longs[atomicAdd(nlong, 1ull)] = (uint32_t)s;
+}
+
+// ---------------------------------------------------------------------------
 // Renumbering of the embedding layout (see launch_renumber).
 // ---------------------------------------------------------------------------
 template <class T, int D>
@@ -446,6 +555,62 @@ void launch_attractive(int D, const uint64_t* rows, const uint32_t* cols, const 
 }
 
 template <class T>
+void build_attr_tasks(AttrTasks& at, int D, const uint64_t* rows, int64_t n, cudaStream_t s) {
+  at.D = D;
+  at.n = n;
+  at.ntasks = at.nlong = 0;
+  if (n <= 0) return;
+  const unsigned g = (unsigned)ceil_div(n, 256);
+  uint32_t* cnt = static_cast<uint32_t*>(at.cnt.ensure((size_t)n * 4));
+  uint64_t* off = static_cast<uint64_t*>(at.off.ensure((size_t)(n + 1) * 8));
+  task_count_kernel<<<g, 256, 0, s>>>(rows, n, cnt);
+  BHG_LAUNCH_CHECK();
+  scan_u32_to_u64(cnt, off, n, at.scan_tmp, s);
+  uint64_t total = 0;
+  BHG_CUDA(cudaMemcpyAsync(&total, off + n, 8, cudaMemcpyDeviceToHost, s));
+  BHG_CUDA(cudaStreamSynchronize(s));
+  at.ntasks = (int64_t)total;
+  AttrTask* tasks = static_cast<AttrTask*>(at.tasks.ensure((size_t)at.ntasks * sizeof(AttrTask)));
+  uint32_t* longs = static_cast<uint32_t*>(at.longs.ensure((size_t)n * 4));
+  unsigned long long* nl = static_cast<unsigned long long*>(at.nlong_dev.ensure(8));
+  BHG_CUDA(cudaMemsetAsync(nl, 0, 8, s));
+  task_fill_kernel<<<g, 256, 0, s>>>(rows, n, off, tasks, longs, nl);
+  BHG_LAUNCH_CHECK();
+  unsigned long long nlong = 0;
+  BHG_CUDA(cudaMemcpyAsync(&nlong, nl, 8, cudaMemcpyDeviceToHost, s));
+  BHG_CUDA(cudaStreamSynchronize(s));
+  at.nlong = (int64_t)nlong;
+  at.part.ensure((size_t)at.ntasks * D * sizeof(T));
+}
+
+template <class T, int D>
+static void launch_attractive_tasks_d(const AttrTasks& at, const uint32_t* cols, const T* vals, const T* y, T* pos,
+                                      cudaStream_t s) {
+  const bool vec = D == 2 && (reinterpret_cast<uintptr_t>(y) % (2 * sizeof(T))) == 0;
+  const unsigned grid = (unsigned)ceil_div(at.ntasks, 8);
+  const AttrTask* tasks = static_cast<const AttrTask*>(at.tasks.ptr);
+  T* part = static_cast<T*>(at.part.ptr);
+  if (vec) attractive_task_kernel<T, D, true><<<grid, 256, 0, s>>>(tasks, at.ntasks, cols, vals, y, pos, part);
+  else attractive_task_kernel<T, D, false><<<grid, 256, 0, s>>>(tasks, at.ntasks, cols, vals, y, pos, part);
+  BHG_LAUNCH_CHECK();
+  if (at.nlong > 0) {
+    attractive_fixup_kernel<T, D><<<(unsigned)ceil_div(at.nlong, 256), 256, 0, s>>>(
+        static_cast<const uint32_t*>(at.longs.ptr), at.nlong, static_cast<const uint64_t*>(at.off.ptr), part, pos);
+    BHG_LAUNCH_CHECK();
+  }
+}
+
+template <class T>
+void launch_attractive_tasks(const AttrTasks& at, const uint32_t* cols, const T* vals, const T* y, T* pos,
+                             cudaStream_t s) {
+  if (at.ntasks <= 0) return;
+  with_dim<1, 7>(at.D, "error: the embedding dimension must be in 1..7.", [&](auto dc) {
+    constexpr int DD = decltype(dc)::value;
+    launch_attractive_tasks_d<T, DD>(at, cols, vals, y, pos, s);
+  });
+}
+
+template <class T>
 void launch_renumber(int D, const uint32_t* order, int64_t n, Renumbering& r, T* y, T* uy, T* gains, T* tmp_a, T* tmp_b,
                      T* tmp_c, const uint64_t* rows, const uint32_t* cols, const T* vals, int64_t nnz, cudaStream_t s) {
   const unsigned g = (unsigned)ceil_div(n, 256);
@@ -577,6 +742,8 @@ void launch_exact_kl(int D, const T* y, const T* p, int64_t n, const double* z, 
   template void launch_renumber<T>(int, const uint32_t*, int64_t, Renumbering&, T*, T*, T*, T*, T*, T*,              \
                                    const uint64_t*, const uint32_t*, const T*, int64_t, cudaStream_t);               \
   template void launch_unpermute<T>(int, const T*, const uint32_t*, int64_t, T*, cudaStream_t);                      \
+  template void build_attr_tasks<T>(AttrTasks&, int, const uint64_t*, int64_t, cudaStream_t);                        \
+  template void launch_attractive_tasks<T>(const AttrTasks&, const uint32_t*, const T*, const T*, T*, cudaStream_t); \
   template void launch_update<T>(int, T*, const T*, const T*, T*, T*, int64_t, const double*, T, T, T, UpdateScratch&,  \
                                  cudaStream_t);                                                                      \
   template void launch_kl_sparse<T>(int, const uint64_t*, const uint32_t*, const T*, const T*, int64_t,             \

@@ -17,6 +17,26 @@ template <class T>
 void launch_attractive(int D, const uint64_t* rows, const uint32_t* cols, const T* vals, const T* y, int64_t n, T* pos,
                        cudaStream_t s, const uint32_t* row_of_slot = nullptr);
 
+// Attractive forces over bounded tasks: every CSR row is cut into tasks of at
+// most kAttrTaskLen entries, one warp per task. A row of one task writes its
+// slot directly; the tasks of a longer row write partial sums that a second
+// kernel adds in task order, so results do not depend on scheduling. Built
+// once per CSR layout (one host synchronisation), replayed every epoch.
+constexpr int kAttrTaskLen = 128;
+struct AttrTasks {
+  DevBuf tasks, off, cnt, longs, nlong_dev, part, scan_tmp;
+  int64_t ntasks = 0, nlong = 0, n = 0;
+  int D = 0;
+  uint64_t gen = ~0ull;  // layout generation the tasks were built for
+};
+
+template <class T>
+void build_attr_tasks(AttrTasks& at, int D, const uint64_t* rows, int64_t n, cudaStream_t s);
+
+template <class T>
+void launch_attractive_tasks(const AttrTasks& at, const uint32_t* cols, const T* vals, const T* y, T* pos,
+                             cudaStream_t s);
+
 // Locality renumbering of the device-resident optimisation state. The points
 // are re-laid out in `order` (a permutation of the current slots, e.g. the
 // Morton order of the embedding); ext[s] is the point (CSR row) held by slot

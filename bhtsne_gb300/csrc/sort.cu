@@ -3,10 +3,16 @@
 // role of `par_sort_unstable_by_key` at src/tsne/arena.rs:191 of the
 // reference) and once per fit to order the symmetric affinity entries.
 //
-// The sort is three kernels per 8-bit digit: a per-tile histogram, one scan of
-// the digit-major count table, and a stable scatter in which each warp ranks
-// its keys with __match_any_sync. Tiles are 4096 keys, read in coalesced
-// rounds of 256.
+// The sort takes 8-bit digits over tiles of 2048 keys, three kernels a pass:
+//  * a histogram per tile (warp-aggregated shared atomics) that also adds
+//    its counts into per-super-tile totals (32 tiles each, digit-major);
+//  * an exclusive scan of the super-tile totals (one block while the table
+//    is small), which also clears them for the next pass;
+//  * a scatter: each tile adds the counts of the earlier tiles of its super
+//    tile to get its output offsets, ranks its keys stably in shared memory
+//    (each warp with __match_any_sync, then one prefix over warps and
+//    digits) and writes them out in sorted order, so that each digit's run
+//    is one contiguous, coalesced store.
 #include "internal.h"
 
 namespace bhg {
@@ -140,71 +146,220 @@ void scan_impl(const In* in, uint64_t* out, int64_t n, DevBuf& tmp, cudaStream_t
 // radix sort
 // ---------------------------------------------------------------------------
 constexpr int kRsThreads = 256;
-constexpr int kRsItems = 16;
-constexpr int kRsTile = kRsThreads * kRsItems;
 constexpr int kRsWarps = kRsThreads / 32;
+constexpr int kRsRounds = 8;                       // rounds of 32 keys per warp
+constexpr int kRsWarpSpan = 32 * kRsRounds;        // 256 consecutive keys per warp
+constexpr int kRsTile = kRsThreads * kRsRounds;    // 2048 keys per tile
+constexpr int kRsSup = 32;                         // tiles per super-tile
+constexpr int kRsInlineSup = 32;                   // up to this many super-tiles, the scatter scans them itself
+constexpr int kSpineThreads = 1024;
+constexpr int64_t kSpineMax = (int64_t)1 << 16;    // largest super-tile table scanned by one block
 
-__global__ void rs_hist_kernel(const uint64_t* __restrict__ keys, int64_t n, int shift, uint32_t* __restrict__ counts,
-                               int64_t nblocks) {
+// Per-tile digit counts (tile-major: counts[b * 256 + d]), also added into
+// the super-tile totals sup[d * ns + b / kRsSup].
+__global__ void __launch_bounds__(kRsThreads) rs_hist_kernel(const uint64_t* __restrict__ keys, int64_t n, int shift,
+                                                             uint32_t* __restrict__ counts, uint32_t* __restrict__ sup,
+                                                             int64_t ns) {
   __shared__ uint32_t h[256];
   h[threadIdx.x] = 0;
   __syncthreads();
+  const int lane = threadIdx.x & 31;
   const int64_t base = (int64_t)blockIdx.x * kRsTile;
-#pragma unroll 4
-  for (int i = 0; i < kRsItems; ++i) {
-    int64_t p = base + (int64_t)i * kRsThreads + threadIdx.x;
-    if (p < n) atomicAdd(&h[(unsigned)(keys[p] >> shift) & 255u], 1u);
+#pragma unroll
+  for (int i = 0; i < kRsRounds; ++i) {
+    const int64_t p = base + (int64_t)i * kRsThreads + threadIdx.x;
+    const unsigned d = p < n ? ((unsigned)(keys[p] >> shift) & 255u) : 256u;
+    const unsigned peers = __match_any_sync(kFull, d);
+    if (d < 256u && lane == __ffs(peers) - 1) atomicAdd(&h[d], (unsigned)__popc(peers));
   }
   __syncthreads();
-  counts[(int64_t)threadIdx.x * nblocks + blockIdx.x] = h[threadIdx.x];
+  const uint32_t c = h[threadIdx.x];
+  counts[(int64_t)blockIdx.x * 256 + threadIdx.x] = c;
+  if (c) atomicAdd(&sup[(int64_t)threadIdx.x * ns + blockIdx.x / kRsSup], c);
+}
+
+// Exclusive scan of m u32 values into u64 offsets by one block, in coalesced
+// rounds of 1024; clears the input afterwards when `clear` is set.
+__global__ void __launch_bounds__(kSpineThreads) rs_spine_kernel(uint32_t* __restrict__ vals, int64_t m,
+                                                                 uint64_t* __restrict__ offsets, int clear) {
+  __shared__ uint64_t wt[kSpineThreads / 32];
+  __shared__ uint64_t carry;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  for (int64_t r0 = 0; r0 < m; r0 += kSpineThreads) {
+    const int64_t i = r0 + threadIdx.x;
+    const uint64_t v = i < m ? vals[i] : 0;
+    uint64_t x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint64_t y = __shfl_up_sync(kFull, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) wt[w] = x;
+    __syncthreads();
+    if (w == 0) {
+      uint64_t t = wt[lane];
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint64_t y = __shfl_up_sync(kFull, t, o);
+        if (lane >= o) t += y;
+      }
+      wt[lane] = t;
+    }
+    __syncthreads();
+    const uint64_t c0 = carry;
+    if (i < m) {
+      offsets[i] = c0 + x - v + (w > 0 ? wt[w - 1] : 0);
+      if (clear) vals[i] = 0;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) carry = c0 + wt[31];
+    __syncthreads();
+  }
 }
 
 template <class V>
-__global__ void __launch_bounds__(kRsThreads) rs_scatter_kernel(const uint64_t* __restrict__ kin, const V* __restrict__ vin,
+struct RsSmem {
+  uint64_t key[kRsTile];
+  V val[kRsTile];
+  uint32_t wcnt[kRsWarps][256];  // per warp and digit: count, then exclusive offset within the digit
+  uint32_t tstart[256];          // first position of each digit in the sorted tile
+  uint64_t gbase[256];           // first output position of the tile's keys of each digit
+  uint32_t wtot[kRsWarps];
+};
+
+// One pass over tile blockIdx.x: output offsets from the super-tile prefix
+// and the earlier tiles of the super-tile, a stable rank in shared memory,
+// and a coalesced write-out.
+template <class V>
+__global__ void __launch_bounds__(kRsThreads, 4) rs_scatter_kernel(const uint64_t* __restrict__ kin, const V* __restrict__ vin,
                                                                 uint64_t* __restrict__ kout, V* __restrict__ vout, int64_t n,
-                                                                int shift, const uint64_t* __restrict__ offsets,
-                                                                int64_t nblocks) {
-  __shared__ uint32_t cnt[kRsWarps][256];
-  __shared__ uint64_t off[kRsWarps][256];
-  __shared__ uint64_t base[256];
+                                                                int shift, const uint32_t* __restrict__ counts,
+                                                                const uint64_t* __restrict__ sup_off,
+                                                                const uint32_t* __restrict__ sup, int64_t ns,
+                                                                uint32_t* __restrict__ sup_clear) {
+  __shared__ RsSmem<V> sm;
   const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
-  base[tid] = offsets[(int64_t)tid * nblocks + blockIdx.x];
-#pragma unroll
-  for (int q = 0; q < kRsWarps; ++q) cnt[q][tid] = 0;
-  __syncthreads();
   const unsigned lt = (1u << lane) - 1u;
-  const int64_t tile = (int64_t)blockIdx.x * kRsTile;
-  for (int i = 0; i < kRsItems; ++i) {
-    const int64_t p = tile + (int64_t)i * kRsThreads + tid;
-    const bool valid = p < n;
-    uint64_t k = 0;
-    V v{};
-    if (valid) {
-      k = kin[p];
-      v = vin[p];
-    }
-    const unsigned d = valid ? ((unsigned)(k >> shift) & 255u) : 256u;
-    const unsigned peers = __match_any_sync(kFull, d);
-    const unsigned rank = __popc(peers & lt);
-    if (valid && rank == 0) cnt[w][d] = __popc(peers);
-    __syncthreads();
-    {
-      uint64_t run = base[tid];
+  const int64_t b = blockIdx.x;
+  const int64_t tile = b * kRsTile;
+  const int64_t wbase = tile + (int64_t)w * kRsWarpSpan;
+  uint64_t k[kRsRounds];
+  V v[kRsRounds];
+  uint32_t rk[kRsRounds];
 #pragma unroll
-      for (int q = 0; q < kRsWarps; ++q) {
-        const uint32_t c = cnt[q][tid];
-        off[q][tid] = run;
-        run += c;
-        cnt[q][tid] = 0;
+  for (int r = 0; r < kRsRounds; ++r) {
+    const int64_t p = wbase + r * 32 + lane;
+    k[r] = 0;
+    v[r] = V{};
+    if (p < n) {
+      k[r] = kin[p];
+      v[r] = vin[p];
+    }
+  }
+  {
+    const int64_t s0 = (b / kRsSup) * kRsSup;
+    const int nq = (int)(b - s0);
+    uint64_t g;
+    if (sup_off) {
+      g = sup_off[(int64_t)tid * ns + b / kRsSup];
+    } else {
+      // few super-tiles: digit totals, their exclusive scan over the block,
+      // and this digit's earlier super-tiles
+      const int S = (int)(b / kRsSup);
+      uint32_t st[kRsInlineSup];
+#pragma unroll
+      for (int q = 0; q < kRsInlineSup; ++q) st[q] = q < ns ? sup[(int64_t)tid * ns + q] : 0u;
+      uint32_t tot = 0, pre = 0;
+#pragma unroll
+      for (int q = 0; q < kRsInlineSup; ++q) {
+        tot += st[q];
+        pre += q < S ? st[q] : 0u;
       }
-      base[tid] = run;
+      uint32_t x = tot;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(kFull, x, o);
+        if (lane >= o) x += y;
+      }
+      if (lane == 31) sm.wtot[w] = x;
+      __syncthreads();
+      uint32_t add = 0;
+      for (int q = 0; q < w; ++q) add += sm.wtot[q];
+      g = (uint64_t)(x - tot + add) + pre;
+      __syncthreads();
+      if (b == 0 && sup_clear)
+        for (int64_t i = tid; i < 256 * ns; i += kRsThreads) sup_clear[i] = 0;
     }
+    uint32_t c[kRsSup - 1];
+#pragma unroll
+    for (int q = 0; q < kRsSup - 1; ++q) c[q] = q < nq ? counts[(s0 + q) * 256 + tid] : 0u;
+#pragma unroll
+    for (int q = 0; q < kRsSup - 1; ++q) g += c[q];
+    sm.gbase[tid] = g;
+  }
+#pragma unroll
+  for (int q = 0; q < kRsWarps; ++q) sm.wcnt[q][tid] = 0;
+  __syncthreads();
+  // rank among the warp's earlier keys of the same digit (round r, lane l is
+  // key wbase + 32 r + l: input order)
+#pragma unroll
+  for (int r = 0; r < kRsRounds; ++r) {
+    const int64_t p = wbase + r * 32 + lane;
+    const unsigned d = p < n ? ((unsigned)(k[r] >> shift) & 255u) : 256u;
+    const unsigned peers = __match_any_sync(kFull, d);
+    const uint32_t prior = d < 256u ? sm.wcnt[w][d] : 0u;
+    __syncwarp();
+    if (d < 256u && lane == __ffs(peers) - 1) sm.wcnt[w][d] = prior + (uint32_t)__popc(peers);
+    __syncwarp();
+    rk[r] = prior + (uint32_t)__popc(peers & lt);
+  }
+  __syncthreads();
+  // thread tid owns digit tid: offsets across warps, then the digit starts
+  {
+    uint32_t tot = 0;
+#pragma unroll
+    for (int q = 0; q < kRsWarps; ++q) {
+      const uint32_t c = sm.wcnt[q][tid];
+      sm.wcnt[q][tid] = tot;
+      tot += c;
+    }
+    uint32_t x = tot;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(kFull, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) sm.wtot[w] = x;
     __syncthreads();
-    if (valid) {
-      const uint64_t pos = off[w][d] + rank;
-      kout[pos] = k;
-      vout[pos] = v;
+    uint32_t add = 0;
+    for (int q = 0; q < w; ++q) add += sm.wtot[q];
+    sm.tstart[tid] = x - tot + add;
+  }
+  __syncthreads();
+#pragma unroll
+  for (int r = 0; r < kRsRounds; ++r) {
+    const int64_t p = wbase + r * 32 + lane;
+    if (p < n) {
+      const unsigned d = (unsigned)(k[r] >> shift) & 255u;
+      const uint32_t lp = sm.tstart[d] + sm.wcnt[w][d] + rk[r];
+      sm.key[lp] = k[r];
+      sm.val[lp] = v[r];
     }
+  }
+  __syncthreads();
+  // write out in sorted order: consecutive positions of a digit go to
+  // consecutive output positions
+  const int64_t left = n - tile;
+  const int cnt = left < kRsTile ? (int)left : kRsTile;
+#pragma unroll 4
+  for (int i = tid; i < cnt; i += kRsThreads) {
+    const uint64_t key = sm.key[i];
+    const unsigned d = (unsigned)(key >> shift) & 255u;
+    const uint64_t gp = sm.gbase[d] + (uint64_t)(i - (int)sm.tstart[d]);
+    kout[gp] = key;
+    vout[gp] = sm.val[i];
   }
 }
 
@@ -221,32 +376,60 @@ void scan_u64(const uint64_t* in, uint64_t* out, int64_t n, DevBuf& tmp, cudaStr
 template <class V>
 void radix_sort_pairs(uint64_t* keys, V* vals, uint64_t* keys_alt, V* vals_alt, int64_t n, int begin_bit,
                       int end_bit, DevBuf& tmp, cudaStream_t s) {
-  if (n <= 1) return;
+  if (n <= 1 || begin_bit >= end_bit) return;
   const int64_t nb = ceil_div(n, kRsTile);
-  const int64_t ncount = 256 * nb;
-  // tmp layout: counts (u32, ncount) | offsets (u64, ncount+1) | scan scratch
-  const size_t counts_bytes = ((size_t)ncount * 4 + 255) / 256 * 256;
-  const size_t off_bytes = ((size_t)(ncount + 1) * 8 + 255) / 256 * 256;
-  const int64_t scan_parts = ceil_div(ncount, kScanTile) + 1;
-  char* base = static_cast<char*>(tmp.ensure(counts_bytes + off_bytes + (size_t)scan_parts * 8 + 256));
+  const int64_t ns = ceil_div(nb, kRsSup);
+  const int64_t ms = 256 * ns;
+  // tmp layout: tile counts (u32, 256 nb) | super-tile totals (u32, ms) |
+  // super-tile offsets (u64, ms + 1) | scan scratch
+  const size_t cb = ((size_t)nb * 256 * 4 + 255) / 256 * 256;
+  const size_t sb = ((size_t)ms * 4 + 255) / 256 * 256;
+  const size_t ob = ((size_t)(ms + 1) * 8 + 255) / 256 * 256;
+  const int64_t scan_parts = ceil_div(ms, kScanTile) + 1;
+  // (the inline spine keeps its second super-tile table where the offsets go)
+  char* base = static_cast<char*>(tmp.ensure(cb + sb + std::max(ob, sb) + (size_t)scan_parts * 8 + 256));
   uint32_t* counts = reinterpret_cast<uint32_t*>(base);
-  uint64_t* offsets = reinterpret_cast<uint64_t*>(base + counts_bytes);
-  uint64_t* partial = reinterpret_cast<uint64_t*>(base + counts_bytes + off_bytes);
+  uint32_t* sup = reinterpret_cast<uint32_t*>(base + cb);
+  uint64_t* sup_off = reinterpret_cast<uint64_t*>(base + cb + sb);
+  uint64_t* partial = reinterpret_cast<uint64_t*>(base + cb + sb + std::max(ob, sb));
+  const bool inline_spine = ns <= kRsInlineSup;
+  const bool one_block = ms <= kSpineMax;
+  // inline spine: two super-tile tables used in turn; the scatter of one
+  // pass clears the table the next pass's histogram fills
+  uint32_t* sup2 = reinterpret_cast<uint32_t*>(base + cb + sb);
+  BHG_CUDA(cudaMemsetAsync(sup, 0, (size_t)(inline_spine ? 2 * sb : ms * 4), s));
 
   uint64_t *ki = keys, *ko = keys_alt;
   V *vi = vals, *vo = vals_alt;
   int passes = 0;
   for (int shift = begin_bit; shift < end_bit; shift += 8) {
-    rs_hist_kernel<<<(unsigned)nb, kRsThreads, 0, s>>>(ki, n, shift, counts, nb);
+    rs_hist_kernel<<<(unsigned)nb, kRsThreads, 0, s>>>(ki, n, shift, counts, sup, ns);
     BHG_LAUNCH_CHECK();
-    const int64_t sb = ceil_div(ncount, kScanTile);
-    scan_reduce_kernel<uint32_t><<<(unsigned)sb, kScanThreads, 0, s>>>(counts, ncount, partial);
-    BHG_LAUNCH_CHECK();
-    scan_partials_kernel<<<1, 1024, 0, s>>>(partial, sb, offsets + ncount);
-    BHG_LAUNCH_CHECK();
-    scan_apply_kernel<uint32_t><<<(unsigned)sb, kScanThreads, 0, s>>>(counts, offsets, ncount, partial);
-    BHG_LAUNCH_CHECK();
-    rs_scatter_kernel<V><<<(unsigned)nb, kRsThreads, 0, s>>>(ki, vi, ko, vo, n, shift, offsets, nb);
+    if (inline_spine) {
+      rs_scatter_kernel<V><<<(unsigned)nb, kRsThreads, 0, s>>>(ki, vi, ko, vo, n, shift, counts, nullptr, sup, ns,
+                                                               sup2);
+      BHG_LAUNCH_CHECK();
+      std::swap(sup, sup2);
+      std::swap(ki, ko);
+      std::swap(vi, vo);
+      ++passes;
+      continue;
+    }
+    if (one_block) {
+      rs_spine_kernel<<<1, kSpineThreads, 0, s>>>(sup, ms, sup_off, 1);
+      BHG_LAUNCH_CHECK();
+    } else {
+      const int64_t nsb = ceil_div(ms, kScanTile);
+      scan_reduce_kernel<uint32_t><<<(unsigned)nsb, kScanThreads, 0, s>>>(sup, ms, partial);
+      BHG_LAUNCH_CHECK();
+      scan_partials_kernel<<<1, 1024, 0, s>>>(partial, nsb, sup_off + ms);
+      BHG_LAUNCH_CHECK();
+      scan_apply_kernel<uint32_t><<<(unsigned)nsb, kScanThreads, 0, s>>>(sup, sup_off, ms, partial);
+      BHG_LAUNCH_CHECK();
+      BHG_CUDA(cudaMemsetAsync(sup, 0, (size_t)ms * 4, s));
+    }
+    rs_scatter_kernel<V><<<(unsigned)nb, kRsThreads, 0, s>>>(ki, vi, ko, vo, n, shift, counts, sup_off, nullptr, ns,
+                                                             nullptr);
     BHG_LAUNCH_CHECK();
     std::swap(ki, ko);
     std::swap(vi, vo);

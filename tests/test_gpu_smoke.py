@@ -58,6 +58,21 @@ def test_symmetrize_bit_exact(gpu, oracle):
     assert np.array_equal(gv, ov)
 
 
+@pytest.mark.parametrize("n", [40_000, 100_000])
+def test_symmetrize_bit_exact_large(gpu, oracle, n):
+    """7.2M and 18M sort keys: the radix sort scans its super-tile totals with
+    one block, and with the multi-block scan (up to 2M keys the scatter scans
+    them itself, as in every smaller case)."""
+    X, _ = blobs(n, 8, 20, 4)
+    gi, gd = gpu.knn_euclidean(X, 90)
+    op, _ = oracle.search_beta(gd, 30.0)
+    gr, gc, gv = gpu.symmetrize(gi, op)
+    orr, oc, ov = oracle.symmetrize(gi.astype(np.uint64), op)
+    assert np.array_equal(gr, orr)
+    assert np.array_equal(gc, oc)
+    assert np.array_equal(gv, ov)
+
+
 @pytest.mark.parametrize("D", [2, 3, 4, 5, 6, 7])
 def test_bh_gradient(gpu, oracle, D):
     X, _ = blobs(2000, 20, 5, 4)
