@@ -1360,6 +1360,7 @@ struct BatchImpl {
   std::vector<int64_t> off, nnz_off;
   DevBuf d_off, job_of, rows, cols, vals, y, uy, gains, pos, neg, q, z, lr, mom, boxes, codes, jobkey, jobkey_alt;
   DevBuf tmp, d_nnz_off;
+  AttrTasks at;  // attractive-pass tasks of the block-diagonal CSR
   BhWorkspace<T> ws;
   SegTiles tiles;
   AffinityScratch<T> aff;
@@ -1603,6 +1604,7 @@ void batch_fit(bhtsne_batch* b) {
   // epoch loop
   const int bits = D == 2 ? 32 : 21;
   T* y = B.y.template as<T>();
+  build_attr_tasks<T>(B.at, D, B.rows.template as<uint64_t>(), total, s);
   BoxParams<T>* boxes = B.boxes.template as<BoxParams<T>>();
   const int64_t* off = B.d_off.template as<int64_t>();
   auto body = [&]() {
@@ -1613,8 +1615,8 @@ void batch_fit(bhtsne_batch* b) {
     sg.off = off;
     bh_traverse<T>(B.ws, D, y, total, (T)P.theta, B.neg.template as<T>(), B.q.template as<T>(), s, sg, boxes);
     batch_z<T>(B.q.template as<T>(), off, B.K, B.z.template as<double>(), s);
-    launch_attractive<T>(D, B.rows.template as<uint64_t>(), B.cols.template as<uint32_t>(), B.vals.template as<T>(), y,
-                         total, B.pos.template as<T>(), s);
+    launch_attractive_tasks<T>(B.at, B.cols.template as<uint32_t>(), B.vals.template as<T>(), y,
+                               B.pos.template as<T>(), s);
     batch_update<T>(D, y, B.pos.template as<T>(), B.neg.template as<T>(), B.uy.template as<T>(),
                     B.gains.template as<T>(), total, B.job_of.template as<uint32_t>(), B.z.template as<double>(),
                     B.lr.template as<T>(), B.mom.template as<T>(), s);

@@ -622,9 +622,10 @@ __global__ void __launch_bounds__(kThreads) bh_traverse_kernel(const T* __restri
       const uint32_t sk_raw = leaf ? i + 1 : (w >> 5);
       // skip > i by construction; max() keeps the walk finite regardless.
       const uint32_t sk = sk_raw > i ? sk_raw : i + 1;
-      const uint32_t lastn = M - 1;
-      const typename TreeNodes<T, D>::Raw nxt_open = nodes.load(i + 1 < M ? i + 1 : lastn);
-      const typename TreeNodes<T, D>::Raw nxt_skip = leaf ? nxt_open : nodes.load(sk < M ? sk : lastn);
+      // i + 1 <= M and the node array holds M + 1 entries (a spare past the
+      // last node), so neither load needs a clamp beyond sk <= M
+      const typename TreeNodes<T, D>::Raw nxt_open = nodes.load(i + 1);
+      const typename TreeNodes<T, D>::Raw nxt_skip = leaf ? nxt_open : nodes.load(sk < M ? sk : M);
       T com[D], mass, r2;
       nodes.decode(cur, com, &mass, &r2);
       T disp[D];
@@ -642,7 +643,7 @@ __global__ void __launch_bounds__(kThreads) bh_traverse_kernel(const T* __restri
       i = sk;
       cur = nxt_skip;
       if (r2 < T(0) && dist == T(0)) continue;
-      const T inv = T(1) / (T(1) + dist);
+      const T inv = rcp_rn(T(1) + dist);
       T m = mass * inv;
       q += m;
       m = m * inv;
@@ -707,7 +708,9 @@ void BhWorkspace<T>::reserve(int64_t n_, int D_) {
   mask.ensure(nn * 4);
   cnt.ensure(nn * 4);
   base.ensure((nn + 1) * 8);
-  const int64_t max_nodes = 2 * nn;
+  // one spare node past the largest tree: the traversal loads node i + 1
+  // while at the last node i = M - 1
+  const int64_t max_nodes = 2 * nn + 1;
   if (D == 2) {
     geom.ensure(max_nodes * sizeof(Node2<T>));
   } else if (D == 3) {

@@ -58,6 +58,10 @@ inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
 constexpr int kWarp = 32;
 constexpr unsigned kFull = 0xffffffffu;
 
+// 1 / x rounded to nearest: the same value as the IEEE quotient T(1) / x.
+__device__ __forceinline__ float rcp_rn(float x) { return __frcp_rn(x); }
+__device__ __forceinline__ double rcp_rn(double x) { return __drcp_rn(x); }
+
 // Numeric limits usable on the device.
 template <class T>
 struct Lim;

@@ -95,6 +95,21 @@ void scan_u64(const uint64_t* in, uint64_t* out, int64_t n, DevBuf& tmp, cudaStr
 // ---- radix sort -----------------------------------------------------------------
 // Stable LSD sort of (u64 key, payload) pairs on key bits [begin_bit, end_bit).
 // Sorted data ends in (keys, vals); (keys_alt, vals_alt) are scratch of equal size.
+// `tmp` holds radix_sort_tmp_bytes(n): per-tile digit counts (tiles of 2048
+// keys), two super-tile tables (32 tiles each; the second doubles as the
+// u64 super-tile offsets) and the scan's per-block partials.
+constexpr int64_t kRadixTile = 2048, kRadixSup = 32, kRadixScanTile = 4096;
+constexpr size_t radix_round256(size_t b) { return (b + 255) / 256 * 256; }
+constexpr size_t radix_sort_tmp_bytes(int64_t n) {
+  return radix_round256((size_t)((n + kRadixTile - 1) / kRadixTile) * 256 * 4) +
+         radix_round256((size_t)(((n + kRadixTile - 1) / kRadixTile + kRadixSup - 1) / kRadixSup) * 256 * 4) +
+         radix_round256((size_t)((((n + kRadixTile - 1) / kRadixTile + kRadixSup - 1) / kRadixSup) * 256 + 1) * 8) +
+         (size_t)(((((n + kRadixTile - 1) / kRadixTile + kRadixSup - 1) / kRadixSup) * 256 + kRadixScanTile - 1) /
+                      kRadixScanTile +
+                  1) *
+             8 +
+         256;
+}
 template <class V>
 void radix_sort_pairs(uint64_t* keys, V* vals, uint64_t* keys_alt, V* vals_alt, int64_t n, int begin_bit,
                       int end_bit, DevBuf& tmp, cudaStream_t s);

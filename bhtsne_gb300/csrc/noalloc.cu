@@ -34,13 +34,12 @@ constexpr int64_t kNoAllocMaxPoints = 32768;
 // Byte offsets of the carved buffers (each rounded up to 256 bytes).
 constexpr size_t al(size_t b) { return (b + 255) / 256 * 256; }
 constexpr int64_t kN = kNoAllocMaxPoints;
-constexpr size_t kSortTiles = (kN + 4095) / 4096;
 constexpr size_t kSzKeys = al(kN * 8), kSzPerm = al(kN * 4), kSzYs = al(kN * 2 * 4), kSzPre = al((kN + 1) * 2 * 8),
                  kSzPrePart = al(((kN + 2047) / 2048 + 1) * 2 * 8), kSzMask = al(kN * 4), kSzCnt = al(kN * 4),
-                 kSzBase = al((kN + 1) * 8), kSzGeom = al(2 * kN * sizeof(Node2<float>)),
+                 kSzBase = al((kN + 1) * 8), kSzGeom = al((2 * kN + 1) * sizeof(Node2<float>)),
                  kSzPart = al(2 * 152 * 3 * 4), kSzSmall = 256, kSzParams = al(sizeof(BoxParams<float>)),
                  kSzZpart = al(((kN + 255) / 256 + 1) * 8),
-                 kSzSort = al(256 * kSortTiles * 4) + al((256 * kSortTiles + 1) * 8) + al(((256 * kSortTiles + 4095) / 4096 + 1) * 8) + 256,
+                 kSzSort = al(radix_sort_tmp_bytes(kN)),
                  kSzScan = al(((kN + 4095) / 4096 + 1) * 8);
 constexpr size_t kNoAllocBytes = 2 * kSzKeys + 2 * kSzPerm + kSzYs + kSzPre + kSzPrePart + kSzMask + kSzCnt + kSzBase +
                                  kSzGeom + 2 * kSzPart + 2 * kSzSmall + kSzParams + kSzZpart + kSzSmall + kSzSort + kSzScan;

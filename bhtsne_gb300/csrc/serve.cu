@@ -175,6 +175,7 @@ struct BhEngine {
   std::vector<std::unique_ptr<Slot<T>>> slots;
   int64_t total = 0, nnz = 0;
   DevBuf d_off, job_of, rows, cols, vals, y, uy, gains, y2, uy2, g2, pos, neg, q, z, lr, mom, active, boxes;
+  AttrTasks attr;  // attractive-pass tasks of the packed CSR, rebuilt at each repack
   DevBuf codes, jobkey, jobkey_alt, klbuf, kltmp, ykl;
   BhWorkspace<T> ws, kws;
   SegTiles tiles;
@@ -394,6 +395,7 @@ struct BhEngine {
     }
     total = tot;
     nnz = nz;
+    build_attr_tasks<T>(attr, sv->D, rows.template as<uint64_t>(), tot, s);
     BHG_CUDA(cudaMemcpyAsync(d_off.ensure(off.size() * 8), off.data(), off.size() * 8, cudaMemcpyHostToDevice, s));
     tiles.build(off, s);
     BHG_CUDA(cudaMemcpyAsync(lr.ensure(K * es), lrh.data(), K * es, cudaMemcpyHostToDevice, s));
@@ -424,8 +426,7 @@ struct BhEngine {
     sg.off = off;
     bh_traverse<T>(ws, D, yp, total, (T)sv->prm.theta, neg.template as<T>(), q.template as<T>(), s, sg, bx);
     batch_z<T>(q.template as<T>(), off, K, z.template as<double>(), s);
-    launch_attractive<T>(D, rows.template as<uint64_t>(), cols.template as<uint32_t>(), vals.template as<T>(), yp, total,
-                         pos.template as<T>(), s);
+    launch_attractive_tasks<T>(attr, cols.template as<uint32_t>(), vals.template as<T>(), yp, pos.template as<T>(), s);
     batch_update<T>(D, yp, pos.template as<T>(), neg.template as<T>(), uy.template as<T>(), gains.template as<T>(), total,
                     job_of.template as<uint32_t>(), z.template as<double>(), lr.template as<T>(), mom.template as<T>(),
                     s, act);

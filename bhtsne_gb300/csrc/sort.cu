@@ -377,21 +377,22 @@ template <class V>
 void radix_sort_pairs(uint64_t* keys, V* vals, uint64_t* keys_alt, V* vals_alt, int64_t n, int begin_bit,
                       int end_bit, DevBuf& tmp, cudaStream_t s) {
   if (n <= 1 || begin_bit >= end_bit) return;
+  static_assert(kRsTile == kRadixTile && kRsSup == kRadixSup && kScanTile == kRadixScanTile,
+                "radix_sort_tmp_bytes describes this layout");
   const int64_t nb = ceil_div(n, kRsTile);
   const int64_t ns = ceil_div(nb, kRsSup);
   const int64_t ms = 256 * ns;
   // tmp layout: tile counts (u32, 256 nb) | super-tile totals (u32, ms) |
-  // super-tile offsets (u64, ms + 1) | scan scratch
-  const size_t cb = ((size_t)nb * 256 * 4 + 255) / 256 * 256;
-  const size_t sb = ((size_t)ms * 4 + 255) / 256 * 256;
-  const size_t ob = ((size_t)(ms + 1) * 8 + 255) / 256 * 256;
-  const int64_t scan_parts = ceil_div(ms, kScanTile) + 1;
-  // (the inline spine keeps its second super-tile table where the offsets go)
-  char* base = static_cast<char*>(tmp.ensure(cb + sb + std::max(ob, sb) + (size_t)scan_parts * 8 + 256));
+  // super-tile offsets (u64, ms + 1; with the inline spine, the second
+  // super-tile table) | scan scratch
+  const size_t cb = radix_round256((size_t)nb * 256 * 4);
+  const size_t sb = radix_round256((size_t)ms * 4);
+  const size_t ob = radix_round256((size_t)(ms + 1) * 8);
+  char* base = static_cast<char*>(tmp.ensure(radix_sort_tmp_bytes(n)));
   uint32_t* counts = reinterpret_cast<uint32_t*>(base);
   uint32_t* sup = reinterpret_cast<uint32_t*>(base + cb);
   uint64_t* sup_off = reinterpret_cast<uint64_t*>(base + cb + sb);
-  uint64_t* partial = reinterpret_cast<uint64_t*>(base + cb + sb + std::max(ob, sb));
+  uint64_t* partial = reinterpret_cast<uint64_t*>(base + cb + sb + ob);
   const bool inline_spine = ns <= kRsInlineSup;
   const bool one_block = ms <= kSpineMax;
   // inline spine: two super-tile tables used in turn; the scatter of one
