@@ -499,7 +499,7 @@ void advance_impl(bhtsne_tsne* t, int64_t epochs) {
       if (fw.cap_L == 0) {
         const int need = fit_needed_length<T>(fw, D, n, S.bh.params.template as<BoxParams<T>>(), s);
         int cap = 64;
-        while (cap < 2 * need) cap <<= 1;
+        while (cap < 2 * need && cap < kFitMaxL) cap <<= 1;
         fw.reserve(D, n, cap);
         t->drop_graph();
         eager_next = true;
@@ -541,7 +541,7 @@ void advance_impl(bhtsne_tsne* t, int64_t epochs) {
         BHG_CUDA(cudaMemcpyAsync(S.uy.ptr, ck + (size_t)n * D, ybytes, cudaMemcpyDeviceToDevice, s));
         BHG_CUDA(cudaMemcpyAsync(S.gains.ptr, ck + 2 * (size_t)n * D, ybytes, cudaMemcpyDeviceToDevice, s));
         launch_recenter_bbox<T>(D, y, n, nullptr, false, S.bh, bits, s);
-        fw.reserve(D, n, 2 * fw.cap_L);
+        fw.reserve(D, n, std::min(2 * fw.cap_L, kFitMaxL));
         t->drop_graph();
         eager_next = true;
         continue;
@@ -549,9 +549,9 @@ void advance_impl(bhtsne_tsne* t, int64_t epochs) {
       for (int64_t i = 0; i < len; ++i) epoch_tail<T>(t, epoch + i, snap);
       t->cursor += len;
       k += len;
-      if (2 * hp.need_L > fw.cap_L) {
+      if (2 * hp.need_L > fw.cap_L && fw.cap_L < kFitMaxL) {
         int cap = fw.cap_L;
-        while (cap < 2 * hp.need_L) cap <<= 1;
+        while (cap < 2 * hp.need_L && cap < kFitMaxL) cap <<= 1;
         fw.reserve(D, n, cap);
         t->drop_graph();
         eager_next = true;

@@ -321,7 +321,7 @@ __global__ void multiply_kernel(typename Cx<T>::type* __restrict__ a, typename C
   }
 }
 
-// Radix-2 FFT of rows of length L (from the parameters) held in shared
+// Power-of-two FFT of rows of length L (from the parameters) held in shared
 // memory, row b at data + b L; rows: 0 -> L rows, 1 -> `nodes` rows, 2 -> one
 // row. tw holds the twiddles of a cap_L transform (L divides cap_L).
 template <class T>
@@ -339,7 +339,62 @@ __global__ void fft_rows_kernel(typename Cx<T>::type* __restrict__ data, const F
   T2* d = data + (int64_t)blockIdx.x * L;
   for (int i = threadIdx.x; i < L; i += blockDim.x) s[__brev((unsigned)i) >> (32 - log2L)] = d[i];
   __syncthreads();
-  for (int lg = 1; lg <= log2L; ++lg) {
+  // Stages lg and lg + 1 together (radix 2^2): a group of 4h elements, h =
+  // 2^(lg-1), passes through both butterfly stages in registers, one shared
+  // memory round trip and one barrier per two stages. Stage lg uses
+  // W_2h^pos for both of its pairs; stage lg + 1 uses W_4h^pos and
+  // W_4h^(pos+h) = W_4h^pos * W_4^1, an exact quarter turn.
+  int lg = 1;
+  for (; lg + 1 <= log2L; lg += 2) {
+    const int h = 1 << (lg - 1);
+    const int st1 = (L >> lg) * tws, st2 = (L >> (lg + 1)) * tws;
+    for (int b = threadIdx.x; b < (L >> 2); b += blockDim.x) {
+      const int pos = b & (h - 1);
+      const int i = ((b >> (lg - 1)) << (lg + 1)) + pos;
+      T2 w1 = tw[pos * st1];
+      T2 w2 = tw[pos * st2];
+      if (inverse) {
+        w1.y = -w1.y;
+        w2.y = -w2.y;
+      }
+      T2 w3;
+      if (inverse) {
+        w3.x = -w2.y;
+        w3.y = w2.x;
+      } else {
+        w3.x = w2.y;
+        w3.y = -w2.x;
+      }
+      T2 x0 = s[i], x1 = s[i + h], x2 = s[i + 2 * h], x3 = s[i + 3 * h];
+      T2 t = cmul(x1, w1);
+      x1.x = x0.x - t.x;
+      x1.y = x0.y - t.y;
+      x0.x = x0.x + t.x;
+      x0.y = x0.y + t.y;
+      t = cmul(x3, w1);
+      x3.x = x2.x - t.x;
+      x3.y = x2.y - t.y;
+      x2.x = x2.x + t.x;
+      x2.y = x2.y + t.y;
+      t = cmul(x2, w2);
+      T2 r;
+      r.x = x0.x + t.x;
+      r.y = x0.y + t.y;
+      s[i] = r;
+      r.x = x0.x - t.x;
+      r.y = x0.y - t.y;
+      s[i + 2 * h] = r;
+      t = cmul(x3, w3);
+      r.x = x1.x + t.x;
+      r.y = x1.y + t.y;
+      s[i + h] = r;
+      r.x = x1.x - t.x;
+      r.y = x1.y - t.y;
+      s[i + 3 * h] = r;
+    }
+    __syncthreads();
+  }
+  for (; lg <= log2L; ++lg) {
     const int half = 1 << (lg - 1);
     const int tstep = L >> lg;
     for (int b = threadIdx.x; b < (L >> 1); b += blockDim.x) {
@@ -440,15 +495,17 @@ __global__ void gather_kernel(const T* __restrict__ y, int64_t n, const FitParam
     phi[D + 1] = phi[D + 1] * p.scale;
     const T density = phi[0];
     const T sqp = phi[D + 1];
-    T norm_sq = T(0), cross = T(0);
+    // Z's per-point term cancels terms of order |y|^2 phi_0; it is assembled
+    // in FP64 from the interpolated potentials (the forces stay in T).
+    double norm_sq = 0.0, cross = 0.0;
 #pragma unroll
     for (int a = 0; a < D; ++a) {
       const T fm = phi[1 + a];
       neg[i * D + a] = yv[a] * density - fm;
-      norm_sq = norm_sq + yv[a] * yv[a];
-      cross = cross + yv[a] * fm;
+      norm_sq += (double)yv[a] * (double)yv[a];
+      cross += (double)yv[a] * (double)fm;
     }
-    zi = (double)((T(1) + norm_sq) * density - T(2) * cross + sqp);
+    zi = (1.0 + norm_sq) * (double)density - 2.0 * cross + (double)sqp;
   }
   const double bs = block_sum(zi, sh);
   if (threadIdx.x == 0) {

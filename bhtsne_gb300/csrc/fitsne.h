@@ -5,6 +5,10 @@
 
 namespace bhg {
 
+// Largest transform length: boxes <= 1000 per axis, 3 nodes per box, the
+// next power of two >= 2 nodes - 1.
+constexpr int kFitMaxL = 8192;
+
 template <class T>
 struct FitParams {
   T lo, extent, box_width, inv_box_width, spacing;
