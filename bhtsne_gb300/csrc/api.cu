@@ -507,7 +507,7 @@ void advance_impl(bhtsne_tsne* t, int64_t epochs) {
       BHG_CUDA(cudaMemcpyAsync(ck, y, ybytes, cudaMemcpyDeviceToDevice, s));
       BHG_CUDA(cudaMemcpyAsync(ck + (size_t)n * D, S.uy.ptr, ybytes, cudaMemcpyDeviceToDevice, s));
       BHG_CUDA(cudaMemcpyAsync(ck + 2 * (size_t)n * D, S.gains.ptr, ybytes, cudaMemcpyDeviceToDevice, s));
-      BHG_CUDA(cudaMemsetAsync(fw.flag.ptr, 0, sizeof(int), s));
+      BHG_CUDA(cudaMemsetAsync(fw.flag.ptr, 0, 2 * sizeof(int), s));  // capacity flag, FFT fault word
       const T mom = (T)t->momentum;
       for (int64_t i = 0; i < len; ++i) {
         if (eager_next) {
@@ -531,11 +531,13 @@ void advance_impl(bhtsne_tsne* t, int64_t epochs) {
         BHG_CUDA(cudaGraphLaunch(t->graph, s));
         g_launches.fetch_add(t->graph_kernels);
       }
-      int over = 0;
+      int flags[2] = {0, 0};
       FitParams<T> hp;
-      BHG_CUDA(cudaMemcpyAsync(&over, fw.flag.ptr, sizeof(int), cudaMemcpyDeviceToHost, s));
+      BHG_CUDA(cudaMemcpyAsync(flags, fw.flag.ptr, sizeof(flags), cudaMemcpyDeviceToHost, s));
       BHG_CUDA(cudaMemcpyAsync(&hp, fw.params.ptr, sizeof(hp), cudaMemcpyDeviceToHost, s));
       BHG_CUDA(cudaStreamSynchronize(s));
+      if (flags[1]) throw Error(ST_ETIMEDOUT, "error: an FFT row load timed out.");
+      const int over = flags[0];
       if (over) {
         BHG_CUDA(cudaMemcpyAsync(y, ck, ybytes, cudaMemcpyDeviceToDevice, s));
         BHG_CUDA(cudaMemcpyAsync(S.uy.ptr, ck + (size_t)n * D, ybytes, cudaMemcpyDeviceToDevice, s));

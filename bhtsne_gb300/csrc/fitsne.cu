@@ -23,10 +23,12 @@
 //    (s, y_1) and (y_2, |y|^2 / s) with s a power of two near max |y|, so both
 //    halves of a pair have similar magnitude and neither one's rounding noise
 //    swamps the other; scaling by a power of two is exact.
-//  * 2-D transforms are row FFTs in shared memory plus tiled transposes; the
-//    spectrum stays in transposed layout, which is harmless because the
-//    kernel spectrum is symmetric in its two axes. Rows that are known to be
-//    zero (charges) or unused (potentials) are skipped.
+//  * 2-D transforms are row FFTs plus tiled transposes. Forward transforms
+//    leave their spectra in bit-reversed order and the inverse transforms read
+//    that order, so there is no reordering pass; the spectrum also stays in
+//    transposed layout, which is harmless because the kernel spectrum goes
+//    through the same pipeline and is symmetric in its two axes. Rows that
+//    are known to be zero (charges) or unused (potentials) are skipped.
 //  * The spread scatters with 64-bit integer atomics on a fixed-point grid
 //    (units of 2^-fix_shift, chosen so no partial sum can overflow), so the
 //    accumulated charges do not depend on the order of the atomics and the fit
@@ -243,179 +245,402 @@ __global__ void spread_kernel(const T* __restrict__ y, int64_t n, const FitParam
   }
 }
 
-// Zeroes the accumulator cells the spread can reach (device-side size).
-template <class T, int D>
-__global__ void zero_acc_kernel(long long* __restrict__ acc, const FitParams<T>* __restrict__ prm) {
-  const int64_t count = 4 * (D == 1 ? (int64_t)prm->L : (int64_t)prm->nodes * prm->L);
-  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < count; e += (int64_t)gridDim.x * blockDim.x)
-    acc[e] = 0;
+
+
+
+
+
+template <class T2>
+__device__ __forceinline__ T2 cadd(T2 a, T2 b) {
+  a.x += b.x;
+  a.y += b.y;
+  return a;
+}
+template <class T2>
+__device__ __forceinline__ T2 csub(T2 a, T2 b) {
+  a.x -= b.x;
+  a.y -= b.y;
+  return a;
+}
+template <class T2>
+__device__ __forceinline__ T2 shfl_xor2(T2 v, int m) {
+  v.x = __shfl_xor_sync(kFull, v.x, m);
+  v.y = __shfl_xor_sync(kFull, v.y, m);
+  return v;
 }
 
-// Fixed-point charges -> the two packed complex grids (rows < charge_rows,
-// all L columns; zero where nothing was spread).
-template <class T, int D>
-__global__ void unfix_kernel(const long long* __restrict__ acc, const FitParams<T>* __restrict__ prm,
-                             typename Cx<T>::type* __restrict__ g0, typename Cx<T>::type* __restrict__ g1) {
-  const double down = ldexp(1.0, -prm->fix_shift);
-  const int64_t count = D == 1 ? (int64_t)prm->L : (int64_t)prm->nodes * prm->L;
-  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < count; e += (int64_t)gridDim.x * blockDim.x) {
-    const long long* c = acc + 4 * e;
-    typename Cx<T>::type a, b;
-    a.x = (T)((double)c[0] * down);
-    a.y = (T)((double)c[1] * down);
-    b.x = (T)((double)c[2] * down);
-    b.y = (T)((double)c[3] * down);
-    g0[e] = a;
-    g1[e] = b;
+__device__ __forceinline__ uint32_t fft_smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// The row into shared memory with one bulk copy (TMA engine) completing on an
+// mbarrier; the wait is bounded: on timeout *fault is raised and false returned.
+__device__ __forceinline__ bool fft_load_row(void* smem_dst, const void* gsrc, uint32_t bytes, uint64_t* bar,
+                                             int* fault) {
+  const uint32_t b = fft_smem_addr(bar);
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(b) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-}
-
-template <class T, int D>
-__global__ void kernel_grid_kernel(const FitParams<T>* __restrict__ prm, typename Cx<T>::type* __restrict__ g) {
-  const int L = prm->L;
-  const T spacing = prm->spacing;
-  const int64_t total = D == 1 ? L : (int64_t)L * L;
-  for (int64_t flat = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; flat < total;
-       flat += (int64_t)gridDim.x * blockDim.x) {
-    T sq = T(0);
-    int64_t rem = flat;
-#pragma unroll
-    for (int a = 0; a < D; ++a) {
-      const int64_t coord = rem % L;
-      rem /= L;
-      const int64_t lag = coord <= L / 2 ? coord : coord - L;
-      const T disp = spacing * (T)(double)lag;
-      sq = sq + disp * disp;
-    }
-    const T cauchy = T(1) / (T(1) + sq);
-    typename Cx<T>::type v;
-    v.x = cauchy * cauchy;
-    v.y = T(0);
-    g[flat] = v;
-  }
-}
-
-template <class T>
-__global__ void take_real_scaled_kernel(const typename Cx<T>::type* __restrict__ g, const FitParams<T>* __restrict__ prm,
-                                        int D, T* __restrict__ khat) {
-  const int L = prm->L;
-  const int64_t total = D == 1 ? (int64_t)L : (int64_t)L * L;
-  const T inv_total = T(1) / (T)(D == 1 ? (double)L : (double)L * (double)L);
-  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x)
-    khat[e] = g[e].x * inv_total;
-}
-
-template <class T>
-__global__ void multiply_kernel(typename Cx<T>::type* __restrict__ a, typename Cx<T>::type* __restrict__ b,
-                                const T* __restrict__ khat, const FitParams<T>* __restrict__ prm, int D) {
-  const int64_t total = D == 1 ? (int64_t)prm->L : (int64_t)prm->L * prm->L;
-  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
-    const T k = khat[e];
-    typename Cx<T>::type u = a[e], v = b[e];
-    u.x *= k;
-    u.y *= k;
-    v.x *= k;
-    v.y *= k;
-    a[e] = u;
-    b[e] = v;
-  }
-}
-
-// Power-of-two FFT of rows of length L (from the parameters) held in shared
-// memory, row b at data + b L; rows: 0 -> L rows, 1 -> `nodes` rows, 2 -> one
-// row. tw holds the twiddles of a cap_L transform (L divides cap_L).
-template <class T>
-__global__ void fft_rows_kernel(typename Cx<T>::type* __restrict__ data, const FitParams<T>* __restrict__ prm,
-                                int rows_sel, const typename Cx<T>::type* __restrict__ tw, int cap_L, int inverse) {
-  typedef typename Cx<T>::type T2;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int L = prm->L;
-  const int rows = rows_sel == 0 ? L : (rows_sel == 1 ? prm->nodes : 1);
-  if ((int)blockIdx.x >= rows) return;
-  int log2L = 0;
-  while ((1 << log2L) < L) ++log2L;
-  const int tws = cap_L / L;
-  T2* s = reinterpret_cast<T2*>(smem_raw);
-  T2* d = data + (int64_t)blockIdx.x * L;
-  for (int i = threadIdx.x; i < L; i += blockDim.x) s[__brev((unsigned)i) >> (32 - log2L)] = d[i];
   __syncthreads();
-  // Stages lg and lg + 1 together (radix 2^2): a group of 4h elements, h =
-  // 2^(lg-1), passes through both butterfly stages in registers, one shared
-  // memory round trip and one barrier per two stages. Stage lg uses
-  // W_2h^pos for both of its pairs; stage lg + 1 uses W_4h^pos and
-  // W_4h^(pos+h) = W_4h^pos * W_4^1, an exact quarter turn.
-  int lg = 1;
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(b), "r"(bytes) : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     fft_smem_addr(smem_dst)),
+                 "l"(gsrc), "r"(bytes), "r"(b)
+                 : "memory");
+  }
+  long long spins = 0;
+  for (;;) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n\tselp.u32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(ok)
+        : "r"(b)
+        : "memory");
+    if (ok) return true;
+    if (++spins >= (1LL << 24)) {
+      atomicExch(fault, 1);
+      return false;
+    }
+  }
+}
+
+// Fixed-point charges -> the two packed complex grids: the first `nodes`
+// entries of the rows < nodes (one row for D = 1) with row stride L, the
+// cells the spread can reach; each cell is cleared after reading, so the
+// accumulator is zero again for the next spread.
+template <class T, int D>
+__global__ void charges_kernel(long long* __restrict__ acc, const FitParams<T>* __restrict__ prm,
+                               typename Cx<T>::type* __restrict__ g0, typename Cx<T>::type* __restrict__ g1) {
+  const double down = ldexp(1.0, -prm->fix_shift);
+  const int L = prm->L, nodes = prm->nodes;
+  const int64_t count = (int64_t)(D == 1 ? 1 : nodes) * nodes;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < count; e += (int64_t)gridDim.x * blockDim.x) {
+    const int r = (int)(e / nodes), c = (int)(e - (int64_t)r * nodes);
+    const int64_t flat = (int64_t)r * L + c;
+    longlong2* cell = reinterpret_cast<longlong2*>(acc + 4 * flat);
+    const longlong2 p = cell[0], q = cell[1];
+    cell[0] = make_longlong2(0, 0);
+    cell[1] = make_longlong2(0, 0);
+    typename Cx<T>::type a, b;
+    a.x = (T)((double)p.x * down);
+    a.y = (T)((double)p.y * down);
+    b.x = (T)((double)q.x * down);
+    b.y = (T)((double)q.y * down);
+    g0[flat] = a;
+    g1[flat] = b;
+  }
+}
+
+// Stages of a power-of-two transform of length L = 2^log2L in place in
+// shared memory. Forward transforms are decimation in frequency (natural order
+// in, bit-reversed spectrum out), inverse transforms decimation in time (bit-
+// reversed in, natural out): no reordering pass exists, every spectrum (the
+// Cauchy kernel's included) is held in the same bit-reversed layout, and
+// pointwise products are unaffected. Stages of span >= 64 run in shared memory
+// two at a time (radix 2^2: four elements through both stages in registers),
+// where consecutive lanes touch consecutive elements; stages of span <= 32 run
+// in registers across a warp with shuffles (lane l holds element 32 g + l).
+// tw holds W_cap^k for k < cap / 2 and tws = cap / L.
+
+// DIF stages of spans L .. 2^(small + 1), ending with a barrier.
+template <class T2>
+__device__ __forceinline__ void dif_smem_stages(T2* s, int L, int log2L, int small, const T2* __restrict__ tw,
+                                                int tws) {
+  int lg = log2L;
+  if (((log2L - small) & 1) != 0) {
+    // one radix-2 stage of span L
+    const int half = L >> 1;
+#pragma unroll 2
+    for (int b = threadIdx.x; b < half; b += blockDim.x) {
+      const T2 a = s[b], c = s[b + half];
+      s[b] = cadd(a, c);
+      s[b + half] = cmul(csub(a, c), tw[b * tws]);
+    }
+    __syncthreads();
+    lg -= 1;
+  }
+  for (; lg - 1 > small; lg -= 2) {
+    // stages of spans S = 2^lg and S/2: quarter q = S/4
+    const int q = 1 << (lg - 2);
+    const int st1 = (L >> lg) * tws, st2 = (L >> (lg - 1)) * tws;
+#pragma unroll 2
+    for (int b = threadIdx.x; b < (L >> 2); b += blockDim.x) {
+      const int pos = b & (q - 1);
+      const int i = ((b >> (lg - 2)) << lg) + pos;
+      const T2 wa = tw[pos * st1];  // W_S^pos
+      T2 wb;                         // W_S^(pos+q) = W_S^pos * (-i)
+      wb.x = wa.y;
+      wb.y = -wa.x;
+      const T2 wc = tw[pos * st2];  // W_(S/2)^pos
+      const T2 x0 = s[i], x1 = s[i + q], x2 = s[i + 2 * q], x3 = s[i + 3 * q];
+      const T2 y0 = cadd(x0, x2), y2 = cmul(csub(x0, x2), wa);
+      const T2 y1 = cadd(x1, x3), y3 = cmul(csub(x1, x3), wb);
+      s[i] = cadd(y0, y1);
+      s[i + q] = cmul(csub(y0, y1), wc);
+      s[i + 2 * q] = cadd(y2, y3);
+      s[i + 3 * q] = cmul(csub(y2, y3), wc);
+    }
+    __syncthreads();
+  }
+}
+
+// DIT stages (conjugate twiddles) of spans 2^(small + 1) .. L, each pass
+// ending with a barrier. Stages lg and lg + 1 together: a group of 4h
+// elements, h = 2^(lg-1); stage lg uses W_2h^pos for both of its pairs,
+// stage lg + 1 uses W_4h^pos and W_4h^(pos+h) = W_4h^pos * W_4^1, an exact
+// quarter turn.
+template <class T2>
+__device__ __forceinline__ void dit_smem_stages(T2* s, int L, int log2L, int small, const T2* __restrict__ tw,
+                                                int tws) {
+  int lg = small + 1;
   for (; lg + 1 <= log2L; lg += 2) {
     const int h = 1 << (lg - 1);
     const int st1 = (L >> lg) * tws, st2 = (L >> (lg + 1)) * tws;
+#pragma unroll 2
     for (int b = threadIdx.x; b < (L >> 2); b += blockDim.x) {
       const int pos = b & (h - 1);
       const int i = ((b >> (lg - 1)) << (lg + 1)) + pos;
       T2 w1 = tw[pos * st1];
       T2 w2 = tw[pos * st2];
-      if (inverse) {
-        w1.y = -w1.y;
-        w2.y = -w2.y;
-      }
-      T2 w3;
-      if (inverse) {
-        w3.x = -w2.y;
-        w3.y = w2.x;
-      } else {
-        w3.x = w2.y;
-        w3.y = -w2.x;
-      }
+      w1.y = -w1.y;
+      w2.y = -w2.y;
+      T2 w3;  // conjugate quarter turn: W_4^-1 = +i
+      w3.x = -w2.y;
+      w3.y = w2.x;
       T2 x0 = s[i], x1 = s[i + h], x2 = s[i + 2 * h], x3 = s[i + 3 * h];
       T2 t = cmul(x1, w1);
-      x1.x = x0.x - t.x;
-      x1.y = x0.y - t.y;
-      x0.x = x0.x + t.x;
-      x0.y = x0.y + t.y;
+      x1 = csub(x0, t);
+      x0 = cadd(x0, t);
       t = cmul(x3, w1);
-      x3.x = x2.x - t.x;
-      x3.y = x2.y - t.y;
-      x2.x = x2.x + t.x;
-      x2.y = x2.y + t.y;
+      x3 = csub(x2, t);
+      x2 = cadd(x2, t);
       t = cmul(x2, w2);
-      T2 r;
-      r.x = x0.x + t.x;
-      r.y = x0.y + t.y;
-      s[i] = r;
-      r.x = x0.x - t.x;
-      r.y = x0.y - t.y;
-      s[i + 2 * h] = r;
+      s[i] = cadd(x0, t);
+      s[i + 2 * h] = csub(x0, t);
       t = cmul(x3, w3);
-      r.x = x1.x + t.x;
-      r.y = x1.y + t.y;
-      s[i + h] = r;
-      r.x = x1.x - t.x;
-      r.y = x1.y - t.y;
-      s[i + 3 * h] = r;
+      s[i + h] = cadd(x1, t);
+      s[i + 3 * h] = csub(x1, t);
     }
     __syncthreads();
   }
   for (; lg <= log2L; ++lg) {
     const int half = 1 << (lg - 1);
-    const int tstep = L >> lg;
+    const int tstep = (L >> lg) * tws;
+#pragma unroll 2
     for (int b = threadIdx.x; b < (L >> 1); b += blockDim.x) {
       const int pos = b & (half - 1);
       const int i = ((b >> (lg - 1)) << lg) + pos;
       const int j = i + half;
-      T2 w = tw[pos * tstep * tws];
-      if (inverse) w.y = -w.y;
+      T2 w = tw[pos * tstep];
+      w.y = -w.y;
       const T2 u = s[i];
       const T2 v = cmul(s[j], w);
-      T2 r0, r1;
-      r0.x = u.x + v.x;
-      r0.y = u.y + v.y;
-      r1.x = u.x - v.x;
-      r1.y = u.y - v.y;
-      s[i] = r0;
-      s[j] = r1;
+      s[i] = cadd(u, v);
+      s[j] = csub(u, v);
     }
     __syncthreads();
   }
+}
+
+// This lane's forward twiddle for each register stage k (span 2^k):
+// W_(2^k)^(lane mod 2^(k-1)).
+template <class T2>
+__device__ __forceinline__ void lane_twiddles(int lane, int L, int small, const T2* __restrict__ tw, int tws,
+                                              T2 (&w)[5]) {
+#pragma unroll
+  for (int k = 1; k <= 5; ++k) {
+    w[k - 1].x = 0;
+    w[k - 1].y = 0;
+    if (k <= small) w[k - 1] = tw[(lane & ((1 << (k - 1)) - 1)) * (L >> k) * tws];
+  }
+}
+
+// DIF spans 2^small .. 2 on one element per lane (forward twiddles w).
+template <class T2>
+__device__ __forceinline__ T2 dif_reg_stages(T2 x, int lane, int small, const T2 (&w)[5]) {
+#pragma unroll
+  for (int k = 5; k >= 1; --k) {
+    if (k > small) continue;
+    const int half = 1 << (k - 1);
+    const T2 o = shfl_xor2(x, half);
+    x = (lane & half) ? cmul(csub(o, x), w[k - 1]) : cadd(x, o);
+  }
+  return x;
+}
+
+// DIT spans 2 .. 2^small on one element per lane (w: forward twiddles, used
+// conjugated).
+template <class T2>
+__device__ __forceinline__ T2 dit_reg_stages(T2 x, int lane, int small, const T2 (&w)[5]) {
+#pragma unroll
+  for (int k = 1; k <= 5; ++k) {
+    if (k > small) continue;
+    const int half = 1 << (k - 1);
+    const bool up = (lane & half) != 0;
+    T2 wc = w[k - 1];
+    wc.y = -wc.y;
+    const T2 t = up ? cmul(x, wc) : x;
+    const T2 o = shfl_xor2(t, half);
+    x = up ? csub(o, t) : cadd(x, o);
+  }
+  return x;
+}
+
+// Source of a row entering a transform: 0 -> data (one bulk copy); 1 -> row
+// `row` of the squared Cauchy kernel over signed lags, computed in place (the
+// arithmetic of the reference's kernel build, src/tsne/interpolation.rs:198-
+// 226); 2 -> a charge row of data: its first `nodes` entries by bulk copy,
+// zeros after them. False when a bulk copy timed out.
+template <class T>
+__device__ __forceinline__ bool fft_fill_row(typename Cx<T>::type* s, const typename Cx<T>::type* d, int src, int row,
+                                             int L, int D, const FitParams<T>* __restrict__ prm, uint64_t* bar,
+                                             int* fault) {
+  typedef typename Cx<T>::type T2;
+  if (src == 0) return fft_load_row(s, d, (uint32_t)(L * sizeof(T2)), bar, fault);
+  if (src == 1) {
+    const T spacing = prm->spacing;
+    const int lr = row <= L / 2 ? row : row - L;
+    const T dr = spacing * (T)(double)lr;
+    for (int c = threadIdx.x; c < L; c += blockDim.x) {
+      const int lc = c <= L / 2 ? c : c - L;
+      const T dc = spacing * (T)(double)lc;
+      T sq = T(0);
+      sq = sq + dc * dc;
+      if (D == 2) sq = sq + dr * dr;
+      const T cauchy = T(1) / (T(1) + sq);
+      T2 v;
+      v.x = cauchy * cauchy;
+      v.y = T(0);
+      s[c] = v;
+    }
+  } else {
+    // the first `nodes` entries (rounded up to 16 bytes), zeros after them
+    const int nodes = prm->nodes;
+    const uint32_t bytes = ((uint32_t)(nodes * sizeof(T2)) + 15u) & ~15u;
+    if (!fft_load_row(s, d, bytes, bar, fault)) return false;
+    for (int c = nodes + (int)threadIdx.x; c < L; c += blockDim.x) {
+      T2 v;
+      v.x = T(0);
+      v.y = T(0);
+      s[c] = v;
+    }
+  }
+  __syncthreads();
+  return true;
+}
+
+constexpr int kFftThreads = 512;
+
+template <class T>
+struct FftRow {
+  typedef typename Cx<T>::type T2;
+  int L, log2L, small, G, ngroups, tws, lane, warp, nw;
+  bool lane_ok;
+  __device__ FftRow(int L_, int cap_L) : L(L_) {
+    log2L = 0;
+    while ((1 << log2L) < L) ++log2L;
+    small = log2L < 5 ? log2L : 5;
+    G = 1 << small;
+    ngroups = L >> small;
+    tws = cap_L / L;
+    lane = threadIdx.x & 31;
+    warp = threadIdx.x >> 5;
+    nw = blockDim.x >> 5;
+    lane_ok = lane < G;
+  }
+};
+
+// Rows of length L (from the parameters), row b at data + b L; rows: 0 -> L
+// rows, 1 -> `nodes` rows, 2 -> one row. The row arrives in shared memory by
+// one bulk copy.
+template <class T>
+__global__ void __launch_bounds__(kFftThreads) fft_rows_kernel(typename Cx<T>::type* __restrict__ data,
+                                                              const FitParams<T>* __restrict__ prm, int rows_sel,
+                                                              const typename Cx<T>::type* __restrict__ tw, int cap_L,
+                                                              int inverse, int* __restrict__ fault, int src,
+                                                              T* __restrict__ khat_out) {
+  typedef typename Cx<T>::type T2;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ uint64_t load_bar;
+  const int L = prm->L;
+  const int rows = rows_sel == 0 ? L : (rows_sel == 1 ? prm->nodes : 1);
+  if ((int)blockIdx.x >= rows) return;
+  const FftRow<T> r(L, cap_L);
+  T2* s = reinterpret_cast<T2*>(smem_raw);
+  T2* d = data + (int64_t)blockIdx.x * L;
+  T2 w[5];
+  lane_twiddles(r.lane, L, r.small, tw, r.tws, w);
+  T2 zero;
+  zero.x = T(0);
+  zero.y = T(0);
+  const int D = rows_sel == 2 ? 1 : 2;
+  if (!fft_fill_row<T>(s, d, inverse ? 0 : src, (int)blockIdx.x, L, D, prm, &load_bar, fault)) return;
+  if (!inverse) {
+    dif_smem_stages(s, L, r.log2L, r.small, tw, r.tws);
+    // khat_out: the real part scaled by 1 / L^D (the kernel spectrum)
+    const T inv_total = T(1) / (T)(D == 1 ? (double)L : (double)L * (double)L);
+    T* kr = khat_out ? khat_out + (int64_t)blockIdx.x * L : nullptr;
+    for (int g = r.warp; g < r.ngroups; g += r.nw) {
+      const T2 x = dif_reg_stages(r.lane_ok ? s[g * r.G + r.lane] : zero, r.lane, r.small, w);
+      if (r.lane_ok) {
+        if (kr) kr[g * r.G + r.lane] = x.x * inv_total;
+        else d[g * r.G + r.lane] = x;
+      }
+    }
+    return;
+  }
+  for (int g = r.warp; g < r.ngroups; g += r.nw) {
+    const T2 x = dit_reg_stages(r.lane_ok ? s[g * r.G + r.lane] : zero, r.lane, r.small, w);
+    if (r.lane_ok) s[g * r.G + r.lane] = x;
+  }
+  __syncthreads();
+  dit_smem_stages(s, L, r.log2L, r.small, tw, r.tws);
   for (int i = threadIdx.x; i < L; i += blockDim.x) d[i] = s[i];
+}
+
+// Convolution of rows with the kernel spectrum: forward transform, product
+// with the real spectrum row (khat, bit-reversed like the row), inverse
+// transform, in one pass over each row. The forward transform's last stages
+// and the inverse's first stages act on the same positions in registers, so
+// the product sits between them without a shared-memory round trip. Only the
+// first `nodes` entries of each output row are stored (all that is read
+// afterwards). rows_sel: 0 -> L rows (2-D, second axis), 2 -> one row (1-D).
+template <class T>
+__global__ void __launch_bounds__(kFftThreads) fft_conv_rows_kernel(typename Cx<T>::type* __restrict__ data,
+                                                                   const T* __restrict__ khat,
+                                                                   const FitParams<T>* __restrict__ prm, int rows_sel,
+                                                                   const typename Cx<T>::type* __restrict__ tw,
+                                                                   int cap_L, int* __restrict__ fault, int src) {
+  typedef typename Cx<T>::type T2;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ uint64_t load_bar;
+  const int L = prm->L;
+  const int rows = rows_sel == 0 ? L : 1;
+  if ((int)blockIdx.x >= rows) return;
+  const int keep = prm->nodes;
+  const FftRow<T> r(L, cap_L);
+  T2* s = reinterpret_cast<T2*>(smem_raw);
+  T2* d = data + (int64_t)blockIdx.x * L;
+  const T* kr = khat + (int64_t)blockIdx.x * L;
+  T2 w[5];
+  lane_twiddles(r.lane, L, r.small, tw, r.tws, w);
+  T2 zero;
+  zero.x = T(0);
+  zero.y = T(0);
+  if (!fft_fill_row<T>(s, d, src, (int)blockIdx.x, L, rows_sel == 2 ? 1 : 2, prm, &load_bar, fault)) return;
+  dif_smem_stages(s, L, r.log2L, r.small, tw, r.tws);
+  for (int g = r.warp; g < r.ngroups; g += r.nw) {
+    const int e = g * r.G + r.lane;
+    T2 x = dif_reg_stages(r.lane_ok ? s[e] : zero, r.lane, r.small, w);
+    const T k = r.lane_ok ? kr[e] : T(0);
+    x.x *= k;
+    x.y *= k;
+    x = dit_reg_stages(x, r.lane, r.small, w);
+    if (r.lane_ok) s[e] = x;
+  }
+  __syncthreads();
+  dit_smem_stages(s, L, r.log2L, r.small, tw, r.tws);
+  for (int i = threadIdx.x; i < keep; i += blockDim.x) d[i] = s[i];
 }
 
 // out[c][r] = in[r][c] for r < rows_in (zero for rows_in <= r < out_cols),
@@ -546,13 +771,28 @@ const typename FitWorkspace<T>::T2* FitWorkspace<T>::twiddles(int L, cudaStream_
   return tw.template as<T2>();
 }
 
+// src: 0 -> rows of `data`, 1 -> Cauchy kernel rows, 2 -> charge rows of
+// `data` (entries past `nodes` are zero); khat_out: write the scaled real part
+// there instead of the complex result (forward only).
 template <class T>
 static void fft_rows(FitWorkspace<T>& ws, typename Cx<T>::type* data, const FitParams<T>* dp, int rows_sel, int cap_L,
-                     bool inverse, cudaStream_t s) {
-  const int threads = std::min(512, std::max(32, cap_L / 2));
+                     bool inverse, cudaStream_t s, int src = 0, T* khat_out = nullptr) {
+  const int threads = std::min(kFftThreads, std::max(32, cap_L / 4));
   const size_t smem = (size_t)cap_L * sizeof(typename Cx<T>::type);
   const int grid = rows_sel == 2 ? 1 : cap_L;
-  fft_rows_kernel<T><<<grid, threads, smem, s>>>(data, dp, rows_sel, ws.twiddles(cap_L, s), cap_L, inverse ? 1 : 0);
+  fft_rows_kernel<T><<<grid, threads, smem, s>>>(data, dp, rows_sel, ws.twiddles(cap_L, s), cap_L, inverse ? 1 : 0,
+                                                  ws.flag.template as<int>() + 1, src, khat_out);
+  BHG_LAUNCH_CHECK();
+}
+
+template <class T>
+static void fft_conv_rows(FitWorkspace<T>& ws, typename Cx<T>::type* data, const T* khat, const FitParams<T>* dp,
+                          int rows_sel, int cap_L, cudaStream_t s, int src = 0) {
+  const int threads = std::min(kFftThreads, std::max(32, cap_L / 4));
+  const size_t smem = (size_t)cap_L * sizeof(typename Cx<T>::type);
+  const int grid = rows_sel == 2 ? 1 : cap_L;
+  fft_conv_rows_kernel<T><<<grid, threads, smem, s>>>(data, khat, dp, rows_sel, ws.twiddles(cap_L, s), cap_L,
+                                                       ws.flag.template as<int>() + 1, src);
   BHG_LAUNCH_CHECK();
 }
 
@@ -577,12 +817,16 @@ void FitWorkspace<T>::reserve(int D, int64_t n, int cap) {
   khat.ensure(total * sizeof(T));
   // the spread reaches rows < nodes <= cap / 2 of an L <= cap grid
   const int64_t cells = D == 1 ? (int64_t)cap : (int64_t)(cap / 2 + 1) * cap;
+  const size_t acc_before = acc.bytes;
   acc.ensure((size_t)cells * 4 * sizeof(long long));
+  if (acc.bytes != acc_before) acc_clean = nullptr;  // new memory: cleared before its first spread
   zpart.ensure((ceil_div(std::max<int64_t>(n, 1), 256) + 1) * sizeof(double));
   flag.ensure(64);
   done.ensure(64);
-  if ((size_t)cap * sizeof(C2) > 48 * 1024)  // set outside any stream capture
+  if ((size_t)cap * sizeof(C2) > 48 * 1024) {  // set outside any stream capture
     BHG_CUDA(cudaFuncSetAttribute(fft_rows_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    BHG_CUDA(cudaFuncSetAttribute(fft_conv_rows_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+  }
   cap_L = cap;
 }
 
@@ -613,64 +857,52 @@ void fit_repulsion_cap(FitWorkspace<T>& ws, int D, const T* y, int64_t n, const 
   T2* h0 = ws.h0.template as<T2>();
   T2* h1 = ws.h1.template as<T2>();
   T* khat = ws.khat.template as<T>();
-  const int64_t cap_total = D == 1 ? (int64_t)cap : (int64_t)cap * cap;
-  const int eb = (int)std::min<int64_t>(ceil_div(cap_total, 256), 4 * 152);
 
-  // kernel spectrum (real, pre-scaled by 1/L^D); symmetric in its axes, so it
-  // serves the transposed spectrum layout unchanged.
-  if (D == 1) kernel_grid_kernel<T, 1><<<eb, 256, 0, s>>>(dp, g0);
-  else kernel_grid_kernel<T, 2><<<eb, 256, 0, s>>>(dp, g0);
-  BHG_LAUNCH_CHECK();
+  // kernel spectrum (real, pre-scaled by 1/L^D): the kernel rows are made in
+  // the first transform and the last one writes the scaled real part. It is
+  // symmetric in its axes, so it serves the transposed spectrum layout.
   if (D == 1) {
-    fft_rows<T>(ws, g0, dp, 2, cap, false, s);
-    take_real_scaled_kernel<T><<<eb, 256, 0, s>>>(g0, dp, D, khat);
+    fft_rows<T>(ws, g0, dp, 2, cap, false, s, 1, khat);
   } else {
-    fft_rows<T>(ws, g0, dp, 0, cap, false, s);
+    fft_rows<T>(ws, g0, dp, 0, cap, false, s, 1);
     transpose<T>(g0, dp, 0, 0, h0, cap, s);
-    fft_rows<T>(ws, h0, dp, 0, cap, false, s);
-    take_real_scaled_kernel<T><<<eb, 256, 0, s>>>(h0, dp, D, khat);
+    fft_rows<T>(ws, h0, dp, 0, cap, false, s, 0, khat);
   }
-  BHG_LAUNCH_CHECK();
 
-  // charges: zero the rows that receive them, spread
+  // charges: spread into the fixed-point accumulator; charges_kernel converts
+  // and clears the cells the spread can reach (so the accumulator is zeroed
+  // here only when newly allocated)
   long long* acc = ws.acc.template as<long long>();
-  const int64_t cap_cells = D == 1 ? (int64_t)cap : (int64_t)(cap / 2 + 1) * cap;
-  const unsigned cb = (unsigned)std::min<int64_t>(ceil_div(cap_cells, 256), 4 * 152);
-  if (D == 1) zero_acc_kernel<T, 1><<<cb, 256, 0, s>>>(acc, dp);
-  else zero_acc_kernel<T, 2><<<cb, 256, 0, s>>>(acc, dp);
-  BHG_LAUNCH_CHECK();
+  if (ws.acc_clean != ws.acc.ptr) {
+    BHG_CUDA(cudaMemsetAsync(ws.acc.ptr, 0, ws.acc.bytes, s));
+    ws.acc_clean = ws.acc.ptr;
+  }
   if (n > 0) {
     if (D == 1) spread_kernel<T, 1><<<(unsigned)ceil_div(n, 256), 256, 0, s>>>(y, n, dp, acc);
     else spread_kernel<T, 2><<<(unsigned)ceil_div(n, 256), 256, 0, s>>>(y, n, dp, acc);
     BHG_LAUNCH_CHECK();
   }
-  if (D == 1) unfix_kernel<T, 1><<<cb, 256, 0, s>>>(acc, dp, g0, g1);
-  else unfix_kernel<T, 2><<<cb, 256, 0, s>>>(acc, dp, g0, g1);
+
+  if (D == 1) charges_kernel<T, 1><<<4 * 152, 256, 0, s>>>(acc, dp, g0, g1);
+  else charges_kernel<T, 2><<<4 * 152, 256, 0, s>>>(acc, dp, g0, g1);
   BHG_LAUNCH_CHECK();
 
   T2 *r0, *r1;
   if (D == 1) {
-    fft_rows<T>(ws, g0, dp, 2, cap, false, s);
-    fft_rows<T>(ws, g1, dp, 2, cap, false, s);
-    multiply_kernel<T><<<eb, 256, 0, s>>>(g0, g1, khat, dp, D);
-    BHG_LAUNCH_CHECK();
-    fft_rows<T>(ws, g0, dp, 2, cap, true, s);
-    fft_rows<T>(ws, g1, dp, 2, cap, true, s);
+    fft_conv_rows<T>(ws, g0, khat, dp, 2, cap, s, 2);
+    fft_conv_rows<T>(ws, g1, khat, dp, 2, cap, s, 2);
     r0 = g0;
     r1 = g1;
   } else {
     // forward: rows n0 < nodes, transpose to [k1][n0], rows over n0
-    fft_rows<T>(ws, g0, dp, 1, cap, false, s);
-    fft_rows<T>(ws, g1, dp, 1, cap, false, s);
+    fft_rows<T>(ws, g0, dp, 1, cap, false, s, 2);
+    fft_rows<T>(ws, g1, dp, 1, cap, false, s, 2);
     transpose<T>(g0, dp, 1, 0, h0, cap, s);
     transpose<T>(g1, dp, 1, 0, h1, cap, s);
-    fft_rows<T>(ws, h0, dp, 0, cap, false, s);
-    fft_rows<T>(ws, h1, dp, 0, cap, false, s);
-    multiply_kernel<T><<<eb, 256, 0, s>>>(h0, h1, khat, dp, D);
-    BHG_LAUNCH_CHECK();
-    // inverse: rows over k0, transpose back (rows n0 < nodes only), rows over k1
-    fft_rows<T>(ws, h0, dp, 0, cap, true, s);
-    fft_rows<T>(ws, h1, dp, 0, cap, true, s);
+    // product with the kernel spectrum and inverse over k0 (columns n0 <
+    // nodes kept), transpose back, rows over k1
+    fft_conv_rows<T>(ws, h0, khat, dp, 0, cap, s);
+    fft_conv_rows<T>(ws, h1, khat, dp, 0, cap, s);
     transpose<T>(h0, dp, 0, 1, g0, cap, s);
     transpose<T>(h1, dp, 0, 1, g1, cap, s);
     fft_rows<T>(ws, g0, dp, 1, cap, true, s);
@@ -703,10 +935,14 @@ FitGrid fit_repulsion(FitWorkspace<T>& ws, int D, const T* y, int64_t n, const B
   const int L = fit_needed_length<T>(ws, D, n, box, s);
   if (ws.cap_L < L) ws.reserve(D, n, L);
   else ws.reserve(D, n, ws.cap_L);
+  BHG_CUDA(cudaMemsetAsync(ws.flag.template as<int>() + 1, 0, sizeof(int), s));
   fit_repulsion_cap<T>(ws, D, y, n, box, neg, z_out, s);
   FitParams<T> hp;
+  int fault = 0;
   BHG_CUDA(cudaMemcpyAsync(&hp, ws.params.ptr, sizeof(hp), cudaMemcpyDeviceToHost, s));
+  BHG_CUDA(cudaMemcpyAsync(&fault, ws.flag.template as<int>() + 1, sizeof(int), cudaMemcpyDeviceToHost, s));
   BHG_CUDA(cudaStreamSynchronize(s));
+  if (fault) throw Error(ST_ETIMEDOUT, "error: an FFT row load timed out.");
   FitGrid fg;
   fg.boxes = hp.boxes;
   fg.nodes = hp.nodes;

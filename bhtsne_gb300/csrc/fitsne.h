@@ -28,6 +28,7 @@ struct FitWorkspace {
   typedef typename std::conditional<sizeof(T) == 4, float2, double2>::type T2;
   DevBuf params, g0, g1, h0, h1, khat, tw, zpart, done, acc, flag;
   int tw_len = 0;
+  const void* acc_clean = nullptr;  // acc allocation known to be all zero
   int cap_L = 0;  // transform length the buffers hold
   bool done_zeroed = false;
   const T2* twiddles(int L, cudaStream_t s);
