@@ -248,6 +248,7 @@ def run_ours(args):
     cpu = None
     if rank == 0 and not args.no_cpu:
         cpu = cpu_baseline_sample(aff, emb.reshape(n, 2), args.cpu_epochs)
+    configs = run_configs(args, ctx, aff, rank) if args.configs else None
 
     out = {
         "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": ws, "steps": args.steps,
@@ -273,8 +274,140 @@ def run_ours(args):
         out["serving"] = serving
     if cpu:
         out["cpu_baseline"] = cpu
+    if configs:
+        out["configs"] = configs
     if rank == 0:
         print(json.dumps(out))
+
+
+def make_c1_workload(n=5000, dim=50, seed=1001):
+    """10 equal-weight isotropic components, means ~ N(0, 10^2 I), unit variance."""
+    rng = np.random.default_rng(seed)
+    centres = rng.normal(0.0, 10.0, size=(10, dim))
+    lab = rng.integers(0, 10, size=n)
+    return (centres[lab] + rng.normal(size=(n, dim))).astype(np.float32)
+
+
+def make_c2_workload(n=70_000, dim=20, seed=1002):
+    """10 anisotropic clusters (per-axis std 1/sqrt(i+1)), centres ~ N(0, 5^2 I),
+    weights ~ Dirichlet(2 * 1_10): the shape of MNIST after PCA to 20."""
+    rng = np.random.default_rng(seed)
+    centres = rng.normal(0.0, 5.0, size=(10, dim))
+    w = rng.dirichlet(np.full(10, 2.0))
+    lab = rng.choice(10, size=n, p=w)
+    std = 1.0 / np.sqrt(np.arange(dim) + 1.0)
+    return (centres[lab] + rng.normal(size=(n, dim)) * std).astype(np.float32)
+
+
+def exact_gradient_f64(y, rows, cols, vals):
+    """The t-SNE gradient direction pos - neg / Z of the sparse-P objective in
+    FP64, all pairs (O(N^2), small N): pos_i = sum_j p_ij q_ij (y_i - y_j),
+    neg_i = sum_{j != i} q_ij^2 (y_i - y_j), Z = sum_{i != j} q_ij. Returns
+    (pos, neg / Z)."""
+    y = y.astype(np.float64)
+    n, D = y.shape
+    r = np.repeat(np.arange(n), np.diff(rows.astype(np.int64)))
+    d = y[r] - y[cols.astype(np.int64)]
+    q = 1.0 / (1.0 + (d * d).sum(1))
+    pos = np.zeros_like(y)
+    np.add.at(pos, r, (vals.astype(np.float64) * q)[:, None] * d)
+    neg = np.zeros_like(y)
+    z = 0.0
+    for a in range(0, n, 1024):
+        diff = y[a:a + 1024, None, :] - y[None, :, :]
+        qq = 1.0 / (1.0 + (diff * diff).sum(2))
+        idx = np.arange(a, min(a + 1024, n))
+        qq[idx - a, idx] = 0.0
+        z += qq.sum()
+        neg[a:a + 1024] = ((qq * qq)[:, :, None] * diff).sum(1)
+    return pos, neg / z
+
+
+def rel_l2(a, b):
+    return float(np.linalg.norm(np.asarray(a, np.float64) - b) / np.linalg.norm(b))
+
+
+def timed_epochs(t, args):
+    """Burn-in, warm-up, then args.steps timed epochs (graph replay) and a
+    profiled pass for the phase split; returns epochs/s and phases (ms)."""
+    t.advance(args.burn_in)
+    t.advance(args.warmup)
+    t.advance(args.steps)
+    ms = t.timings()["loop_ms"] / args.steps
+    t.profile(True)
+    t.advance(10)
+    ph = t.phase_times()
+    t.profile(False)
+    return round(1e3 / ms, 3), {k: round(v / 10, 4) for k, v in ph.items() if k != "epochs"}
+
+
+def run_configs(args, ctx, aff, rank):
+    """The other configurations of the path, each measured here: 1M points in
+    3-D Barnes-Hut and 2-D FIt-SNE (on the 1M affinities), the 70k MNIST-shape
+    fits, and the 5k error against an FP64 all-pairs gradient."""
+    import bhtsne_gb300 as bg
+    out = {}
+    n = aff.rows.size - 1
+    for name, D, method in (("bh3d_1M", 3, "bh"), ("fitsne2d_1M", 2, "fit")):
+        t = bg.TSNE(n, D=D, ctx=ctx).with_affinities(aff).epochs(0).random_seed(42)
+        t.barnes_hut(0.5) if method == "bh" else t.fit_sne()
+        eps, ph = timed_epochs(t, args)
+        out[name] = {"epochs_per_s": eps, "phase_ms_per_epoch": ph, "burn_in_epochs": args.burn_in,
+                     "steps": args.steps, "note": "affinities of the 1M bh2d workload"}
+        del t
+
+    X2 = make_c2_workload()
+    c2 = {"workload": "70k x 20, 10 anisotropic clusters, Dirichlet(2) weights, perplexity 30, 2-D, 1000 epochs"}
+    for method in ("bh", "fit"):
+        t = bg.TSNE(X2, D=2, ctx=ctx).perplexity(30).epochs(1000).random_seed(7)
+        w0 = time.perf_counter()
+        t.barnes_hut(0.5) if method == "bh" else t.fit_sne()
+        emb = t.embedding()
+        wall = time.perf_counter() - w0
+        tm = t.timings()
+        c2[method] = {"fit_s": round(wall, 3), "setup_ms": round(tm["affinity_ms"], 1),
+                      "epochs_per_s": round(1e3 * tm["loop_epochs"] / tm["loop_ms"], 2),
+                      "kl": round(t.kl_divergence(True), 5)}
+        if method == "bh":
+            c2_aff, c2_y = t.affinities(), emb.reshape(-1, 2)
+    if rank == 0 and not args.no_cpu:
+        from oracle import pyoracle as O
+        O.build()
+        O.set_threads(os.cpu_count() or 1)
+        h = O.TSNE(X2.shape[0]).epochs(20).initial_embedding(c2_y)
+        h.with_affinities(c2_aff.rows, c2_aff.columns, c2_aff.values, c2_aff.perplexity)
+        w0 = time.perf_counter()
+        h.barnes_hut(0.5, np.zeros((X2.shape[0], 1), np.float32))
+        c2["cpu_bh_epochs_per_s"] = round(20 / (time.perf_counter() - w0), 3)
+        c2["cpu_cores"] = os.cpu_count() or 1
+    out["c2_70k"] = c2
+
+    # C1: the gradient at a fixed Y against FP64 all pairs. At epoch 100 (P
+    # exaggerated x12, the embedding still moving) the full direction pos -
+    # neg / Z; at the converged embedding of epoch 1000 pos and neg / Z nearly
+    # cancel, so there the approximated term neg / Z is compared.
+    X1 = make_c1_workload()
+    t = bg.TSNE(X1, D=2, ctx=ctx).perplexity(30).epochs(100).random_seed(5)
+    t.barnes_hut(0.5)
+    y100 = t.embedding().reshape(-1, 2)
+    t.advance(900)
+    y1000 = t.embedding().reshape(-1, 2)
+    a1 = t.affinities()
+    vals = a1.values.astype(np.float64)
+    vals = vals / vals.sum()
+    acc = {"workload": "5k x 50, 10 components, perplexity 30; Y of a Barnes-Hut fit at epochs 100 and 1000",
+           "reference": "FP64 all pairs"}
+    cases = (("epoch_100_gradient", y100, (12.0 * vals).astype(np.float32)),
+             ("epoch_1000_repulsion", y1000, vals.astype(np.float32)))
+    for label, yy, pv in cases:
+        p64, r64 = exact_gradient_f64(yy, a1.rows, a1.columns, pv)
+        for name, m in (("bh_theta_0.5_f32", bg.METHOD_BARNES_HUT), ("fitsne_f32", bg.METHOD_FIT_SNE)):
+            pos, neg, z = bg.gradient(m, yy, a1.rows, a1.columns, pv, theta=0.5, ctx=ctx)
+            rep = neg.astype(np.float64) / z
+            err = rel_l2(pos.astype(np.float64) - rep, p64 - r64) if label.endswith("gradient") else rel_l2(rep, r64)
+            acc.setdefault(label, {})[name] = round(err, 6)
+    out["c1_5k_vs_fp64_exact"] = acc
+    return out
 
 
 def make_batch_workload(jobs=512, dim=32, seed=2024):
@@ -473,6 +606,26 @@ def run_reference(args):
     print(json.dumps(out))
 
 
+def run_fft_only(args):
+    """FIt-SNE repulsion alone (spread, transforms, gather) for --n points
+    spread uniformly over [-700, 700]^2: the 1000-box cap, transforms of
+    length 8192. --warmup untimed calls, then --steps timed ones."""
+    import bhtsne_gb300 as bg
+    ctx = bg.Context(0)
+    y = np.random.default_rng(args.seed).uniform(-700, 700, size=(args.n, 2)).astype(np.float32)
+    rows = np.zeros(args.n + 1, np.uint64)
+    empty_c, empty_v = np.zeros(0, np.uint32), np.zeros(0, np.float32)
+    for _ in range(args.warmup):
+        bg.gradient(bg.METHOD_FIT_SNE, y, rows, empty_c, empty_v, ctx=ctx)
+    w0 = time.perf_counter()
+    for _ in range(args.steps):
+        bg.gradient(bg.METHOD_FIT_SNE, y, rows, empty_c, empty_v, ctx=ctx)
+    ms = 1e3 * (time.perf_counter() - w0) / args.steps
+    print(json.dumps({"fft_only": {"n_points": args.n, "grid": "1000 boxes per axis, L = 8192",
+                                   "ms_per_call": round(ms, 3),
+                                   "note": "host wall time per call, including the copies of y in and forces out"}}))
+
+
 def run_knn_only(args):
     """The affinity build's kNN alone on the 1M workload's distribution at --n
     points (k = 90): a 2,000-row warm-up call, then all rows, timed on the host."""
@@ -504,7 +657,13 @@ def main():
     ap.add_argument("--serve-rate", type=float, default=64.0, help="Poisson arrivals per second")
     ap.add_argument("--serve-fit-workers", type=int, default=8, help="server streams for FIt-SNE requests")
     ap.add_argument("--knn-only", action="store_true", help="time only the kNN of the workload at --n points")
+    ap.add_argument("--fft-only", action="store_true",
+                    help="time only the FIt-SNE repulsion of --n points at the largest grid")
+    ap.add_argument("--no-configs", dest="configs", action="store_false",
+                    help="skip the other configurations (3-D, FIt-SNE, 70k, 5k accuracy)")
     args = ap.parse_args()
+    if args.fft_only:
+        return run_fft_only(args)
     if args.knn_only:
         run_knn_only(args)
         return

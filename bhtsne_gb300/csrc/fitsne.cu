@@ -312,10 +312,11 @@ template <class T, int D>
 __global__ void charges_kernel(long long* __restrict__ acc, const FitParams<T>* __restrict__ prm,
                                typename Cx<T>::type* __restrict__ g0, typename Cx<T>::type* __restrict__ g1) {
   const double down = ldexp(1.0, -prm->fix_shift);
-  const int L = prm->L, nodes = prm->nodes;
-  const int64_t count = (int64_t)(D == 1 ? 1 : nodes) * nodes;
-  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < count; e += (int64_t)gridDim.x * blockDim.x) {
-    const int r = (int)(e / nodes), c = (int)(e - (int64_t)r * nodes);
+  const int L = prm->L;
+  const unsigned nodes = (unsigned)prm->nodes;
+  const unsigned count = (D == 1 ? 1u : nodes) * nodes;  // <= 3000^2
+  for (unsigned e = blockIdx.x * blockDim.x + threadIdx.x; e < count; e += gridDim.x * blockDim.x) {
+    const unsigned r = e / nodes, c = e - r * nodes;
     const int64_t flat = (int64_t)r * L + c;
     longlong2* cell = reinterpret_cast<longlong2*>(acc + 4 * flat);
     const longlong2 p = cell[0], q = cell[1];
