@@ -129,10 +129,6 @@ __global__ void match_neighbors_kernel(const uint64_t* __restrict__ rows, const 
   if ((int64_t)(t - s) != k || cols[s + j] != idx[e]) *mismatch = 1;
 }
 
-uint64_t lcg_next(uint64_t& s) {
-  s = s * 6364136223846793005ULL + 1442695040888963407ULL;
-  return s;
-}
 
 }  // namespace
 
@@ -260,17 +256,6 @@ T resolve_lr(const bhtsne_tsne* t) {
   return a > (T)50.0 ? a : (T)50.0;
 }
 
-template <class T>
-void host_random_init(const bhtsne_tsne* t, std::vector<T>& y) {
-  uint64_t s = t->seed;
-  for (size_t e = 0; e < y.size(); e += 2) {
-    const double u1 = ((lcg_next(s) >> 11) + 0.5) * (1.0 / 9007199254740992.0);
-    const double u2 = ((lcg_next(s) >> 11) + 0.5) * (1.0 / 9007199254740992.0);
-    const double r = std::sqrt(-2.0 * std::log(u1));
-    y[e] = (T)(1e-4 * r * std::cos(2 * M_PI * u2));
-    if (e + 1 < y.size()) y[e + 1] = (T)(1e-4 * r * std::sin(2 * M_PI * u2));
-  }
-}
 
 // finalize_p_and_seed: src/lib.rs:663-685 (plus the optimisation buffers that
 // the reference resizes in build_affinities / prepare_cached).
@@ -296,10 +281,7 @@ void finalize_p_and_seed(bhtsne_tsne* t, bool dense) {
     BHG_CUDA(cudaStreamSynchronize(s));
     t->init.clear();
   } else {
-    std::vector<T> h(ge);
-    host_random_init<T>(t, h);
-    BHG_CUDA(cudaMemcpyAsync(S.y.ptr, h.data(), ge * sizeof(T), cudaMemcpyHostToDevice, s));
-    BHG_CUDA(cudaStreamSynchronize(s));
+    launch_random_init<T>(S.y.template as<T>(), ge, t->seed, s);
   }
   S.uy.ensure(ge * sizeof(T));
   S.gains.ensure(ge * sizeof(T));
@@ -1558,23 +1540,17 @@ void batch_fit(bhtsne_batch* b) {
   upload<T>(B.d_off, B.off.data(), B.off.size() * 8, s);
   B.tiles.build(B.off, s);
   // seeds, velocity, gains, per-job learning rate and momentum
-  std::vector<T> yh((size_t)total * D);
+  const size_t ybytes = (size_t)total * D * sizeof(T);
+  T* yd = static_cast<T*>(B.y.ensure(ybytes));
   std::vector<T> lrh(B.K), momh(B.K, (T)P.momentum);
   for (int j = 0; j < B.K; ++j) {
     BatchJob<T>& J = *B.jobs[j];
-    T* dst = yh.data() + B.off[j] * D;
+    T* dst = yd + B.off[j] * D;
     if (J.has_init) {
-      std::copy(J.init.begin(), J.init.end(), dst);
+      BHG_CUDA(cudaMemcpyAsync(dst, J.init.data(), J.init.size() * sizeof(T), cudaMemcpyHostToDevice, s));
       J.has_init = false;
     } else {
-      uint64_t sd = P.seed + (uint64_t)j;
-      for (int64_t e = 0; e < J.n * D; e += 2) {
-        const double u1 = ((lcg_next(sd) >> 11) + 0.5) * (1.0 / 9007199254740992.0);
-        const double u2 = ((lcg_next(sd) >> 11) + 0.5) * (1.0 / 9007199254740992.0);
-        const double r = std::sqrt(-2.0 * std::log(u1));
-        dst[e] = (T)(1e-4 * r * std::cos(2 * M_PI * u2));
-        if (e + 1 < J.n * D) dst[e + 1] = (T)(1e-4 * r * std::sin(2 * M_PI * u2));
-      }
+      launch_random_init<T>(dst, J.n * D, P.seed + (uint64_t)j, s);
     }
     if (P.learning_rate > 0) lrh[j] = (T)P.learning_rate;
     else {
@@ -1582,8 +1558,7 @@ void batch_fit(bhtsne_batch* b) {
       lrh[j] = a > (T)50.0 ? a : (T)50.0;
     }
   }
-  const size_t ybytes = (size_t)total * D * sizeof(T);
-  upload<T>(B.y, yh.data(), ybytes, s);
+  BHG_CUDA(cudaStreamSynchronize(s));  // the host copies of initial embeddings are staged
   B.uy.ensure(ybytes);
   B.gains.ensure(ybytes);
   B.pos.ensure(ybytes);

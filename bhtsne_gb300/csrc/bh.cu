@@ -486,7 +486,7 @@ __global__ void tree_mark_kernel(const typename MortonD<D>::Code* __restrict__ c
   const int l = boundary_level<D>(c0, c1);
   int64_t lo, hi, a, e;
   seg_bounds(sg, s, n, &lo, &hi);
-  cell_range_in<D>(codes, lo, hi, c1, l, &a, &e);
+  cell_range_near<D>(codes, lo, hi, c1, l, s, &a, &e, false);
   const int sh1 = D * (B - l - 1);
   if ((c0 >> sh1) == (codes[a] >> sh1)) atomicOr(&mask[a], 1u << l);
 }
@@ -518,7 +518,7 @@ __global__ void tree_emit_kernel(const typename MortonD<D>::Code* __restrict__ c
     const Code c0 = codes[s - 1];
     const int l = boundary_level<D>(c0, c1);
     int64_t a, e;
-    cell_range_in<D>(codes, lo, hi, c1, l, &a, &e);
+    cell_range_near<D>(codes, lo, hi, c1, l, s, &a, &e, true);
     const int sh1 = D * (B - l - 1);
     if ((c0 >> sh1) == (codes[a] >> sh1)) {
       const uint32_t m = mask[a];

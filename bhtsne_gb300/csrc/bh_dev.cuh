@@ -120,11 +120,48 @@ __device__ __forceinline__ int boundary_level(typename MortonD<D>::Code c0, type
   return (B - 1) - msb_pos(c0 ^ c1) / D;
 }
 
-// Range [a, e) of the depth-l Morton cell holding code c, searched within [lo, hi).
+// First index in [lo, s] whose code is >= key, given codes[s] >= key: a
+// galloping search leftwards from s (about 2 log2 of the distance probes,
+// the same answer as a binary search over [lo, s]).
+template <class C>
+__device__ __forceinline__ int64_t gallop_down(const C* __restrict__ c, int64_t lo, int64_t s, C key) {
+  int64_t good = s, bad = lo - 1, step = 1;
+  while (good - step >= lo) {
+    const int64_t probe = good - step;
+    if (c[probe] < key) {
+      bad = probe;
+      break;
+    }
+    good = probe;
+    step <<= 1;
+  }
+  return lower_bound_code<C>(c, bad + 1, good, key);
+}
+
+// First index in (s, hi) whose code is >= key, or hi, given codes[s] < key:
+// a galloping search rightwards from s.
+template <class C>
+__device__ __forceinline__ int64_t gallop_up(const C* __restrict__ c, int64_t s, int64_t hi, C key) {
+  int64_t bad = s, good = hi, step = 1;
+  while (bad + step < hi) {
+    const int64_t probe = bad + step;
+    if (c[probe] >= key) {
+      good = probe;
+      break;
+    }
+    bad = probe;
+    step <<= 1;
+  }
+  return lower_bound_code<C>(c, bad + 1, good, key);
+}
+
+// Range [a, e) of the depth-l Morton cell holding code c = codes[s], within
+// [lo, hi): galloping searches outwards from s. With need_end false only *a
+// is computed.
 template <int D>
-__device__ __forceinline__ void cell_range_in(const typename MortonD<D>::Code* __restrict__ codes, int64_t lo,
-                                              int64_t hi, typename MortonD<D>::Code c, int l, int64_t* a,
-                                              int64_t* e) {
+__device__ __forceinline__ void cell_range_near(const typename MortonD<D>::Code* __restrict__ codes, int64_t lo,
+                                                int64_t hi, typename MortonD<D>::Code c, int l, int64_t s,
+                                                int64_t* a, int64_t* e, bool need_end) {
   typedef typename MortonD<D>::Code Code;
   constexpr int B = MortonD<D>::BITS;
   if (l == 0) {
@@ -134,10 +171,11 @@ __device__ __forceinline__ void cell_range_in(const typename MortonD<D>::Code* _
   }
   const int shift = D * (B - l);
   const Code prefix = c >> shift;
-  *a = lower_bound_code<Code>(codes, lo, hi, prefix << shift);
+  *a = gallop_down<Code>(codes, lo, s, prefix << shift);
+  if (!need_end) return;
   const Code limit = ~(Code)0 >> shift;  // largest prefix representable
   if (prefix >= limit) *e = hi;
-  else *e = lower_bound_code<Code>(codes, *a, hi, (prefix + 1) << shift);
+  else *e = gallop_up<Code>(codes, s, hi, (prefix + 1) << shift);
 }
 
 }  // namespace bhg

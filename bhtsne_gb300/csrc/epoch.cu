@@ -212,6 +212,41 @@ __global__ void task_fill_kernel(const uint64_t* __restrict__ rows, int64_t n, c
 }
 
 // ---------------------------------------------------------------------------
+// Seeded initial embedding. Pair i needs LCG states 2i + 1 and 2i + 2: the
+// state 2i is reached from the seed by composing the affine step with itself
+// (binary powers, O(log i)), so every pair is independent.
+// ---------------------------------------------------------------------------
+constexpr uint64_t kLcgMul = 6364136223846793005ULL, kLcgAdd = 1442695040888963407ULL;
+
+__device__ __forceinline__ uint64_t lcg_jump(uint64_t state, uint64_t steps) {
+  uint64_t acc_mul = 1, acc_add = 0, cur_mul = kLcgMul, cur_add = kLcgAdd;
+  while (steps) {
+    if (steps & 1) {
+      acc_mul *= cur_mul;
+      acc_add = acc_add * cur_mul + cur_add;
+    }
+    cur_add = (cur_mul + 1) * cur_add;
+    cur_mul *= cur_mul;
+    steps >>= 1;
+  }
+  return acc_mul * state + acc_add;
+}
+
+template <class T>
+__global__ void random_init_kernel(T* __restrict__ y, int64_t count, uint64_t seed) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (2 * i >= count) return;
+  const uint64_t s1 = lcg_jump(seed, 2 * (uint64_t)i + 1);
+  const uint64_t s2 = s1 * kLcgMul + kLcgAdd;
+  const double u1 = ((double)(s1 >> 11) + 0.5) * (1.0 / 9007199254740992.0);
+  const double u2 = ((double)(s2 >> 11) + 0.5) * (1.0 / 9007199254740992.0);
+  const double r = sqrt(-2.0 * log(u1));
+  const double a = 2 * 3.14159265358979323846 * u2;
+  y[2 * i] = (T)(1e-4 * r * cos(a));
+  if (2 * i + 1 < count) y[2 * i + 1] = (T)(1e-4 * r * sin(a));
+}
+
+// ---------------------------------------------------------------------------
 // Renumbering of the embedding layout (see launch_renumber).
 // ---------------------------------------------------------------------------
 template <class T, int D>
@@ -555,6 +590,13 @@ void launch_attractive(int D, const uint64_t* rows, const uint32_t* cols, const 
 }
 
 template <class T>
+void launch_random_init(T* y, int64_t count, uint64_t seed, cudaStream_t s) {
+  if (count <= 0) return;
+  random_init_kernel<T><<<(unsigned)ceil_div(ceil_div(count, 2), 256), 256, 0, s>>>(y, count, seed);
+  BHG_LAUNCH_CHECK();
+}
+
+template <class T>
 void build_attr_tasks(AttrTasks& at, int D, const uint64_t* rows, int64_t n, cudaStream_t s) {
   at.D = D;
   at.n = n;
@@ -743,6 +785,7 @@ void launch_exact_kl(int D, const T* y, const T* p, int64_t n, const double* z, 
                                    const uint64_t*, const uint32_t*, const T*, int64_t, cudaStream_t);               \
   template void launch_unpermute<T>(int, const T*, const uint32_t*, int64_t, T*, cudaStream_t);                      \
   template void build_attr_tasks<T>(AttrTasks&, int, const uint64_t*, int64_t, cudaStream_t);                        \
+  template void launch_random_init<T>(T*, int64_t, uint64_t, cudaStream_t);                                          \
   template void launch_attractive_tasks<T>(const AttrTasks&, const uint32_t*, const T*, const T*, T*, cudaStream_t); \
   template void launch_update<T>(int, T*, const T*, const T*, T*, T*, int64_t, const double*, T, T, T, UpdateScratch&,  \
                                  cudaStream_t);                                                                      \

@@ -37,6 +37,12 @@ template <class T>
 void launch_attractive_tasks(const AttrTasks& at, const uint32_t* cols, const T* vals, const T* y, T* pos,
                              cudaStream_t s);
 
+// random_init (the reference's is unseeded, src/tsne/mod.rs:142-147): a
+// seeded Box-Muller N(0, 1e-4) over the LCG s <- 6364136223846793005 s +
+// 1442695040888963407, values 2i and 2i + 1 from states 2i + 1 and 2i + 2.
+template <class T>
+void launch_random_init(T* y, int64_t count, uint64_t seed, cudaStream_t s);
+
 // Locality renumbering of the device-resident optimisation state. The points
 // are re-laid out in `order` (a permutation of the current slots, e.g. the
 // Morton order of the embedding); ext[s] is the point (CSR row) held by slot

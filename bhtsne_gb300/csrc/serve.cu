@@ -52,10 +52,6 @@ double now_s() {
   return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
 }
 
-uint64_t lcg_step(uint64_t& s) {
-  s = s * 6364136223846793005ULL + 1442695040888963407ULL;
-  return s;
-}
 
 struct Request {
   int64_t id = 0;
@@ -340,23 +336,15 @@ struct BhEngine {
     // fresh jobs: random_init (seeded Box-Muller, N(0, 1e-4)), zero velocity, unit gains
     const int64_t fresh_rows = tot - at;
     if (fresh_rows > 0) {
-      std::vector<T> h((size_t)fresh_rows * D);
+      const size_t cnt_all = (size_t)fresh_rows * D;
       int64_t p = 0;
       for (auto& sl : fresh) {
-        uint64_t sd = sl->req->seed;
         const int64_t cnt = sl->n * D;
-        for (int64_t e = 0; e < cnt; e += 2) {
-          const double u1 = ((lcg_step(sd) >> 11) + 0.5) * (1.0 / 9007199254740992.0);
-          const double u2 = ((lcg_step(sd) >> 11) + 0.5) * (1.0 / 9007199254740992.0);
-          const double rr = std::sqrt(-2.0 * std::log(u1));
-          h[p + e] = (T)(1e-4 * rr * std::cos(2 * M_PI * u2));
-          if (e + 1 < cnt) h[p + e + 1] = (T)(1e-4 * rr * std::sin(2 * M_PI * u2));
-        }
+        launch_random_init<T>(y2.template as<T>() + at * D + p, cnt, sl->req->seed, s);
         p += cnt;
       }
-      BHG_CUDA(cudaMemcpyAsync(y2.template as<T>() + at * D, h.data(), h.size() * es, cudaMemcpyHostToDevice, s));
-      BHG_CUDA(cudaMemsetAsync(uy2.template as<T>() + at * D, 0, h.size() * es, s));
-      std::vector<T> ones(h.size(), T(1));
+      BHG_CUDA(cudaMemsetAsync(uy2.template as<T>() + at * D, 0, cnt_all * es, s));
+      std::vector<T> ones(cnt_all, T(1));
       BHG_CUDA(cudaMemcpyAsync(g2.template as<T>() + at * D, ones.data(), ones.size() * es, cudaMemcpyHostToDevice, s));
       BHG_CUDA(cudaStreamSynchronize(s));
     }
