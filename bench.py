@@ -608,8 +608,9 @@ def run_reference(args):
 
 def run_fft_only(args):
     """FIt-SNE repulsion alone (spread, transforms, gather) for --n points
-    spread uniformly over [-700, 700]^2: the 1000-box cap, transforms of
-    length 8192. --warmup untimed calls, then --steps timed ones."""
+    spread uniformly over [-700, 700]^2: the 1000-box cap, 3000 nodes per
+    axis, transforms of length 6144. --warmup untimed calls, then --steps
+    timed ones."""
     import bhtsne_gb300 as bg
     ctx = bg.Context(0)
     y = np.random.default_rng(args.seed).uniform(-700, 700, size=(args.n, 2)).astype(np.float32)
@@ -621,7 +622,7 @@ def run_fft_only(args):
     for _ in range(args.steps):
         bg.gradient(bg.METHOD_FIT_SNE, y, rows, empty_c, empty_v, ctx=ctx)
     ms = 1e3 * (time.perf_counter() - w0) / args.steps
-    print(json.dumps({"fft_only": {"n_points": args.n, "grid": "1000 boxes per axis, L = 8192",
+    print(json.dumps({"fft_only": {"n_points": args.n, "grid": "1000 boxes per axis, transforms of length 6144",
                                    "ms_per_call": round(ms, 3),
                                    "note": "host wall time per call, including the copies of y in and forces out"}}))
 

@@ -112,8 +112,12 @@ __global__ void fit_params_kernel(const BoxParams<T>* __restrict__ box, int64_t 
   if (scaled > T(0)) boxes = scaled >= T(9.0e18) ? INT64_MAX : (int64_t)scaled;
   boxes = boxes < 10 ? 10 : (boxes > 1000 ? 1000 : boxes);
   int nodes = (int)boxes * 3;
+  // the shorter of the next power of two and the next 3 * 2^j (>= 24)
   int L = 16;
   while (L < 2 * nodes - 1) L <<= 1;
+  int L3 = 24;
+  while (L3 < 2 * nodes - 1) L3 <<= 1;
+  if (L3 < L) L = L3;
   out->need_L = L;
   if (cap_L > 0 && L > cap_L) {
     *overflow = 1;
@@ -343,19 +347,22 @@ __global__ void charges_kernel(long long* __restrict__ acc, const FitParams<T>* 
 // in registers across a warp with shuffles (lane l holds element 32 g + l).
 // tw holds W_cap^k for k < cap / 2 and tws = cap / L.
 
-// DIF stages of spans L .. 2^(small + 1), ending with a barrier.
+// DIF stages of spans L .. 2^(small + 1) of `nsub` consecutive rows of
+// length L held back to back, ending with a barrier.
 template <class T2>
 __device__ __forceinline__ void dif_smem_stages(T2* s, int L, int log2L, int small, const T2* __restrict__ tw,
-                                                int tws) {
+                                                int tws, int nsub) {
   int lg = log2L;
   if (((log2L - small) & 1) != 0) {
     // one radix-2 stage of span L
     const int half = L >> 1;
 #pragma unroll 2
-    for (int b = threadIdx.x; b < half; b += blockDim.x) {
-      const T2 a = s[b], c = s[b + half];
-      s[b] = cadd(a, c);
-      s[b + half] = cmul(csub(a, c), tw[b * tws]);
+    for (int b0 = threadIdx.x; b0 < nsub * half; b0 += blockDim.x) {
+      const int b = b0 & (half - 1);
+      T2* r = s + (b0 >> (log2L - 1)) * L;
+      const T2 a = r[b], c = r[b + half];
+      r[b] = cadd(a, c);
+      r[b + half] = cmul(csub(a, c), tw[b * tws]);
     }
     __syncthreads();
     lg -= 1;
@@ -365,9 +372,10 @@ __device__ __forceinline__ void dif_smem_stages(T2* s, int L, int log2L, int sma
     const int q = 1 << (lg - 2);
     const int st1 = (L >> lg) * tws, st2 = (L >> (lg - 1)) * tws;
 #pragma unroll 2
-    for (int b = threadIdx.x; b < (L >> 2); b += blockDim.x) {
+    for (int b0 = threadIdx.x; b0 < nsub * (L >> 2); b0 += blockDim.x) {
+      const int b = b0 & ((L >> 2) - 1);
       const int pos = b & (q - 1);
-      const int i = ((b >> (lg - 2)) << lg) + pos;
+      const int i = (b0 >> (log2L - 2)) * L + ((b >> (lg - 2)) << lg) + pos;
       const T2 wa = tw[pos * st1];  // W_S^pos
       T2 wb;                         // W_S^(pos+q) = W_S^pos * (-i)
       wb.x = wa.y;
@@ -392,15 +400,16 @@ __device__ __forceinline__ void dif_smem_stages(T2* s, int L, int log2L, int sma
 // quarter turn.
 template <class T2>
 __device__ __forceinline__ void dit_smem_stages(T2* s, int L, int log2L, int small, const T2* __restrict__ tw,
-                                                int tws) {
+                                                int tws, int nsub) {
   int lg = small + 1;
   for (; lg + 1 <= log2L; lg += 2) {
     const int h = 1 << (lg - 1);
     const int st1 = (L >> lg) * tws, st2 = (L >> (lg + 1)) * tws;
 #pragma unroll 2
-    for (int b = threadIdx.x; b < (L >> 2); b += blockDim.x) {
+    for (int b0 = threadIdx.x; b0 < nsub * (L >> 2); b0 += blockDim.x) {
+      const int b = b0 & ((L >> 2) - 1);
       const int pos = b & (h - 1);
-      const int i = ((b >> (lg - 1)) << (lg + 1)) + pos;
+      const int i = (b0 >> (log2L - 2)) * L + ((b >> (lg - 1)) << (lg + 1)) + pos;
       T2 w1 = tw[pos * st1];
       T2 w2 = tw[pos * st2];
       w1.y = -w1.y;
@@ -428,9 +437,10 @@ __device__ __forceinline__ void dit_smem_stages(T2* s, int L, int log2L, int sma
     const int half = 1 << (lg - 1);
     const int tstep = (L >> lg) * tws;
 #pragma unroll 2
-    for (int b = threadIdx.x; b < (L >> 1); b += blockDim.x) {
+    for (int b0 = threadIdx.x; b0 < nsub * (L >> 1); b0 += blockDim.x) {
+      const int b = b0 & ((L >> 1) - 1);
       const int pos = b & (half - 1);
-      const int i = ((b >> (lg - 1)) << lg) + pos;
+      const int i = (b0 >> (log2L - 1)) * L + ((b >> (lg - 1)) << lg) + pos;
       const int j = i + half;
       T2 w = tw[pos * tstep];
       w.y = -w.y;
@@ -441,6 +451,50 @@ __device__ __forceinline__ void dit_smem_stages(T2* s, int L, int log2L, int sma
     }
     __syncthreads();
   }
+}
+
+// Lengths L = 3 M: a radix-3 stage of span L splits the row into three
+// consecutive power-of-two rows of length M (decimation in frequency:
+// position k M + p then holds frequency 3 bitrev(p) + k), and the inverse
+// ends with the matching combination. tw3 holds W_cap3^k for k < cap3 and
+// tws3 = cap3 / L. W_3 = -1/2 - i sqrt(3)/2.
+template <class T2, class T>
+__device__ __forceinline__ void r3_dif_stage(T2* s, int M, const T2* __restrict__ tw3, int tws3) {
+  const T h = T(0.86602540378443864676);
+  for (int n = threadIdx.x; n < M; n += blockDim.x) {
+    const T2 x0 = s[n], x1 = s[n + M], x2 = s[n + 2 * M];
+    const T2 a = cadd(x1, x2), b = csub(x1, x2);
+    T2 t, u;
+    t.x = x0.x - T(0.5) * a.x;
+    t.y = x0.y - T(0.5) * a.y;
+    u.x = h * b.y;  // -i sqrt(3)/2 (x1 - x2)
+    u.y = -(h * b.x);
+    s[n] = cadd(x0, a);
+    s[n + M] = cmul(cadd(t, u), tw3[n * tws3]);
+    s[n + 2 * M] = cmul(csub(t, u), tw3[2 * n * tws3]);
+  }
+  __syncthreads();
+}
+
+template <class T2, class T>
+__device__ __forceinline__ void r3_dit_stage(T2* s, int M, const T2* __restrict__ tw3, int tws3) {
+  const T h = T(0.86602540378443864676);
+  for (int n = threadIdx.x; n < M; n += blockDim.x) {
+    T2 w1 = tw3[n * tws3], w2 = tw3[2 * n * tws3];
+    w1.y = -w1.y;
+    w2.y = -w2.y;
+    const T2 z0 = s[n], t1 = cmul(s[n + M], w1), t2 = cmul(s[n + 2 * M], w2);
+    const T2 a = cadd(t1, t2), b = csub(t1, t2);
+    T2 t, v;
+    t.x = z0.x - T(0.5) * a.x;
+    t.y = z0.y - T(0.5) * a.y;
+    v.x = -(h * b.y);  // +i sqrt(3)/2 (t1 - t2)
+    v.y = h * b.x;
+    s[n] = cadd(z0, a);
+    s[n + M] = cadd(t, v);
+    s[n + 2 * M] = csub(t, v);
+  }
+  __syncthreads();
 }
 
 // This lane's forward twiddle for each register stage k (span 2^k):
@@ -532,18 +586,22 @@ __device__ __forceinline__ bool fft_fill_row(typename Cx<T>::type* s, const type
 
 constexpr int kFftThreads = 512;
 
+// Row geometry: L = nsub * M with M a power of two and nsub 1 or 3.
 template <class T>
 struct FftRow {
   typedef typename Cx<T>::type T2;
-  int L, log2L, small, G, ngroups, tws, lane, warp, nw;
+  int L, M, nsub, log2M, small, G, ngroups, tws, tws3, lane, warp, nw;
   bool lane_ok;
   __device__ FftRow(int L_, int cap_L) : L(L_) {
-    log2L = 0;
-    while ((1 << log2L) < L) ++log2L;
-    small = log2L < 5 ? log2L : 5;
+    nsub = (L % 3 == 0) ? 3 : 1;
+    M = L / nsub;
+    log2M = 0;
+    while ((1 << log2M) < M) ++log2M;
+    small = log2M < 5 ? log2M : 5;
     G = 1 << small;
     ngroups = L >> small;
-    tws = cap_L / L;
+    tws = cap_L / M;
+    tws3 = nsub == 3 ? (3 * (cap_L >> 2)) / L : 0;
     lane = threadIdx.x & 31;
     warp = threadIdx.x >> 5;
     nw = blockDim.x >> 5;
@@ -557,7 +615,8 @@ struct FftRow {
 template <class T>
 __global__ void __launch_bounds__(kFftThreads) fft_rows_kernel(typename Cx<T>::type* __restrict__ data,
                                                               const FitParams<T>* __restrict__ prm, int rows_sel,
-                                                              const typename Cx<T>::type* __restrict__ tw, int cap_L,
+                                                              const typename Cx<T>::type* __restrict__ tw,
+                                                              const typename Cx<T>::type* __restrict__ tw3, int cap_L,
                                                               int inverse, int* __restrict__ fault, int src,
                                                               T* __restrict__ khat_out) {
   typedef typename Cx<T>::type T2;
@@ -570,14 +629,15 @@ __global__ void __launch_bounds__(kFftThreads) fft_rows_kernel(typename Cx<T>::t
   T2* s = reinterpret_cast<T2*>(smem_raw);
   T2* d = data + (int64_t)blockIdx.x * L;
   T2 w[5];
-  lane_twiddles(r.lane, L, r.small, tw, r.tws, w);
+  lane_twiddles(r.lane, r.M, r.small, tw, r.tws, w);
   T2 zero;
   zero.x = T(0);
   zero.y = T(0);
   const int D = rows_sel == 2 ? 1 : 2;
   if (!fft_fill_row<T>(s, d, inverse ? 0 : src, (int)blockIdx.x, L, D, prm, &load_bar, fault)) return;
   if (!inverse) {
-    dif_smem_stages(s, L, r.log2L, r.small, tw, r.tws);
+    if (r.nsub == 3) r3_dif_stage<T2, T>(s, r.M, tw3, r.tws3);
+    dif_smem_stages(s, r.M, r.log2M, r.small, tw, r.tws, r.nsub);
     // khat_out: the real part scaled by 1 / L^D (the kernel spectrum)
     const T inv_total = T(1) / (T)(D == 1 ? (double)L : (double)L * (double)L);
     T* kr = khat_out ? khat_out + (int64_t)blockIdx.x * L : nullptr;
@@ -595,7 +655,8 @@ __global__ void __launch_bounds__(kFftThreads) fft_rows_kernel(typename Cx<T>::t
     if (r.lane_ok) s[g * r.G + r.lane] = x;
   }
   __syncthreads();
-  dit_smem_stages(s, L, r.log2L, r.small, tw, r.tws);
+  dit_smem_stages(s, r.M, r.log2M, r.small, tw, r.tws, r.nsub);
+  if (r.nsub == 3) r3_dit_stage<T2, T>(s, r.M, tw3, r.tws3);
   for (int i = threadIdx.x; i < L; i += blockDim.x) d[i] = s[i];
 }
 
@@ -611,6 +672,7 @@ __global__ void __launch_bounds__(kFftThreads) fft_conv_rows_kernel(typename Cx<
                                                                    const T* __restrict__ khat,
                                                                    const FitParams<T>* __restrict__ prm, int rows_sel,
                                                                    const typename Cx<T>::type* __restrict__ tw,
+                                                                   const typename Cx<T>::type* __restrict__ tw3,
                                                                    int cap_L, int* __restrict__ fault, int src) {
   typedef typename Cx<T>::type T2;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -624,12 +686,13 @@ __global__ void __launch_bounds__(kFftThreads) fft_conv_rows_kernel(typename Cx<
   T2* d = data + (int64_t)blockIdx.x * L;
   const T* kr = khat + (int64_t)blockIdx.x * L;
   T2 w[5];
-  lane_twiddles(r.lane, L, r.small, tw, r.tws, w);
+  lane_twiddles(r.lane, r.M, r.small, tw, r.tws, w);
   T2 zero;
   zero.x = T(0);
   zero.y = T(0);
   if (!fft_fill_row<T>(s, d, src, (int)blockIdx.x, L, rows_sel == 2 ? 1 : 2, prm, &load_bar, fault)) return;
-  dif_smem_stages(s, L, r.log2L, r.small, tw, r.tws);
+  if (r.nsub == 3) r3_dif_stage<T2, T>(s, r.M, tw3, r.tws3);
+  dif_smem_stages(s, r.M, r.log2M, r.small, tw, r.tws, r.nsub);
   for (int g = r.warp; g < r.ngroups; g += r.nw) {
     const int e = g * r.G + r.lane;
     T2 x = dif_reg_stages(r.lane_ok ? s[e] : zero, r.lane, r.small, w);
@@ -640,7 +703,8 @@ __global__ void __launch_bounds__(kFftThreads) fft_conv_rows_kernel(typename Cx<
     if (r.lane_ok) s[e] = x;
   }
   __syncthreads();
-  dit_smem_stages(s, L, r.log2L, r.small, tw, r.tws);
+  dit_smem_stages(s, r.M, r.log2M, r.small, tw, r.tws, r.nsub);
+  if (r.nsub == 3) r3_dit_stage<T2, T>(s, r.M, tw3, r.tws3);
   for (int i = threadIdx.x; i < keep; i += blockDim.x) d[i] = s[i];
 }
 
@@ -753,6 +817,25 @@ __global__ void gather_kernel(const T* __restrict__ y, int64_t n, const FitParam
 
 }  // namespace
 
+// W_cap3^k for k < cap3 = 3 cap_L / 4 (the full circle): the radix-3 stage of
+// any length 3 * 2^j <= cap3.
+template <class T>
+const typename FitWorkspace<T>::T2* FitWorkspace<T>::twiddles3(int cap_L, cudaStream_t s) {
+  const int c3 = 3 * (cap_L / 4);
+  if (tw3_len != c3) {
+    std::vector<T2> h(c3 > 0 ? c3 : 1);
+    for (int k = 0; k < c3; ++k) {
+      const double ang = -2.0 * M_PI * (double)k / (double)c3;
+      h[k].x = (T)std::cos(ang);
+      h[k].y = (T)std::sin(ang);
+    }
+    tw3.ensure(h.size() * sizeof(T2));
+    BHG_CUDA(cudaMemcpyAsync(tw3.ptr, h.data(), h.size() * sizeof(T2), cudaMemcpyHostToDevice, s));
+    tw3_len = c3;
+  }
+  return tw3.template as<T2>();
+}
+
 template <class T>
 const typename FitWorkspace<T>::T2* FitWorkspace<T>::twiddles(int L, cudaStream_t s) {
   if (tw_len != L) {
@@ -781,7 +864,8 @@ static void fft_rows(FitWorkspace<T>& ws, typename Cx<T>::type* data, const FitP
   const int threads = std::min(kFftThreads, std::max(32, cap_L / 4));
   const size_t smem = (size_t)cap_L * sizeof(typename Cx<T>::type);
   const int grid = rows_sel == 2 ? 1 : cap_L;
-  fft_rows_kernel<T><<<grid, threads, smem, s>>>(data, dp, rows_sel, ws.twiddles(cap_L, s), cap_L, inverse ? 1 : 0,
+  fft_rows_kernel<T><<<grid, threads, smem, s>>>(data, dp, rows_sel, ws.twiddles(cap_L, s), ws.twiddles3(cap_L, s),
+                                                  cap_L, inverse ? 1 : 0,
                                                   ws.flag.template as<int>() + 1, src, khat_out);
   BHG_LAUNCH_CHECK();
 }
@@ -792,7 +876,8 @@ static void fft_conv_rows(FitWorkspace<T>& ws, typename Cx<T>::type* data, const
   const int threads = std::min(kFftThreads, std::max(32, cap_L / 4));
   const size_t smem = (size_t)cap_L * sizeof(typename Cx<T>::type);
   const int grid = rows_sel == 2 ? 1 : cap_L;
-  fft_conv_rows_kernel<T><<<grid, threads, smem, s>>>(data, khat, dp, rows_sel, ws.twiddles(cap_L, s), cap_L,
+  fft_conv_rows_kernel<T><<<grid, threads, smem, s>>>(data, khat, dp, rows_sel, ws.twiddles(cap_L, s),
+                                                       ws.twiddles3(cap_L, s), cap_L,
                                                        ws.flag.template as<int>() + 1, src);
   BHG_LAUNCH_CHECK();
 }
@@ -808,6 +893,7 @@ static void transpose(const typename Cx<T>::type* in, const FitParams<T>* dp, in
 
 template <class T>
 void FitWorkspace<T>::reserve(int D, int64_t n, int cap) {
+  if (cap < 16 || (cap & (cap - 1)) != 0) throw Error(ST_EINTERNAL, "error: FIt-SNE capacity must be a power of two.");
   typedef typename Cx<T>::type C2;
   const int64_t total = D == 1 ? (int64_t)cap : (int64_t)cap * cap;
   params.ensure(sizeof(FitParams<T>));
@@ -824,7 +910,7 @@ void FitWorkspace<T>::reserve(int D, int64_t n, int cap) {
   zpart.ensure((ceil_div(std::max<int64_t>(n, 1), 256) + 1) * sizeof(double));
   flag.ensure(64);
   done.ensure(64);
-  if ((size_t)cap * sizeof(C2) > 48 * 1024) {  // set outside any stream capture
+  if ((size_t)cap * sizeof(C2) >= 40 * 1024) {  // set outside any stream capture
     BHG_CUDA(cudaFuncSetAttribute(fft_rows_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     BHG_CUDA(cudaFuncSetAttribute(fft_conv_rows_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
   }
@@ -934,8 +1020,9 @@ template <class T>
 FitGrid fit_repulsion(FitWorkspace<T>& ws, int D, const T* y, int64_t n, const BoxParams<T>* box, T* neg, double* z_out,
                       cudaStream_t s) {
   const int L = fit_needed_length<T>(ws, D, n, box, s);
-  if (ws.cap_L < L) ws.reserve(D, n, L);
-  else ws.reserve(D, n, ws.cap_L);
+  int cap = 16;  // capacities are powers of two (the twiddle tables assume it)
+  while (cap < L) cap <<= 1;
+  ws.reserve(D, n, std::max(ws.cap_L, cap));
   BHG_CUDA(cudaMemsetAsync(ws.flag.template as<int>() + 1, 0, sizeof(int), s));
   fit_repulsion_cap<T>(ws, D, y, n, box, neg, z_out, s);
   FitParams<T> hp;

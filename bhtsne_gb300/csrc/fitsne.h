@@ -5,8 +5,9 @@
 
 namespace bhg {
 
-// Largest transform length: boxes <= 1000 per axis, 3 nodes per box, the
-// next power of two >= 2 nodes - 1.
+// Transform lengths are the shorter of the next power of two and the next
+// 3 * 2^j >= 2 nodes - 1; the capacity is a power of two, at most 8192 (boxes
+// <= 1000 per axis, 3 nodes per box: 6144 or shorter is used).
 constexpr int kFitMaxL = 8192;
 
 template <class T>
@@ -26,12 +27,13 @@ struct FitGrid {
 template <class T>
 struct FitWorkspace {
   typedef typename std::conditional<sizeof(T) == 4, float2, double2>::type T2;
-  DevBuf params, g0, g1, h0, h1, khat, tw, zpart, done, acc, flag;
-  int tw_len = 0;
+  DevBuf params, g0, g1, h0, h1, khat, tw, tw3, zpart, done, acc, flag;
+  int tw_len = 0, tw3_len = 0;
   const void* acc_clean = nullptr;  // acc allocation known to be all zero
   int cap_L = 0;  // transform length the buffers hold
   bool done_zeroed = false;
   const T2* twiddles(int L, cudaStream_t s);
+  const T2* twiddles3(int cap_L, cudaStream_t s);
   // Buffers for transforms up to cap (a power of two) at n points.
   void reserve(int D, int64_t n, int cap);
 };
