@@ -1266,7 +1266,9 @@ int bhtsne_gradient(bhtsne_ctx* ctx, int dtype, int32_t method, int32_t embed_di
         } else {
           invalid("error: unknown method.");
         }
-        launch_attractive<T>(D, rd.as<uint64_t>(), cd.as<uint32_t>(), vd.as<T>(), yd.as<T>(), n, pd.as<T>(), s);
+        AttrTasks at;
+        build_attr_tasks<T>(at, D, rd.as<uint64_t>(), n, s);
+        launch_attractive_tasks<T>(at, cd.as<uint32_t>(), vd.as<T>(), yd.as<T>(), pd.as<T>(), s);
         if (neg) BHG_CUDA(cudaMemcpyAsync(neg, nd.ptr, (size_t)n * D * sizeof(T), cudaMemcpyDeviceToHost, s));
       }
       BHG_CUDA(cudaMemcpyAsync(pos, pd.ptr, (size_t)n * D * sizeof(T), cudaMemcpyDeviceToHost, s));

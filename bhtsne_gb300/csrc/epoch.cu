@@ -24,11 +24,6 @@ namespace bhg {
 
 namespace {
 
-// G lanes per embedding slot (32 / G slots per warp); each lane keeps kU
-// entries in flight (column, value and gathered y loaded before any
-// arithmetic). With a renumbered layout slot s holds the point of CSR row
-// row_of_slot[s] and `cols` holds slots, so a row's gathers stay near s and
-// neighbouring warps share lines.
 // y[j] as one 2-wide load when D = 2 and y is aligned for it (VEC), else per axis.
 template <class T, int D, bool VEC>
 __device__ __forceinline__ void load_point(const T* __restrict__ y, int64_t j, T (&v)[D]) {
@@ -43,62 +38,6 @@ __device__ __forceinline__ void load_point(const T* __restrict__ y, int64_t j, T
   } else {
 #pragma unroll
     for (int a = 0; a < D; ++a) v[a] = y[j * D + a];
-  }
-}
-
-// One warp per row (slot); consecutive warps take consecutive slots, so the
-// rows in flight are a contiguous window of P and their sorted slot columns
-// gather nearby y[j].
-template <class T, int D, int kU, bool VEC>
-__global__ void __launch_bounds__(256) attractive_kernel(const uint64_t* __restrict__ rows, const uint32_t* __restrict__ cols,
-                                                         const T* __restrict__ vals, const T* __restrict__ y, int64_t n,
-                                                         const uint32_t* __restrict__ row_of_slot, T* __restrict__ pos) {
-  constexpr int G = 32;
-  const int64_t slot = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / G;
-  const int lane = threadIdx.x & (G - 1);
-  if (slot >= n) return;
-  const int64_t row = row_of_slot ? (int64_t)row_of_slot[slot] : slot;
-  T yi[D], acc[D];
-#pragma unroll
-  for (int a = 0; a < D; ++a) {
-    yi[a] = y[slot * D + a];
-    acc[a] = T(0);
-  }
-  const int64_t e0 = (int64_t)rows[row], e1 = (int64_t)rows[row + 1];
-  for (int64_t base = e0; base < e1; base += G * kU) {
-    uint32_t j[kU];
-    T p[kU];
-    T yj[kU][D];
-#pragma unroll
-    for (int u = 0; u < kU; ++u) {
-      const int64_t e = base + lane + G * u;
-      j[u] = e < e1 ? __ldg(cols + e) : (uint32_t)slot;
-      p[u] = e < e1 ? __ldg(vals + e) : T(0);
-    }
-#pragma unroll
-    for (int u = 0; u < kU; ++u) load_point<T, D, VEC>(y, (int64_t)j[u], yj[u]);
-#pragma unroll
-    for (int u = 0; u < kU; ++u) {
-      T disp[D];
-      T dist = T(0);
-#pragma unroll
-      for (int a = 0; a < D; ++a) {
-        disp[a] = yi[a] - yj[u][a];
-        dist += disp[a] * disp[a];
-      }
-      const T factor = p[u] / (dist + T(1));
-#pragma unroll
-      for (int a = 0; a < D; ++a) acc[a] += factor * disp[a];
-    }
-  }
-#pragma unroll
-  for (int a = 0; a < D; ++a) {
-#pragma unroll
-    for (int o = G / 2; o > 0; o >>= 1) acc[a] += __shfl_xor_sync(kFull, acc[a], o);
-  }
-  if (lane == 0) {
-#pragma unroll
-    for (int a = 0; a < D; ++a) pos[slot * D + a] = acc[a];
   }
 }
 
@@ -569,26 +508,6 @@ constexpr int kUpdBlocks = 2 * 152;
 
 }  // namespace
 
-template <class T, int D>
-static void launch_attractive_d(const uint64_t* rows, const uint32_t* cols, const T* vals, const T* y, int64_t n, T* pos,
-                                cudaStream_t s, const uint32_t* row_of_slot) {
-  const bool vec = D == 2 && (reinterpret_cast<uintptr_t>(y) % (2 * sizeof(T))) == 0;
-  const unsigned grid = (unsigned)ceil_div(n, 8);
-  if (vec) attractive_kernel<T, D, 4, true><<<grid, 256, 0, s>>>(rows, cols, vals, y, n, row_of_slot, pos);
-  else attractive_kernel<T, D, 4, false><<<grid, 256, 0, s>>>(rows, cols, vals, y, n, row_of_slot, pos);
-}
-
-template <class T>
-void launch_attractive(int D, const uint64_t* rows, const uint32_t* cols, const T* vals, const T* y, int64_t n, T* pos,
-                       cudaStream_t s, const uint32_t* row_of_slot) {
-  if (n <= 0) return;
-  with_dim<1, 7>(D, "error: the embedding dimension must be in 1..7.", [&](auto dc) {
-    constexpr int DD = decltype(dc)::value;
-    launch_attractive_d<T, DD>(rows, cols, vals, y, n, pos, s, row_of_slot);
-  });
-  BHG_LAUNCH_CHECK();
-}
-
 template <class T>
 void launch_random_init(T* y, int64_t count, uint64_t seed, cudaStream_t s) {
   if (count <= 0) return;
@@ -779,8 +698,6 @@ void launch_exact_kl(int D, const T* y, const T* p, int64_t n, const double* z, 
 }
 
 #define BHG_INST(T)                                                                                                  \
-  template void launch_attractive<T>(int, const uint64_t*, const uint32_t*, const T*, const T*, int64_t, T*,         \
-                                     cudaStream_t, const uint32_t*);                                                 \
   template void launch_renumber<T>(int, const uint32_t*, int64_t, Renumbering&, T*, T*, T*, T*, T*, T*,              \
                                    const uint64_t*, const uint32_t*, const T*, int64_t, cudaStream_t);               \
   template void launch_unpermute<T>(int, const T*, const uint32_t*, int64_t, T*, cudaStream_t);                      \

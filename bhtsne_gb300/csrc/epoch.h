@@ -11,12 +11,6 @@ struct UpdateScratch {
   const double* mean() const { return static_cast<const double*>(mean_sum.ptr); }
 };
 
-// Attractive forces. With row_of_slot == nullptr slot s is CSR row s; with a
-// renumbered layout slot s holds CSR row row_of_slot[s] and `cols` are slots.
-template <class T>
-void launch_attractive(int D, const uint64_t* rows, const uint32_t* cols, const T* vals, const T* y, int64_t n, T* pos,
-                       cudaStream_t s, const uint32_t* row_of_slot = nullptr);
-
 // Attractive forces over bounded tasks: every CSR row is cut into tasks of at
 // most kAttrTaskLen entries, one warp per task. A row of one task writes its
 // slot directly; the tasks of a longer row write partial sums that a second
