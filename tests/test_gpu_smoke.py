@@ -127,3 +127,20 @@ def test_fit_gradient_large_grid(gpu, oracle, D, half, z_floor):
     err_ref, err_gpu = rel_l2(oneg, ref64), rel_l2(neg, ref64)
     assert err_gpu <= max(2 * err_ref, 1e-4), (err_gpu, err_ref)
     assert abs(z - z64) / abs(z64) <= max(2 * abs(oz - z64) / abs(z64), z_floor)
+
+
+@pytest.mark.parametrize("D", [1, 2])
+@pytest.mark.parametrize("half", [5.4, 10.9, 44.8])
+def test_fit_gradient_three_smooth_lengths(gpu, oracle, D, half):
+    """Extents of 11, 22 and 90 boxes: transform lengths 96, 192 and 768 (3 x
+    2^k, a radix-3 stage around power-of-two sub-transforms), against the
+    oracle and within 2x of the reference's own f32 error against f64."""
+    rng = np.random.default_rng(8)
+    y = rng.uniform(-half, half, size=(3000, D)).astype(np.float32)
+    rows = np.zeros(3001, np.uint64)
+    _, neg, z = gpu.gradient(gpu.METHOD_FIT_SNE, y, rows, np.zeros(0, np.uint32), np.zeros(0, np.float32))
+    oneg, oz, info = oracle.fit_repulsion(y)
+    ref64, z64, _ = oracle.fit_repulsion(y.astype(np.float64))
+    assert info["boxes"] in (11, 22, 90)
+    assert rel_l2(neg, ref64) <= max(2 * rel_l2(oneg, ref64), 1e-4)
+    assert abs(z - z64) / abs(z64) <= max(2 * abs(oz - z64) / abs(z64), 1e-4)
