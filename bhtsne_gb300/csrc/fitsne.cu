@@ -667,6 +667,102 @@ __global__ void __launch_bounds__(kFftThreads) fft_rows_kernel(typename Cx<T>::t
   for (int i = threadIdx.x; i < L; i += blockDim.x) d[i] = s[i];
 }
 
+// The kernel spectrum in 2-D from real transforms packed two to a complex
+// one. The kernel K(i, j) = (1 + spacing^2 (lag(i)^2 + lag(j)^2))^-2 is real
+// and even in both indices, so every transform of its rows (and then of its
+// columns) is real: rows a and b packed as a + i b transform to A + i B with
+// A and B the two real transforms. Only rows 0 .. L/2 are distinct (row L - r
+// equals row r).
+//  pass 0: block b transforms kernel rows 2b and 2b + 1 (<= L/2) and writes
+//          the two real rows of `out` (row stride L);
+//  pass 1: block b takes rows 2b and 2b + 1 of the transposed table `in` (row
+//          p holds column p for rows 0 .. L/2, stride L), extends each evenly
+//          to length L, transforms the pair and writes rows 2b and 2b + 1 of
+//          the spectrum times `scale` (1 / L^2).
+// The spectrum is symmetric, so its rows and columns need no distinction.
+template <class T>
+__global__ void __launch_bounds__(kFftThreads) kspec_kernel(int pass, const FitParams<T>* __restrict__ prm,
+                                                           const typename Cx<T>::type* __restrict__ tw,
+                                                           const typename Cx<T>::type* __restrict__ tw3, int cap_L,
+                                                           const T* __restrict__ in, T* __restrict__ out) {
+  typedef typename Cx<T>::type T2;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int L = prm->L, half = L / 2;
+  const int b = (int)blockIdx.x;
+  const int r1 = 2 * b, r2 = 2 * b + 1;
+  if (pass == 0 ? r1 > half : r1 >= L) return;
+  const bool two = pass == 0 ? r2 <= half : true;
+  const FftRow<T> r(L, cap_L);
+  T2* s = reinterpret_cast<T2*>(smem_raw);
+  T2 w[5];
+  lane_twiddles(r.lane, r.M, r.small, tw, r.tws, w);
+  T2 zero;
+  zero.x = T(0);
+  zero.y = T(0);
+  if (pass == 0) {
+    const T spacing = prm->spacing;
+    const int l1 = r1 <= half ? r1 : r1 - L, l2 = r2 <= half ? r2 : r2 - L;
+    const T d1 = spacing * (T)(double)l1, d2 = spacing * (T)(double)l2;
+    for (int c = threadIdx.x; c < L; c += blockDim.x) {
+      const int lc = c <= half ? c : c - L;
+      const T dc = spacing * (T)(double)lc;
+      T sq1 = T(0), sq2 = T(0);
+      sq1 = sq1 + dc * dc;
+      sq1 = sq1 + d1 * d1;
+      sq2 = sq2 + dc * dc;
+      sq2 = sq2 + d2 * d2;
+      const T c1 = T(1) / (T(1) + sq1), c2 = T(1) / (T(1) + sq2);
+      T2 v;
+      v.x = c1 * c1;
+      v.y = two ? c2 * c2 : T(0);
+      s[c] = v;
+    }
+  } else {
+    const T* a = in + (int64_t)r1 * L;
+    const T* c = in + (int64_t)r2 * L;
+    for (int i = threadIdx.x; i < L; i += blockDim.x) {
+      const int e = i <= half ? i : L - i;
+      T2 v;
+      v.x = a[e];
+      v.y = c[e];
+      s[i] = v;
+    }
+  }
+  __syncthreads();
+  if (r.nsub == 3) r3_dif_stage<T2, T>(s, r.M, tw3, r.tws3);
+  dif_smem_stages(s, r.M, r.log2M, r.small, tw, r.tws, r.nsub);
+  const T scale = pass == 0 ? T(1) : T(1) / (T)((double)L * (double)L);
+  T* o1 = out + (int64_t)r1 * L;
+  T* o2 = out + (int64_t)r2 * L;
+  for (int g = r.warp; g < r.ngroups; g += r.nw) {
+    const T2 x = dif_reg_stages(r.lane_ok ? s[g * r.G + r.lane] : zero, r.lane, r.small, w);
+    if (r.lane_ok) {
+      o1[g * r.G + r.lane] = x.x * scale;
+      if (two) o2[g * r.G + r.lane] = x.y * scale;
+    }
+  }
+}
+
+// out[c][r] = in[r][c] for the real table of pass 0 above: rows r <= L/2,
+// columns c < L, row stride L in and out.
+template <class T>
+__global__ void transpose_half_kernel(const T* __restrict__ in, const FitParams<T>* __restrict__ prm,
+                                      T* __restrict__ out) {
+  __shared__ T tile[32][33];
+  const int L = prm->L, rows = L / 2 + 1;
+  const int c0 = blockIdx.x * 32, r0 = blockIdx.y * 32;
+  if (c0 >= L || r0 >= rows) return;
+  for (int k = threadIdx.y; k < 32; k += blockDim.y) {
+    const int r = r0 + k, c = c0 + threadIdx.x;
+    tile[k][threadIdx.x] = (r < rows && c < L) ? in[(int64_t)r * L + c] : T(0);
+  }
+  __syncthreads();
+  for (int k = threadIdx.y; k < 32; k += blockDim.y) {
+    const int c = c0 + k, r = r0 + threadIdx.x;
+    if (c < L && r < rows) out[(int64_t)c * L + r] = tile[threadIdx.x][k];
+  }
+}
+
 // Convolution of rows with the kernel spectrum: forward transform, product
 // with the real spectrum row (khat, bit-reversed like the row), inverse
 // transform, in one pass over each row. The forward transform's last stages
@@ -920,6 +1016,7 @@ void FitWorkspace<T>::reserve(int D, int64_t n, int cap) {
   if ((size_t)cap * sizeof(C2) >= 40 * 1024) {  // set outside any stream capture
     BHG_CUDA(cudaFuncSetAttribute(fft_rows_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     BHG_CUDA(cudaFuncSetAttribute(fft_conv_rows_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    BHG_CUDA(cudaFuncSetAttribute(kspec_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
   }
   cap_L = cap;
 }
@@ -958,9 +1055,20 @@ void fit_repulsion_cap(FitWorkspace<T>& ws, int D, const T* y, int64_t n, const 
   if (D == 1) {
     fft_rows<T>(ws, g0, dp, 2, cap, false, s, 1, khat);
   } else {
-    fft_rows<T>(ws, g0, dp, 0, cap, false, s, 1);
-    transpose<T>(g0, dp, 0, 0, h0, cap, s);
-    fft_rows<T>(ws, h0, dp, 0, cap, false, s, 0, khat);
+    // packed real transforms (kspec_kernel); g0 and h0 serve as real tables
+    T* a = reinterpret_cast<T*>(g0);
+    T* at = reinterpret_cast<T*>(h0);
+    const int threads = std::min(kFftThreads, std::max(32, cap / 4));
+    const size_t smem = (size_t)cap * sizeof(T2);
+    kspec_kernel<T><<<(unsigned)(cap / 4 + 1), threads, smem, s>>>(0, dp, ws.twiddles(cap, s), ws.twiddles3(cap, s),
+                                                                 cap, nullptr, a);
+    BHG_LAUNCH_CHECK();
+    dim3 tb(32, 8), tg((unsigned)ceil_div(cap, 32), (unsigned)ceil_div(cap / 2 + 1, 32));
+    transpose_half_kernel<T><<<tg, tb, 0, s>>>(a, dp, at);
+    BHG_LAUNCH_CHECK();
+    kspec_kernel<T><<<(unsigned)(cap / 2), threads, smem, s>>>(1, dp, ws.twiddles(cap, s), ws.twiddles3(cap, s), cap,
+                                                             at, khat);
+    BHG_LAUNCH_CHECK();
   }
 
   // charges: spread into the fixed-point accumulator; charges_kernel converts
