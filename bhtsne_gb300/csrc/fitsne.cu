@@ -813,16 +813,17 @@ __global__ void __launch_bounds__(kFftThreads) fft_conv_rows_kernel(typename Cx<
 
 // out[c][r] = in[r][c] for r < rows_in (zero for rows_in <= r < out_cols),
 // c < cols; rows of length L in and out. Sizes from the parameters: sel 0 ->
-// L, 1 -> nodes. Blocks past the current sizes exit.
+// L, 1 -> nodes (out_sel 1: output rows end at column nodes, for a consumer
+// that fills the rest with zeros itself). Blocks past the current sizes exit.
 template <class T>
 __global__ void transpose_kernel(const typename Cx<T>::type* __restrict__ in, const FitParams<T>* __restrict__ prm,
-                                 int rows_sel, int cols_sel, typename Cx<T>::type* __restrict__ out) {
+                                 int rows_sel, int cols_sel, int out_sel, typename Cx<T>::type* __restrict__ out) {
   typedef typename Cx<T>::type T2;
   __shared__ T2 tile[32][33];
   const int L = prm->L;
   const int rows_in = rows_sel == 0 ? L : prm->nodes;
   const int cols = cols_sel == 0 ? L : prm->nodes;
-  const int out_cols = L;
+  const int out_cols = out_sel == 0 ? L : prm->nodes;
   const int64_t ld_in = L, ld_out = L;
   const int c0 = blockIdx.x * 32, r0 = blockIdx.y * 32;
   if (c0 >= cols || r0 >= out_cols) return;
@@ -987,10 +988,10 @@ static void fft_conv_rows(FitWorkspace<T>& ws, typename Cx<T>::type* data, const
 
 template <class T>
 static void transpose(const typename Cx<T>::type* in, const FitParams<T>* dp, int rows_sel, int cols_sel,
-                      typename Cx<T>::type* out, int cap_L, cudaStream_t s) {
+                      typename Cx<T>::type* out, int cap_L, cudaStream_t s, int out_sel = 0) {
   dim3 b(32, 8);
   dim3 g((unsigned)ceil_div(cap_L, 32), (unsigned)ceil_div(cap_L, 32));
-  transpose_kernel<T><<<g, b, 0, s>>>(in, dp, rows_sel, cols_sel, out);
+  transpose_kernel<T><<<g, b, 0, s>>>(in, dp, rows_sel, cols_sel, out_sel, out);
   BHG_LAUNCH_CHECK();
 }
 
@@ -1103,12 +1104,13 @@ void fit_repulsion_cap(FitWorkspace<T>& ws, int D, const T* y, int64_t n, const 
     // forward: rows n0 < nodes, transpose to [k1][n0], rows over n0
     fft_rows<T>(ws, g0, dp, 1, cap, false, s, 2);
     fft_rows<T>(ws, g1, dp, 1, cap, false, s, 2);
-    transpose<T>(g0, dp, 1, 0, h0, cap, s);
-    transpose<T>(g1, dp, 1, 0, h1, cap, s);
+    // (columns n0 >= nodes are zero: not written, filled in by the next pass)
+    transpose<T>(g0, dp, 1, 0, h0, cap, s, 1);
+    transpose<T>(g1, dp, 1, 0, h1, cap, s, 1);
     // product with the kernel spectrum and inverse over k0 (columns n0 <
     // nodes kept), transpose back, rows over k1
-    fft_conv_rows<T>(ws, h0, khat, dp, 0, cap, s);
-    fft_conv_rows<T>(ws, h1, khat, dp, 0, cap, s);
+    fft_conv_rows<T>(ws, h0, khat, dp, 0, cap, s, 2);
+    fft_conv_rows<T>(ws, h1, khat, dp, 0, cap, s, 2);
     transpose<T>(h0, dp, 0, 1, g0, cap, s);
     transpose<T>(h1, dp, 0, 1, g1, cap, s);
     fft_rows<T>(ws, g0, dp, 1, cap, true, s);
