@@ -310,15 +310,25 @@ __device__ __forceinline__ bool fft_load_row(void* smem_dst, const void* gsrc, u
 
 // Fixed-point charges -> the two packed complex grids: the first `nodes`
 // entries of the rows < nodes (one row for D = 1) with row stride L, the
-// cells the spread can reach; each cell is cleared after reading, so the
-// accumulator is zero again for the next spread.
+// cells the spread can reach. clear_cells_kernel then zeroes those cells
+// (write-only), so the accumulator is zero again for the next spread.
 // Fixed-point value times 2^-fix_shift in T: one rounding of the exact
 // product (the scale is a power of two), without the FP64 pipe for f32.
 __device__ __forceinline__ float unfix_value(long long v, float down) { return __ll2float_rn(v) * down; }
 __device__ __forceinline__ double unfix_value(long long v, double down) { return (double)v * down; }
 
 template <class T, int D>
-__global__ void charges_kernel(long long* __restrict__ acc, const FitParams<T>* __restrict__ prm,
+__global__ void clear_cells_kernel(long long* __restrict__ acc, const FitParams<T>* __restrict__ prm) {
+  const int nodes = prm->nodes;
+  const int r = (int)blockIdx.y, c = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+  if (r >= (D == 1 ? 1 : nodes) || c >= nodes) return;
+  longlong2* cell = reinterpret_cast<longlong2*>(acc + 4 * ((int64_t)r * prm->L + c));
+  __stcs(cell, make_longlong2(0, 0));
+  __stcs(cell + 1, make_longlong2(0, 0));
+}
+
+template <class T, int D>
+__global__ void charges_kernel(const long long* __restrict__ acc, const FitParams<T>* __restrict__ prm,
                                typename Cx<T>::type* __restrict__ g0, typename Cx<T>::type* __restrict__ g1) {
   // one cell per thread: row blockIdx.y, column blockIdx.x * blockDim.x +
   // threadIdx.x (the grid covers the capacity; blocks past nodes exit)
@@ -329,10 +339,8 @@ __global__ void charges_kernel(long long* __restrict__ acc, const FitParams<T>* 
   const int L = prm->L;
   {
     const int64_t flat = (int64_t)r * L + c;
-    longlong2* cell = reinterpret_cast<longlong2*>(acc + 4 * flat);
-    const longlong2 p = cell[0], q = cell[1];
-    cell[0] = make_longlong2(0, 0);
-    cell[1] = make_longlong2(0, 0);
+    const longlong2* cell = reinterpret_cast<const longlong2*>(acc + 4 * flat);
+    const longlong2 p = __ldcs(cell), q = __ldcs(cell + 1);
     typename Cx<T>::type a, b;
     a.x = unfix_value(p.x, down);
     a.y = unfix_value(p.y, down);
@@ -1089,8 +1097,13 @@ void fit_repulsion_cap(FitWorkspace<T>& ws, int D, const T* y, int64_t n, const 
   {
     // nodes <= cap / 2 (L <= cap, L >= 2 nodes - 1)
     const dim3 cg((unsigned)ceil_div(cap / 2, 256), D == 1 ? 1u : (unsigned)(cap / 2));
-    if (D == 1) charges_kernel<T, 1><<<cg, 256, 0, s>>>(acc, dp, g0, g1);
-    else charges_kernel<T, 2><<<cg, 256, 0, s>>>(acc, dp, g0, g1);
+    if (D == 1) {
+      charges_kernel<T, 1><<<cg, 256, 0, s>>>(acc, dp, g0, g1);
+      clear_cells_kernel<T, 1><<<cg, 256, 0, s>>>(acc, dp);
+    } else {
+      charges_kernel<T, 2><<<cg, 256, 0, s>>>(acc, dp, g0, g1);
+      clear_cells_kernel<T, 2><<<cg, 256, 0, s>>>(acc, dp);
+    }
   }
   BHG_LAUNCH_CHECK();
 
