@@ -599,6 +599,48 @@ __device__ __forceinline__ bool fft_fill_row(typename Cx<T>::type* s, const type
   return true;
 }
 
+// Wide register phase (sub-rows of M >= 128): each lane holds the four
+// elements 32 k + lane (k = 0..3) of a group of 128, so the stages of spans
+// 128 and 64 are butterflies inside the lane and spans <= 32 are shuffles.
+// w128 = W_128^lane and w64 = W_64^lane; W_128^(32 + lane) = w128 * (-i).
+template <class T2>
+__device__ __forceinline__ void dif_wide_stages(T2 (&x)[4], int lane, const T2 (&w)[5], T2 w64, T2 w128) {
+  T2 w128b;
+  w128b.x = w128.y;
+  w128b.y = -w128.x;
+  const T2 a = cadd(x[0], x[2]), b = cmul(csub(x[0], x[2]), w128);
+  const T2 c = cadd(x[1], x[3]), d = cmul(csub(x[1], x[3]), w128b);
+  x[0] = cadd(a, c);
+  x[1] = cmul(csub(a, c), w64);
+  x[2] = cadd(b, d);
+  x[3] = cmul(csub(b, d), w64);
+#pragma unroll
+  for (int k = 0; k < 4; ++k) x[k] = dif_reg_stages(x[k], lane, 5, w);
+}
+
+template <class T2>
+__device__ __forceinline__ void dit_wide_stages(T2 (&x)[4], int lane, const T2 (&w)[5], T2 w64, T2 w128) {
+#pragma unroll
+  for (int k = 0; k < 4; ++k) x[k] = dit_reg_stages(x[k], lane, 5, w);
+  T2 c64 = w64, c128 = w128, c128b;
+  c64.y = -c64.y;
+  c128.y = -c128.y;
+  c128b.x = -c128.y;  // conj(W_128^(32 + lane)) = conj(w128) * (+i)
+  c128b.y = c128.x;
+  T2 t = cmul(x[1], c64);
+  x[1] = csub(x[0], t);
+  x[0] = cadd(x[0], t);
+  t = cmul(x[3], c64);
+  x[3] = csub(x[2], t);
+  x[2] = cadd(x[2], t);
+  t = cmul(x[2], c128);
+  x[2] = csub(x[0], t);
+  x[0] = cadd(x[0], t);
+  t = cmul(x[3], c128b);
+  x[3] = csub(x[1], t);
+  x[1] = cadd(x[1], t);
+}
+
 constexpr int kFftThreads = 512;
 
 // Row geometry: L = nsub * M with M a power of two and nsub 1 or 3.
@@ -606,13 +648,14 @@ template <class T>
 struct FftRow {
   typedef typename Cx<T>::type T2;
   int L, M, nsub, log2M, small, G, ngroups, tws, tws3, lane, warp, nw;
-  bool lane_ok;
+  bool lane_ok, wide;
   __device__ FftRow(int L_, int cap_L) : L(L_) {
     nsub = (L % 3 == 0) ? 3 : 1;
     M = L / nsub;
     log2M = 0;
     while ((1 << log2M) < M) ++log2M;
-    small = log2M < 5 ? log2M : 5;
+    wide = log2M >= 7;  // groups of 128: stages of span <= 128 in registers
+    small = wide ? 7 : (log2M < 5 ? log2M : 5);
     G = 1 << small;
     ngroups = L >> small;
     tws = cap_L / M;
@@ -620,7 +663,12 @@ struct FftRow {
     lane = threadIdx.x & 31;
     warp = threadIdx.x >> 5;
     nw = blockDim.x >> 5;
-    lane_ok = lane < G;
+    lane_ok = wide || lane < G;
+  }
+  // W_128^lane, W_64^lane of the sub-row length (wide mode)
+  __device__ void wide_twiddles(const T2* __restrict__ tw, T2* w64, T2* w128) const {
+    *w64 = tw[lane * (M >> 6) * tws];
+    *w128 = tw[lane * (M >> 7) * tws];
   }
 };
 
@@ -628,7 +676,7 @@ struct FftRow {
 // rows, 1 -> `nodes` rows, 2 -> one row. The row arrives in shared memory by
 // one bulk copy.
 template <class T>
-__global__ void __launch_bounds__(kFftThreads) fft_rows_kernel(typename Cx<T>::type* __restrict__ data,
+__global__ void __launch_bounds__(kFftThreads, sizeof(T) == 4 ? 3 : 1) fft_rows_kernel(typename Cx<T>::type* __restrict__ data,
                                                               const FitParams<T>* __restrict__ prm, int rows_sel,
                                                               const typename Cx<T>::type* __restrict__ tw,
                                                               const typename Cx<T>::type* __restrict__ tw3, int cap_L,
@@ -644,7 +692,9 @@ __global__ void __launch_bounds__(kFftThreads) fft_rows_kernel(typename Cx<T>::t
   T2* s = reinterpret_cast<T2*>(smem_raw);
   T2* d = data + (int64_t)blockIdx.x * L;
   T2 w[5];
-  lane_twiddles(r.lane, r.M, r.small, tw, r.tws, w);
+  lane_twiddles(r.lane, r.M, r.wide ? 5 : r.small, tw, r.tws, w);
+  T2 w64, w128;
+  if (r.wide) r.wide_twiddles(tw, &w64, &w128);
   T2 zero;
   zero.x = T(0);
   zero.y = T(0);
@@ -657,6 +707,19 @@ __global__ void __launch_bounds__(kFftThreads) fft_rows_kernel(typename Cx<T>::t
     const T inv_total = T(1) / (T)(D == 1 ? (double)L : (double)L * (double)L);
     T* kr = khat_out ? khat_out + (int64_t)blockIdx.x * L : nullptr;
     for (int g = r.warp; g < r.ngroups; g += r.nw) {
+      if (r.wide) {
+        T2 x[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) x[k] = s[g * 128 + 32 * k + r.lane];
+        dif_wide_stages(x, r.lane, w, w64, w128);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          const int e = g * 128 + 32 * k + r.lane;
+          if (kr) kr[e] = x[k].x * inv_total;
+          else d[e] = x[k];
+        }
+        continue;
+      }
       const T2 x = dif_reg_stages(r.lane_ok ? s[g * r.G + r.lane] : zero, r.lane, r.small, w);
       if (r.lane_ok) {
         if (kr) kr[g * r.G + r.lane] = x.x * inv_total;
@@ -666,6 +729,15 @@ __global__ void __launch_bounds__(kFftThreads) fft_rows_kernel(typename Cx<T>::t
     return;
   }
   for (int g = r.warp; g < r.ngroups; g += r.nw) {
+    if (r.wide) {
+      T2 x[4];
+#pragma unroll
+      for (int k = 0; k < 4; ++k) x[k] = s[g * 128 + 32 * k + r.lane];
+      dit_wide_stages(x, r.lane, w, w64, w128);
+#pragma unroll
+      for (int k = 0; k < 4; ++k) s[g * 128 + 32 * k + r.lane] = x[k];
+      continue;
+    }
     const T2 x = dit_reg_stages(r.lane_ok ? s[g * r.G + r.lane] : zero, r.lane, r.small, w);
     if (r.lane_ok) s[g * r.G + r.lane] = x;
   }
@@ -689,7 +761,7 @@ __global__ void __launch_bounds__(kFftThreads) fft_rows_kernel(typename Cx<T>::t
 //          the spectrum times `scale` (1 / L^2).
 // The spectrum is symmetric, so its rows and columns need no distinction.
 template <class T>
-__global__ void __launch_bounds__(kFftThreads) kspec_kernel(int pass, const FitParams<T>* __restrict__ prm,
+__global__ void __launch_bounds__(kFftThreads, sizeof(T) == 4 ? 3 : 1) kspec_kernel(int pass, const FitParams<T>* __restrict__ prm,
                                                            const typename Cx<T>::type* __restrict__ tw,
                                                            const typename Cx<T>::type* __restrict__ tw3, int cap_L,
                                                            const T* __restrict__ in, T* __restrict__ out) {
@@ -703,7 +775,9 @@ __global__ void __launch_bounds__(kFftThreads) kspec_kernel(int pass, const FitP
   const FftRow<T> r(L, cap_L);
   T2* s = reinterpret_cast<T2*>(smem_raw);
   T2 w[5];
-  lane_twiddles(r.lane, r.M, r.small, tw, r.tws, w);
+  lane_twiddles(r.lane, r.M, r.wide ? 5 : r.small, tw, r.tws, w);
+  T2 w64, w128;
+  if (r.wide) r.wide_twiddles(tw, &w64, &w128);
   T2 zero;
   zero.x = T(0);
   zero.y = T(0);
@@ -743,6 +817,19 @@ __global__ void __launch_bounds__(kFftThreads) kspec_kernel(int pass, const FitP
   T* o1 = out + (int64_t)r1 * L;
   T* o2 = out + (int64_t)r2 * L;
   for (int g = r.warp; g < r.ngroups; g += r.nw) {
+    if (r.wide) {
+      T2 x[4];
+#pragma unroll
+      for (int k = 0; k < 4; ++k) x[k] = s[g * 128 + 32 * k + r.lane];
+      dif_wide_stages(x, r.lane, w, w64, w128);
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const int e = g * 128 + 32 * k + r.lane;
+        o1[e] = x[k].x * scale;
+        if (two) o2[e] = x[k].y * scale;
+      }
+      continue;
+    }
     const T2 x = dif_reg_stages(r.lane_ok ? s[g * r.G + r.lane] : zero, r.lane, r.small, w);
     if (r.lane_ok) {
       o1[g * r.G + r.lane] = x.x * scale;
@@ -779,7 +866,7 @@ __global__ void transpose_half_kernel(const T* __restrict__ in, const FitParams<
 // first `nodes` entries of each output row are stored (all that is read
 // afterwards). rows_sel: 0 -> L rows (2-D, second axis), 2 -> one row (1-D).
 template <class T>
-__global__ void __launch_bounds__(kFftThreads) fft_conv_rows_kernel(typename Cx<T>::type* __restrict__ data,
+__global__ void __launch_bounds__(kFftThreads, sizeof(T) == 4 ? 3 : 1) fft_conv_rows_kernel(typename Cx<T>::type* __restrict__ data,
                                                                    const T* __restrict__ khat,
                                                                    const FitParams<T>* __restrict__ prm, int rows_sel,
                                                                    const typename Cx<T>::type* __restrict__ tw,
@@ -797,7 +884,9 @@ __global__ void __launch_bounds__(kFftThreads) fft_conv_rows_kernel(typename Cx<
   T2* d = data + (int64_t)blockIdx.x * L;
   const T* kr = khat + (int64_t)blockIdx.x * L;
   T2 w[5];
-  lane_twiddles(r.lane, r.M, r.small, tw, r.tws, w);
+  lane_twiddles(r.lane, r.M, r.wide ? 5 : r.small, tw, r.tws, w);
+  T2 w64, w128;
+  if (r.wide) r.wide_twiddles(tw, &w64, &w128);
   T2 zero;
   zero.x = T(0);
   zero.y = T(0);
@@ -805,6 +894,22 @@ __global__ void __launch_bounds__(kFftThreads) fft_conv_rows_kernel(typename Cx<
   if (r.nsub == 3) r3_dif_stage<T2, T>(s, r.M, tw3, r.tws3);
   dif_smem_stages(s, r.M, r.log2M, r.small, tw, r.tws, r.nsub);
   for (int g = r.warp; g < r.ngroups; g += r.nw) {
+    if (r.wide) {
+      T2 x[4];
+#pragma unroll
+      for (int k = 0; k < 4; ++k) x[k] = s[g * 128 + 32 * k + r.lane];
+      dif_wide_stages(x, r.lane, w, w64, w128);
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const T kv = kr[g * 128 + 32 * k + r.lane];
+        x[k].x *= kv;
+        x[k].y *= kv;
+      }
+      dit_wide_stages(x, r.lane, w, w64, w128);
+#pragma unroll
+      for (int k = 0; k < 4; ++k) s[g * 128 + 32 * k + r.lane] = x[k];
+      continue;
+    }
     const int e = g * r.G + r.lane;
     T2 x = dif_reg_stages(r.lane_ok ? s[e] : zero, r.lane, r.small, w);
     const T k = r.lane_ok ? kr[e] : T(0);
