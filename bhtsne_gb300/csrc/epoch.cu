@@ -219,28 +219,132 @@ __global__ void slot_len_kernel(const uint64_t* __restrict__ rows, const uint32_
 }
 
 // One warp per slot: the CSR row of row_of_slot[s] moved to slot order with
-// its columns mapped to slots and sorted by slot (bitonic in shared memory),
-// so that a warp's neighbour gathers fall on few cache lines. Columns within
-// a row are distinct, so the order is unique. Rows longer than kSlotSortMax
-// keep their order (only locality is lost).
+// its columns mapped to slots and sorted by slot, so that a warp's neighbour
+// gathers fall on few cache lines. Columns within a row are distinct, so the
+// order is unique whatever the sorting network. Rows of at most kSlotRegMax
+// entries sort in registers (slot_rows_short_kernel), which lists the longer
+// ones (hub points of the kNN graph); those sort in shared memory up to
+// kSlotSortMax entries (slot_rows_long_kernel), and rows longer still keep
+// their order (only locality is lost: sorting them as well saved 2 % of the
+// attractive pass and cost more than that in the re-layout).
+constexpr int kSlotRegMax = 256;
 constexpr int kSlotSortMax = 1024;
 constexpr int kSlotWarps = 4;
 
+// Bitonic sort of one row of L <= 32 E entries held E per lane: element e of
+// the padded row is register e % E of lane e / E. Strides below E compare
+// registers within a lane; larger strides pair lane l with lane l ^ (stride /
+// E) by shuffles (the partner's value from before the step).
+template <class T, int E>
+__device__ __forceinline__ void slot_row_sort_regs(const uint32_t* __restrict__ crow, const T* __restrict__ vrow, int L,
+                                                   const uint32_t* __restrict__ inv, uint32_t* __restrict__ cout,
+                                                   T* __restrict__ vout, int lane) {
+  uint32_t k[E];
+  T v[E];
+#pragma unroll
+  for (int r = 0; r < E; ++r) {
+    const int e = lane * E + r;
+    k[r] = e < L ? inv[crow[e]] : 0xffffffffu;  // padding sorts last
+    v[r] = e < L ? vrow[e] : T(0);
+  }
+#pragma unroll
+  for (int size = 2; size <= 32 * E; size <<= 1) {
+#pragma unroll
+    for (int stride = size >> 1; stride > 0; stride >>= 1) {
+      if (stride < E) {
+#pragma unroll
+        for (int r = 0; r < E; ++r) {
+          if (r & stride) continue;
+          const bool up = ((lane * E + r) & size) == 0;
+          const uint32_t a = k[r], b = k[r | stride];
+          if ((a > b) == up) {
+            k[r] = b;
+            k[r | stride] = a;
+            const T t = v[r];
+            v[r] = v[r | stride];
+            v[r | stride] = t;
+          }
+        }
+      } else {
+#pragma unroll
+        for (int r = 0; r < E; ++r) {
+          const int e = lane * E + r;
+          const uint32_t pk = __shfl_xor_sync(kFull, k[r], stride / E);
+          const T pv = __shfl_xor_sync(kFull, v[r], stride / E);
+          // the lower element of an ascending pair (or the upper of a
+          // descending one) keeps the minimum
+          const bool take_min = ((e & stride) == 0) == ((e & size) == 0);
+          if (take_min ? pk < k[r] : pk > k[r]) {
+            k[r] = pk;
+            v[r] = pv;
+          }
+        }
+      }
+    }
+  }
+#pragma unroll
+  for (int r = 0; r < E; ++r) {
+    const int e = lane * E + r;
+    if (e < L) {
+      cout[e] = k[r];
+      vout[e] = v[r];
+    }
+  }
+}
+
 template <class T>
-__global__ void __launch_bounds__(kSlotWarps * 32) slot_rows_kernel(
+__global__ void __launch_bounds__(256, 4) slot_rows_short_kernel(
     const uint64_t* __restrict__ rows, const uint32_t* __restrict__ cols, const T* __restrict__ vals,
     const uint32_t* __restrict__ row_of_slot, const uint32_t* __restrict__ inv, int64_t n,
+    const uint64_t* __restrict__ rows_s, uint32_t* __restrict__ cols_s, T* __restrict__ vals_s,
+    uint32_t* __restrict__ long_rows) {
+  const int lane = threadIdx.x & 31;
+  const int64_t nwarps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  for (int64_t slot = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; slot < n; slot += nwarps) {
+    const int64_t r = row_of_slot[slot];
+    const int64_t e0 = (int64_t)rows[r];
+    const int L = (int)(rows[r + 1] - rows[r] > (uint64_t)kSlotRegMax ? kSlotRegMax + 1 : rows[r + 1] - rows[r]);
+    if (L > kSlotRegMax) {  // listed for slot_rows_long_kernel
+      if (lane == 0) long_rows[1 + atomicAdd(long_rows, 1u)] = (uint32_t)slot;
+      continue;
+    }
+    const int64_t o = (int64_t)rows_s[slot];
+    if (L <= 1) {
+      if (L == 1 && lane == 0) {
+        cols_s[o] = inv[cols[e0]];
+        vals_s[o] = vals[e0];
+      }
+    } else if (L <= 32) {
+      slot_row_sort_regs<T, 1>(cols + e0, vals + e0, L, inv, cols_s + o, vals_s + o, lane);
+    } else if (L <= 64) {
+      slot_row_sort_regs<T, 2>(cols + e0, vals + e0, L, inv, cols_s + o, vals_s + o, lane);
+    } else if (L <= 128) {
+      slot_row_sort_regs<T, 4>(cols + e0, vals + e0, L, inv, cols_s + o, vals_s + o, lane);
+    } else {
+      slot_row_sort_regs<T, 8>(cols + e0, vals + e0, L, inv, cols_s + o, vals_s + o, lane);
+    }
+  }
+}
+
+// The listed rows, one warp each: a bitonic sort over the next power of two
+// >= L in the warp's shared-memory slice.
+template <class T>
+__global__ void __launch_bounds__(kSlotWarps * 32) slot_rows_long_kernel(
+    const uint64_t* __restrict__ rows, const uint32_t* __restrict__ cols, const T* __restrict__ vals,
+    const uint32_t* __restrict__ row_of_slot, const uint32_t* __restrict__ inv, const uint32_t* __restrict__ long_rows,
     const uint64_t* __restrict__ rows_s, uint32_t* __restrict__ cols_s, T* __restrict__ vals_s) {
   __shared__ uint32_t sk[kSlotWarps][kSlotSortMax];
   __shared__ T sv[kSlotWarps][kSlotSortMax];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int64_t nwarps = (int64_t)gridDim.x * kSlotWarps;
-  for (int64_t slot = (int64_t)blockIdx.x * kSlotWarps + w; slot < n; slot += nwarps) {
+  const uint32_t count = long_rows[0];
+  const uint32_t nwarps = gridDim.x * kSlotWarps;
+  for (uint32_t q = blockIdx.x * kSlotWarps + w; q < count; q += nwarps) {
+    const int64_t slot = long_rows[1 + q];
     const int64_t r = row_of_slot[slot];
     const int64_t e0 = (int64_t)rows[r];
     const int64_t L = (int64_t)(rows[r + 1] - rows[r]);
     const int64_t o = (int64_t)rows_s[slot];
-    if (L > kSlotSortMax || L <= 1) {
+    if (L > kSlotSortMax) {
       for (int64_t t = lane; t < L; t += 32) {
         cols_s[o + t] = inv[cols[e0 + t]];
         vals_s[o + t] = vals[e0 + t];
@@ -250,7 +354,7 @@ __global__ void __launch_bounds__(kSlotWarps * 32) slot_rows_kernel(
     int P = 32;
     while (P < L) P <<= 1;
     for (int t = lane; t < P; t += 32) {
-      sk[w][t] = t < L ? inv[cols[e0 + t]] : 0xffffffffu;
+      sk[w][t] = t < L ? inv[cols[e0 + t]] : 0xffffffffu;  // padding sorts last
       sv[w][t] = t < L ? vals[e0 + t] : T(0);
     }
     __syncwarp();
@@ -600,8 +704,13 @@ void launch_renumber(int D, const uint32_t* order, int64_t n, Renumbering& r, T*
   uint32_t* cols_s = static_cast<uint32_t*>(r.cols.ensure((size_t)std::max<int64_t>(nnz, 1) * 4));
   T* vals_s = static_cast<T*>(r.vals.ensure((size_t)std::max<int64_t>(nnz, 1) * sizeof(T)));
   if (nnz > 0) {
-    slot_rows_kernel<T><<<(unsigned)std::min<int64_t>(ceil_div(n, kSlotWarps), 16 * 152), kSlotWarps * 32, 0, s>>>(
-        rows, cols, vals, r.ext.template as<uint32_t>(), inv, n, rows_s, cols_s, vals_s);
+    uint32_t* long_rows = static_cast<uint32_t*>(r.long_rows.ensure((size_t)(n + 1) * 4));
+    BHG_CUDA(cudaMemsetAsync(long_rows, 0, 4, s));
+    slot_rows_short_kernel<T><<<(unsigned)std::min<int64_t>(ceil_div(n, 8), 4 * 152), 256, 0, s>>>(
+        rows, cols, vals, r.ext.template as<uint32_t>(), inv, n, rows_s, cols_s, vals_s, long_rows);
+    BHG_LAUNCH_CHECK();
+    slot_rows_long_kernel<T><<<(unsigned)std::min<int64_t>(ceil_div(n, kSlotWarps), 8 * 152), kSlotWarps * 32, 0, s>>>(
+        rows, cols, vals, r.ext.template as<uint32_t>(), inv, long_rows, rows_s, cols_s, vals_s);
     BHG_LAUNCH_CHECK();
   }
   r.active = true;

@@ -47,6 +47,7 @@ void launch_random_init(T* y, int64_t count, uint64_t seed, cudaStream_t s);
 struct Renumbering {
   bool active = false;
   DevBuf ext, ext_alt, inv, rows, cols, vals, len, scan_tmp;
+  DevBuf long_rows;  // u32 count, then the slots of the rows longer than the register sort takes
 };
 
 template <class T>

@@ -273,6 +273,47 @@ def test_locality_renumbering_preserves_the_fit(gpu, monkeypatch, method):
     assert same_cluster_fraction(e1, lab) > 0.95
 
 
+def hub_inputs(case, oracle):
+    """kNN tables whose symmetrised rows reach every re-layout path: 'hubs'
+    (128-d blobs: rows of 30 to ~1300 entries), 'star' (points on the unit
+    sphere in 128-d plus one at the origin, which is every point's nearest
+    neighbour: one row of n - 1 = 8999 entries)."""
+    if case == "hubs":
+        X, _ = blobs(4000, 128, 2, 7, spread=3.0)
+    else:
+        rng = np.random.default_rng(3)
+        X = rng.normal(size=(9000, 128))
+        X /= np.linalg.norm(X, axis=1, keepdims=True)
+        X[0] = 0.0
+        X = X.astype(np.float32)
+    idx, dist = oracle.knn(X, 90 if case == "hubs" else 30)
+    return X, idx, dist
+
+
+@pytest.mark.parametrize("case,dtype", [("hubs", np.float32), ("hubs", np.float64), ("star", np.float32)])
+def test_renumbering_keeps_every_affinity(gpu, oracle, monkeypatch, case, dtype):
+    """The slot-ordered CSR of the locality renumbering (rows of <= 256
+    entries sorted in registers, longer ones in shared memory, rows past 1024
+    copied in order) holds exactly the original entries: one epoch after the first
+    renumbering (epoch 50) the embedding equals an un-renumbered fit's up to
+    summation order. A lost or doubled entry moves its point by lr * p_ij."""
+    X, idx, dist = hub_inputs(case, oracle)
+    n = X.shape[0]
+    perp = 30.0 if case == "hubs" else 10.0
+    rows = oracle.symmetrize(idx.astype(np.uint64), oracle.search_beta(dist, perp)[0])[0]
+    assert np.diff(rows.astype(np.int64)).max() > (1024 if case == "hubs" else 8192)
+    seed = lcg_samples(n, 2, 17).astype(dtype)
+    out = {}
+    for every in ("0", "50"):
+        monkeypatch.setenv("BHTSNE_RENUMBER_EVERY", every)
+        t = gpu.TSNE(n, D=2, dtype=dtype).perplexity(perp).epochs(51).initial_embedding(seed)
+        t.barnes_hut_with_neighbors(0.5, (idx, dist.astype(dtype)))
+        out[every] = t.embedding()
+    e0, e1 = out["0"], out["50"]
+    assert np.all(np.isfinite(e1))
+    assert np.abs(e1 - e0).max() <= 1e-4 * np.abs(e0).max(), np.abs(e1 - e0).max() / np.abs(e0).max()
+
+
 @pytest.mark.parametrize("D", [4, 5, 7])
 def test_wide_barnes_hut_fit_matches_oracle(gpu, oracle, D):
     """Barnes-Hut into D = 4..7 (128-bit Morton codes from D = 5): same
