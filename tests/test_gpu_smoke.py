@@ -105,10 +105,10 @@ def test_fit_gradient(gpu, oracle, D):
 
 @pytest.mark.parametrize("D,half,z_floor", [(1, 900.0, 3e-2), (2, 350.0, 1e-4), (2, 150.0, 1e-4)])
 def test_fit_gradient_large_grid(gpu, oracle, D, half, z_floor):
-    """Extents up to the 1000-box cap: the largest transforms (L = 8192 here,
+    """Extents up to the 1000-box cap: the largest transforms (L = 6144 here,
     7-smooth lengths up to 6000 in the oracle). At |y| in the hundreds the
     force y phi_0 - phi_1 cancels in f32, so the reference's own f32 result
-    carries errors near 1e-3; both f32 results are judged against the same
+    carries errors near 1e-3; both f32 results are measured against the same
     interpolation in f64, and the GPU must be as accurate as the reference's
     f32 path (within 2x of its error, or 1e-4).
 
