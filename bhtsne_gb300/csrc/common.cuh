@@ -62,6 +62,78 @@ constexpr unsigned kFull = 0xffffffffu;
 __device__ __forceinline__ float rcp_rn(float x) { return __frcp_rn(x); }
 __device__ __forceinline__ double rcp_rn(double x) { return __drcp_rn(x); }
 
+// Conversions between f32 and int64 with round-to-nearest-even, written with
+// 32/64-bit integer operations only (the hardware conversions of 64-bit
+// integers are slow on this part). f32_to_i64_rn saturates like the IEEE
+// conversion (NaN and -inf to INT64_MIN, +inf to INT64_MAX).
+__host__ __device__ __forceinline__ uint32_t f32_bits(float x) {
+#ifdef __CUDA_ARCH__
+  return __float_as_uint(x);
+#else
+  uint32_t b;
+  __builtin_memcpy(&b, &x, 4);
+  return b;
+#endif
+}
+
+__host__ __device__ __forceinline__ float f32_from_bits(uint32_t b) {
+#ifdef __CUDA_ARCH__
+  return __uint_as_float(b);
+#else
+  float x;
+  __builtin_memcpy(&x, &b, 4);
+  return x;
+#endif
+}
+
+__host__ __device__ __forceinline__ float i64_to_f32_rn(long long v) {
+  const unsigned long long a = v < 0 ? 0ull - (unsigned long long)v : (unsigned long long)v;
+  if (a == 0) return 0.0f;
+#ifdef __CUDA_ARCH__
+  const int e = 63 - __clzll((long long)a);  // position of the leading one
+#else
+  const int e = 63 - __builtin_clzll(a);
+#endif
+  unsigned long long m;
+  uint32_t ex = (uint32_t)(e + 127);
+  if (e <= 23) {
+    m = a << (23 - e);
+  } else {
+    const int sh = e - 23;
+    m = a >> sh;
+    const unsigned long long rem = a & ((1ull << sh) - 1), half = 1ull << (sh - 1);
+    if (rem > half || (rem == half && (m & 1))) ++m;
+    if (m == (1ull << 24)) {  // rounded up to the next power of two
+      m >>= 1;
+      ++ex;
+    }
+  }
+  return f32_from_bits((v < 0 ? 0x80000000u : 0u) | (ex << 23) | ((uint32_t)m & 0x7FFFFFu));
+}
+
+__host__ __device__ __forceinline__ long long f32_to_i64_rn(float x) {
+  const uint32_t b = f32_bits(x);
+  const uint32_t ex = (b >> 23) & 0xFFu;
+  const bool neg = (b >> 31) != 0;
+  if (ex < 126) return 0;  // |x| < 0.5
+  if (ex >= 190) {         // |x| >= 2^63, inf, NaN
+    const bool nan = ex == 255 && (b & 0x7FFFFFu) != 0;
+    return (neg || nan) ? (long long)0x8000000000000000ull : 0x7FFFFFFFFFFFFFFFll;
+  }
+  const unsigned long long m = (b & 0x7FFFFFu) | 0x800000u;
+  const int k = (int)ex - 150;  // x = m 2^k
+  unsigned long long a;
+  if (k >= 0) {
+    a = m << k;
+  } else {
+    const int sh = -k;  // 1 .. 24
+    a = m >> sh;
+    const unsigned long long rem = m & ((1ull << sh) - 1), half = 1ull << (sh - 1);
+    if (rem > half || (rem == half && (a & 1))) ++a;
+  }
+  return neg ? (long long)(0ull - a) : (long long)a;
+}
+
 // Numeric limits usable on the device.
 template <class T>
 struct Lim;

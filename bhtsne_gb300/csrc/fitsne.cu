@@ -136,6 +136,8 @@ __global__ void fit_params_kernel(const BoxParams<T>* __restrict__ box, int64_t 
   int eb = 0;
   frexp(bound, &eb);
   out->fix_shift = 62 - eb;
+  out->up = (T)ldexp(1.0, out->fix_shift);
+  out->down = (T)ldexp(1.0, -out->fix_shift);
   out->lo = lo;
   out->extent = extent;
   out->box_width = box_width;
@@ -161,6 +163,12 @@ __device__ __forceinline__ void locate(T v, const FitParams<T>& p, const Lagrang
   lb.weights(local, w);
 }
 
+// A charge already scaled by 2^fix_shift (exact: a power of two) rounded to the
+// nearest integer. f32 goes through integer operations (no FP64 pipe); the
+// result equals the FP64 conversion of the same value.
+__device__ __forceinline__ long long to_fixed(float x) { return f32_to_i64_rn(x); }
+__device__ __forceinline__ long long to_fixed(double x) { return __double2ll_rn(x); }
+
 // Charges of one point in fixed point: 3^D nodes x (D + 2) values. Integer
 // sums are exact and order-free, so the grid does not depend on how the adds
 // are grouped.
@@ -173,7 +181,6 @@ __global__ void spread_kernel(const T* __restrict__ y, int64_t n, const FitParam
   const FitParams<T> p = *prm;
   const Lagrange3<T> lb;
   const int L = p.L;
-  const double up = ldexp(1.0, p.fix_shift);
   constexpr int combos = D == 1 ? 3 : 9;
   constexpr int NV = D + 2;
   int box[D];
@@ -198,10 +205,10 @@ __global__ void spread_kernel(const T* __restrict__ y, int64_t n, const FitParam
       rem /= 3;
       wt = wt * w[a][k];
     }
-    v[c][0] = __double2ll_rn((double)(wt * p.scale) * up);
-    v[c][1] = __double2ll_rn((double)(wt * yv[0]) * up);
-    if (D == 2) v[c][D] = __double2ll_rn((double)(wt * yv[D - 1]) * up);
-    v[c][NV - 1] = __double2ll_rn((double)(wt * (sq / p.scale)) * up);
+    v[c][0] = to_fixed((wt * p.scale) * p.up);
+    v[c][1] = to_fixed((wt * yv[0]) * p.up);
+    if (D == 2) v[c][D] = to_fixed((wt * yv[D - 1]) * p.up);
+    v[c][NV - 1] = to_fixed((wt * (sq / p.scale)) * p.up);
     if (!valid) {
 #pragma unroll
       for (int q = 0; q < NV; ++q) v[c][q] = 0;
@@ -314,7 +321,7 @@ __device__ __forceinline__ bool fft_load_row(void* smem_dst, const void* gsrc, u
 // (write-only), so the accumulator is zero again for the next spread.
 // Fixed-point value times 2^-fix_shift in T: one rounding of the exact
 // product (the scale is a power of two), without the FP64 pipe for f32.
-__device__ __forceinline__ float unfix_value(long long v, float down) { return __ll2float_rn(v) * down; }
+__device__ __forceinline__ float unfix_value(long long v, float down) { return i64_to_f32_rn(v) * down; }
 __device__ __forceinline__ double unfix_value(long long v, double down) { return (double)v * down; }
 
 template <class T, int D>
@@ -335,7 +342,7 @@ __global__ void charges_kernel(const long long* __restrict__ acc, const FitParam
   const int nodes = prm->nodes;
   const int r = (int)blockIdx.y, c = (int)(blockIdx.x * blockDim.x + threadIdx.x);
   if (r >= (D == 1 ? 1 : nodes) || c >= nodes) return;
-  const T down = (T)ldexp(1.0, -prm->fix_shift);
+  const T down = prm->down;
   const int L = prm->L;
   {
     const int64_t flat = (int64_t)r * L + c;

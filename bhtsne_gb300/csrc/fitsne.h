@@ -17,6 +17,7 @@ struct FitParams {
   int boxes, nodes, L;
   int need_L;     // transform length the embedding needs (L unless the capacity was too small)
   int fix_shift;  // charges are accumulated as integers in units of 2^-fix_shift
+  T up, down;     // 2^fix_shift and 2^-fix_shift
 };
 
 struct FitGrid {
