@@ -186,6 +186,9 @@ def run_ours(args):
     launches = ctx.lib.bhtsne_launch_count() - launches0
     loop_ms = t.timings()["loop_ms"]
     loop_ms = barrier_and_max(loop_ms, ws)
+    # the embedding the profiled epochs start from (its Barnes-Hut work is
+    # counted in the CPU leg); copied out after the timed region
+    y_profiled = t.embedding().reshape(n, 2) if rank == 0 and not args.no_cpu else None
     # per-phase device times from a separate profiled pass (events between
     # phases force eager launches, so it is not the timed region)
     t.profile(True)
@@ -227,7 +230,6 @@ def run_ours(args):
     # kernel at N = 300,000 (429.7 MB for 52.5M CSR entries), scaled by this
     # run's entries; null for the other phases
     traffic = {"attractive": int(429.7e6 * nnz / 52.5e6)}
-    interactions = None
     roofline = {"kernel": {"repulsion": "bh_traverse_kernel", "attractive": "attractive_task_kernel+attractive_fixup_kernel",
                            "update": "update_kernel+recenter_bbox_kernel", "tree": "morton+radix sort+tree build"}[dom],
                 "bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
@@ -259,7 +261,17 @@ def run_ours(args):
 
     cpu = None
     if rank == 0 and not args.no_cpu:
-        cpu = cpu_baseline_sample(aff, emb.reshape(n, 2), args.cpu_epochs)
+        cpu = cpu_baseline_sample(aff, emb.reshape(n, 2), args.cpu_epochs, count_at=y_profiled)
+    traversal = None
+    if cpu and "bh_work_per_epoch" in cpu:
+        w = cpu["bh_work_per_epoch"]
+        sec = per["repulsion"] / 1e3
+        traversal = {"kernel": "bh_traverse_kernel", "interactions_per_epoch": w["interactions"],
+                     "theta_tests_per_epoch": w["theta_tests"],
+                     "interactions_per_s": round(w["interactions"] / sec, 1),
+                     "theta_tests_per_s": round(w["theta_tests"] / sec, 1),
+                     "note": "work counted by the oracle's walk of the same tree and theta test at the embedding "
+                             "the profiled epochs start from, over the profiled repulsion time"}
     configs = run_configs(args, ctx, aff, rank) if args.configs else None
 
     out = {
@@ -277,6 +289,7 @@ def run_ours(args):
                                 "frac": round(att_gbs / peak, 4)},
         "phase_ms_per_epoch": {k: round(v, 4) for k, v in per.items()},
         "epochs_per_s_incl_renumbering": period,
+        "traversal": traversal,
         "setup_s": round(setup_s, 3), "affinity_ms": round(tm["affinity_ms"], 2),
         "gpu_launches": int(launches),
         "clocks": clk.summary(),
@@ -562,9 +575,11 @@ def run_serving(args, ctx):
     }
 
 
-def cpu_baseline_sample(aff, y0, epochs):
+def cpu_baseline_sample(aff, y0, epochs, count_at=None):
     """The oracle (C++/OpenMP restatement) on the same CSR and a 1M-point
-    embedding for a bounded number of epochs."""
+    embedding for a bounded number of epochs. With count_at, also the work of
+    one Barnes-Hut repulsion pass at that embedding (theta tests and accepted
+    cells of the reference's walk), untimed."""
     from oracle import pyoracle as O
     n = y0.shape[0]
     O.build()
@@ -576,8 +591,15 @@ def cpu_baseline_sample(aff, y0, epochs):
     w0 = time.perf_counter()
     t.barnes_hut(0.5, dummy)
     s = time.perf_counter() - w0
-    return {"value": round(epochs / s, 4), "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"{epochs} Barnes-Hut epochs at N={n} on the same CSR (oracle C++ restatement, OpenMP)"}
+    out = {"value": round(epochs / s, 4), "unit": UNIT, "cores": threads, "kind": "port",
+           "sample": f"{epochs} Barnes-Hut epochs at N={n} on the same CSR (oracle C++ restatement, OpenMP)"}
+    if count_at is not None:
+        try:
+            vis, inter = O.bh_interactions(np.ascontiguousarray(count_at, dtype=np.float32), 0.5)
+            out["bh_work_per_epoch"] = {"theta_tests": int(vis), "interactions": int(inter)}
+        except Exception as exc:  # a measurement aid: never fails the run
+            out["bh_work_per_epoch_error"] = str(exc)[:200]
+    return out
 
 
 def run_reference(args):

@@ -542,6 +542,35 @@ struct Arena {
       for (int a = 0; a < D; ++a) neg[a] += magnitude * disp[a];
     }
   }
+
+  // The same walk counting theta tests (node visits) and accepted cells
+  // (interactions); the self leaf and its duplicates are visited, not counted.
+  void count_visits(int64_t index, T theta_sq, const T* y, int64_t* visits, int64_t* interactions,
+                    std::vector<uint32_t>& stack) const {
+    if (nodes.empty()) return;
+    const T* q = y + index * D;
+    size_t top = 0;
+    if (stack.size() < 64) stack.resize(64);
+    stack[top++] = 0;
+    while (top > 0) {
+      top -= 1;
+      const Node<T, D>& nd = nodes[stack[top]];
+      *visits += 1;
+      T dist = T(0);
+      for (int a = 0; a < D; ++a) {
+        T delta = q[a] - nd.com[a];
+        dist += delta * delta;
+      }
+      if (nd.first_child == SENTINEL) {
+        if (dist == T(0)) continue;
+      } else if (level_half_width_sq[nd.level] >= theta_sq * dist) {
+        if (stack.size() < top + nd.child_count + 1) stack.resize(2 * (top + nd.child_count + 1));
+        for (uint32_t c = 0; c < nd.child_count; ++c) stack[top++] = nd.first_child + c;
+        continue;
+      }
+      *interactions += 1;
+    }
+  }
 };
 
 template <class T, int D>
@@ -596,6 +625,24 @@ T bh_repulsion(Arena<T, D>& arena, const T* y, int64_t n, T theta, T* neg, T* q_
   T z = T(0);
   for (int64_t i = 0; i < n; ++i) z = z + q_sums[i];
   return z;
+}
+
+// Work of one Barnes-Hut repulsion pass at y: theta tests and accepted cells
+// summed over all points (measurement aid for the traversal's rate).
+template <class T, int D>
+void bh_count(const T* y, int64_t n, T theta, int64_t* visits_out, int64_t* interactions_out) {
+  Arena<T, D> a;
+  a.rebuild(y, n);
+  const T theta_sq = theta * theta;
+  int64_t vis = 0, inter = 0;
+#pragma omp parallel reduction(+ : vis, inter)
+  {
+    std::vector<uint32_t> stack(256);
+#pragma omp for schedule(dynamic, 256)
+    for (int64_t i = 0; i < n; ++i) a.count_visits(i, theta_sq, y, &vis, &inter, stack);
+  }
+  *visits_out = vis;
+  *interactions_out = inter;
 }
 
 // ---------------------------------------------------------------------------
@@ -1420,6 +1467,19 @@ int orc_bh_repulsion(int dtype, int32_t D, const void* y, int64_t n, double thet
         }))
       return 22;
     *z_out = (double)z;
+  });
+  return 0;
+}
+
+// Theta tests and accepted cells of one Barnes-Hut repulsion pass at y.
+int orc_bh_interactions(int dtype, int32_t D, const void* y, int64_t n, double theta, int64_t* visits_out,
+                        int64_t* interactions_out) {
+  ORC_T(dtype, {
+    if (!with_d<2, 7>(D, [&](auto dc) {
+          constexpr int DD = decltype(dc)::value;
+          bh_count<T, DD>((const T*)y, n, (T)theta, visits_out, interactions_out);
+        }))
+      return 22;
   });
   return 0;
 }

@@ -51,6 +51,7 @@ def lib():
             "orc_normalize": (None, [C.c_int, vp, i64, dbl]),
             "orc_edge_forces": (C.c_int, [C.c_int, i32, vp, i64, u64p, u32p, vp, vp]),
             "orc_bh_repulsion": (C.c_int, [C.c_int, i32, vp, i64, dbl, vp, vp, C.POINTER(C.c_double)]),
+            "orc_bh_interactions": (C.c_int, [C.c_int, i32, vp, i64, dbl, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
             "orc_bh_tree": (i64, [C.c_int, i32, vp, i64, vp, vp, vp, vp, vp, vp, vp]),
             "orc_fit_repulsion": (C.c_int, [C.c_int, i32, vp, i64, vp, C.POINTER(C.c_double), vp]),
             "orc_gradient_step": (None, [C.c_int, vp, vp, vp, vp, vp, i64, dbl, dbl, dbl]),
@@ -157,6 +158,16 @@ def bh_repulsion(y, theta):
     rc = lib().orc_bh_repulsion(_dt(y), D, _p(y), n, float(theta), _p(neg), _p(q), C.byref(z))
     assert rc == 0
     return neg, q, z.value
+
+
+def bh_interactions(y, theta):
+    """Theta tests and accepted cells of one Barnes-Hut repulsion pass at y."""
+    y = np.ascontiguousarray(y)
+    n, D = y.shape
+    vis, inter = C.c_int64(), C.c_int64()
+    rc = lib().orc_bh_interactions(_dt(y), D, _p(y), n, float(theta), C.byref(vis), C.byref(inter))
+    assert rc == 0
+    return vis.value, inter.value
 
 
 def bh_tree(y):

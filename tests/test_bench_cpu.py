@@ -45,3 +45,29 @@ def test_reference_arm_prints_the_contract_line():
     assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["cores"] >= 1
     assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["d2h_bytes_per_step"] == 0
     assert line["config"]["workload"] == "bh2d_1M_d128" and line["config"]["n_points"] == 20000
+
+
+def test_interaction_count_at_tiny_theta_is_all_pairs(oracle):
+    """With theta -> 0 every internal cell is opened, so each point interacts
+    with every other leaf once: n (n - 1) accepted cells."""
+    rng = np.random.default_rng(4)
+    y = rng.normal(size=(400, 2)).astype(np.float32)
+    vis, inter = oracle.bh_interactions(y, 1e-6)
+    assert inter == 400 * 399 and vis > inter
+    vis5, inter5 = oracle.bh_interactions(y, 0.5)
+    assert 0 < inter5 < inter and inter5 <= vis5
+
+
+def test_cpu_leg_counts_barnes_hut_work(oracle):
+    from types import SimpleNamespace
+    X, _ = bench.make_workload(6000)
+    idx, dist = oracle.knn(X, 30)
+    t = oracle.TSNE(6000).perplexity(10.0).epochs(0).seed(3)
+    t.barnes_hut_with_neighbors(0.5, idx, dist)
+    rows, cols, vals, perp = t.affinities()
+    aff = SimpleNamespace(rows=rows, columns=cols, values=vals, perplexity=perp)
+    y0 = t.embedding().reshape(6000, 2)
+    out = bench.cpu_baseline_sample(aff, y0, 2, count_at=y0)
+    assert out["kind"] == "port" and out["value"] > 0
+    w = out["bh_work_per_epoch"]
+    assert 0 < w["interactions"] <= w["theta_tests"]
