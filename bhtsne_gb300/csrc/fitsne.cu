@@ -358,6 +358,64 @@ __global__ void charges_kernel(const long long* __restrict__ acc, const FitParam
   }
 }
 
+// 1-D grids (at most 3000 nodes): the linear convolution of the three charge
+// rows with the squared Cauchy kernel, summed directly in FP64 instead of by
+// f32 transforms. The kernel values are the reference's (computed in T as the
+// transform path builds its rows), the charges the exact fixed-point sums; the
+// result is the convolution the transforms compute, without their rounding,
+// which the 1-D Z terms (|y|^2 phi_0 against phi_2, both near 1e6 at the
+// 1000-box cap) would amplify to percent level.
+// tab: kernel K(lag) at [0, nodes), charge row k at [cap (1 + k), + nodes),
+// potential k at [cap (4 + k), + nodes).
+template <class T>
+__global__ void conv1d_prep_kernel(const long long* __restrict__ acc, const FitParams<T>* __restrict__ prm, int cap,
+                                   double* __restrict__ tab) {
+  const int nodes = prm->nodes;
+  const int i = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+  if (i >= nodes) return;
+  const T dc = prm->spacing * (T)(double)i;
+  T sq = T(0);
+  sq = sq + dc * dc;
+  const T cauchy = T(1) / (T(1) + sq);
+  tab[i] = (double)(cauchy * cauchy);
+  const double down = (double)prm->down;  // a power of two
+#pragma unroll
+  for (int k = 0; k < 3; ++k) tab[(int64_t)cap * (1 + k) + i] = (double)acc[4 * (int64_t)i + k] * down;
+}
+
+// One warp per output node j: lanes take the source nodes i = lane + 32 t,
+// then a fixed shuffle tree adds the 32 partial sums (deterministic). The
+// node potentials stay in FP64 (tab at [cap (4 + k), + nodes)) for the
+// gather, which interpolates them in FP64.
+template <class T>
+__global__ void conv1d_direct_kernel(double* __restrict__ tab, const FitParams<T>* __restrict__ prm, int cap) {
+  const int nodes = prm->nodes;
+  const int j = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (j >= nodes) return;  // uniform per warp
+  const double* q0 = tab + cap;
+  const double* q1 = tab + 2 * (int64_t)cap;
+  const double* q2 = tab + 3 * (int64_t)cap;
+  double s0 = 0.0, s1 = 0.0, s2 = 0.0;
+  for (int i = lane; i < nodes; i += 32) {
+    const double k = tab[j > i ? j - i : i - j];
+    s0 = fma(k, q0[i], s0);
+    s1 = fma(k, q1[i], s1);
+    s2 = fma(k, q2[i], s2);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    s0 += __shfl_xor_sync(kFull, s0, o);
+    s1 += __shfl_xor_sync(kFull, s1, o);
+    s2 += __shfl_xor_sync(kFull, s2, o);
+  }
+  if (lane == 0) {
+    tab[4 * (int64_t)cap + j] = s0;
+    tab[5 * (int64_t)cap + j] = s1;
+    tab[6 * (int64_t)cap + j] = s2;
+  }
+}
+
 // Stages of a power-of-two transform of length L = 2^log2L in place in
 // shared memory. Forward transforms are decimation in frequency (natural order
 // in, bit-reversed spectrum out), inverse transforms decimation in time (bit-
@@ -962,11 +1020,14 @@ __global__ void transpose_kernel(const typename Cx<T>::type* __restrict__ in, co
   }
 }
 
+// phi64 (1-D): the node potentials in FP64, potential k at phi64[k stride +
+// node], interpolated in FP64 (the forces rounded to T once); otherwise the
+// potentials of the packed complex grids g0, g1 in T.
 template <class T, int D>
 __global__ void gather_kernel(const T* __restrict__ y, int64_t n, const FitParams<T>* __restrict__ prm,
                               const typename Cx<T>::type* __restrict__ g0, const typename Cx<T>::type* __restrict__ g1,
-                              T* __restrict__ neg, double* __restrict__ zpart, unsigned* __restrict__ done,
-                              double* __restrict__ z_out) {
+                              const double* __restrict__ phi64, int phi_stride, T* __restrict__ neg,
+                              double* __restrict__ zpart, unsigned* __restrict__ done, double* __restrict__ z_out) {
   __shared__ double sh[32];
   __shared__ bool last;
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -984,42 +1045,63 @@ __global__ void gather_kernel(const T* __restrict__ y, int64_t n, const FitParam
       locate<T>(yv[a], p, lb, &box[a], w[a]);
     }
     constexpr int combos = D == 1 ? 3 : 9;
-    T phi[D + 2];
+    bool in_fp64 = false;
+    if constexpr (D == 1) {
+      if (phi64 != nullptr) {
+        double pd[3] = {0.0, 0.0, 0.0};
 #pragma unroll
-    for (int t = 0; t < D + 2; ++t) phi[t] = T(0);
+        for (int c = 0; c < 3; ++c) {
+          const int64_t node = (int64_t)box[0] * 3 + c;
+          const double wt = (double)w[0][c];
 #pragma unroll
-    for (int c = 0; c < combos; ++c) {
-      int rem = c;
-      int64_t flat = 0;
-      T wt = T(1);
+          for (int t = 0; t < 3; ++t) pd[t] += wt * phi64[(int64_t)t * phi_stride + node];
+        }
+        const double dens = pd[0] / (double)p.scale;
+        const double sqp = pd[2] * (double)p.scale;
+        const double yd = (double)yv[0];
+        neg[i] = (T)(yd * dens - pd[1]);
+        zi = (1.0 + yd * yd) * dens - 2.0 * yd * pd[1] + sqp;
+        in_fp64 = true;
+      }
+    }
+    if (!in_fp64) {
+      T phi[D + 2];
+#pragma unroll
+      for (int t = 0; t < D + 2; ++t) phi[t] = T(0);
+#pragma unroll
+      for (int c = 0; c < combos; ++c) {
+        int rem = c;
+        int64_t flat = 0;
+        T wt = T(1);
+#pragma unroll
+        for (int a = 0; a < D; ++a) {
+          const int k = rem % 3;
+          rem /= 3;
+          flat = flat * L + (box[a] * 3 + k);
+          wt = wt * w[a][k];
+        }
+        const typename Cx<T>::type a0 = g0[flat], a1 = g1[flat];
+        phi[0] = phi[0] + wt * a0.x;
+        phi[1] = phi[1] + wt * a0.y;
+        phi[2] = phi[2] + wt * a1.x;
+        if (D == 2) phi[3] = phi[3] + wt * a1.y;
+      }
+      phi[0] = phi[0] / p.scale;
+      phi[D + 1] = phi[D + 1] * p.scale;
+      const T density = phi[0];
+      const T sqp = phi[D + 1];
+      // Z's per-point term cancels terms of order |y|^2 phi_0; it is assembled
+      // in FP64 from the interpolated potentials (the forces stay in T).
+      double norm_sq = 0.0, cross = 0.0;
 #pragma unroll
       for (int a = 0; a < D; ++a) {
-        const int k = rem % 3;
-        rem /= 3;
-        flat = flat * L + (box[a] * 3 + k);
-        wt = wt * w[a][k];
+        const T fm = phi[1 + a];
+        neg[i * D + a] = yv[a] * density - fm;
+        norm_sq += (double)yv[a] * (double)yv[a];
+        cross += (double)yv[a] * (double)fm;
       }
-      const typename Cx<T>::type a0 = g0[flat], a1 = g1[flat];
-      phi[0] = phi[0] + wt * a0.x;
-      phi[1] = phi[1] + wt * a0.y;
-      phi[2] = phi[2] + wt * a1.x;
-      if (D == 2) phi[3] = phi[3] + wt * a1.y;
+      zi = (1.0 + norm_sq) * (double)density - 2.0 * cross + (double)sqp;
     }
-    phi[0] = phi[0] / p.scale;
-    phi[D + 1] = phi[D + 1] * p.scale;
-    const T density = phi[0];
-    const T sqp = phi[D + 1];
-    // Z's per-point term cancels terms of order |y|^2 phi_0; it is assembled
-    // in FP64 from the interpolated potentials (the forces stay in T).
-    double norm_sq = 0.0, cross = 0.0;
-#pragma unroll
-    for (int a = 0; a < D; ++a) {
-      const T fm = phi[1 + a];
-      neg[i * D + a] = yv[a] * density - fm;
-      norm_sq += (double)yv[a] * (double)yv[a];
-      cross += (double)yv[a] * (double)fm;
-    }
-    zi = (1.0 + norm_sq) * (double)density - 2.0 * cross + (double)sqp;
   }
   const double bs = block_sum(zi, sh);
   if (threadIdx.x == 0) {
@@ -1132,6 +1214,7 @@ void FitWorkspace<T>::reserve(int D, int64_t n, int cap) {
   acc.ensure((size_t)cells * 4 * sizeof(long long));
   if (acc.bytes != acc_before) acc_clean = nullptr;  // new memory: cleared before its first spread
   zpart.ensure((ceil_div(std::max<int64_t>(n, 1), 256) + 1) * sizeof(double));
+  if (D == 1) direct.ensure((size_t)7 * cap * sizeof(double));
   flag.ensure(64);
   done.ensure(64);
   if ((size_t)cap * sizeof(C2) >= 40 * 1024) {  // set outside any stream capture
@@ -1170,12 +1253,11 @@ void fit_repulsion_cap(FitWorkspace<T>& ws, int D, const T* y, int64_t n, const 
   T2* h1 = ws.h1.template as<T2>();
   T* khat = ws.khat.template as<T>();
 
-  // kernel spectrum (real, pre-scaled by 1/L^D): the kernel rows are made in
+  // kernel spectrum (real, pre-scaled by 1/L^2): the kernel rows are made in
   // the first transform and the last one writes the scaled real part. It is
-  // symmetric in its axes, so it serves the transposed spectrum layout.
-  if (D == 1) {
-    fft_rows<T>(ws, g0, dp, 2, cap, false, s, 1, khat);
-  } else {
+  // symmetric in its axes, so it serves the transposed spectrum layout. (1-D:
+  // the convolution is summed directly, conv1d_*.)
+  if (D == 2) {
     // packed real transforms (kspec_kernel); g0 and h0 serve as real tables
     T* a = reinterpret_cast<T*>(g0);
     T* at = reinterpret_cast<T*>(h0);
@@ -1192,9 +1274,10 @@ void fit_repulsion_cap(FitWorkspace<T>& ws, int D, const T* y, int64_t n, const 
     BHG_LAUNCH_CHECK();
   }
 
-  // charges: spread into the fixed-point accumulator; charges_kernel converts
-  // and clears the cells the spread can reach (so the accumulator is zeroed
-  // here only when newly allocated)
+  // charges: spread into the fixed-point accumulator; charges_kernel (2-D) or
+  // conv1d_prep_kernel (1-D) converts, clear_cells_kernel clears the cells the
+  // spread can reach (so the accumulator is zeroed here only when newly
+  // allocated)
   long long* acc = ws.acc.template as<long long>();
   if (ws.acc_clean != ws.acc.ptr) {
     BHG_CUDA(cudaMemsetAsync(ws.acc.ptr, 0, ws.acc.bytes, s));
@@ -1210,7 +1293,7 @@ void fit_repulsion_cap(FitWorkspace<T>& ws, int D, const T* y, int64_t n, const 
     // nodes <= cap / 2 (L <= cap, L >= 2 nodes - 1)
     const dim3 cg((unsigned)ceil_div(cap / 2, 256), D == 1 ? 1u : (unsigned)(cap / 2));
     if (D == 1) {
-      charges_kernel<T, 1><<<cg, 256, 0, s>>>(acc, dp, g0, g1);
+      conv1d_prep_kernel<T><<<cg, 256, 0, s>>>(acc, dp, cap, ws.direct.template as<double>());
       clear_cells_kernel<T, 1><<<cg, 256, 0, s>>>(acc, dp);
     } else {
       charges_kernel<T, 2><<<cg, 256, 0, s>>>(acc, dp, g0, g1);
@@ -1221,8 +1304,9 @@ void fit_repulsion_cap(FitWorkspace<T>& ws, int D, const T* y, int64_t n, const 
 
   T2 *r0, *r1;
   if (D == 1) {
-    fft_conv_rows<T>(ws, g0, khat, dp, 2, cap, s, 2);
-    fft_conv_rows<T>(ws, g1, khat, dp, 2, cap, s, 2);
+    conv1d_direct_kernel<T><<<(unsigned)ceil_div((int64_t)(cap / 2) * 32, 256), 256, 0, s>>>(
+        ws.direct.template as<double>(), dp, cap);
+    BHG_LAUNCH_CHECK();
     r0 = g0;
     r1 = g1;
   } else {
@@ -1251,10 +1335,11 @@ void fit_repulsion_cap(FitWorkspace<T>& ws, int D, const T* y, int64_t n, const 
   if (n > 0) {
     const unsigned g = (unsigned)ceil_div(n, 256);
     if (D == 1)
-      gather_kernel<T, 1><<<g, 256, 0, s>>>(y, n, dp, r0, r1, neg, ws.zpart.template as<double>(),
-                                            ws.done.template as<unsigned>(), z_out);
+      gather_kernel<T, 1><<<g, 256, 0, s>>>(y, n, dp, r0, r1, ws.direct.template as<double>() + 4 * (int64_t)cap, cap,
+                                            neg, ws.zpart.template as<double>(), ws.done.template as<unsigned>(),
+                                            z_out);
     else
-      gather_kernel<T, 2><<<g, 256, 0, s>>>(y, n, dp, r0, r1, neg, ws.zpart.template as<double>(),
+      gather_kernel<T, 2><<<g, 256, 0, s>>>(y, n, dp, r0, r1, nullptr, 0, neg, ws.zpart.template as<double>(),
                                             ws.done.template as<unsigned>(), z_out);
     BHG_LAUNCH_CHECK();
   } else {

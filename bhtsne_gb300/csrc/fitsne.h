@@ -29,6 +29,7 @@ template <class T>
 struct FitWorkspace {
   typedef typename std::conditional<sizeof(T) == 4, float2, double2>::type T2;
   DevBuf params, g0, g1, h0, h1, khat, tw, tw3, zpart, done, acc, flag;
+  DevBuf direct;  // 1-D: FP64 kernel table and charge rows of the direct convolution
   int tw_len = 0, tw3_len = 0;
   const void* acc_clean = nullptr;  // acc allocation known to be all zero
   int cap_L = 0;  // transform length the buffers hold

@@ -103,7 +103,7 @@ def test_fit_gradient(gpu, oracle, D):
     assert abs(z - oz) / abs(oz) < 1e-4
 
 
-@pytest.mark.parametrize("D,half,z_floor", [(1, 900.0, 3e-2), (2, 350.0, 1e-4), (2, 150.0, 1e-4)])
+@pytest.mark.parametrize("D,half,z_floor", [(1, 900.0, 1e-4), (2, 350.0, 1e-4), (2, 150.0, 1e-4)])
 def test_fit_gradient_large_grid(gpu, oracle, D, half, z_floor):
     """Extents up to the 1000-box cap: the largest transforms (L = 6144 here,
     7-smooth lengths up to 6000 in the oracle). At |y| in the hundreds the
@@ -113,10 +113,10 @@ def test_fit_gradient_large_grid(gpu, oracle, D, half, z_floor):
     f32 path (within 2x of its error, or 1e-4).
 
     Z cancels (1 + |y|^2) phi_0 against phi_2, terms near 1e6 per point at
-    |y| = 900. In 1-D at the box cap every f32 FFT convolution leaves percent-
-    level noise there: the same radix-2 algorithm emulated in numpy f32 gives
-    3.6e-2, scipy's single-precision FFT 5e-4 to 9e-3 (L = 6000 or 8192,
-    packed or not), the oracle 9e-4. That case has its own floor, 3e-2."""
+    |y| = 900. In 1-D at the box cap an f32 FFT convolution leaves percent-
+    level noise there (numpy f32 emulation of a radix-2 transform 3.6e-2,
+    scipy's single-precision FFT 5e-4 to 9e-3, the oracle 9e-4); the GPU sums
+    the 1-D convolution directly in FP64, so the same bar applies."""
     rng = np.random.default_rng(7)
     y = rng.uniform(-half, half, size=(4000, D)).astype(np.float32)
     rows = np.zeros(4001, np.uint64)
