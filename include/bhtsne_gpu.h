@@ -133,7 +133,7 @@ int bhtsne_tsne_timings(const bhtsne_tsne* t, double* affinity_ms, double* loop_
  * around the phases below; bhtsne_tsne_phase_times returns the summed ms and
  * the number of timed epochs of the last finisher or advance call. */
 #define BHTSNE_PHASE_TREE 0       /* Morton codes, radix sort, tree build */
-#define BHTSNE_PHASE_REPULSION 1  /* BH traversal, or FIt-SNE spread/FFT/gather, or exact gradient */
+#define BHTSNE_PHASE_REPULSION 1  /* BH traversal, or FIt-SNE spread/convolution/gather, or exact gradient */
 #define BHTSNE_PHASE_ATTRACTIVE 2 /* CSR attractive forces */
 #define BHTSNE_PHASE_UPDATE 3     /* fused update + recentre + bounding box */
 #define BHTSNE_PHASES 4
