@@ -25,6 +25,7 @@ SIGNATURES = {
     "bhtsne_ctx_create": (C.c_int, [C.c_int, C.POINTER(C.c_void_p)]),
     "bhtsne_ctx_destroy": (C.c_int, [_vp]),
     "bhtsne_ctx_last_error": (C.c_char_p, [_vp]),
+    "bhtsne_ctx_knn_fallback_rows": (C.c_int, [_vp, _i64p]),
     "bhtsne_tsne_new": (C.c_int, [_vp, C.c_int, _i32, _i64, C.POINTER(C.c_void_p)]),
     "bhtsne_tsne_free": (C.c_int, [_vp]),
     "bhtsne_tsne_last_error": (C.c_char_p, [_vp]),
@@ -53,6 +54,7 @@ SIGNATURES = {
     "bhtsne_tsne_timings": (C.c_int, [_vp, _dblp, _dblp, _i64p]),
     "bhtsne_tsne_profile": (C.c_int, [_vp, _i32]),
     "bhtsne_tsne_phase_times": (C.c_int, [_vp, _dblp, _i64p]),
+    "bhtsne_tsne_relayout_times": (C.c_int, [_vp, _dblp, _i64p]),
     "bhtsne_launch_count": (C.c_int64, []),
     "bhtsne_knn_euclidean": (C.c_int, [_vp, C.c_int, _vp, _i64, _i32, _i32, _u32p, _vp]),
     "bhtsne_conditional_p": (C.c_int, [_vp, C.c_int, _vp, _i64, _i32, _dbl, _vp, _i32p]),
@@ -174,6 +176,13 @@ class Context:
     def check(self, rc: int) -> None:
         if rc != OK:
             raise BhtsneError(rc, self.lib.bhtsne_ctx_last_error(self.handle).decode())
+
+    def knn_fallback_rows(self) -> int:
+        """Rows of the last Euclidean kNN on this context that failed the
+        tensor-core pass's exactness certificate and were recomputed."""
+        v = C.c_int64()
+        self.check(self.lib.bhtsne_ctx_knn_fallback_rows(self.handle, C.byref(v)))
+        return v.value
 
     def close(self) -> None:
         if getattr(self, "handle", None):

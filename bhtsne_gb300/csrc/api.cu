@@ -50,6 +50,7 @@ struct bhtsne_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
   std::string err;
+  int64_t knn_fallback_rows = 0;  // rows of the last kNN on this context recomputed by brute force
 };
 
 namespace bhg {
@@ -166,6 +167,8 @@ struct bhtsne_tsne {
   bool profile = false;
   double phase_ms[BHTSNE_PHASES] = {0, 0, 0, 0};
   int64_t phase_epochs = 0;
+  double relayout_ms = 0;  // locality re-layouts of the last finisher or advance call
+  int64_t relayouts = 0;
   // CUDA graph of one epoch body (Barnes-Hut and exact), re-captured when the
   // momentum changes or a new fit starts.
   cudaGraphExec_t graph = nullptr;
@@ -407,9 +410,15 @@ void advance_impl(bhtsne_tsne* t, int64_t epochs) {
       launch_attractive_tasks<T>(S.at, S.cols.template as<uint32_t>(), S.vals.template as<T>(), y,
                                  S.pos.template as<T>(), s);
   };
+  // CUDA events around each re-layout, read after the loop's final sync.
+  std::vector<cudaEvent_t> rl_ev;
   auto maybe_renumber = [&](int64_t epoch) {
     if (!sparse || renumber_every <= 0 || epoch == 0 || epoch % renumber_every != 0) return;
     if (D < 2 || D > 3) return;
+    rl_ev.resize(rl_ev.size() + 2);
+    BHG_CUDA(cudaEventCreate(&rl_ev[rl_ev.size() - 2]));
+    BHG_CUDA(cudaEventCreate(&rl_ev[rl_ev.size() - 1]));
+    BHG_CUDA(cudaEventRecord(rl_ev[rl_ev.size() - 2], s));
     // the Morton order of the current y (the Barnes-Hut build computes it every
     // epoch; the FIt-SNE loop builds it here)
     if (t->loop_kind != BHTSNE_METHOD_BARNES_HUT) {
@@ -424,6 +433,7 @@ void advance_impl(bhtsne_tsne* t, int64_t epochs) {
       launch_recenter_bbox<T>(D, y, n, nullptr, false, S.bh, bits, s);
     ++S.layout_gen;
     ensure_tasks();
+    BHG_CUDA(cudaEventRecord(rl_ev.back(), s));
     if (!was_active) t->drop_graph();  // the attractive pass now reads the slot arrays
   };
   ensure_tasks();
@@ -609,6 +619,14 @@ void advance_impl(bhtsne_tsne* t, int64_t epochs) {
   BHG_CUDA(cudaEventDestroy(e1));
   t->loop_ms = ms;
   t->loop_epochs = epochs;
+  t->relayout_ms = 0;
+  t->relayouts = (int64_t)rl_ev.size() / 2;
+  for (size_t i = 0; i + 1 < rl_ev.size(); i += 2) {
+    float rm = 0;
+    BHG_CUDA(cudaEventElapsedTime(&rm, rl_ev[i], rl_ev[i + 1]));
+    t->relayout_ms += rm;
+  }
+  for (auto& e : rl_ev) cudaEventDestroy(e);
   if (prof) {
     for (int ph = 0; ph < BHTSNE_PHASES; ++ph) t->phase_ms[ph] = 0;
     for (int64_t k = 0; k < epochs; ++k)
@@ -690,8 +708,8 @@ void fit_euclidean(bhtsne_tsne* t, int kind, double theta, const void* data, int
     upload<T>(S.xin, data, (size_t)n * dim * sizeof(T), s);
     S.kidx.ensure(n * k * 4);
     S.kdist.ensure(n * k * sizeof(T));
-    knn_euclidean<T>(S.xin.template as<T>(), n, dim, (int)k, S.kidx.template as<uint32_t>(), S.kdist.template as<T>(),
-                     S.knn, s);
+    t->ctx->knn_fallback_rows = knn_euclidean<T>(S.xin.template as<T>(), n, dim, (int)k,
+                                                 S.kidx.template as<uint32_t>(), S.kdist.template as<T>(), S.knn, s);
     S.xin.release();
     S.knn.release();
     build_affinities<T>(t, k);
@@ -762,8 +780,7 @@ void exact_from_device_distances(bhtsne_tsne* t) {
     // search_beta over full rows, diagonal (distance 0) included.
     S.kp.ensure(n * n * sizeof(T));
     launch_search_beta<T>(S.pdense.template as<T>(), n, n, (T)t->perplexity, S.kp.template as<T>(), nullptr, s);
-    std::swap(S.pdense.ptr, S.kp.ptr);
-    std::swap(S.pdense.bytes, S.kp.bytes);
+    S.pdense.swap(S.kp);
     S.kp.release();
     launch_dense_symmetrize<T>(S.pdense.template as<T>(), n, s);
   });
@@ -912,6 +929,12 @@ int bhtsne_ctx_destroy(bhtsne_ctx* ctx) {
 }
 
 const char* bhtsne_ctx_last_error(const bhtsne_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+int bhtsne_ctx_knn_fallback_rows(const bhtsne_ctx* ctx, int64_t* rows) {
+  if (!ctx || !rows) return BHTSNE_EINVAL;
+  *rows = ctx->knn_fallback_rows;
+  return BHTSNE_OK;
+}
 
 int bhtsne_tsne_new(bhtsne_ctx* ctx, int dtype, int32_t embed_dim, int64_t n_samples, bhtsne_tsne** out) {
   if (!ctx || !out) return BHTSNE_EINVAL;
@@ -1144,6 +1167,13 @@ int bhtsne_tsne_profile(bhtsne_tsne* t, int32_t enable) {
   return BHTSNE_OK;
 }
 
+int bhtsne_tsne_relayout_times(const bhtsne_tsne* t, double* ms, int64_t* count) {
+  if (!t) return BHTSNE_EINVAL;
+  if (ms) *ms = t->relayout_ms;
+  if (count) *count = t->relayouts;
+  return BHTSNE_OK;
+}
+
 int bhtsne_tsne_phase_times(const bhtsne_tsne* t, double* ms, int64_t* epochs) {
   if (!t) return BHTSNE_EINVAL;
   if (ms)
@@ -1174,7 +1204,7 @@ int bhtsne_knn_euclidean(bhtsne_ctx* ctx, int dtype, const void* data, int64_t n
       upload<T>(x, data, (size_t)n * dim * sizeof(T), s);
       idx.ensure((size_t)n * k * 4);
       dist.ensure((size_t)n * k * sizeof(T));
-      knn_euclidean<T>(x.as<T>(), n, dim, k, idx.as<uint32_t>(), dist.as<T>(), ws, s);
+      ctx->knn_fallback_rows = knn_euclidean<T>(x.as<T>(), n, dim, k, idx.as<uint32_t>(), dist.as<T>(), ws, s);
       BHG_CUDA(cudaMemcpyAsync(indices, idx.ptr, (size_t)n * k * 4, cudaMemcpyDeviceToHost, s));
       BHG_CUDA(cudaMemcpyAsync(distances, dist.ptr, (size_t)n * k * sizeof(T), cudaMemcpyDeviceToHost, s));
       BHG_CUDA(cudaStreamSynchronize(s));

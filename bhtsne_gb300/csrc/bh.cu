@@ -39,6 +39,7 @@ namespace bhg {
 namespace {
 
 constexpr int kThreads = 256;
+static_assert(kThreads == kBhThreads, "bh_sizes sizes the Z partials by this block size");
 
 // ---------------------------------------------------------------------------
 // Recentre (optional) + per-axis bounding box; the last block to finish
@@ -179,6 +180,7 @@ __global__ void compose_wide_kernel(const uint32_t* __restrict__ perm, const uin
 constexpr int kPsThreads = 256;
 constexpr int kPsItems = 8;
 constexpr int kPsTile = kPsThreads * kPsItems;
+static_assert(kPsTile == kBhPrefixTile, "bh_sizes sizes the prefix-sum partials by this tile");
 
 template <class T, int D>
 __global__ void prefix_reduce_kernel(const T* __restrict__ y, const uint32_t* __restrict__ perm, int64_t n,
@@ -680,7 +682,7 @@ __global__ void __launch_bounds__(kThreads) bh_traverse_kernel(const T* __restri
 template <class T>
 void launch_recenter_bbox(int D, T* y, int64_t n, const double* mean_sum, bool apply_mean, BhWorkspace<T>& ws,
                           int bits, cudaStream_t s) {
-  const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(n, kThreads), 2 * 152));
+  const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(n, kThreads), kBhBoxBlocks));
   ws.zero_counters(s);
   T* pmin = ws.part_min.template as<T>();
   T* pmax = ws.part_max.template as<T>();
@@ -697,42 +699,31 @@ template <class T>
 void BhWorkspace<T>::reserve(int64_t n_, int D_) {
   n = n_;
   D = D_;
-  const int64_t nn = std::max<int64_t>(n, 1);
-  keys.ensure(nn * 8);
-  keys_alt.ensure(nn * 8);
-  perm.ensure(nn * 4);
-  perm_alt.ensure(nn * 4);
-  ys.ensure(nn * D * sizeof(T));
-  pre.ensure((nn + 1) * D * sizeof(double));
-  pre_part.ensure((ceil_div(nn, kPsTile) + 1) * D * sizeof(double));
-  mask.ensure(nn * 4);
-  cnt.ensure(nn * 4);
-  base.ensure((nn + 1) * 8);
-  // one spare node past the largest tree: the traversal loads node i + 1
-  // while at the last node i = M - 1
-  const int64_t max_nodes = 2 * nn + 1;
-  if (D == 2) {
-    geom.ensure(max_nodes * sizeof(Node2<T>));
-  } else if (D == 3) {
-    geom.ensure(max_nodes * sizeof(Quad<T>));
-    word.ensure(max_nodes * sizeof(uint32_t));
-  } else {
-    geom.ensure(max_nodes * sizeof(Oct<T>));
-    word.ensure(max_nodes * sizeof(uint32_t));
+  const BhSizes z = bh_sizes<T>(n, D);
+  keys.ensure(z.keys);
+  keys_alt.ensure(z.keys);
+  perm.ensure(z.perm);
+  perm_alt.ensure(z.perm);
+  ys.ensure(z.ys);
+  pre.ensure(z.pre);
+  pre_part.ensure(z.pre_part);
+  mask.ensure(z.mask);
+  cnt.ensure(z.cnt);
+  base.ensure(z.base);
+  geom.ensure(z.geom);
+  if (z.word) word.ensure(z.word);
+  if (z.wide) {
+    wide.ensure(z.wide);
+    lo_orig.ensure(z.wide / 2);
+    hi_orig.ensure(z.wide / 2);
   }
-  if (D >= 5) {
-    wide.ensure(nn * 16);
-    lo_orig.ensure(nn * 8);
-    hi_orig.ensure(nn * 8);
-  }
-  part_min.ensure(2 * 152 * 8 * sizeof(T));
-  part_max.ensure(2 * 152 * 8 * sizeof(T));
-  done.ensure(64);
-  zdone.ensure(64);
-  params.ensure(sizeof(BoxParams<T>));
-  zpart.ensure((ceil_div(nn, kThreads) + 1) * sizeof(double));
-  zval.ensure(sizeof(double));
-
+  part_min.ensure(z.part);
+  part_max.ensure(z.part);
+  done.ensure(z.small);
+  zdone.ensure(z.small);
+  params.ensure(z.params);
+  zpart.ensure(z.zpart);
+  zval.ensure(z.zval);
 }
 
 template <class T, int D>

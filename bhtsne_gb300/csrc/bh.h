@@ -156,6 +156,45 @@ struct TreeNodes<T, 3> {
   }
 };
 
+// Launch shapes that fix scratch sizes: points per prefix-sum tile of the
+// centre-of-mass sums, the most blocks of the bounding-box reduction, and the
+// threads per block of the per-point kernels (one Z partial per block).
+constexpr int64_t kBhPrefixTile = 2048;
+constexpr int64_t kBhBoxBlocks = 2 * 152;
+constexpr int64_t kBhThreads = 256;
+
+// Bytes of each Barnes-Hut workspace buffer for n points in D dimensions.
+// BhWorkspace::reserve requests exactly these, and callers that carve a
+// workspace out of fixed memory size their slices from the same table.
+struct BhSizes {
+  size_t keys, perm, ys, pre, pre_part, mask, cnt, base, geom, word, wide, part, small, params, zpart, zval;
+};
+template <class T>
+constexpr BhSizes bh_sizes(int64_t n, int D) {
+  const int64_t nn = n > 1 ? n : 1;
+  // one spare node past the largest tree: the traversal loads node i + 1
+  // while at the last node i = M - 1
+  const int64_t max_nodes = 2 * nn + 1;
+  BhSizes z{};
+  z.keys = (size_t)nn * 8;
+  z.perm = (size_t)nn * 4;
+  z.ys = (size_t)nn * D * sizeof(T);
+  z.pre = (size_t)(nn + 1) * D * sizeof(double);
+  z.pre_part = (size_t)((nn + kBhPrefixTile - 1) / kBhPrefixTile + 1) * D * sizeof(double);
+  z.mask = (size_t)nn * 4;
+  z.cnt = (size_t)nn * 4;
+  z.base = (size_t)(nn + 1) * 8;
+  z.geom = (size_t)max_nodes * (D == 2 ? sizeof(Node2<T>) : D == 3 ? sizeof(Quad<T>) : sizeof(Oct<T>));
+  z.word = D == 2 ? 0 : (size_t)max_nodes * sizeof(uint32_t);
+  z.wide = D >= 5 ? (size_t)nn * 16 : 0;  // also lo_orig and hi_orig at half this each
+  z.part = (size_t)kBhBoxBlocks * 8 * sizeof(T);
+  z.small = 64;
+  z.params = sizeof(BoxParams<T>);
+  z.zpart = (size_t)((nn + kBhThreads - 1) / kBhThreads + 1) * sizeof(double);
+  z.zval = sizeof(double);
+  return z;
+}
+
 template <class T>
 struct BhWorkspace {
   int64_t n = 0;

@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <utility>
 #include <vector>
 
 #include "common.cuh"
@@ -31,17 +32,23 @@ struct AllocStreamScope {
 // A grow-only device allocation owned by a context or a fit workspace. A
 // buffer allocated on a stream is freed on that stream (after its work), so
 // it must be used on that stream, or on another one only after synchronising.
+//
+// A borrowed buffer is a view of memory owned elsewhere (a slice of a fixed
+// scratch array): it is never freed, and a request for more than it holds
+// throws BHTSNE_EINTERNAL instead of reallocating, so code running on borrowed
+// buffers can never allocate.
 struct DevBuf {
   void* ptr = nullptr;
   size_t bytes = 0;
   cudaStream_t stream = nullptr;
   bool async = false;
+  bool borrowed = false;
   DevBuf() = default;
   DevBuf(const DevBuf&) = delete;
   DevBuf& operator=(const DevBuf&) = delete;
   ~DevBuf() { release(); }
   void release() {
-    if (ptr) {
+    if (ptr && !borrowed) {
       if (async) cudaFreeAsync(ptr, stream);
       else cudaFree(ptr);
     }
@@ -49,9 +56,18 @@ struct DevBuf {
     bytes = 0;
     async = false;
     stream = nullptr;
+    borrowed = false;
+  }
+  // Makes this buffer a view of `bytes` bytes at `p`, owned by the caller.
+  void borrow(void* p, size_t b) {
+    release();
+    ptr = p;
+    bytes = b;
+    borrowed = true;
   }
   void* ensure(size_t want) {
     if (want <= bytes && ptr) return ptr;
+    if (borrowed) throw Error(ST_EINTERNAL, "error: a fixed scratch buffer is smaller than this call needs.");
     release();
     size_t b = want < 256 ? 256 : want;
     if (g_alloc_stream) {
@@ -67,18 +83,11 @@ struct DevBuf {
   template <class V>
   V* as() const { return static_cast<V*>(ptr); }
   void swap(DevBuf& o) {
-    void* p = ptr;
-    size_t b = bytes;
-    cudaStream_t st = stream;
-    bool as_ = async;
-    ptr = o.ptr;
-    bytes = o.bytes;
-    stream = o.stream;
-    async = o.async;
-    o.ptr = p;
-    o.bytes = b;
-    o.stream = st;
-    o.async = as_;
+    std::swap(ptr, o.ptr);
+    std::swap(bytes, o.bytes);
+    std::swap(stream, o.stream);
+    std::swap(async, o.async);
+    std::swap(borrowed, o.borrowed);
   }
 };
 

@@ -31,18 +31,25 @@ namespace {
 
 constexpr int64_t kNoAllocMaxPoints = 32768;
 
-// Byte offsets of the carved buffers (each rounded up to 256 bytes).
+// Slice sizes, each rounded up to 256 bytes. The Barnes-Hut buffers come from
+// the same table BhWorkspace::reserve allocates from (bh_sizes), the sort and
+// scan scratch from the sizes their launchers request, so the carve cannot
+// fall behind a change of tile size; and every slice is a borrowed DevBuf,
+// which throws instead of reallocating if a request ever exceeds it.
 constexpr size_t al(size_t b) { return (b + 255) / 256 * 256; }
 constexpr int64_t kN = kNoAllocMaxPoints;
-constexpr size_t kSzKeys = al(kN * 8), kSzPerm = al(kN * 4), kSzYs = al(kN * 2 * 4), kSzPre = al((kN + 1) * 2 * 8),
-                 kSzPrePart = al(((kN + 2047) / 2048 + 1) * 2 * 8), kSzMask = al(kN * 4), kSzCnt = al(kN * 4),
-                 kSzBase = al((kN + 1) * 8), kSzGeom = al((2 * kN + 1) * sizeof(Node2<float>)),
-                 kSzPart = al(2 * 152 * 3 * 4), kSzSmall = 256, kSzParams = al(sizeof(BoxParams<float>)),
-                 kSzZpart = al(((kN + 255) / 256 + 1) * 8),
+constexpr BhSizes kBh = bh_sizes<float>(kN, 2);
+static_assert(kBh.word == 0 && kBh.wide == 0, "D = 2 needs no word or 128-bit code arrays");
+constexpr size_t kSzKeys = al(kBh.keys), kSzPerm = al(kBh.perm), kSzYs = al(kBh.ys), kSzPre = al(kBh.pre),
+                 kSzPrePart = al(kBh.pre_part), kSzMask = al(kBh.mask), kSzCnt = al(kBh.cnt), kSzBase = al(kBh.base),
+                 kSzGeom = al(kBh.geom), kSzPart = al(kBh.part), kSzSmall = al(kBh.small),
+                 kSzParams = al(kBh.params), kSzZpart = al(kBh.zpart), kSzZval = al(kBh.zval),
                  kSzSort = al(radix_sort_tmp_bytes(kN)),
-                 kSzScan = al(((kN + 4095) / 4096 + 1) * 8);
+                 kSzScan = al((size_t)((kN + kRadixScanTile - 1) / kRadixScanTile + 1) * 8);
 constexpr size_t kNoAllocBytes = 2 * kSzKeys + 2 * kSzPerm + kSzYs + kSzPre + kSzPrePart + kSzMask + kSzCnt + kSzBase +
-                                 kSzGeom + 2 * kSzPart + 2 * kSzSmall + kSzParams + kSzZpart + kSzSmall + kSzSort + kSzScan;
+                                 kSzGeom + 2 * kSzPart + 2 * kSzSmall + kSzParams + kSzZpart + kSzZval + kSzSort +
+                                 kSzScan;
+static_assert(kNoAllocBytes < 4 * 1024 * 1024, "the fixed scratch array stays under 4 MB");
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 
@@ -71,8 +78,7 @@ void* scratch_address(std::string* err) {
 
 // Points a DevBuf at a slice of the array without taking ownership.
 void view(DevBuf& b, unsigned char*& cur, size_t bytes) {
-  b.ptr = cur;
-  b.bytes = bytes;
+  b.borrow(cur, bytes);
   cur += bytes;
 }
 
@@ -109,14 +115,15 @@ int bhtsne_bh_repulsion_noalloc(const float* y, int64_t n, double theta, float* 
   view(ws.zdone, cur, kSzSmall);
   view(ws.params, cur, kSzParams);
   view(ws.zpart, cur, kSzZpart);
-  view(ws.zval, cur, kSzSmall);
+  view(ws.zval, cur, kSzZval);
   view(ws.sort_tmp, cur, kSzSort);
   view(ws.scan_tmp, cur, kSzScan);
-  ws.n = n;
-  ws.D = 2;
-  ws.zeroed = true;
   int rc = BHTSNE_OK;
   try {
+    // Every request of the normal path goes through the borrowed slices:
+    // one that does not fit throws BHTSNE_EINTERNAL, nothing is allocated.
+    ws.reserve(n, 2);
+    ws.zeroed = true;
     // The completion tickets of the last-block reductions must start at zero.
     BHG_CUDA(cudaMemsetAsync(ws.done.ptr, 0, kSzSmall, s));
     BHG_CUDA(cudaMemsetAsync(ws.zdone.ptr, 0, kSzSmall, s));
@@ -129,13 +136,7 @@ int bhtsne_bh_repulsion_noalloc(const float* y, int64_t n, double theta, float* 
   } catch (const Error& e) {
     rc = e.code;
   }
-  // The views do not own their memory: detach them before ws is destroyed.
-  for (DevBuf* b : {&ws.keys, &ws.keys_alt, &ws.perm, &ws.perm_alt, &ws.ys, &ws.pre, &ws.pre_part, &ws.mask, &ws.cnt,
-                    &ws.base, &ws.geom, &ws.word, &ws.part_min, &ws.part_max, &ws.done, &ws.zdone, &ws.params, &ws.zpart,
-                    &ws.zval, &ws.sort_tmp, &ws.scan_tmp}) {
-    b->ptr = nullptr;
-    b->bytes = 0;
-  }
+  // The borrowed slices are detached, never freed, when ws goes out of scope.
   return rc;
 }
 

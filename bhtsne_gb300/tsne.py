@@ -250,6 +250,13 @@ class TSNE:
         self.lib.bhtsne_tsne_phase_times(self.handle, ms, C.byref(e))
         return {"tree": ms[0], "repulsion": ms[1], "attractive": ms[2], "update": ms[3], "epochs": e.value}
 
+    def relayout_times(self):
+        """Device ms and count of the locality re-layouts of the last finisher
+        or advance call (no reference counterpart)."""
+        ms, c = C.c_double(), C.c_int64()
+        self._check(self.lib.bhtsne_tsne_relayout_times(self.handle, C.byref(ms), C.byref(c)))
+        return {"ms": ms.value, "count": c.value}
+
     def timings(self):
         a, lp, e = C.c_double(), C.c_double(), C.c_int64()
         self.lib.bhtsne_tsne_timings(self.handle, C.byref(a), C.byref(lp), C.byref(e))

@@ -60,6 +60,11 @@ int bhtsne_ctx_create(int device, bhtsne_ctx** out);
 int bhtsne_ctx_destroy(bhtsne_ctx* ctx);
 const char* bhtsne_ctx_last_error(const bhtsne_ctx* ctx);
 const char* bhtsne_version(void);
+/* No reference counterpart: the number of rows of the last Euclidean kNN run
+ * on this context (bhtsne_knn_euclidean, or the affinity build of a dense
+ * barnes_hut / fit_sne finisher) whose tensor-core candidate list failed the
+ * exactness certificate and were recomputed by exact brute force. */
+int bhtsne_ctx_knn_fallback_rows(const bhtsne_ctx* ctx, int64_t* rows);
 
 /* ---- builder ------------------------------------------------------------- */
 /* tSNE::new (src/lib.rs:241-266): defaults lr auto, 1000 epochs, momentum
@@ -139,6 +144,11 @@ int bhtsne_tsne_timings(const bhtsne_tsne* t, double* affinity_ms, double* loop_
 #define BHTSNE_PHASES 4
 int bhtsne_tsne_profile(bhtsne_tsne* t, int32_t enable);
 int bhtsne_tsne_phase_times(const bhtsne_tsne* t, double* ms, int64_t* epochs);
+/* No reference counterpart: device time (CUDA events, ms, summed) and number of
+ * the locality re-layouts run by the last finisher or advance call. The sparse
+ * methods re-lay out y, the velocity, the gains and the CSR in the Morton
+ * order of the current embedding every 50 epochs (epochs 50, 100, ...). */
+int bhtsne_tsne_relayout_times(const bhtsne_tsne* t, double* ms, int64_t* count);
 /* Number of CUDA kernel launches this library has issued since it was loaded. */
 int64_t bhtsne_launch_count(void);
 

@@ -118,6 +118,45 @@ void knn_brute(const T* X, int64_t n, int32_t dim, int32_t k, uint32_t* idx, T* 
   }
 }
 
+// The same neighbours for selected query rows only (a bounded max-heap by
+// (distance, index) instead of a partial sort of the whole row): the k
+// smallest pairs in that order, which is what knn_brute returns for the row.
+template <class T>
+void knn_brute_rows(const T* X, int64_t n, int32_t dim, int32_t k, const int64_t* rows, int64_t nrows,
+                    uint32_t* idx, T* dist) {
+  auto less = [](const std::pair<T, uint32_t>& a, const std::pair<T, uint32_t>& b) {
+    if (a.first < b.first) return true;
+    if (b.first < a.first) return false;
+    return a.second < b.second;
+  };
+#pragma omp parallel
+  {
+    std::vector<std::pair<T, uint32_t>> heap;
+#pragma omp for schedule(dynamic, 4)
+    for (int64_t r = 0; r < nrows; ++r) {
+      const int64_t i = rows[r];
+      heap.clear();
+      for (int64_t j = 0; j < n; ++j) {
+        if (j == i) continue;
+        std::pair<T, uint32_t> c(euclidean(X + i * dim, X + j * dim, dim), (uint32_t)j);
+        if ((int32_t)heap.size() < k) {
+          heap.push_back(c);
+          std::push_heap(heap.begin(), heap.end(), less);
+        } else if (less(c, heap.front())) {
+          std::pop_heap(heap.begin(), heap.end(), less);
+          heap.back() = c;
+          std::push_heap(heap.begin(), heap.end(), less);
+        }
+      }
+      std::sort_heap(heap.begin(), heap.end(), less);
+      for (int32_t c = 0; c < k; ++c) {
+        idx[r * k + c] = heap[c].second;
+        dist[r * k + c] = heap[c].first;
+      }
+    }
+  }
+}
+
 // ---------------------------------------------------------------------------
 // search_beta: src/tsne/mod.rs:201-275.
 // ---------------------------------------------------------------------------
@@ -1025,6 +1064,66 @@ T exact_kl(const T* p, const T* y, int64_t n) {
   return c;
 }
 
+// The exact method's joint P before normalisation: src/lib.rs:512-554. The
+// caller's distance closure is evaluated on the strict upper triangle and
+// mirrored, the diagonal stays zero (src/tsne/mod.rs:161-189); search_beta runs
+// over each full row, the zero self-distance included, so p_ii is not zero;
+// then p_ij + p_ji is stored on both sides, without the sparse path's halving.
+template <class T>
+void exact_affinities(const T* dist_in, int64_t n, T perplexity, T* p, std::vector<T>& distances) {
+  distances.assign((size_t)(n * n), T(0));
+  for (int64_t i = 0; i < n; ++i)
+    for (int64_t j = i + 1; j < n; ++j) {
+      distances[i * n + j] = dist_in[i * n + j];
+      distances[j * n + i] = dist_in[i * n + j];
+    }
+  std::fill(p, p + n * n, T(0));
+#pragma omp parallel for schedule(dynamic, 16)
+  for (int64_t i = 0; i < n; ++i) search_beta(&p[i * n], &distances[i * n], n, perplexity);
+  for (int64_t i = 0; i < n; ++i)
+    for (int64_t j = i + 1; j < n; ++j) {
+      T s = p[j * n + i];
+      p[i * n + j] += s;
+      p[j * n + i] = p[i * n + j];
+    }
+}
+
+// One exact gradient: src/lib.rs:567-619. Squared embedding distances on the
+// upper triangle, mirrored; q = 1 / (1 + d) over all n^2 entries, the diagonal
+// included (q_ii = 1, so Z counts n); Z summed in T; then
+// dy_i += (y_i - y_j) (p_ij - q_ij / Z) q_ij over every j. dy is overwritten.
+// Returns Z.
+template <class T, int D>
+T exact_gradient(const T* p, const T* y, int64_t n, T* dy, std::vector<T>& distances, std::vector<T>& q) {
+  const int64_t pe = n * n;
+  distances.assign((size_t)pe, T(0));
+  q.resize((size_t)pe);
+#pragma omp parallel for schedule(dynamic, 16)
+  for (int64_t i = 0; i < n; ++i)
+    for (int64_t j = i + 1; j < n; ++j) {
+      T s = T(0);
+      for (int c = 0; c < D; ++c) {
+        T d = y[i * D + c] - y[j * D + c];
+        s = s + d * d;
+      }
+      distances[i * n + j] = s;
+    }
+  for (int64_t i = 0; i < n; ++i)
+    for (int64_t j = i + 1; j < n; ++j) distances[j * n + i] = distances[i * n + j];
+  for (int64_t e = 0; e < pe; ++e) q[e] = T(1) / (T(1) + distances[e]);
+  T qs = T(0);
+  for (int64_t e = 0; e < pe; ++e) qs = qs + q[e];
+  const T inv = T(1) / qs;
+  std::fill(dy, dy + n * D, T(0));
+#pragma omp parallel for schedule(dynamic, 16)
+  for (int64_t i = 0; i < n; ++i)
+    for (int64_t j = 0; j < n; ++j) {
+      T m = (p[i * n + j] - q[i * n + j] * inv) * q[i * n + j];
+      for (int c = 0; c < D; ++c) dy[i * D + c] += (y[i * D + c] - y[j * D + c]) * m;
+    }
+  return qs;
+}
+
 // ---------------------------------------------------------------------------
 // The tSNE builder state machine: src/lib.rs:149-176 (fields), :241-266
 // (defaults), :489-646 (exact), :652-659 (learning rate), :663-685
@@ -1288,48 +1387,14 @@ struct TSNE {
     uy.resize(ge, T(0));
     gains.resize(ge, T(1));
     p_values.assign(pe, T(0));
-    // The closure is evaluated on the strict upper triangle and mirrored
-    // (src/tsne/mod.rs:161-189); the diagonal stays zero.
-    std::vector<T> distances(pe, T(0));
-    for (int64_t i = 0; i < n; ++i)
-      for (int64_t j = i + 1; j < n; ++j) {
-        distances[i * n + j] = dist_in[i * n + j];
-        distances[j * n + i] = dist_in[i * n + j];
-      }
-#pragma omp parallel for schedule(dynamic, 16)
-    for (int64_t i = 0; i < n; ++i) search_beta(&p_values[i * n], &distances[i * n], n, perplexity);
-    for (int64_t i = 0; i < n; ++i)
-      for (int64_t j = i + 1; j < n; ++j) {
-        T s = p_values[j * n + i];
-        p_values[i * n + j] += s;
-        p_values[j * n + i] = p_values[i * n + j];
-      }
+    std::vector<T> distances, q;
+    exact_affinities(dist_in, n, perplexity, p_values.data(), distances);
     if (int rc = finalize_p_and_seed(ge)) return rc;
     const T lr = resolve_lr();
-    std::vector<T> q(pe);
     for (int64_t epoch = 0; epoch < epochs; ++epoch) {
-#pragma omp parallel for schedule(dynamic, 16)
-      for (int64_t i = 0; i < n; ++i)
-        for (int64_t j = i + 1; j < n; ++j) {
-          T s = T(0);
-          for (int c = 0; c < D; ++c) {
-            T d = y[i * D + c] - y[j * D + c];
-            s = s + d * d;
-          }
-          distances[i * n + j] = s;
-        }
-      for (int64_t i = 0; i < n; ++i)
-        for (int64_t j = i + 1; j < n; ++j) distances[j * n + i] = distances[i * n + j];
-      for (int64_t e = 0; e < pe; ++e) q[e] = T(1) / (T(1) + distances[e]);
-      T qs = T(0);
-      for (int64_t e = 0; e < pe; ++e) qs = qs + q[e];
-      T inv = T(1) / qs;
-#pragma omp parallel for schedule(dynamic, 16)
-      for (int64_t i = 0; i < n; ++i)
-        for (int64_t j = 0; j < n; ++j) {
-          T m = (p_values[i * n + j] - q[i * n + j] * inv) * q[i * n + j];
-          for (int c = 0; c < D; ++c) dy[i * D + c] += (y[i * D + c] - y[j * D + c]) * m;
-        }
+      with_d<1, 7>(D, [&](auto dc) {
+        exact_gradient<T, decltype(dc)::value>(p_values.data(), y.data(), n, dy.data(), distances, q);
+      });
       update_solution(y.data(), dy.data(), uy.data(), gains.data(), ge, lr, momentum);
       std::fill(dy.begin(), dy.end(), T(0));
       zero_mean(y.data(), n, D);
@@ -1408,6 +1473,11 @@ void orc_set_threads(int t) {
 
 void orc_knn(int dtype, const void* X, int64_t n, int32_t dim, int32_t k, uint32_t* idx, void* dist) {
   ORC_T(dtype, knn_brute<T>((const T*)X, n, dim, k, idx, (T*)dist));
+}
+
+void orc_knn_rows(int dtype, const void* X, int64_t n, int32_t dim, int32_t k, const int64_t* rows, int64_t nrows,
+                  uint32_t* idx, void* dist) {
+  ORC_T(dtype, knn_brute_rows<T>((const T*)X, n, dim, k, rows, nrows, idx, (T*)dist));
 }
 
 int orc_search_beta(int dtype, const void* dist, int64_t n, int32_t k, double perplexity, void* p,
@@ -1540,6 +1610,25 @@ void orc_gradient_step(int dtype, void* y, const void* pos, const void* neg, voi
                        int64_t len, double lr, double momentum, double inv_norm) {
   ORC_T(dtype, gradient_step<T>((T*)y, (const T*)pos, (const T*)neg, (T*)uy, (T*)gains, len, (T)lr,
                                 (T)momentum, (T)inv_norm));
+}
+
+int orc_exact_affinities(int dtype, const void* dist, int64_t n, double perplexity, void* p) {
+  ORC_T(dtype, {
+    std::vector<T> distances;
+    exact_affinities<T>((const T*)dist, n, (T)perplexity, (T*)p, distances);
+  });
+  return 0;
+}
+
+double orc_exact_gradient(int dtype, int32_t D, const void* p, const void* y, int64_t n, void* dy) {
+  double z = 0;
+  ORC_T(dtype, {
+    std::vector<T> distances, q;
+    with_d<1, 7>(D, [&](auto dc) {
+      z = (double)exact_gradient<T, decltype(dc)::value>((const T*)p, (const T*)y, n, (T*)dy, distances, q);
+    });
+  });
+  return z;
 }
 
 void orc_zero_mean(int dtype, void* y, int64_t n, int32_t D) {

@@ -46,6 +46,7 @@ def lib():
             "orc_num_threads": (C.c_int, []),
             "orc_set_threads": (None, [C.c_int]),
             "orc_knn": (None, [C.c_int, vp, i64, i32, i32, u32p, vp]),
+            "orc_knn_rows": (None, [C.c_int, vp, i64, i32, i32, vp, i64, u32p, vp]),
             "orc_search_beta": (C.c_int, [C.c_int, vp, i64, i32, dbl, vp, vp]),
             "orc_symmetrize": (i64, [C.c_int, u32p, vp, i64, i32, u64p, u32p, vp]),
             "orc_normalize": (None, [C.c_int, vp, i64, dbl]),
@@ -56,6 +57,8 @@ def lib():
             "orc_fit_repulsion": (C.c_int, [C.c_int, i32, vp, i64, vp, C.POINTER(C.c_double), vp]),
             "orc_gradient_step": (None, [C.c_int, vp, vp, vp, vp, vp, i64, dbl, dbl, dbl]),
             "orc_zero_mean": (None, [C.c_int, vp, i64, i32]),
+            "orc_exact_affinities": (C.c_int, [C.c_int, vp, i64, dbl, vp]),
+            "orc_exact_gradient": (dbl, [C.c_int, i32, vp, vp, i64, vp]),
             "orc_sparse_kl": (dbl, [C.c_int, i32, u64p, u32p, vp, vp, i64, dbl, C.c_int]),
             "orc_morton": (C.c_int, [i32, vp, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
             "orc_morton2": (C.c_uint64, [C.c_uint32, C.c_uint32]),
@@ -110,6 +113,17 @@ def knn(X: np.ndarray, k: int):
     idx = np.empty((n, k), np.uint32)
     dist = np.empty((n, k), X.dtype)
     lib().orc_knn(_dt(X), _p(X), n, d, k, _p(idx), _p(dist))
+    return idx, dist
+
+
+def knn_rows(X: np.ndarray, k: int, rows):
+    """Brute-force neighbours of the listed query rows over all n points."""
+    X = np.ascontiguousarray(X)
+    n, d = X.shape
+    rows = np.ascontiguousarray(rows, dtype=np.int64)
+    idx = np.empty((rows.size, k), np.uint32)
+    dist = np.empty((rows.size, k), X.dtype)
+    lib().orc_knn_rows(_dt(X), _p(X), n, d, k, _p(rows), rows.size, _p(idx), _p(dist))
     return idx, dist
 
 
@@ -215,6 +229,27 @@ def zero_mean(y):
     n, D = y.shape
     lib().orc_zero_mean(_dt(y), _p(y), n, D)
     return y
+
+
+def exact_affinities(dist_matrix, perplexity):
+    """The exact method's joint P before normalisation: search_beta over each
+    full row of the mirrored distance matrix (diagonal included), then
+    p_ij + p_ji on both sides."""
+    d = np.ascontiguousarray(dist_matrix)
+    n = d.shape[0]
+    p = np.zeros_like(d)
+    lib().orc_exact_affinities(_dt(d), _p(d), n, float(perplexity), _p(p))
+    return p
+
+
+def exact_gradient(p, y):
+    """One exact gradient dy at a fixed y and dense P; returns (dy, Z)."""
+    y = np.ascontiguousarray(y)
+    p = np.ascontiguousarray(p, dtype=y.dtype)
+    n, D = y.shape
+    dy = np.zeros_like(y)
+    z = lib().orc_exact_gradient(_dt(y), D, _p(p), _p(y), n, _p(dy))
+    return dy, z
 
 
 def sparse_kl(rows, cols, vals, y, inv_q_sum, quirk=True):

@@ -28,7 +28,8 @@ def test_noalloc_matches_allocating_entry_point_twice():
     lib = bg.load()
     rng = np.random.default_rng(2024)
     dev = torch.device("cuda:0")
-    for n, scale in ((20000, 4.0), (6000, 0.5)):
+    calls = 0
+    for n, scale in ((20000, 4.0), (6000, 0.5), (20000, 4.0)):
         y = rng.normal(0.0, scale, size=(n, 2)).astype(np.float32)
         # the allocating entry point (host buffers)
         rows = np.zeros(n + 1, np.uint64)
@@ -39,10 +40,17 @@ def test_noalloc_matches_allocating_entry_point_twice():
         neg_d = torch.zeros((n, 2), dtype=torch.float32, device=dev)
         z_d = torch.zeros(1, dtype=torch.float64, device=dev)
         torch.cuda.synchronize()
+        free_before = torch.cuda.mem_get_info()[0]
         rc = lib.bhtsne_bh_repulsion_noalloc(C.c_void_p(y_d.data_ptr()), n, 0.5, C.c_void_p(neg_d.data_ptr()),
                                              C.c_void_p(z_d.data_ptr()), None)
         torch.cuda.synchronize()
+        free_after = torch.cuda.mem_get_info()[0]
         assert rc == 0
+        if calls > 0:
+            # after the first call (which may load the library's device code and
+            # its fixed array), a call leaves the device's free memory unchanged
+            assert free_after == free_before, (free_before, free_after)
+        calls += 1
         neg = neg_d.cpu().numpy()
         z = float(z_d.cpu().numpy()[0])
         assert rel_l2(neg, neg_ref) < 1e-4
