@@ -150,6 +150,7 @@ struct bhtsne_tsne {
   bool has_init = false;
   std::vector<unsigned char> init;
   int64_t init_len = 0;
+  bool caller_init = false;  // the current fit started from the caller's embedding
   bool stop_lying_fired = false;
   bool has_cached_perplexity = false;
   double cached_perplexity = 0;
@@ -272,6 +273,7 @@ void finalize_p_and_seed(bhtsne_tsne* t, bool dense) {
   launch_normalize<T>(p, np, (T)t->early_exaggeration, S.zbuf.template as<double>() + 2, S.tmp, s);
   if (t->stop_lying_epoch == 0) launch_scale<T>(p, np, T(1) / (T)t->early_exaggeration, s);
   S.y.ensure(ge * sizeof(T));
+  t->caller_init = t->has_init;
   if (t->has_init) {
     t->has_init = false;
     if (t->init_len != ge) {
@@ -413,7 +415,10 @@ void advance_impl(bhtsne_tsne* t, int64_t epochs) {
   // CUDA events around each re-layout, read after the loop's final sync.
   std::vector<cudaEvent_t> rl_ev;
   auto maybe_renumber = [&](int64_t epoch) {
-    if (!sparse || renumber_every <= 0 || epoch == 0 || epoch % renumber_every != 0) return;
+    if (!sparse || renumber_every <= 0 || epoch % renumber_every != 0) return;
+    // At epoch 0 only a caller's embedding (a warm start) has a layout worth
+    // following; the seeded random start has none.
+    if (epoch == 0 && !t->caller_init) return;
     if (D < 2 || D > 3) return;
     rl_ev.resize(rl_ev.size() + 2);
     BHG_CUDA(cudaEventCreate(&rl_ev[rl_ev.size() - 2]));
@@ -421,7 +426,7 @@ void advance_impl(bhtsne_tsne* t, int64_t epochs) {
     BHG_CUDA(cudaEventRecord(rl_ev[rl_ev.size() - 2], s));
     // the Morton order of the current y (the Barnes-Hut build computes it every
     // epoch; the FIt-SNE loop builds it here)
-    if (t->loop_kind != BHTSNE_METHOD_BARNES_HUT) {
+    if (t->loop_kind != BHTSNE_METHOD_BARNES_HUT || epoch == 0) {
       launch_recenter_bbox<T>(D, y, n, nullptr, false, S.bh, bh_bits<T>(D), s);
       bh_build<T>(S.bh, D, y, n, s);
     }
@@ -429,7 +434,7 @@ void advance_impl(bhtsne_tsne* t, int64_t epochs) {
     launch_renumber<T>(D, S.bh.perm.template as<uint32_t>(), n, S.rn, y, S.uy.template as<T>(), S.gains.template as<T>(),
                        S.pos.template as<T>(), S.neg.template as<T>(), static_cast<T*>(S.yext.ensure((size_t)n * D * sizeof(T))),
                        S.rows.template as<uint64_t>(), S.cols.template as<uint32_t>(), S.vals.template as<T>(), S.nnz, s);
-    if (t->loop_kind != BHTSNE_METHOD_BARNES_HUT)
+    if (t->loop_kind != BHTSNE_METHOD_BARNES_HUT || epoch == 0)
       launch_recenter_bbox<T>(D, y, n, nullptr, false, S.bh, bits, s);
     ++S.layout_gen;
     ensure_tasks();

@@ -4,6 +4,7 @@
 
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cstdint>
 #include <utility>
 #include <vector>
@@ -90,6 +91,19 @@ struct DevBuf {
     std::swap(borrowed, o.borrowed);
   }
 };
+
+// Streaming multiprocessors of the current device, looked up once per device.
+inline int device_sm_count() {
+  static std::atomic<int> cache[64];
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) dev = 0;
+  int v = cache[dev].load(std::memory_order_relaxed);
+  if (v <= 0) {
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v <= 0) v = 1;
+    cache[dev].store(v, std::memory_order_relaxed);
+  }
+  return v;
+}
 
 // Keeps the freed memory of the device's default pool cached (no release
 // back to the driver at synchronisations), once per device.

@@ -212,6 +212,14 @@ class TSNE:
         self._check(self.lib.bhtsne_tsne_embedding(self.handle, _ptr(out)))
         return out
 
+    def embedding_into(self, out: np.ndarray) -> np.ndarray:
+        """embedding() into a caller buffer (for instance page-locked memory)
+        of n * D values of the handle's type."""
+        if out.dtype != self.dtype or out.size != self.n * self.D or not out.flags.c_contiguous:
+            raise L.BhtsneError(L.EINVAL, "error: the output buffer must hold n_samples * D contiguous values.")
+        self._check(self.lib.bhtsne_tsne_embedding(self.handle, _ptr(out)))
+        return out
+
     def kl_divergence(self, quirk: bool = True) -> Optional[float]:
         v = C.c_double()
         has = C.c_int32()

@@ -59,6 +59,25 @@ static inline T signum(T x) {
   return std::copysign(T(1), x);
 }
 
+// rayon's par_iter().sum() (src/tsne/mod.rs:288, :597-601, :603-617, :668,
+// :774; src/tsne/interpolation.rs:309-328; src/lib.rs:589) splits the slice in
+// halves across the thread pool and adds the halves' sums. Its split points
+// follow the pool size and work stealing, so the reference's own result varies
+// with the thread count; restated here as a balanced tree of halves with
+// leaves of at most 256 values summed in order, in T: the accuracy of a
+// parallel reduction (error growing with log n, not with n), independent of
+// the thread count. Sums the reference forms sequentially stay sequential.
+template <class T>
+T tree_sum(const T* v, int64_t n) {
+  if (n <= 256) {
+    T s = T(0);
+    for (int64_t i = 0; i < n; ++i) s = s + v[i];
+    return s;
+  }
+  const int64_t h = n / 2;
+  return tree_sum(v, h) + tree_sum(v + h, n - h);
+}
+
 // Rust `f32::min` / `f32::max` return the non-NaN operand.
 template <class T>
 static inline T fmin_(T a, T b) { return std::fmin(a, b); }
@@ -209,8 +228,7 @@ int search_beta(T* p, const T* d, int64_t k, T perplexity) {
 // ---------------------------------------------------------------------------
 template <class T>
 void normalize_p(T* p, int64_t nnz, T exaggeration) {
-  T s = T(0);
-  for (int64_t e = 0; e < nnz; ++e) s = s + p[e];
+  const T s = tree_sum(p, nnz);
   T scale = exaggeration / (s + Num<T>::eps());
   for (int64_t e = 0; e < nnz; ++e) p[e] *= scale;
 }
@@ -949,7 +967,7 @@ T fit_repulsion(const T* y, int64_t n, T* neg, FitGridInfo* info) {
   }
   // reconstruct
   const T two = T(2);
-  T z_sum = T(0);
+  std::vector<T> z_terms((size_t)n);
   for (int64_t i = 0; i < n; ++i) {
     const T* phi = &potentials[i * (D + 2)];
     T density = phi[0];
@@ -961,9 +979,9 @@ T fit_repulsion(const T* y, int64_t n, T* neg, FitGridInfo* info) {
       norm_sq = norm_sq + y[i * D + a] * y[i * D + a];
       cross = cross + y[i * D + a] * fm;
     }
-    z_sum = z_sum + ((T(1) + norm_sq) * density - two * cross + sqn);
+    z_terms[i] = (T(1) + norm_sq) * density - two * cross + sqn;
   }
-  return z_sum - T((double)n);
+  return tree_sum(z_terms.data(), n) - T((double)n);
 }
 
 // ---------------------------------------------------------------------------
@@ -1034,9 +1052,7 @@ T sparse_kl(const uint64_t* rows, const uint32_t* cols, const T* vals, const T* 
     }
     partial[i] = cost;
   }
-  T s = T(0);
-  for (int64_t i = 0; i < n; ++i) s = s + partial[i];
-  return s;
+  return tree_sum(partial.data(), n);
 }
 
 // evaluate_error (exact KL): src/tsne/mod.rs:579-618.
@@ -1053,15 +1069,14 @@ T exact_kl(const T* p, const T* y, int64_t n) {
       dist[i * n + j] = s;
       dist[j * n + i] = s;
     }
-  T zs = T(0);
-  for (auto d : dist) zs = zs + T(1) / (T(1) + d);
-  T inv = T(1) / zs;
-  T c = T(0);
+  std::vector<T> terms((size_t)(n * n));
+  for (int64_t e = 0; e < n * n; ++e) terms[e] = T(1) / (T(1) + dist[e]);
+  const T inv = T(1) / tree_sum(terms.data(), n * n);
   for (int64_t e = 0; e < n * n; ++e) {
     T q = T(1) / (T(1) + dist[e]) * inv;
-    c = c + p[e] * std::log((p[e] + Num<T>::min_pos()) / (q + Num<T>::min_pos()));
+    terms[e] = p[e] * std::log((p[e] + Num<T>::min_pos()) / (q + Num<T>::min_pos()));
   }
-  return c;
+  return tree_sum(terms.data(), n * n);
 }
 
 // The exact method's joint P before normalisation: src/lib.rs:512-554. The
@@ -1111,8 +1126,7 @@ T exact_gradient(const T* p, const T* y, int64_t n, T* dy, std::vector<T>& dista
   for (int64_t i = 0; i < n; ++i)
     for (int64_t j = i + 1; j < n; ++j) distances[j * n + i] = distances[i * n + j];
   for (int64_t e = 0; e < pe; ++e) q[e] = T(1) / (T(1) + distances[e]);
-  T qs = T(0);
-  for (int64_t e = 0; e < pe; ++e) qs = qs + q[e];
+  const T qs = tree_sum(q.data(), pe);
   const T inv = T(1) / qs;
   std::fill(dy, dy + n * D, T(0));
 #pragma omp parallel for schedule(dynamic, 16)
@@ -1420,8 +1434,10 @@ struct TSNE {
       with_d<2, 7>(D, [&](auto dc) {
         constexpr int DD = decltype(dc)::value;
         Arena<T, DD> a;
-        z = bh_repulsion<T, DD>(a, y.data(), n, fit_theta, neg.data(), qs.data());
+        bh_repulsion<T, DD>(a, y.data(), n, fit_theta, neg.data(), qs.data());
       });
+      // evaluate_error_approximately sums the q_sums in parallel (src/tsne/mod.rs:668)
+      z = tree_sum(qs.data(), n);
     } else {
       if (D == 1) z = fit_repulsion<T, 1>(y.data(), n, neg.data(), nullptr);
       else z = fit_repulsion<T, 2>(y.data(), n, neg.data(), nullptr);

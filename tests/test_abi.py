@@ -56,3 +56,31 @@ def test_neighbor_table_shape_checks():
         neighbors_to_arrays([[], []])
     idx, dist = neighbors_to_arrays(rows[:2] + [[Neighbor(0, 0.7), Neighbor(1, 0.9)]])
     assert idx.dtype == np.uint64 and idx.shape == (3, 2) and dist.dtype == np.float32
+
+
+def _c_params(decl):
+    """Parameter count of a C declaration's argument list."""
+    inner = decl[decl.index("(") + 1:decl.rindex(")")].strip()
+    return 0 if inner in ("", "void") else len(inner.split(","))
+
+
+def test_rust_sys_crate_declares_every_header_function():
+    """bindings/rust/bhtsne-gpu-sys/src/lib.rs (not compiled here: no cargo)
+    declares every function of the header with the same number of parameters,
+    and the three #[repr(C)] structs with the header's fields in order."""
+    sys_rs = open(os.path.join(ROOT, "bindings", "rust", "bhtsne-gpu-sys", "src", "lib.rs")).read()
+    header = re.sub(r"/\*.*?\*/", "", open(HEADER).read(), flags=re.S)
+    decls = {m.group(1): m.group(0) for m in re.finditer(r"\b(bhtsne_[a-z0-9_]+)\s*\([^;]*\)\s*;", header)}
+    decls.pop("bhtsne_epoch_cb", None)
+    rust = {m.group(1): m.group(0) for m in re.finditer(r"pub fn (bhtsne_[a-z0-9_]+)\s*\((.*?)\)", sys_rs, flags=re.S)}
+    assert set(decls) == set(rust), set(decls) ^ set(rust)
+    for name, decl in decls.items():
+        inner = rust[name][rust[name].index("(") + 1:-1].strip()
+        n_rust = 0 if not inner else len([p for p in inner.split(",") if p.strip()])
+        assert n_rust == _c_params(decl), name
+    for struct in ("bhtsne_batch_params", "bhtsne_server_params", "bhtsne_request"):
+        c_body = re.search(r"typedef struct %s \{(.*?)\}" % struct, header, flags=re.S).group(1)
+        c_fields = re.findall(r"\b([a-z_]+)\s*;", c_body)
+        r_body = re.search(r"pub struct %s \{(.*?)\}" % struct, sys_rs, flags=re.S).group(1)
+        r_fields = re.findall(r"pub ([a-z_]+):", r_body)
+        assert c_fields == r_fields, struct

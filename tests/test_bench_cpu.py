@@ -45,6 +45,11 @@ def test_reference_arm_prints_the_contract_line():
     assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["cores"] >= 1
     assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["d2h_bytes_per_step"] == 0
     assert line["config"]["workload"] == "bh2d_1M_d128" and line["config"]["n_points"] == 20000
+    # the same config object the GPU arm prints, window included (250 burn-in
+    # + 3 warm-up epochs, then the 2 timed ones)
+    from types import SimpleNamespace
+    assert line["config"] == bench.workload_config(SimpleNamespace(n=20000, burn_in=250, warmup=3, steps=2), 1)
+    assert "epochs 253-254" in line["config"]["window"]
 
 
 def test_interaction_count_at_tiny_theta_is_all_pairs(oracle):

@@ -117,7 +117,9 @@ def test_exact_fit_first_epochs(gpu, oracle, variant, dtype):
 def test_exact_fit_final_kl_within_one_percent(gpu, oracle, dtype, n):
     """A full exact fit (1,000 epochs, reference defaults, perplexity 30) from
     the same initial embedding: final KL within 1 % of the oracle's."""
-    X, _ = blobs(n, 20, 5, 15)
+    # 10 overlapping clusters: final KL near 0.59, where the oracle's own
+    # spread over initial embeddings 1e-6 apart is 0.2 %
+    X, _ = blobs(n, 20, 10, 15, spread=3.0)
     X = X.astype(dtype)
     rng = np.random.default_rng(16)
     y0 = rng.normal(0.0, 1e-2, size=(n, 2)).astype(dtype)

@@ -290,13 +290,16 @@ def hub_inputs(case, oracle):
     return X, idx, dist
 
 
+@pytest.mark.parametrize("start", ["seeded", "caller"])
 @pytest.mark.parametrize("case,dtype", [("hubs", np.float32), ("hubs", np.float64), ("star", np.float32)])
-def test_renumbering_keeps_every_affinity(gpu, oracle, monkeypatch, case, dtype):
+def test_renumbering_keeps_every_affinity(gpu, oracle, monkeypatch, case, dtype, start):
     """The slot-ordered CSR of the locality renumbering (rows of <= 256
     entries sorted in registers, longer ones in shared memory, rows past 1024
-    copied in order) holds exactly the original entries: one epoch after the first
-    renumbering (epoch 50) the embedding equals an un-renumbered fit's up to
-    summation order. A lost or doubled entry moves its point by lr * p_ij."""
+    copied in order) holds exactly the original entries: one epoch after a
+    renumbering the embedding equals an un-renumbered fit's up to summation
+    order. A lost or doubled entry moves its point by lr * p_ij. A seeded
+    start is first renumbered at epoch 50; a caller's embedding (a warm start)
+    already at epoch 0."""
     X, idx, dist = hub_inputs(case, oracle)
     n = X.shape[0]
     perp = 30.0 if case == "hubs" else 10.0
@@ -306,9 +309,15 @@ def test_renumbering_keeps_every_affinity(gpu, oracle, monkeypatch, case, dtype)
     out = {}
     for every in ("0", "50"):
         monkeypatch.setenv("BHTSNE_RENUMBER_EVERY", every)
-        t = gpu.TSNE(n, D=2, dtype=dtype).perplexity(perp).epochs(51).initial_embedding(seed)
+        t = gpu.TSNE(n, D=2, dtype=dtype).perplexity(perp)
+        if start == "seeded":
+            t.epochs(51).random_seed(17)
+        else:
+            t.epochs(1).initial_embedding(seed)
         t.barnes_hut_with_neighbors(0.5, (idx, dist.astype(dtype)))
         out[every] = t.embedding()
+        relayouts = t.relayout_times()["count"]
+        assert relayouts == (0 if every == "0" else 1), relayouts
     e0, e1 = out["0"], out["50"]
     assert np.all(np.isfinite(e1))
     assert np.abs(e1 - e0).max() <= 1e-4 * np.abs(e0).max(), np.abs(e1 - e0).max() / np.abs(e0).max()

@@ -144,3 +144,4 @@ def test_fit_gradient_three_smooth_lengths(gpu, oracle, D, half):
     assert info["boxes"] in (11, 22, 90)
     assert rel_l2(neg, ref64) <= max(2 * rel_l2(oneg, ref64), 1e-4)
     assert abs(z - z64) / abs(z64) <= max(2 * abs(oz - z64) / abs(z64), 1e-4)
+
