@@ -8,11 +8,11 @@ from ._lib import (BhtsneError, Context, F32, F64, METHOD_BARNES_HUT, METHOD_EXA
                    default_context, library_path, load)
 from .batch import Batch
 from .serve import Server
-from .tsne import (Neighbor, SparseAffinities, TSNE, conditional_p, gradient, knn_euclidean, neighbors_to_arrays,
-                   symmetrize, update)
+from .tsne import (Neighbor, SparseAffinities, TSNE, conditional_p, gradient, knn_euclidean, load_csv,
+                   neighbors_to_arrays, symmetrize, update, write_csv)
 
 __all__ = [
     "Batch", "BhtsneError", "Server", "Context", "F32", "F64", "METHOD_BARNES_HUT", "METHOD_EXACT", "METHOD_FIT_SNE", "SIGNATURES",
     "default_context", "library_path", "load", "Neighbor", "SparseAffinities", "TSNE", "conditional_p", "gradient",
-    "knn_euclidean", "neighbors_to_arrays", "symmetrize", "update",
+    "knn_euclidean", "load_csv", "neighbors_to_arrays", "symmetrize", "update", "write_csv",
 ]

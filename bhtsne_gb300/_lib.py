@@ -11,7 +11,7 @@ import threading
 
 from . import build as _build
 
-OK, ENOMEM, EINVAL, ETIMEDOUT, ECUDA, EINTERNAL = 0, 12, 22, 110, 1001, 1002
+OK, EIO, ENOMEM, EINVAL, ETIMEDOUT, ECUDA, EINTERNAL = 0, 5, 12, 22, 110, 1001, 1002
 F32, F64 = 0, 1
 METHOD_EXACT, METHOD_BARNES_HUT, METHOD_FIT_SNE = 1, 2, 3
 
@@ -62,6 +62,10 @@ SIGNATURES = {
     "bhtsne_gradient": (C.c_int, [_vp, C.c_int, _i32, _i32, _vp, _i64, _u64p, _u32p, _vp, _i64, _dbl, _vp, _vp,
                                   _dblp]),
     "bhtsne_update": (C.c_int, [_vp, C.c_int, _i32, _vp, _vp, _vp, _vp, _vp, _i64, _dbl, _dbl, _dbl]),
+    "bhtsne_load_csv": (C.c_int, [C.c_char_p, _i32, _i64p, _i64, C.c_int, _vp, _i64p, _i64p]),
+    "bhtsne_tsne_write_csv": (C.c_int, [_vp, C.c_char_p]),
+    "bhtsne_write_csv": (C.c_int, [_vp, _i64, _i32, C.c_int, C.c_char_p]),
+    "bhtsne_io_last_error": (C.c_char_p, []),
     "bhtsne_bh_repulsion_noalloc": (C.c_int, [_vp, _i64, _dbl, _vp, _vp, _vp]),
     "bhtsne_batch_params_default": (None, [_vp]),
     "bhtsne_batch_new": (C.c_int, [_vp, C.c_int, _i32, _vp, C.POINTER(C.c_void_p)]),

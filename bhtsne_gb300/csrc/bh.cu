@@ -32,6 +32,8 @@
 //    the children. Leaves are summed in T exactly like the reference so that
 //    a singleton leaf's centre is bit-identical to its point (the self test).
 #include "bh.h"
+
+#include <type_traits>
 #include "bh_dev.cuh"
 
 namespace bhg {
@@ -613,6 +615,15 @@ __global__ void __launch_bounds__(kThreads) bh_traverse_kernel(const T* __restri
 #pragma unroll
     for (int a = 0; a < D; ++a) f[a] = T(0);
     T q = T(0);
+    // 2-D single precision: the displacement, its squares and the force
+    // update in paired f32x2 instructions (each half the scalar operation, so
+    // the same values as the per-axis code)
+    constexpr bool kPair = D == 2 && std::is_same<T, float>::value;
+    F32x2 q2 = {0ull}, f2 = {0ull};
+    if constexpr (kPair) {
+      q2 = f2_make((float)qv[0], (float)qv[D - 1]);
+      f2 = f2_make(0.0f, 0.0f);
+    }
     // Software-pipelined walk: both possible successors of the current node
     // (i + 1 if it is opened, its skip target if it is summarised) are loaded
     // before the decision, so the next visit never waits on a dependent load.
@@ -632,10 +643,17 @@ __global__ void __launch_bounds__(kThreads) bh_traverse_kernel(const T* __restri
       nodes.decode(cur, com, &mass, &r2);
       T disp[D];
       T dist = T(0);
+      F32x2 d2 = {0ull};
+      if constexpr (kPair) {
+        d2 = f2_sub(q2, f2_make((float)com[0], (float)com[D - 1]));
+        const F32x2 s2 = f2_mul(d2, d2);
+        dist = (T)(f2_lo(s2) + f2_hi(s2));  // (0 + dx^2) + dy^2, as the per-axis sum
+      } else {
 #pragma unroll
-      for (int a = 0; a < D; ++a) {
-        disp[a] = qv[a] - com[a];
-        dist += disp[a] * disp[a];
+        for (int a = 0; a < D; ++a) {
+          disp[a] = qv[a] - com[a];
+          dist += disp[a] * disp[a];
+        }
       }
       if (r2 >= theta_sq * dist) {
         i = i + 1;
@@ -649,8 +667,16 @@ __global__ void __launch_bounds__(kThreads) bh_traverse_kernel(const T* __restri
       T m = mass * inv;
       q += m;
       m = m * inv;
+      if constexpr (kPair) {
+        f2 = f2_add(f2, f2_mul(f2_make((float)m, (float)m), d2));
+      } else {
 #pragma unroll
-      for (int a = 0; a < D; ++a) f[a] += m * disp[a];
+        for (int a = 0; a < D; ++a) f[a] += m * disp[a];
+      }
+    }
+    if constexpr (kPair) {
+      f[0] = (T)f2_lo(f2);
+      f[D - 1] = (T)f2_hi(f2);
     }
 #pragma unroll
     for (int a = 0; a < D; ++a) neg[pi * D + a] = f[a];

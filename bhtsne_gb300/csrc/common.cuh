@@ -62,6 +62,44 @@ constexpr unsigned kFull = 0xffffffffu;
 __device__ __forceinline__ float rcp_rn(float x) { return __frcp_rn(x); }
 __device__ __forceinline__ double rcp_rn(double x) { return __drcp_rn(x); }
 
+// Two single-precision values in one 64-bit register pair, for the paired
+// f32x2 instructions of sm_100 and later: each lane of a paired add, subtract
+// or multiply is the scalar IEEE operation rounded to nearest, so results are
+// those of the two scalar operations (no contraction into a fused multiply-add).
+struct F32x2 {
+  unsigned long long v;
+};
+__device__ __forceinline__ F32x2 f2_make(float a, float b) {
+  F32x2 r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r.v) : "f"(a), "f"(b));
+  return r;
+}
+__device__ __forceinline__ float f2_lo(F32x2 x) {
+  float a, b;
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(x.v));
+  return a;
+}
+__device__ __forceinline__ float f2_hi(F32x2 x) {
+  float a, b;
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(x.v));
+  return b;
+}
+__device__ __forceinline__ F32x2 f2_add(F32x2 x, F32x2 y) {
+  F32x2 r;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r.v) : "l"(x.v), "l"(y.v));
+  return r;
+}
+__device__ __forceinline__ F32x2 f2_sub(F32x2 x, F32x2 y) {
+  F32x2 r;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r.v) : "l"(x.v), "l"(y.v));
+  return r;
+}
+__device__ __forceinline__ F32x2 f2_mul(F32x2 x, F32x2 y) {
+  F32x2 r;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r.v) : "l"(x.v), "l"(y.v));
+  return r;
+}
+
 // Conversions between f32 and int64 with round-to-nearest-even, written with
 // 32/64-bit integer operations only (the hardware conversions of 64-bit
 // integers are slow on this part). f32_to_i64_rn saturates like the IEEE

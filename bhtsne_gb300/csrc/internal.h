@@ -105,6 +105,10 @@ inline int device_sm_count() {
   return v;
 }
 
+// write_csv of a host embedding (io.cu); returns a status, the message in
+// bhtsne_io_last_error.
+int write_csv_file(const void* embedding, int64_t n, int32_t embed_dim, int dtype, const char* path);
+
 // Keeps the freed memory of the device's default pool cached (no release
 // back to the driver at synchronisations), once per device.
 void keep_pool_cached(int device);

@@ -11,6 +11,7 @@ for `exact`, through a dense distance matrix.
 from __future__ import annotations
 
 import ctypes as C
+import os
 from dataclasses import dataclass
 from typing import Callable, Optional, Sequence
 
@@ -248,6 +249,11 @@ class TSNE:
         return self._check(self.lib.bhtsne_tsne_with_affinities(self.handle, _ptr(rows), rows.size, _ptr(cols),
                                                                 _ptr(vals), vals.size, float(aff.perplexity)))
 
+    def write_csv(self, path: str):
+        """write_csv (src/csv.rs:31-58): the embedding, one point per record,
+        headers x,y (D = 2) or x,y,z (D = 3)."""
+        return self._check(self.lib.bhtsne_tsne_write_csv(self.handle, os.fsencode(path)))
+
     def profile(self, enable: bool = True):
         """Per-phase CUDA-event timing of subsequent epochs (no reference counterpart)."""
         return self._check(self.lib.bhtsne_tsne_profile(self.handle, 1 if enable else 0))
@@ -341,3 +347,34 @@ def update(y, pos, neg, uy, gains, learning_rate, momentum, inverse_z, ctx: Opti
     ctx.check(ctx.lib.bhtsne_update(ctx.handle, _dtype_code(y.dtype), D, _ptr(y), _ptr(pos), _ptr(neg), _ptr(uy),
                                     _ptr(gains), n, float(learning_rate), float(momentum), float(inverse_z)))
     return y, uy, gains
+
+
+# ---- CSV input and output (src/csv.rs) -------------------------------------------
+def load_csv(path: str, has_headers: bool = False, skip=None, dtype=np.float32) -> np.ndarray:
+    """load_csv (src/csv.rs:61-118) for numeric fields: every field except the
+    columns in `skip`, parsed as `dtype`, flattened in file order (the
+    reference's Vec<T>)."""
+    lib = L.load()
+    code = _dtype_code(dtype)
+    sk = np.ascontiguousarray(np.asarray(list(skip or []), dtype=np.int64))
+    count, records = C.c_int64(0), C.c_int64(0)
+    p = os.fsencode(path)
+    rc = lib.bhtsne_load_csv(p, 1 if has_headers else 0, _ptr(sk) if sk.size else None, sk.size, code, None,
+                             C.byref(count), C.byref(records))
+    if rc != L.OK:
+        raise L.BhtsneError(rc, lib.bhtsne_io_last_error().decode())
+    out = np.zeros(count.value, np.dtype(dtype))
+    rc = lib.bhtsne_load_csv(p, 1 if has_headers else 0, _ptr(sk) if sk.size else None, sk.size, code, _ptr(out),
+                             C.byref(count), C.byref(records))
+    if rc != L.OK:
+        raise L.BhtsneError(rc, lib.bhtsne_io_last_error().decode())
+    return out
+
+
+def write_csv(embedding: np.ndarray, path: str, D: int = 2):
+    """write_csv of an embedding held by the caller (n x D values)."""
+    lib = L.load()
+    e = np.ascontiguousarray(embedding)
+    rc = lib.bhtsne_write_csv(_ptr(e), e.size // D, D, _dtype_code(e.dtype), os.fsencode(path))
+    if rc != L.OK:
+        raise L.BhtsneError(rc, lib.bhtsne_io_last_error().decode())

@@ -10,6 +10,7 @@
 use std::os::raw::{c_char, c_int, c_void};
 
 pub const BHTSNE_OK: c_int = 0;
+pub const BHTSNE_EIO: c_int = 5;
 pub const BHTSNE_ENOMEM: c_int = 12;
 pub const BHTSNE_EINVAL: c_int = 22;
 pub const BHTSNE_ETIMEDOUT: c_int = 110;
@@ -160,6 +161,13 @@ extern "C" {
     pub fn bhtsne_update(ctx: *mut bhtsne_ctx, dtype: c_int, embed_dim: i32, y: *mut c_void, pos: *const c_void,
                          neg: *const c_void, uy: *mut c_void, gains: *mut c_void, n: i64, learning_rate: f64,
                          momentum: f64, inverse_z: f64) -> c_int;
+
+    // ---- CSV input and output (src/csv.rs:31-118); host only
+    pub fn bhtsne_load_csv(path: *const c_char, has_headers: i32, skip: *const i64, n_skip: i64, dtype: c_int,
+                           out: *mut c_void, count: *mut i64, records: *mut i64) -> c_int;
+    pub fn bhtsne_tsne_write_csv(t: *mut bhtsne_tsne, path: *const c_char) -> c_int;
+    pub fn bhtsne_write_csv(embedding: *const c_void, n: i64, embed_dim: i32, dtype: c_int, path: *const c_char) -> c_int;
+    pub fn bhtsne_io_last_error() -> *const c_char;
 
     // ---- batches of independent fits
     pub fn bhtsne_batch_params_default(p: *mut bhtsne_batch_params);

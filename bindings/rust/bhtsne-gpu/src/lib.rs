@@ -367,6 +367,43 @@ impl<'data, T: GpuFloat, const D: usize> tSNE<'data, T, &'data [T], D> {
     }
 }
 
+impl<'data, T: GpuFloat, U, const D: usize> tSNE<'data, T, U, D> {
+    /// `write_csv` (src/csv.rs:31-58).
+    pub fn write_csv(&mut self, path: &str) -> Result<&mut Self, Box<dyn std::error::Error>> {
+        let p = std::ffi::CString::new(path)?;
+        let rc = unsafe { sys::bhtsne_tsne_write_csv(self.raw, p.as_ptr()) };
+        if rc != 0 {
+            let msg = unsafe { CStr::from_ptr(sys::bhtsne_tsne_last_error(self.raw)) }.to_string_lossy().into_owned();
+            return Err(msg.into());
+        }
+        Ok(self)
+    }
+}
+
+/// `load_csv` (src/csv.rs:61-118) for numeric fields: the reference converts
+/// each field with a closure; here fields are parsed as Rust's `str::parse`.
+pub fn load_csv<T: GpuFloat>(path: &str, has_headers: bool, skip: Option<&[usize]>)
+                             -> Result<Vec<T>, Box<dyn std::error::Error>> {
+    let p = std::ffi::CString::new(path)?;
+    let skip: Vec<i64> = skip.unwrap_or(&[]).iter().map(|&c| c as i64).collect();
+    let (mut count, mut records) = (0i64, 0i64);
+    let call = |out: *mut c_void, count: &mut i64, records: &mut i64| unsafe {
+        sys::bhtsne_load_csv(p.as_ptr(), has_headers as i32, skip.as_ptr(), skip.len() as i64, T::DTYPE, out, count,
+                             records)
+    };
+    let fail = || -> Box<dyn std::error::Error> {
+        unsafe { CStr::from_ptr(sys::bhtsne_io_last_error()) }.to_string_lossy().into_owned().into()
+    };
+    if call(std::ptr::null_mut(), &mut count, &mut records) != 0 {
+        return Err(fail());
+    }
+    let mut data = vec![T::default(); count as usize];
+    if call(data.as_mut_ptr().cast(), &mut count, &mut records) != 0 {
+        return Err(fail());
+    }
+    Ok(data)
+}
+
 impl<'data, T: GpuFloat, U, const D: usize> Drop for tSNE<'data, T, U, D> {
     fn drop(&mut self) {
         unsafe {

@@ -32,6 +32,7 @@ extern "C" {
 #endif
 
 #define BHTSNE_OK 0
+#define BHTSNE_EIO 5
 #define BHTSNE_ENOMEM 12
 #define BHTSNE_EINVAL 22
 #define BHTSNE_ETIMEDOUT 110
@@ -194,6 +195,27 @@ int bhtsne_bh_repulsion_noalloc(const float* y, int64_t n, double theta, float* 
  * host arrays (n x D), in place. */
 int bhtsne_update(bhtsne_ctx* ctx, int dtype, int32_t embed_dim, void* y, const void* pos, const void* neg, void* uy,
                   void* gains, int64_t n, double learning_rate, double momentum, double inverse_z);
+
+/* ---- CSV input and output (host only; no GPU needed) ----------------------- */
+/* load_csv (src/csv.rs:61-118) for numeric data: the fields of every record,
+ * except the columns listed in skip (n_skip of them), parsed as the dtype's
+ * float in file order; has_headers skips the first record. The reference
+ * converts fields with a caller's closure; here they are parsed as Rust's
+ * str::parse does. Call with out == NULL to get *count (values) and *records;
+ * then with out holding *count values. Records must all have the first
+ * record's field count. Errors: BHTSNE_EIO (file), BHTSNE_EINVAL (a field
+ * that does not parse, a ragged record), with a message from
+ * bhtsne_io_last_error (per thread). */
+int bhtsne_load_csv(const char* path, int32_t has_headers, const int64_t* skip, int64_t n_skip, int dtype, void* out,
+                    int64_t* count, int64_t* records);
+/* write_csv (src/csv.rs:31-58) of a fitted handle's embedding: one point per
+ * record, headers "x,y" (D = 2) or "x,y,z" (D = 3), values printed as Rust's
+ * Display prints a float (shortest round-trip decimal, no exponent). */
+int bhtsne_tsne_write_csv(bhtsne_tsne* t, const char* path);
+/* No reference counterpart: write_csv of an embedding held by the caller
+ * (n x embed_dim values of dtype), e.g. a batch or server result. */
+int bhtsne_write_csv(const void* embedding, int64_t n, int32_t embed_dim, int dtype, const char* path);
+const char* bhtsne_io_last_error(void);
 
 /* ---- batches of independent fits (no reference counterpart) --------------- */
 /* Many independent Barnes-Hut embeddings of uneven size, fitted together: every

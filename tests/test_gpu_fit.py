@@ -209,22 +209,31 @@ def test_affinities_round_trip_and_cache(gpu, oracle):
 
 def test_final_kl_within_one_percent_of_oracle(gpu, oracle):
     """Same inputs (kNN table, seed) through the GPU and the oracle; trajectories
-    are chaotic, so the final cost is compared (reference-compatible and true KL)."""
+    are chaotic, so the final cost is compared (reference-compatible and true KL).
+    At this size the oracle's own reference-compatible FIt-SNE KL moves by about
+    1 % between starts 1e-6 apart (the quirk reads one value per row), so the
+    GPU's cost is held to 1 % of the mean over three such starts."""
     X, _ = blobs(2000, 50, 10, 1001)
     idx, dist = oracle.knn(X, 90)
     seed = np.random.default_rng(5).normal(0, 1e-4, size=(2000, 2)).astype(np.float32)
     for method in ("bh", "fit"):
         g = gpu.TSNE(2000).perplexity(30).epochs(1000).initial_embedding(seed)
-        o = oracle.TSNE(2000).perplexity(30).epochs(1000).initial_embedding(seed)
         if method == "bh":
             g.barnes_hut_with_neighbors(0.5, (idx, dist))
-            o.barnes_hut_with_neighbors(0.5, idx.astype(np.uint64), dist)
         else:
             g.fit_sne_with_neighbors((idx, dist))
-            o.fit_sne_with_neighbors(idx.astype(np.uint64), dist)
+        ko = {True: [], False: []}
+        for eps in (0.0, 1e-6, -1e-6):
+            o = oracle.TSNE(2000).perplexity(30).epochs(1000).initial_embedding((seed * np.float32(1 + eps)))
+            if method == "bh":
+                o.barnes_hut_with_neighbors(0.5, idx.astype(np.uint64), dist)
+            else:
+                o.fit_sne_with_neighbors(idx.astype(np.uint64), dist)
+            for quirk in (True, False):
+                ko[quirk].append(o.kl_divergence(quirk))
         for quirk in (True, False):
-            kg, ko = g.kl_divergence(quirk), o.kl_divergence(quirk)
-            assert abs(kg - ko) / abs(ko) < 0.01, (method, quirk, kg, ko)
+            kg, km = g.kl_divergence(quirk), float(np.mean(ko[quirk]))
+            assert abs(kg - km) / abs(km) < 0.01, (method, quirk, kg, ko[quirk])
 
 
 @pytest.mark.parametrize("method", ["bh", "exact"])
@@ -338,3 +347,23 @@ def test_wide_barnes_hut_fit_matches_oracle(gpu, oracle, D):
     for quirk in (True, False):
         kg, ko = g.kl_divergence(quirk), o.kl_divergence(quirk)
         assert abs(kg - ko) / abs(ko) < 0.01, (D, quirk, kg, ko)
+
+
+@pytest.mark.parametrize("D", [2, 3])
+def test_write_csv_of_a_fit(gpu, tmp_path, D):
+    """write_csv (src/csv.rs:31-58) of a fitted handle: the header for D and
+    one record per point in the caller's order, each value printed as Rust's
+    Display (shortest round-trip digits), so it reads back bit for bit; before
+    a fit only the header is written."""
+    X, _ = blobs(600, 10, 4, 61)
+    t = gpu.TSNE(X, D=D).perplexity(10).epochs(60).random_seed(3)
+    p0 = tmp_path / "empty.csv"
+    t.write_csv(str(p0))
+    assert p0.read_text() == ("x,y\n" if D == 2 else "x,y,z\n")
+    t.barnes_hut(0.5)
+    p = tmp_path / "emb.csv"
+    t.write_csv(str(p))
+    lines = p.read_text().split("\n")
+    assert lines[0] == ("x,y" if D == 2 else "x,y,z") and lines[-1] == "" and len(lines) == 602
+    back = gpu.load_csv(str(p), has_headers=True)
+    assert np.array_equal(back, t.embedding())
