@@ -95,8 +95,6 @@ struct State {
   DevBuf kidx, kdist, kp, xin, yext, ckpt;
   Renumbering rn;  // locality layout of y/uy/gains (see launch_renumber)
   AttrTasks at;    // attractive-pass tasks of the current CSR layout
-  AttrBlocks ab;   // the 2-D blocked copy of P for the attractive pass (D <= 3, large n)
-  int blk_log = 0; // its block size (log2) for the current fit; 0: the task pass
   uint64_t layout_gen = 0;
   // y in the caller's point order (a copy when the layout is renumbered).
   const T* y_external(cudaStream_t s) {
@@ -341,10 +339,7 @@ void epoch_tail(bhtsne_tsne* t, int64_t epoch, std::vector<T>& snap) {
     const T scale = T(1) / (T)t->early_exaggeration;
     if (t->loop_kind == BHTSNE_METHOD_EXACT) launch_scale<T>(S.pdense.template as<T>(), t->n * t->n, scale, s);
     else launch_scale<T>(S.vals.template as<T>(), S.nnz, scale, s);
-    if (S.rn.active && S.rn.csr && t->loop_kind != BHTSNE_METHOD_EXACT)
-      launch_scale<T>(S.rn.vals.template as<T>(), S.nnz, scale, s);
-    if (S.ab.tile_log > 0 && t->loop_kind != BHTSNE_METHOD_EXACT)
-      launch_scale<T>(S.ab.val.template as<T>(), S.nnz, scale, s);
+    if (S.rn.active && t->loop_kind != BHTSNE_METHOD_EXACT) launch_scale<T>(S.rn.vals.template as<T>(), S.nnz, scale, s);
     t->stop_lying_fired = true;
   }
   if (epoch == t->momentum_switch_epoch) t->momentum = t->final_momentum;
@@ -402,28 +397,15 @@ void advance_impl(bhtsne_tsne* t, int64_t epochs) {
   const char* rev = getenv("BHTSNE_RENUMBER_EVERY");
   const int64_t renumber_every = rev ? atoll(rev) : 50;
   const bool sparse = t->loop_kind != BHTSNE_METHOD_EXACT;
-  // The attractive pass of the current layout, rebuilt (outside any capture)
-  // when the layout changes: at a fit's start and at each renumbering. Large
-  // fits in D <= 3 use the 2-D blocked copy of P (read through the slot maps),
-  // the others bounded row tasks over the CSR in the current slot order.
-  const int blk_log = sparse ? S.blk_log : 0;
+  // Tasks of the current CSR layout, rebuilt (outside any capture) when the
+  // layout changes: at a fit's start and at each renumbering.
   auto ensure_tasks = [&]() {
-    if (!sparse) return;
-    if (blk_log > 0) {
-      if (S.ab.gen == S.layout_gen && S.ab.tile_log == blk_log) return;
-      build_attr_blocks<T>(S.ab, D, S.rows.template as<uint64_t>(), S.cols.template as<uint32_t>(),
-                           S.vals.template as<T>(), n, S.nnz, blk_log, s);
-      S.ab.gen = S.layout_gen;
-      return;
-    }
-    if (S.at.gen == S.layout_gen) return;
+    if (!sparse || S.at.gen == S.layout_gen) return;
     build_attr_tasks<T>(S.at, D, (S.rn.active ? S.rn.rows : S.rows).template as<uint64_t>(), n, s);
     S.at.gen = S.layout_gen;
   };
   auto attractive = [&]() {
-    if (blk_log > 0)
-      launch_attractive_blocked<T>(S.ab, y, S.pos.template as<T>(), s);
-    else if (S.rn.active)
+    if (S.rn.active)
       launch_attractive_tasks<T>(S.at, S.rn.cols.template as<uint32_t>(), S.rn.vals.template as<T>(), y,
                                  S.pos.template as<T>(), s);
     else
@@ -434,8 +416,6 @@ void advance_impl(bhtsne_tsne* t, int64_t epochs) {
   std::vector<cudaEvent_t> rl_ev;
   auto maybe_renumber = [&](int64_t epoch) {
     if (!sparse || renumber_every <= 0 || epoch % renumber_every != 0) return;
-    // the blocked attractive pass gathers y from shared-memory tiles, whatever the layout
-    if (blk_log > 0) return;
     // At epoch 0 only a caller's embedding (a warm start) has a layout worth
     // following; the seeded random start has none.
     if (epoch == 0 && !t->caller_init) return;
@@ -644,8 +624,6 @@ void advance_impl(bhtsne_tsne* t, int64_t epochs) {
   BHG_CUDA(cudaEventDestroy(e1));
   t->loop_ms = ms;
   t->loop_epochs = epochs;
-  if (blk_log > 0 && attr_blocks_fault(S.ab, s))
-    throw Error(ST_ETIMEDOUT, "error: a tile copy of the attractive pass timed out.");
   t->relayout_ms = 0;
   t->relayouts = (int64_t)rl_ev.size() / 2;
   for (size_t i = 0; i + 1 < rl_ev.size(); i += 2) {
@@ -673,7 +651,6 @@ void run_loop(bhtsne_tsne* t, int kind, double theta) {
   t->drop_graph();
   st<T>(t).rn.active = false;  // the fit starts from y in the caller's order
   ++st<T>(t).layout_gen;
-  st<T>(t).blk_log = kind != BHTSNE_METHOD_EXACT ? attr_blocks_tile_log(t->D, sizeof(T), t->n) : 0;
   t->armed = true;
   t->loop_kind = kind;
   t->loop_theta = theta;
@@ -1344,18 +1321,9 @@ int bhtsne_gradient(bhtsne_ctx* ctx, int dtype, int32_t method, int32_t embed_di
         } else {
           invalid("error: unknown method.");
         }
-        const int blk_log = attr_blocks_tile_log(D, sizeof(T), n);
-        if (blk_log > 0) {
-          AttrBlocks ab;
-          build_attr_blocks<T>(ab, D, rd.as<uint64_t>(), cd.as<uint32_t>(), vd.as<T>(), n, std::max<int64_t>(nnz, 0),
-                               blk_log, s);
-          launch_attractive_blocked<T>(ab, yd.as<T>(), pd.as<T>(), s);
-          if (attr_blocks_fault(ab, s)) throw Error(ST_ETIMEDOUT, "error: a tile copy of the attractive pass timed out.");
-        } else {
-          AttrTasks at;
-          build_attr_tasks<T>(at, D, rd.as<uint64_t>(), n, s);
-          launch_attractive_tasks<T>(at, cd.as<uint32_t>(), vd.as<T>(), yd.as<T>(), pd.as<T>(), s);
-        }
+        AttrTasks at;
+        build_attr_tasks<T>(at, D, rd.as<uint64_t>(), n, s);
+        launch_attractive_tasks<T>(at, cd.as<uint32_t>(), vd.as<T>(), yd.as<T>(), pd.as<T>(), s);
         if (neg) BHG_CUDA(cudaMemcpyAsync(neg, nd.ptr, (size_t)n * D * sizeof(T), cudaMemcpyDeviceToHost, s));
       }
       BHG_CUDA(cudaMemcpyAsync(pos, pd.ptr, (size_t)n * D * sizeof(T), cudaMemcpyDeviceToHost, s));

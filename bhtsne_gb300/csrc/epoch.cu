@@ -677,8 +677,7 @@ void launch_attractive_tasks(const AttrTasks& at, const uint32_t* cols, const T*
 
 template <class T>
 void launch_renumber(int D, const uint32_t* order, int64_t n, Renumbering& r, T* y, T* uy, T* gains, T* tmp_a, T* tmp_b,
-                     T* tmp_c, const uint64_t* rows, const uint32_t* cols, const T* vals, int64_t nnz, cudaStream_t s,
-                     bool build_csr) {
+                     T* tmp_c, const uint64_t* rows, const uint32_t* cols, const T* vals, int64_t nnz, cudaStream_t s) {
   const unsigned g = (unsigned)ceil_div(n, 256);
   uint32_t* ext_new = static_cast<uint32_t*>(r.ext_alt.ensure((size_t)n * 4));
   const uint32_t* ext_old = r.active ? r.ext.template as<uint32_t>() : nullptr;
@@ -696,9 +695,6 @@ void launch_renumber(int D, const uint32_t* order, int64_t n, Renumbering& r, T*
   uint32_t* inv = static_cast<uint32_t*>(r.inv.ensure((size_t)n * 4));
   invert_kernel<<<g, 256, 0, s>>>(r.ext.template as<uint32_t>(), n, inv);
   BHG_LAUNCH_CHECK();
-  r.active = true;
-  r.csr = build_csr;
-  if (!build_csr) return;
   // CSR in slot order with slot columns, sorted within each row
   uint32_t* len = static_cast<uint32_t*>(r.len.ensure((size_t)n * 4));
   slot_len_kernel<<<g, 256, 0, s>>>(rows, r.ext.template as<uint32_t>(), n, len);
@@ -812,7 +808,7 @@ void launch_exact_kl(int D, const T* y, const T* p, int64_t n, const double* z, 
 
 #define BHG_INST(T)                                                                                                  \
   template void launch_renumber<T>(int, const uint32_t*, int64_t, Renumbering&, T*, T*, T*, T*, T*, T*,              \
-                                   const uint64_t*, const uint32_t*, const T*, int64_t, cudaStream_t, bool);         \
+                                   const uint64_t*, const uint32_t*, const T*, int64_t, cudaStream_t);               \
   template void launch_unpermute<T>(int, const T*, const uint32_t*, int64_t, T*, cudaStream_t);                      \
   template void build_attr_tasks<T>(AttrTasks&, int, const uint64_t*, int64_t, cudaStream_t);                        \
   template void launch_random_init<T>(T*, int64_t, uint64_t, cudaStream_t);                                          \

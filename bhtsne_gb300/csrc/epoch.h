@@ -31,42 +31,6 @@ template <class T>
 void launch_attractive_tasks(const AttrTasks& at, const uint32_t* cols, const T* vals, const T* y, T* pos,
                              cudaStream_t s);
 
-// The attractive pass over a 2-D blocked copy of P (attract.cu): points cut
-// into blocks of 2^tile_log consecutive rows, entries grouped by (row block,
-// column tile), each tile of y staged in shared memory while its entries are
-// summed. It reads y through no locality at all, so fits that use it are not
-// re-laid out. Built once per fit from the CSR; its values are a copy: a
-// rescale of P (stop lying) must rescale val too.
-struct AttrBlocks {
-  int tile_log = 0;  // 0: not built (use the task pass)
-  int D = 0, nb = 0, groups = 0, grid = 0;
-  size_t smem = 0;
-  int64_t n = 0, nnz = 0;
-  DevBuf base;     // u64 [nb * nb * segments + 1]: start of each (row block, column tile, row segment)
-  DevBuf idx;      // u32 [nnz]: (local row << tile_log) | local column
-  DevBuf val;      // T [nnz]
-  DevBuf part;     // T [nb * groups][2^tile_log][D]: partial forces per unit
-  DevBuf counter;  // u32 work counter (reset by the pass), then the i32 fault word
-  DevBuf cnt, scan_tmp;
-  uint64_t gen = ~0ull;  // layout generation it was built for
-};
-
-// log2 of the block size for D and the value type, or 0 where the task pass
-// is used (D > 3, fewer than 8 row blocks, more than 2048, or
-// BHTSNE_ATTR_BLOCKED=0).
-int attr_blocks_tile_log(int D, size_t value_bytes, int64_t n);
-
-template <class T>
-void build_attr_blocks(AttrBlocks& ab, int D, const uint64_t* rows, const uint32_t* cols, const T* vals, int64_t n,
-                       int64_t nnz, int tile_log, cudaStream_t s);
-
-template <class T>
-void launch_attractive_blocked(const AttrBlocks& ab, const T* y, T* pos, cudaStream_t s);
-
-// Whether a blocked pass since the build gave up on a bulk copy (a bounded
-// wait ran out); synchronises the stream.
-bool attr_blocks_fault(const AttrBlocks& ab, cudaStream_t s);
-
 // random_init (the reference's is unseeded, src/tsne/mod.rs:142-147): a
 // seeded Box-Muller N(0, 1e-4) over the LCG s <- 6364136223846793005 s +
 // 1442695040888963407, values 2i and 2i + 1 from states 2i + 1 and 2i + 2.
@@ -82,18 +46,13 @@ void launch_random_init(T* y, int64_t count, uint64_t seed, cudaStream_t s);
 // CSR row of ext[s] with columns as slots, sorted within the row.
 struct Renumbering {
   bool active = false;
-  bool csr = false;  // rows/cols/vals hold P in the current slot order
   DevBuf ext, ext_alt, inv, rows, cols, vals, len, scan_tmp;
   DevBuf long_rows;  // u32 count, then the slots of the rows longer than the register sort takes
 };
 
-// With build_csr false only the state and the slot maps are re-laid out (the
-// slot-ordered CSR is left unbuilt: the blocked attractive pass reads P
-// through the maps); r.csr says whether rows/cols/vals are current.
 template <class T>
 void launch_renumber(int D, const uint32_t* order, int64_t n, Renumbering& r, T* y, T* uy, T* gains, T* tmp_a, T* tmp_b,
-                     T* tmp_c, const uint64_t* rows, const uint32_t* cols, const T* vals, int64_t nnz, cudaStream_t s,
-                     bool build_csr = true);
+                     T* tmp_c, const uint64_t* rows, const uint32_t* cols, const T* vals, int64_t nnz, cudaStream_t s);
 
 // out[ext[s]] = y[s]: back to the caller's point order.
 template <class T>

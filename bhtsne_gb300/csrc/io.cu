@@ -281,7 +281,8 @@ int bhtsne_load_csv(const char* path, int32_t has_headers, const int64_t* skip, 
 }
 
 int bhtsne_write_csv(const void* embedding, int64_t n, int32_t embed_dim, int dtype, const char* path) {
-  if (!embedding || !path || n < 0 || embed_dim < 1) return io_fail(BHTSNE_EINVAL, "error: invalid write_csv arguments.");
+  if ((!embedding && n > 0) || !path || n < 0 || embed_dim < 1)
+    return io_fail(BHTSNE_EINVAL, "error: invalid write_csv arguments.");
   if (dtype == BHTSNE_F32) return write_csv_impl<float>((const float*)embedding, n, embed_dim, path);
   if (dtype == BHTSNE_F64) return write_csv_impl<double>((const double*)embedding, n, embed_dim, path);
   return io_fail(BHTSNE_EINVAL, "error: dtype must be BHTSNE_F32 or BHTSNE_F64.");
