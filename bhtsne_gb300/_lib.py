@@ -66,6 +66,10 @@ SIGNATURES = {
     "bhtsne_tsne_write_csv": (C.c_int, [_vp, C.c_char_p]),
     "bhtsne_write_csv": (C.c_int, [_vp, _i64, _i32, C.c_int, C.c_char_p]),
     "bhtsne_io_last_error": (C.c_char_p, []),
+    "bhtsne_tune": (C.c_int, [_vp, C.c_int, _i32, _i64, _i32, _i32]),
+    "bhtsne_tune_config": (C.c_int, [C.c_int, _i32, _i64, C.c_char_p, _i64]),
+    "bhtsne_tune_load": (C.c_int, [C.c_char_p]),
+    "bhtsne_tune_save": (C.c_int, [C.c_char_p]),
     "bhtsne_bh_repulsion_noalloc": (C.c_int, [_vp, _i64, _dbl, _vp, _vp, _vp]),
     "bhtsne_batch_params_default": (None, [_vp]),
     "bhtsne_batch_new": (C.c_int, [_vp, C.c_int, _i32, _vp, C.POINTER(C.c_void_p)]),
@@ -181,6 +185,12 @@ class Context:
         if rc != OK:
             raise BhtsneError(rc, self.lib.bhtsne_ctx_last_error(self.handle).decode())
 
+    def tune(self, dtype: int, embed_dim: int, n: int, k: int, dim: int = 0) -> str:
+        """Autotunes the launch shapes for fits of that shape on this device
+        (bhtsne_tune); returns the candidates' timings."""
+        self.check(self.lib.bhtsne_tune(self.handle, int(dtype), int(embed_dim), int(n), int(k), int(dim)))
+        return self.lib.bhtsne_ctx_last_error(self.handle).decode()
+
     def knn_fallback_rows(self) -> int:
         """Rows of the last Euclidean kNN on this context that failed the
         tensor-core pass's exactness certificate and were recomputed."""
@@ -208,3 +218,28 @@ def default_context() -> Context:
     if _default_ctx is None:
         _default_ctx = Context(0)
     return _default_ctx
+
+
+def tune_config(dtype: int, embed_dim: int, n: int) -> dict:
+    """The launch shapes a fit of (dtype, embed_dim, n) would use on the current device."""
+    import json
+    lib = load()
+    buf = C.create_string_buffer(1024)
+    rc = lib.bhtsne_tune_config(int(dtype), int(embed_dim), int(n), buf, len(buf))
+    if rc != OK:
+        raise BhtsneError(rc, lib.bhtsne_io_last_error().decode())
+    return json.loads(buf.value.decode())
+
+
+def tune_load(path: str) -> None:
+    lib = load()
+    rc = lib.bhtsne_tune_load(os.fsencode(path))
+    if rc != OK:
+        raise BhtsneError(rc, lib.bhtsne_io_last_error().decode())
+
+
+def tune_save(path: str) -> None:
+    lib = load()
+    rc = lib.bhtsne_tune_save(os.fsencode(path))
+    if rc != OK:
+        raise BhtsneError(rc, lib.bhtsne_io_last_error().decode())

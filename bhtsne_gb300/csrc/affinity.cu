@@ -268,7 +268,7 @@ int bits_for(int64_t n) {
   return b;
 }
 
-constexpr int kSumBlocks = 2 * 152;
+constexpr int kSumBlocksMax = 1024;  // partials of launch_sum (two blocks per SM)
 
 }  // namespace
 
@@ -283,31 +283,32 @@ void launch_search_beta(const T* dist, int64_t n, int64_t k, T perplexity, T* p,
 
 template <class T>
 void launch_sum(const T* v, int64_t n, double* out, DevBuf& tmp, cudaStream_t s) {
-  double* part = static_cast<double*>(tmp.ensure(kSumBlocks * sizeof(double)));
-  sum_partial_kernel<T><<<kSumBlocks, 256, 0, s>>>(v, n, part);
+  const int blocks = sm_grid(2, kSumBlocksMax);
+  double* part = static_cast<double*>(tmp.ensure(kSumBlocksMax * sizeof(double)));
+  sum_partial_kernel<T><<<blocks, 256, 0, s>>>(v, n, part);
   BHG_LAUNCH_CHECK();
-  sum_final_kernel<<<1, 32, 0, s>>>(part, kSumBlocks, out);
+  sum_final_kernel<<<1, 32, 0, s>>>(part, blocks, out);
   BHG_LAUNCH_CHECK();
 }
 
 template <class T>
 void launch_normalize(T* v, int64_t n, T exaggeration, double* sum_dev, DevBuf& tmp, cudaStream_t s) {
   launch_sum<T>(v, n, sum_dev, tmp, s);
-  normalize_kernel<T><<<kSumBlocks, 256, 0, s>>>(v, n, sum_dev, exaggeration);
+  normalize_kernel<T><<<sm_grid(2, kSumBlocksMax), 256, 0, s>>>(v, n, sum_dev, exaggeration);
   BHG_LAUNCH_CHECK();
 }
 
 template <class T>
 void launch_scale(T* v, int64_t n, T scale, cudaStream_t s) {
   if (n <= 0) return;
-  scale_kernel<T><<<kSumBlocks, 256, 0, s>>>(v, n, scale);
+  scale_kernel<T><<<sm_grid(2, kSumBlocksMax), 256, 0, s>>>(v, n, scale);
   BHG_LAUNCH_CHECK();
 }
 
 template <class T>
 void launch_scaled_copy(const T* v, int64_t n, T scale, T* out, cudaStream_t s) {
   if (n <= 0) return;
-  scaled_copy_kernel<T><<<kSumBlocks, 256, 0, s>>>(v, n, scale, out);
+  scaled_copy_kernel<T><<<sm_grid(2, kSumBlocksMax), 256, 0, s>>>(v, n, scale, out);
   BHG_LAUNCH_CHECK();
 }
 

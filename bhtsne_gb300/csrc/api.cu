@@ -24,6 +24,7 @@
 #include "epoch.h"
 #include "fitsne.h"
 #include "knn.h"
+#include "tune.h"
 #include "batch.h"
 
 using namespace bhg;
@@ -69,6 +70,7 @@ int ctx_create_with_priority(int device, int priority, bhtsne_ctx** out) {
     return BHTSNE_ECUDA;
   }
   keep_pool_cached(device);
+  tune_load_env_once();
   *out = c;
   return BHTSNE_OK;
 }
@@ -95,6 +97,7 @@ struct State {
   DevBuf kidx, kdist, kp, xin, yext, ckpt;
   Renumbering rn;  // locality layout of y/uy/gains (see launch_renumber)
   AttrTasks at;    // attractive-pass tasks of the current CSR layout
+  int task_len = kAttrTaskLen;  // the tuned task length of the current fit
   uint64_t layout_gen = 0;
   // y in the caller's point order (a copy when the layout is renumbered).
   const T* y_external(cudaStream_t s) {
@@ -401,7 +404,7 @@ void advance_impl(bhtsne_tsne* t, int64_t epochs) {
   // layout changes: at a fit's start and at each renumbering.
   auto ensure_tasks = [&]() {
     if (!sparse || S.at.gen == S.layout_gen) return;
-    build_attr_tasks<T>(S.at, D, (S.rn.active ? S.rn.rows : S.rows).template as<uint64_t>(), n, s);
+    build_attr_tasks<T>(S.at, D, (S.rn.active ? S.rn.rows : S.rows).template as<uint64_t>(), n, s, S.task_len);
     S.at.gen = S.layout_gen;
   };
   auto attractive = [&]() {
@@ -651,6 +654,10 @@ void run_loop(bhtsne_tsne* t, int kind, double theta) {
   t->drop_graph();
   st<T>(t).rn.active = false;  // the fit starts from y in the caller's order
   ++st<T>(t).layout_gen;
+  // launch shapes of this fit: tuned for (T, D, N) on this device, or the defaults
+  const TuneKnobs kn = tune_lookup(t->dtype, t->D, t->n);
+  st<T>(t).task_len = kn.attr_task_len;
+  st<T>(t).bh.traverse_threads = kn.bh_threads;
   t->armed = true;
   t->loop_kind = kind;
   t->loop_theta = theta;
@@ -713,6 +720,7 @@ void fit_euclidean(bhtsne_tsne* t, int kind, double theta, const void* data, int
     upload<T>(S.xin, data, (size_t)n * dim * sizeof(T), s);
     S.kidx.ensure(n * k * 4);
     S.kdist.ensure(n * k * sizeof(T));
+    S.knn.pass = tune_lookup(t->dtype, t->D, n).knn_pass;
     t->ctx->knn_fallback_rows = knn_euclidean<T>(S.xin.template as<T>(), n, dim, (int)k,
                                                  S.kidx.template as<uint32_t>(), S.kdist.template as<T>(), S.knn, s);
     S.xin.release();
@@ -921,6 +929,7 @@ int bhtsne_ctx_create(int device, bhtsne_ctx** out) {
     return BHTSNE_ECUDA;
   }
   keep_pool_cached(device);
+  tune_load_env_once();
   *out = c;
   return BHTSNE_OK;
 }
@@ -934,6 +943,16 @@ int bhtsne_ctx_destroy(bhtsne_ctx* ctx) {
 }
 
 const char* bhtsne_ctx_last_error(const bhtsne_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+int bhtsne_tune(bhtsne_ctx* ctx, int dtype, int32_t embed_dim, int64_t n, int32_t k, int32_t dim) {
+  std::string report;
+  const int rc = guard_ctx(ctx, [&] {
+    if (dtype != BHTSNE_F32 && dtype != BHTSNE_F64) invalid("error: dtype must be BHTSNE_F32 or BHTSNE_F64.");
+    tune_run(dtype, embed_dim, n, k, dim, ctx->stream, &report);
+  });
+  if (rc == BHTSNE_OK) ctx->err = report;  // the timings, readable through bhtsne_ctx_last_error
+  return rc;
+}
 
 int bhtsne_ctx_knn_fallback_rows(const bhtsne_ctx* ctx, int64_t* rows) {
   if (!ctx || !rows) return BHTSNE_EINVAL;
@@ -1293,6 +1312,8 @@ int bhtsne_gradient(bhtsne_ctx* ctx, int dtype, int32_t method, int32_t embed_di
       DevBuf yd, rd, cd, vd, pd, nd, zd, tmp;
       BhWorkspace<T> bh;
       FitWorkspace<T> fw;
+      const TuneKnobs kn = tune_lookup(dtype, D, n);
+      bh.traverse_threads = kn.bh_threads;
       upload<T>(yd, y, (size_t)n * D * sizeof(T), s);
       pd.ensure((size_t)n * D * sizeof(T));
       nd.ensure((size_t)n * D * sizeof(T));
@@ -1322,7 +1343,7 @@ int bhtsne_gradient(bhtsne_ctx* ctx, int dtype, int32_t method, int32_t embed_di
           invalid("error: unknown method.");
         }
         AttrTasks at;
-        build_attr_tasks<T>(at, D, rd.as<uint64_t>(), n, s);
+        build_attr_tasks<T>(at, D, rd.as<uint64_t>(), n, s, kn.attr_task_len);
         launch_attractive_tasks<T>(at, cd.as<uint32_t>(), vd.as<T>(), yd.as<T>(), pd.as<T>(), s);
         if (neg) BHG_CUDA(cudaMemcpyAsync(neg, nd.ptr, (size_t)n * D * sizeof(T), cudaMemcpyDeviceToHost, s));
       }

@@ -310,7 +310,7 @@ void batch_append_csr(const uint64_t* rows, const uint32_t* cols, int64_t n, int
   offset_rows_kernel<<<(unsigned)ceil_div(n + 1, 256), 256, 0, s>>>(rows, n + 1, row_add, rows_out);
   BHG_LAUNCH_CHECK();
   if (nnz > 0) {
-    offset_cols_kernel<<<(unsigned)std::min<int64_t>(ceil_div(nnz, 256), 4 * 152), 256, 0, s>>>(cols, nnz, col_add,
+    offset_cols_kernel<<<(unsigned)std::min<int64_t>(ceil_div(nnz, 256), sm_grid(4, 4096)), 256, 0, s>>>(cols, nnz, col_add,
                                                                                                  cols_out);
     BHG_LAUNCH_CHECK();
   }
@@ -321,7 +321,7 @@ void batch_extract_csr(const uint64_t* rows, const uint32_t* cols, int64_t n, in
   sub_rows_kernel<<<(unsigned)ceil_div(n + 1, 256), 256, 0, s>>>(rows, n + 1, row_sub, rows_out);
   BHG_LAUNCH_CHECK();
   if (nnz > 0) {
-    sub_cols_kernel<<<(unsigned)std::min<int64_t>(ceil_div(nnz, 256), 4 * 152), 256, 0, s>>>(cols, nnz, col_sub,
+    sub_cols_kernel<<<(unsigned)std::min<int64_t>(ceil_div(nnz, 256), sm_grid(4, 4096)), 256, 0, s>>>(cols, nnz, col_sub,
                                                                                               cols_out);
     BHG_LAUNCH_CHECK();
   }
@@ -336,7 +336,7 @@ void batch_normalize(T* vals, const int64_t* nnz_off, int K, T exaggeration, boo
 
 void batch_offset_indices(const uint32_t* in, int64_t count, uint32_t add, uint32_t* out, cudaStream_t s) {
   if (count <= 0) return;
-  offset_u32_kernel<<<(unsigned)std::min<int64_t>(ceil_div(count, 256), 8 * 152), 256, 0, s>>>(in, count, add, out);
+  offset_u32_kernel<<<(unsigned)std::min<int64_t>(ceil_div(count, 256), sm_grid(8, 8192)), 256, 0, s>>>(in, count, add, out);
   BHG_LAUNCH_CHECK();
 }
 

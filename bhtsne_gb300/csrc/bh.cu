@@ -41,7 +41,8 @@ namespace bhg {
 namespace {
 
 constexpr int kThreads = 256;
-static_assert(kThreads == kBhThreads, "bh_sizes sizes the Z partials by this block size");
+constexpr int kTraverseMax = 512;
+static_assert(kBhThreads == 128, "bh_sizes sizes the Z partials for traversal blocks of at least 128 threads");
 
 // ---------------------------------------------------------------------------
 // Recentre (optional) + per-axis bounding box; the last block to finish
@@ -579,7 +580,7 @@ __global__ void tree_emit_kernel(const typename MortonD<D>::Code* __restrict__ c
 // block order by the last block).
 // ---------------------------------------------------------------------------
 template <class T, int D>
-__global__ void __launch_bounds__(kThreads) bh_traverse_kernel(const T* __restrict__ y, const uint32_t* __restrict__ perm,
+__global__ void __launch_bounds__(kTraverseMax) bh_traverse_kernel(const T* __restrict__ y, const uint32_t* __restrict__ perm,
                                                                int64_t n, TreeNodes<T, D> nodes, const uint64_t* __restrict__ n_nodes_p,
                                                                int64_t max_nodes, const BoxParams<T>* __restrict__ prm,
                                                                T theta_sq, T* __restrict__ neg, T* __restrict__ qout,
@@ -708,7 +709,8 @@ __global__ void __launch_bounds__(kThreads) bh_traverse_kernel(const T* __restri
 template <class T>
 void launch_recenter_bbox(int D, T* y, int64_t n, const double* mean_sum, bool apply_mean, BhWorkspace<T>& ws,
                           int bits, cudaStream_t s) {
-  const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(n, kThreads), kBhBoxBlocks));
+  const int grid =
+      (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(n, kThreads), sm_grid(2, (int)kBhBoxBlocksMax)));
   ws.zero_counters(s);
   T* pmin = ws.part_min.template as<T>();
   T* pmax = ws.part_max.template as<T>();
@@ -875,12 +877,13 @@ void bh_traverse(BhWorkspace<T>& ws, int D, const T* y, int64_t n, T theta, T* n
     return;
   }
   ws.zero_counters(s);
-  const unsigned g = (unsigned)ceil_div(n, kThreads);
+  const int bt = ws.traverse_threads == 128 || ws.traverse_threads == 512 ? ws.traverse_threads : 256;
+  const unsigned g = (unsigned)ceil_div(n, bt);
   const T theta_sq = theta * theta;
   const uint64_t* M = ws.base.template as<uint64_t>() + n;
   with_dim<2, 7>(D, "error: Barnes-Hut covers D in 2..7.", [&](auto dc) {
     constexpr int DD = decltype(dc)::value;
-    bh_traverse_kernel<T, DD><<<g, kThreads, 0, s>>>(
+    bh_traverse_kernel<T, DD><<<g, bt, 0, s>>>(
         y, ws.perm.template as<uint32_t>(), n, nodes_of<T, DD>(ws), M, 2 * n, ws.params.template as<BoxParams<T>>(),
         theta_sq, neg, qout, ws.zpart.template as<double>(), ws.zdone.template as<unsigned>(),
         ws.zval.template as<double>(), segs, boxes, ws.base.template as<uint64_t>());

@@ -157,11 +157,12 @@ struct TreeNodes<T, 3> {
 };
 
 // Launch shapes that fix scratch sizes: points per prefix-sum tile of the
-// centre-of-mass sums, the most blocks of the bounding-box reduction, and the
-// threads per block of the per-point kernels (one Z partial per block).
+// centre-of-mass sums, the most blocks of the bounding-box reduction (it runs
+// two per SM, up to this many), and the smallest threads per block of the
+// traversal (one Z partial per block).
 constexpr int64_t kBhPrefixTile = 2048;
-constexpr int64_t kBhBoxBlocks = 2 * 152;
-constexpr int64_t kBhThreads = 256;
+constexpr int64_t kBhBoxBlocksMax = 1024;
+constexpr int64_t kBhThreads = 128;
 
 // Bytes of each Barnes-Hut workspace buffer for n points in D dimensions.
 // BhWorkspace::reserve requests exactly these, and callers that carve a
@@ -187,7 +188,7 @@ constexpr BhSizes bh_sizes(int64_t n, int D) {
   z.geom = (size_t)max_nodes * (D == 2 ? sizeof(Node2<T>) : D == 3 ? sizeof(Quad<T>) : sizeof(Oct<T>));
   z.word = D == 2 ? 0 : (size_t)max_nodes * sizeof(uint32_t);
   z.wide = D >= 5 ? (size_t)nn * 16 : 0;  // also lo_orig and hi_orig at half this each
-  z.part = (size_t)kBhBoxBlocks * 8 * sizeof(T);
+  z.part = (size_t)kBhBoxBlocksMax * 8 * sizeof(T);
   z.small = 64;
   z.params = sizeof(BoxParams<T>);
   z.zpart = (size_t)((nn + kBhThreads - 1) / kBhThreads + 1) * sizeof(double);
@@ -200,6 +201,7 @@ struct BhWorkspace {
   int64_t n = 0;
   int D = 0;
   bool zeroed = false;
+  int traverse_threads = 256;  // threads per block of the traversal: 128, 256 or 512
   DevBuf keys, keys_alt, perm, perm_alt, ys, pre, pre_part, mask, cnt, base, geom, word;
   DevBuf wide, lo_orig, hi_orig;  // 128-bit codes (D >= 5): sorted codes and the unsorted halves
   DevBuf seg_tot;                 // per-set coordinate sums (job-relative prefix sums)

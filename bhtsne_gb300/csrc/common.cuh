@@ -77,11 +77,13 @@ __device__ __forceinline__ F32x2 f2_make(float a, float b) {
 __device__ __forceinline__ float f2_lo(F32x2 x) {
   float a, b;
   asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(x.v));
+  (void)b;
   return a;
 }
 __device__ __forceinline__ float f2_hi(F32x2 x) {
   float a, b;
   asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(x.v));
+  (void)a;
   return b;
 }
 __device__ __forceinline__ F32x2 f2_add(F32x2 x, F32x2 y) {

@@ -43,8 +43,8 @@ __device__ __forceinline__ void load_point(const T* __restrict__ y, int64_t j, T
 
 // ---------------------------------------------------------------------------
 // Attractive forces over bounded tasks (see AttrTasks). A task is at most
-// kAttrTaskLen = 4 x 32 entries: each lane issues its four column/value loads
-// (streaming, so that L1 keeps the gathered y lines) and four gathers at once.
+// kU x 32 entries: each lane issues its kU column/value loads (streaming, so
+// that L1 keeps the gathered y lines) and kU gathers at once.
 // ---------------------------------------------------------------------------
 struct AttrTask {
   uint64_t begin;  // first CSR entry
@@ -54,12 +54,11 @@ struct AttrTask {
 
 constexpr uint32_t kPartialBit = 0x80000000u;
 
-template <class T, int D, bool VEC>
+template <class T, int D, bool VEC, int kU>
 __global__ void __launch_bounds__(256) attractive_task_kernel(const AttrTask* __restrict__ tasks, int64_t ntasks,
                                                               const uint32_t* __restrict__ cols,
                                                               const T* __restrict__ vals, const T* __restrict__ y,
                                                               T* __restrict__ pos, T* __restrict__ part) {
-  constexpr int kU = kAttrTaskLen / 32;
   const int64_t t = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (t >= ntasks) return;  // uniform per warp
@@ -127,24 +126,25 @@ __global__ void attractive_fixup_kernel(const uint32_t* __restrict__ longs, int6
   for (int a = 0; a < D; ++a) pos[slot * D + a] = acc[a];
 }
 
-__global__ void task_count_kernel(const uint64_t* __restrict__ rows, int64_t n, uint32_t* __restrict__ cnt) {
+__global__ void task_count_kernel(const uint64_t* __restrict__ rows, int64_t n, int task_len,
+                                  uint32_t* __restrict__ cnt) {
   const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= n) return;
   const uint64_t len = rows[s + 1] - rows[s];
-  cnt[s] = len <= (uint64_t)kAttrTaskLen ? 1u : (uint32_t)((len + kAttrTaskLen - 1) / kAttrTaskLen);
+  cnt[s] = len <= (uint64_t)task_len ? 1u : (uint32_t)((len + task_len - 1) / task_len);
 }
 
-__global__ void task_fill_kernel(const uint64_t* __restrict__ rows, int64_t n, const uint64_t* __restrict__ off,
-                                 AttrTask* __restrict__ tasks, uint32_t* __restrict__ longs,
-                                 unsigned long long* __restrict__ nlong) {
+__global__ void task_fill_kernel(const uint64_t* __restrict__ rows, int64_t n, int task_len,
+                                 const uint64_t* __restrict__ off, AttrTask* __restrict__ tasks,
+                                 uint32_t* __restrict__ longs, unsigned long long* __restrict__ nlong) {
   const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= n) return;
   const uint64_t r0 = rows[s], len = rows[s + 1] - r0;
   const uint64_t t0 = off[s], c = off[s + 1] - t0;
   const uint32_t flag = c > 1 ? kPartialBit : 0u;
   for (uint64_t q = 0; q < c; ++q) {
-    const uint64_t b = q * kAttrTaskLen;
-    const uint64_t l = len - b < (uint64_t)kAttrTaskLen ? len - b : (uint64_t)kAttrTaskLen;
+    const uint64_t b = q * (uint64_t)task_len;
+    const uint64_t l = len - b < (uint64_t)task_len ? len - b : (uint64_t)task_len;
     tasks[t0 + q] = AttrTask{r0 + b, (uint32_t)s, (uint32_t)l | flag};
   }
   if (c > 1) longs[atomicAdd(nlong, 1ull)] = (uint32_t)s;
@@ -608,7 +608,7 @@ __global__ void exact_kl_kernel(const T* __restrict__ y, const T* __restrict__ p
   if (threadIdx.x == 0) part[i] = bs;
 }
 
-constexpr int kUpdBlocks = 2 * 152;
+constexpr int kUpdBlocksMax = 1024;  // partials of the update's mean (two blocks per SM)
 
 }  // namespace
 
@@ -620,15 +620,17 @@ void launch_random_init(T* y, int64_t count, uint64_t seed, cudaStream_t s) {
 }
 
 template <class T>
-void build_attr_tasks(AttrTasks& at, int D, const uint64_t* rows, int64_t n, cudaStream_t s) {
+void build_attr_tasks(AttrTasks& at, int D, const uint64_t* rows, int64_t n, cudaStream_t s, int task_len) {
+  if (task_len != 64 && task_len != 128 && task_len != 256) task_len = kAttrTaskLen;
   at.D = D;
   at.n = n;
+  at.task_len = task_len;
   at.ntasks = at.nlong = 0;
   if (n <= 0) return;
   const unsigned g = (unsigned)ceil_div(n, 256);
   uint32_t* cnt = static_cast<uint32_t*>(at.cnt.ensure((size_t)n * 4));
   uint64_t* off = static_cast<uint64_t*>(at.off.ensure((size_t)(n + 1) * 8));
-  task_count_kernel<<<g, 256, 0, s>>>(rows, n, cnt);
+  task_count_kernel<<<g, 256, 0, s>>>(rows, n, task_len, cnt);
   BHG_LAUNCH_CHECK();
   scan_u32_to_u64(cnt, off, n, at.scan_tmp, s);
   uint64_t total = 0;
@@ -639,7 +641,7 @@ void build_attr_tasks(AttrTasks& at, int D, const uint64_t* rows, int64_t n, cud
   uint32_t* longs = static_cast<uint32_t*>(at.longs.ensure((size_t)n * 4));
   unsigned long long* nl = static_cast<unsigned long long*>(at.nlong_dev.ensure(8));
   BHG_CUDA(cudaMemsetAsync(nl, 0, 8, s));
-  task_fill_kernel<<<g, 256, 0, s>>>(rows, n, off, tasks, longs, nl);
+  task_fill_kernel<<<g, 256, 0, s>>>(rows, n, task_len, off, tasks, longs, nl);
   BHG_LAUNCH_CHECK();
   unsigned long long nlong = 0;
   BHG_CUDA(cudaMemcpyAsync(&nlong, nl, 8, cudaMemcpyDeviceToHost, s));
@@ -655,8 +657,14 @@ static void launch_attractive_tasks_d(const AttrTasks& at, const uint32_t* cols,
   const unsigned grid = (unsigned)ceil_div(at.ntasks, 8);
   const AttrTask* tasks = static_cast<const AttrTask*>(at.tasks.ptr);
   T* part = static_cast<T*>(at.part.ptr);
-  if (vec) attractive_task_kernel<T, D, true><<<grid, 256, 0, s>>>(tasks, at.ntasks, cols, vals, y, pos, part);
-  else attractive_task_kernel<T, D, false><<<grid, 256, 0, s>>>(tasks, at.ntasks, cols, vals, y, pos, part);
+  auto go = [&](auto ku) {
+    constexpr int KU = decltype(ku)::value;
+    if (vec) attractive_task_kernel<T, D, true, KU><<<grid, 256, 0, s>>>(tasks, at.ntasks, cols, vals, y, pos, part);
+    else attractive_task_kernel<T, D, false, KU><<<grid, 256, 0, s>>>(tasks, at.ntasks, cols, vals, y, pos, part);
+  };
+  if (at.task_len == 64) go(std::integral_constant<int, 2>());
+  else if (at.task_len == 256) go(std::integral_constant<int, 8>());
+  else go(std::integral_constant<int, 4>());
   BHG_LAUNCH_CHECK();
   if (at.nlong > 0) {
     attractive_fixup_kernel<T, D><<<(unsigned)ceil_div(at.nlong, 256), 256, 0, s>>>(
@@ -706,10 +714,10 @@ void launch_renumber(int D, const uint32_t* order, int64_t n, Renumbering& r, T*
   if (nnz > 0) {
     uint32_t* long_rows = static_cast<uint32_t*>(r.long_rows.ensure((size_t)(n + 1) * 4));
     BHG_CUDA(cudaMemsetAsync(long_rows, 0, 4, s));
-    slot_rows_short_kernel<T><<<(unsigned)std::min<int64_t>(ceil_div(n, 8), 4 * 152), 256, 0, s>>>(
+    slot_rows_short_kernel<T><<<(unsigned)std::min<int64_t>(ceil_div(n, 8), sm_grid(4, 4096)), 256, 0, s>>>(
         rows, cols, vals, r.ext.template as<uint32_t>(), inv, n, rows_s, cols_s, vals_s, long_rows);
     BHG_LAUNCH_CHECK();
-    slot_rows_long_kernel<T><<<(unsigned)std::min<int64_t>(ceil_div(n, kSlotWarps), 8 * 152), kSlotWarps * 32, 0, s>>>(
+    slot_rows_long_kernel<T><<<(unsigned)std::min<int64_t>(ceil_div(n, kSlotWarps), sm_grid(8, 8192)), kSlotWarps * 32, 0, s>>>(
         rows, cols, vals, r.ext.template as<uint32_t>(), inv, long_rows, rows_s, cols_s, vals_s);
     BHG_LAUNCH_CHECK();
   }
@@ -729,14 +737,14 @@ void launch_unpermute(int D, const T* y, const uint32_t* ext, int64_t n, T* out,
 template <class T>
 void launch_update(int D, T* y, const T* pos, const T* neg, T* uy, T* gains, int64_t n, const double* z, T inv_norm,
                    T lr, T momentum, UpdateScratch& us, cudaStream_t s) {
-  double* part = static_cast<double*>(us.part.ensure(kUpdBlocks * 8 * sizeof(double)));
+  double* part = static_cast<double*>(us.part.ensure(kUpdBlocksMax * 8 * sizeof(double)));
   unsigned* done = static_cast<unsigned*>(us.done.ensure(64));
   if (!us.zeroed) {
     BHG_CUDA(cudaMemsetAsync(done, 0, 64, s));
     us.zeroed = true;
   }
   double* mean_sum = static_cast<double*>(us.mean_sum.ensure(8 * sizeof(double)));
-  const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(n, 256), kUpdBlocks));
+  const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(n, 256), sm_grid(2, kUpdBlocksMax)));
   with_dim<1, 7>(D, "error: the embedding dimension must be in 1..7.", [&](auto dc) {
     constexpr int DD = decltype(dc)::value;
     update_kernel<T, DD><<<grid, 256, 0, s>>>(y, pos, neg, uy, gains, n, z, inv_norm, lr, momentum, part, done, mean_sum);
@@ -747,7 +755,7 @@ void launch_update(int D, T* y, const T* pos, const T* neg, T* uy, T* gains, int
 template <class T>
 void launch_kl_sparse(int D, const uint64_t* rows, const uint32_t* cols, const T* vals, const T* y, int64_t n,
                       const double* z, bool quirk, double* out, DevBuf& tmp, cudaStream_t s) {
-  const int blocks = 2 * 152;
+  const int blocks = sm_grid(2, 1024);
   double* part = static_cast<double*>(tmp.ensure(blocks * sizeof(double)));
   with_dim<1, 7>(D, "error: the embedding dimension must be in 1..7.", [&](auto dc) {
     constexpr int DD = decltype(dc)::value;
@@ -810,7 +818,7 @@ void launch_exact_kl(int D, const T* y, const T* p, int64_t n, const double* z, 
   template void launch_renumber<T>(int, const uint32_t*, int64_t, Renumbering&, T*, T*, T*, T*, T*, T*,              \
                                    const uint64_t*, const uint32_t*, const T*, int64_t, cudaStream_t);               \
   template void launch_unpermute<T>(int, const T*, const uint32_t*, int64_t, T*, cudaStream_t);                      \
-  template void build_attr_tasks<T>(AttrTasks&, int, const uint64_t*, int64_t, cudaStream_t);                        \
+  template void build_attr_tasks<T>(AttrTasks&, int, const uint64_t*, int64_t, cudaStream_t, int);                   \
   template void launch_random_init<T>(T*, int64_t, uint64_t, cudaStream_t);                                          \
   template void launch_attractive_tasks<T>(const AttrTasks&, const uint32_t*, const T*, const T*, T*, cudaStream_t); \
   template void launch_update<T>(int, T*, const T*, const T*, T*, T*, int64_t, const double*, T, T, T, UpdateScratch&,  \

@@ -12,20 +12,24 @@ struct UpdateScratch {
 };
 
 // Attractive forces over bounded tasks: every CSR row is cut into tasks of at
-// most kAttrTaskLen entries, one warp per task. A row of one task writes its
-// slot directly; the tasks of a longer row write partial sums that a second
-// kernel adds in task order, so results do not depend on scheduling. Built
-// once per CSR layout (one host synchronisation), replayed every epoch.
-constexpr int kAttrTaskLen = 128;
+// most task_len entries (64, 128 or 256: 2, 4 or 8 per lane), one warp per
+// task. A row of one task writes its slot directly; the tasks of a longer row
+// write partial sums that a second kernel adds in task order, so results do
+// not depend on scheduling (they do depend on task_len, which sets how a row's
+// terms are grouped). Built once per CSR layout (one host synchronisation),
+// replayed every epoch.
+constexpr int kAttrTaskLen = 128;  // the default task length
 struct AttrTasks {
   DevBuf tasks, off, cnt, longs, nlong_dev, part, scan_tmp;
   int64_t ntasks = 0, nlong = 0, n = 0;
   int D = 0;
+  int task_len = kAttrTaskLen;
   uint64_t gen = ~0ull;  // layout generation the tasks were built for
 };
 
 template <class T>
-void build_attr_tasks(AttrTasks& at, int D, const uint64_t* rows, int64_t n, cudaStream_t s);
+void build_attr_tasks(AttrTasks& at, int D, const uint64_t* rows, int64_t n, cudaStream_t s,
+                      int task_len = kAttrTaskLen);
 
 template <class T>
 void launch_attractive_tasks(const AttrTasks& at, const uint32_t* cols, const T* vals, const T* y, T* pos,

@@ -6,6 +6,7 @@
 
 #include <atomic>
 #include <cstdint>
+#include <string>
 #include <utility>
 #include <vector>
 
@@ -105,9 +106,18 @@ inline int device_sm_count() {
   return v;
 }
 
+// A grid of per_sm blocks for every SM of the current device, at most cap
+// (for grid-stride kernels and for reductions whose partials are sized by cap).
+inline int sm_grid(int per_sm, int cap) {
+  const int g = per_sm * device_sm_count();
+  return g < cap ? g : cap;
+}
+
 // write_csv of a host embedding (io.cu); returns a status, the message in
 // bhtsne_io_last_error.
 int write_csv_file(const void* embedding, int64_t n, int32_t embed_dim, int dtype, const char* path);
+// Sets the message of a host-only call (read by bhtsne_io_last_error).
+void set_host_error(const std::string& msg);
 
 // Keeps the freed memory of the device's default pool cached (no release
 // back to the driver at synchronisations), once per device.

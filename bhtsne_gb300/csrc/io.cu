@@ -291,6 +291,8 @@ int bhtsne_write_csv(const void* embedding, int64_t n, int32_t embed_dim, int dt
 }  // extern "C"
 
 namespace bhg {
+void set_host_error(const std::string& msg) { g_io_error = msg; }
+
 int write_csv_file(const void* embedding, int64_t n, int32_t embed_dim, int dtype, const char* path) {
   return bhtsne_write_csv(embedding, n, embed_dim, dtype, path);
 }

@@ -672,7 +672,7 @@ int64_t knn_euclidean(const T* X, int64_t n, int dim, int k, uint32_t* out_idx, 
   const size_t smem = ((size_t)dim * QB + DK * CB + QB * (CB + 1) + (size_t)QB * C * 2 + 2 * QB) * 4;
   const unsigned grid = (unsigned)ceil_div(n, QB);
   const double simt_coef = (4.0 * dim + 16.0) / 16777216.0;
-  if (C == 128 && use_tensor_cores()) {
+  if (C == 128 && (ws.pass == 0 || (ws.pass < 0 && use_tensor_cores()))) {
     knn_tc_candidates(Xf, n, dim, norms, nullptr, nullptr, nullptr, ceil_div(n, 128), cand, thr, ws.tc, s);
     knn_rerank_kernel<T, 128><<<(unsigned)ceil_div(n, 4), 128, 0, s>>>(X, n, dim, k, cand, thr, norms, max_bits, out_idx,
                                                                        out_dist, fails, fail_count,
@@ -775,7 +775,7 @@ int64_t knn_euclidean_segmented(const T* X, int64_t total, int dim, int k, const
   uint32_t* fails = static_cast<uint32_t*>(ws.fails.ensure((size_t)total * sizeof(uint32_t)));
   const size_t smem = ((size_t)dim * QB + DK * CB + QB * (CB + 1) + (size_t)QB * C * 2 + 2 * QB) * 4;
   const double simt_coef = (4.0 * dim + 16.0) / 16777216.0;
-  if (C == 128 && use_tensor_cores()) {
+  if (C == 128 && (ws.pass == 0 || (ws.pass < 0 && use_tensor_cores()))) {
     // 128-query blocks per set, largest sets first
     std::vector<int64_t> tq0;
     std::vector<int32_t> tbj;

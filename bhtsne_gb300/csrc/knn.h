@@ -12,6 +12,9 @@ struct KnnWorkspace {
   DevBuf xf, norms, cand, thr, fails, counters, blk, tc_blk;
   KnnTcScratch tc;
   int64_t last_fallback_rows = 0;
+  // candidate pass: -1 the default (tensor cores unless BHTSNE_KNN_SIMT is
+  // set), 0 tensor cores, 1 CUDA cores; both give the same neighbours
+  int pass = -1;
   void release() {
     xf.release();
     norms.release();

@@ -422,7 +422,7 @@ void knn_tc_candidates(const float* X, int64_t n, int dim, const float* norms, c
   const float* Xp = X;
   if (dim_pad != dim) {
     float* pad = static_cast<float*>(ws.xhi.ensure((size_t)n * dim_pad * 4));
-    pad_rows_kernel<<<(unsigned)std::min<int64_t>(ceil_div(n * dim_pad, 256), 8 * 152), 256, 0, s>>>(X, n, dim, dim_pad,
+    pad_rows_kernel<<<(unsigned)std::min<int64_t>(ceil_div(n * dim_pad, 256), sm_grid(8, 8192)), 256, 0, s>>>(X, n, dim, dim_pad,
                                                                                                     pad);
     BHG_LAUNCH_CHECK();
     Xp = pad;

@@ -162,6 +162,12 @@ extern "C" {
                          neg: *const c_void, uy: *mut c_void, gains: *mut c_void, n: i64, learning_rate: f64,
                          momentum: f64, inverse_z: f64) -> c_int;
 
+    // ---- autotuning
+    pub fn bhtsne_tune(ctx: *mut bhtsne_ctx, dtype: c_int, embed_dim: i32, n: i64, k: i32, dim: i32) -> c_int;
+    pub fn bhtsne_tune_config(dtype: c_int, embed_dim: i32, n: i64, json: *mut c_char, len: i64) -> c_int;
+    pub fn bhtsne_tune_load(path: *const c_char) -> c_int;
+    pub fn bhtsne_tune_save(path: *const c_char) -> c_int;
+
     // ---- CSV input and output (src/csv.rs:31-118); host only
     pub fn bhtsne_load_csv(path: *const c_char, has_headers: i32, skip: *const i64, n_skip: i64, dtype: c_int,
                            out: *mut c_void, count: *mut i64, records: *mut i64) -> c_int;

@@ -196,6 +196,28 @@ int bhtsne_bh_repulsion_noalloc(const float* y, int64_t n, double theta, float* 
 int bhtsne_update(bhtsne_ctx* ctx, int dtype, int32_t embed_dim, void* y, const void* pos, const void* neg, void* uy,
                   void* gains, int64_t n, double learning_rate, double momentum, double inverse_z);
 
+/* ---- autotuning (no reference counterpart) --------------------------------- */
+/* Times the candidates of three launch-shape knobs on synthetic data of the
+ * given shape (n points in embed_dim dimensions, k neighbours per row; dim > 0
+ * also tunes the kNN candidate pass on a sample of dim-dimensional points):
+ * the attractive pass's task length (64, 128, 256 entries), the Barnes-Hut
+ * traversal's block size (128, 256, 512 threads) and the kNN candidate pass
+ * (tensor cores or CUDA cores). The fastest of each is kept for this GPU, the
+ * value type, embed_dim and the N bucket floor(log2 n); fits that start later
+ * use them. The traversal block size and the kNN pass do not change results;
+ * the task length changes the grouping of each row's attractive terms, so a
+ * fit's forces move by rounding. The timings are left in
+ * bhtsne_ctx_last_error. When BHTSNE_TUNE_FILE is set, contexts read that
+ * JSON table when the first one is created, and bhtsne_tune rewrites it. */
+int bhtsne_tune(bhtsne_ctx* ctx, int dtype, int32_t embed_dim, int64_t n, int32_t k, int32_t dim);
+/* The configuration a fit of (dtype, embed_dim, n) on the current device would
+ * use, as JSON: {"key": ..., "knobs": {...}}. Host only. */
+int bhtsne_tune_config(int dtype, int32_t embed_dim, int64_t n, char* json, int64_t len);
+/* Adds the entries of a tuning table file / writes the table. Host only;
+ * errors from bhtsne_io_last_error. */
+int bhtsne_tune_load(const char* path);
+int bhtsne_tune_save(const char* path);
+
 /* ---- CSV input and output (host only; no GPU needed) ----------------------- */
 /* load_csv (src/csv.rs:61-118) for numeric data: the fields of every record,
  * except the columns listed in skip (n_skip of them), parsed as the dtype's
