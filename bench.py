@@ -3,7 +3,7 @@
 Workload (the 1M-point configuration): N = 1,000,000 points, input dim 128,
 float32, a 100-cluster mixture with Student-t (nu = 5) radial spread and
 centres ~ N(0, 8^2 I); perplexity 30 (k = 90); Barnes-Hut theta 0.5 into 2-D.
-Both arms start from the same seeded N(0, 1e-4) embedding and time the same
+Both arms start from the same seeded normal embedding (sigma 1e-4) and time the same
 window of the fit: --steps epochs after --burn-in (250, the end of the early
 exaggeration) and --warmup epochs, i.e. epochs 255-274 by default. A "step"
 is one optimisation epoch (tree build, traversal, attractive pass, fused
@@ -57,9 +57,10 @@ INIT_SEED = 42
 
 
 def initial_embedding(n, D=2, seed=INIT_SEED):
-    """Seeded N(0, 1e-4) start, the distribution of the reference's
-    random_init (src/tsne/mod.rs:142-147); both arms start from it."""
-    return np.random.default_rng(seed).normal(0.0, 1e-2, size=(n, D)).astype(np.float32)
+    """Seeded normal start with mean 0 and standard deviation 1e-4, the
+    distribution of the reference's random_init (src/tsne/mod.rs:142-147,
+    rand_distr Normal::new(0.0, 1e-4)); both arms start from it."""
+    return np.random.default_rng(seed).normal(0.0, 1e-4, size=(n, D)).astype(np.float32)
 
 
 def workload_config(args, ws):
@@ -67,7 +68,7 @@ def workload_config(args, ws):
     first = args.burn_in + args.warmup
     return {"workload": "bh2d_1M_d128", "n_points": args.n, "input_dim": 128, "clusters": 100,
             "perplexity": 30.0, "k": 90, "theta": 0.5, "embed_dim": 2,
-            "window": "epochs %d-%d of one fit from a seeded N(0, 1e-4) start" % (first, first + args.steps - 1),
+            "window": "epochs %d-%d of one fit from a seeded normal start (sigma 1e-4)" % (first, first + args.steps - 1),
             "l2": "inputs larger than L2 (CSR P of about 1.4 GB per epoch)",
             "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"}
 

@@ -425,13 +425,21 @@ __global__ void conv1d_direct_kernel(double* __restrict__ tab, const FitParams<T
 // two at a time (radix 2^2: four elements through both stages in registers),
 // where consecutive lanes touch consecutive elements; stages of span <= 32 run
 // in registers across a warp with shuffles (lane l holds element 32 g + l).
-// tw holds W_cap^k for k < cap / 2 and tws = cap / L.
+// tw holds the twiddles stage by stage: W_S^k at tw[S / 2 - 1 + k] for every
+// power of two S <= cap and k < S / 2, so the butterflies of a stage, whose
+// positions are consecutive across lanes, read consecutive entries (a strided
+// view of one W_cap table costs one L1 wavefront per lane at the short spans).
+
+template <class T2>
+__device__ __forceinline__ T2 twid(const T2* __restrict__ tw, int S, int k) {
+  return tw[(S >> 1) - 1 + k];
+}
 
 // DIF stages of spans L .. 2^(small + 1) of `nsub` consecutive rows of
 // length L held back to back, ending with a barrier.
 template <class T2>
 __device__ __forceinline__ void dif_smem_stages(T2* s, int L, int log2L, int small, const T2* __restrict__ tw,
-                                                int tws, int nsub) {
+                                                int nsub) {
   int lg = log2L;
   if (((log2L - small) & 1) != 0) {
     // one radix-2 stage of span L
@@ -442,7 +450,7 @@ __device__ __forceinline__ void dif_smem_stages(T2* s, int L, int log2L, int sma
       T2* r = s + (b0 >> (log2L - 1)) * L;
       const T2 a = r[b], c = r[b + half];
       r[b] = cadd(a, c);
-      r[b + half] = cmul(csub(a, c), tw[b * tws]);
+      r[b + half] = cmul(csub(a, c), twid(tw, L, b));
     }
     __syncthreads();
     lg -= 1;
@@ -450,17 +458,16 @@ __device__ __forceinline__ void dif_smem_stages(T2* s, int L, int log2L, int sma
   for (; lg - 1 > small; lg -= 2) {
     // stages of spans S = 2^lg and S/2: quarter q = S/4
     const int q = 1 << (lg - 2);
-    const int st1 = (L >> lg) * tws, st2 = (L >> (lg - 1)) * tws;
 #pragma unroll 2
     for (int b0 = threadIdx.x; b0 < nsub * (L >> 2); b0 += blockDim.x) {
       const int b = b0 & ((L >> 2) - 1);
       const int pos = b & (q - 1);
       const int i = (b0 >> (log2L - 2)) * L + ((b >> (lg - 2)) << lg) + pos;
-      const T2 wa = tw[pos * st1];  // W_S^pos
+      const T2 wa = twid(tw, 1 << lg, pos);  // W_S^pos
       T2 wb;                         // W_S^(pos+q) = W_S^pos * (-i)
       wb.x = wa.y;
       wb.y = -wa.x;
-      const T2 wc = tw[pos * st2];  // W_(S/2)^pos
+      const T2 wc = twid(tw, 1 << (lg - 1), pos);  // W_(S/2)^pos
       const T2 x0 = s[i], x1 = s[i + q], x2 = s[i + 2 * q], x3 = s[i + 3 * q];
       const T2 y0 = cadd(x0, x2), y2 = cmul(csub(x0, x2), wa);
       const T2 y1 = cadd(x1, x3), y3 = cmul(csub(x1, x3), wb);
@@ -480,18 +487,17 @@ __device__ __forceinline__ void dif_smem_stages(T2* s, int L, int log2L, int sma
 // quarter turn.
 template <class T2>
 __device__ __forceinline__ void dit_smem_stages(T2* s, int L, int log2L, int small, const T2* __restrict__ tw,
-                                                int tws, int nsub) {
+                                                int nsub) {
   int lg = small + 1;
   for (; lg + 1 <= log2L; lg += 2) {
     const int h = 1 << (lg - 1);
-    const int st1 = (L >> lg) * tws, st2 = (L >> (lg + 1)) * tws;
 #pragma unroll 2
     for (int b0 = threadIdx.x; b0 < nsub * (L >> 2); b0 += blockDim.x) {
       const int b = b0 & ((L >> 2) - 1);
       const int pos = b & (h - 1);
       const int i = (b0 >> (log2L - 2)) * L + ((b >> (lg - 1)) << (lg + 1)) + pos;
-      T2 w1 = tw[pos * st1];
-      T2 w2 = tw[pos * st2];
+      T2 w1 = twid(tw, 1 << lg, pos);
+      T2 w2 = twid(tw, 1 << (lg + 1), pos);
       w1.y = -w1.y;
       w2.y = -w2.y;
       T2 w3;  // conjugate quarter turn: W_4^-1 = +i
@@ -515,14 +521,13 @@ __device__ __forceinline__ void dit_smem_stages(T2* s, int L, int log2L, int sma
   }
   for (; lg <= log2L; ++lg) {
     const int half = 1 << (lg - 1);
-    const int tstep = (L >> lg) * tws;
 #pragma unroll 2
     for (int b0 = threadIdx.x; b0 < nsub * (L >> 1); b0 += blockDim.x) {
       const int b = b0 & ((L >> 1) - 1);
       const int pos = b & (half - 1);
       const int i = (b0 >> (log2L - 1)) * L + ((b >> (lg - 1)) << lg) + pos;
       const int j = i + half;
-      T2 w = tw[pos * tstep];
+      T2 w = twid(tw, 1 << lg, pos);
       w.y = -w.y;
       const T2 u = s[i];
       const T2 v = cmul(s[j], w);
@@ -580,13 +585,12 @@ __device__ __forceinline__ void r3_dit_stage(T2* s, int M, const T2* __restrict_
 // This lane's forward twiddle for each register stage k (span 2^k):
 // W_(2^k)^(lane mod 2^(k-1)).
 template <class T2>
-__device__ __forceinline__ void lane_twiddles(int lane, int L, int small, const T2* __restrict__ tw, int tws,
-                                              T2 (&w)[5]) {
+__device__ __forceinline__ void lane_twiddles(int lane, int small, const T2* __restrict__ tw, T2 (&w)[5]) {
 #pragma unroll
   for (int k = 1; k <= 5; ++k) {
     w[k - 1].x = 0;
     w[k - 1].y = 0;
-    if (k <= small) w[k - 1] = tw[(lane & ((1 << (k - 1)) - 1)) * (L >> k) * tws];
+    if (k <= small) w[k - 1] = twid(tw, 1 << k, lane & ((1 << (k - 1)) - 1));
   }
 }
 
@@ -712,7 +716,7 @@ constexpr int kFftThreads = 512;
 template <class T>
 struct FftRow {
   typedef typename Cx<T>::type T2;
-  int L, M, nsub, log2M, small, G, ngroups, tws, tws3, lane, warp, nw;
+  int L, M, nsub, log2M, small, G, ngroups, tws3, lane, warp, nw;
   bool lane_ok, wide;
   __device__ FftRow(int L_, int cap_L) : L(L_) {
     nsub = (L % 3 == 0) ? 3 : 1;
@@ -723,17 +727,29 @@ struct FftRow {
     small = wide ? 7 : (log2M < 5 ? log2M : 5);
     G = 1 << small;
     ngroups = L >> small;
-    tws = cap_L / M;
     tws3 = nsub == 3 ? (3 * (cap_L >> 2)) / L : 0;
     lane = threadIdx.x & 31;
     warp = threadIdx.x >> 5;
     nw = blockDim.x >> 5;
     lane_ok = wide || lane < G;
   }
+  // The frequency a forward transform leaves at position p, and the position
+  // of frequency f: sub-row k of a 3 M row holds frequencies 3 m + k at the
+  // bit-reversed positions of m; a power-of-two row is bit-reversed.
+  __device__ int freq_at(int p) const {
+    const int k = nsub == 3 ? p / M : 0;
+    const int m = (int)(__brev((unsigned)(p - k * M)) >> (32 - log2M));
+    return nsub == 3 ? 3 * m + k : m;
+  }
+  __device__ int pos_of(int f) const {
+    const int k = nsub == 3 ? f % 3 : 0;
+    const int m = nsub == 3 ? f / 3 : f;
+    return k * M + (int)(__brev((unsigned)m) >> (32 - log2M));
+  }
   // W_128^lane, W_64^lane of the sub-row length (wide mode)
   __device__ void wide_twiddles(const T2* __restrict__ tw, T2* w64, T2* w128) const {
-    *w64 = tw[lane * (M >> 6) * tws];
-    *w128 = tw[lane * (M >> 7) * tws];
+    *w64 = twid(tw, 64, lane);
+    *w128 = twid(tw, 128, lane);
   }
 };
 
@@ -757,7 +773,7 @@ __global__ void __launch_bounds__(kFftThreads, sizeof(T) == 4 ? 3 : 1) fft_rows_
   T2* s = reinterpret_cast<T2*>(smem_raw);
   T2* d = data + (int64_t)blockIdx.x * L;
   T2 w[5];
-  lane_twiddles(r.lane, r.M, r.wide ? 5 : r.small, tw, r.tws, w);
+  lane_twiddles(r.lane, r.wide ? 5 : r.small, tw, w);
   T2 w64, w128;
   if (r.wide) r.wide_twiddles(tw, &w64, &w128);
   T2 zero;
@@ -767,7 +783,7 @@ __global__ void __launch_bounds__(kFftThreads, sizeof(T) == 4 ? 3 : 1) fft_rows_
   if (!fft_fill_row<T>(s, d, inverse ? 0 : src, (int)blockIdx.x, L, D, prm, &load_bar, fault)) return;
   if (!inverse) {
     if (r.nsub == 3) r3_dif_stage<T2, T>(s, r.M, tw3, r.tws3);
-    dif_smem_stages(s, r.M, r.log2M, r.small, tw, r.tws, r.nsub);
+    dif_smem_stages(s, r.M, r.log2M, r.small, tw, r.nsub);
     // khat_out: the real part scaled by 1 / L^D (the kernel spectrum)
     const T inv_total = T(1) / (T)(D == 1 ? (double)L : (double)L * (double)L);
     T* kr = khat_out ? khat_out + (int64_t)blockIdx.x * L : nullptr;
@@ -807,9 +823,11 @@ __global__ void __launch_bounds__(kFftThreads, sizeof(T) == 4 ? 3 : 1) fft_rows_
     if (r.lane_ok) s[g * r.G + r.lane] = x;
   }
   __syncthreads();
-  dit_smem_stages(s, r.M, r.log2M, r.small, tw, r.tws, r.nsub);
+  dit_smem_stages(s, r.M, r.log2M, r.small, tw, r.nsub);
   if (r.nsub == 3) r3_dit_stage<T2, T>(s, r.M, tw3, r.tws3);
-  for (int i = threadIdx.x; i < L; i += blockDim.x) d[i] = s[i];
+  // the potentials of the node rows: only their first `nodes` columns are read
+  const int keep = rows_sel == 1 ? prm->nodes : L;
+  for (int i = threadIdx.x; i < keep; i += blockDim.x) d[i] = s[i];
 }
 
 // The kernel spectrum in 2-D from real transforms packed two to a complex
@@ -820,10 +838,13 @@ __global__ void __launch_bounds__(kFftThreads, sizeof(T) == 4 ? 3 : 1) fft_rows_
 // equals row r).
 //  pass 0: block b transforms kernel rows 2b and 2b + 1 (<= L/2) and writes
 //          the two real rows of `out` (row stride L);
-//  pass 1: block b takes rows 2b and 2b + 1 of the transposed table `in` (row
-//          p holds column p for rows 0 .. L/2, stride L), extends each evenly
-//          to length L, transforms the pair and writes rows 2b and 2b + 1 of
-//          the spectrum times `scale` (1 / L^2).
+//  pass 1: block b takes the rows of the transposed table `in` (row p holds
+//          column p for rows 0 .. L/2, stride L) at the positions of the
+//          frequencies 2b and 2b + 1 (<= L/2), extends each evenly to length L,
+//          transforms the pair and writes those rows of the spectrum times
+//          `scale` (1 / L^2). Rows of frequencies above L/2 equal the rows of
+//          L minus them and are not written: the convolution pass reads the
+//          mirrored row (kspec_row).
 // The spectrum is symmetric, so its rows and columns need no distinction.
 template <class T>
 __global__ void __launch_bounds__(kFftThreads, sizeof(T) == 4 ? 3 : 1) kspec_kernel(int pass, const FitParams<T>* __restrict__ prm,
@@ -834,13 +855,16 @@ __global__ void __launch_bounds__(kFftThreads, sizeof(T) == 4 ? 3 : 1) kspec_ker
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int L = prm->L, half = L / 2;
   const int b = (int)blockIdx.x;
-  const int r1 = 2 * b, r2 = 2 * b + 1;
-  if (pass == 0 ? r1 > half : r1 >= L) return;
-  const bool two = pass == 0 ? r2 <= half : true;
   const FftRow<T> r(L, cap_L);
+  // pass 0: kernel rows (lags); pass 1: table rows at the frequencies' positions
+  const int f1 = 2 * b, f2 = 2 * b + 1;
+  if (f1 > half) return;
+  const bool two = f2 <= half;
+  const int r1 = pass == 0 ? f1 : r.pos_of(f1);
+  const int r2 = pass == 0 ? f2 : (two ? r.pos_of(f2) : r1);
   T2* s = reinterpret_cast<T2*>(smem_raw);
   T2 w[5];
-  lane_twiddles(r.lane, r.M, r.wide ? 5 : r.small, tw, r.tws, w);
+  lane_twiddles(r.lane, r.wide ? 5 : r.small, tw, w);
   T2 w64, w128;
   if (r.wide) r.wide_twiddles(tw, &w64, &w128);
   T2 zero;
@@ -866,7 +890,7 @@ __global__ void __launch_bounds__(kFftThreads, sizeof(T) == 4 ? 3 : 1) kspec_ker
     }
   } else {
     const T* a = in + (int64_t)r1 * L;
-    const T* c = in + (int64_t)r2 * L;
+    const T* c = in + (int64_t)r2 * L;  // r1 again when there is one row
     for (int i = threadIdx.x; i < L; i += blockDim.x) {
       const int e = i <= half ? i : L - i;
       T2 v;
@@ -877,7 +901,7 @@ __global__ void __launch_bounds__(kFftThreads, sizeof(T) == 4 ? 3 : 1) kspec_ker
   }
   __syncthreads();
   if (r.nsub == 3) r3_dif_stage<T2, T>(s, r.M, tw3, r.tws3);
-  dif_smem_stages(s, r.M, r.log2M, r.small, tw, r.tws, r.nsub);
+  dif_smem_stages(s, r.M, r.log2M, r.small, tw, r.nsub);
   const T scale = pass == 0 ? T(1) : T(1) / (T)((double)L * (double)L);
   T* o1 = out + (int64_t)r1 * L;
   T* o2 = out + (int64_t)r2 * L;
@@ -947,9 +971,16 @@ __global__ void __launch_bounds__(kFftThreads, sizeof(T) == 4 ? 3 : 1) fft_conv_
   const FftRow<T> r(L, cap_L);
   T2* s = reinterpret_cast<T2*>(smem_raw);
   T2* d = data + (int64_t)blockIdx.x * L;
-  const T* kr = khat + (int64_t)blockIdx.x * L;
+  // the spectrum row of this row's frequency (2-D: rows of frequencies above
+  // L/2 are the rows of L minus them, see kspec_kernel)
+  int krow = (int)blockIdx.x;
+  if (rows_sel == 0) {
+    const int f = r.freq_at(krow);
+    if (f > L / 2) krow = r.pos_of(L - f);
+  }
+  const T* kr = khat + (int64_t)krow * L;
   T2 w[5];
-  lane_twiddles(r.lane, r.M, r.wide ? 5 : r.small, tw, r.tws, w);
+  lane_twiddles(r.lane, r.wide ? 5 : r.small, tw, w);
   T2 w64, w128;
   if (r.wide) r.wide_twiddles(tw, &w64, &w128);
   T2 zero;
@@ -957,7 +988,7 @@ __global__ void __launch_bounds__(kFftThreads, sizeof(T) == 4 ? 3 : 1) fft_conv_
   zero.y = T(0);
   if (!fft_fill_row<T>(s, d, src, (int)blockIdx.x, L, rows_sel == 2 ? 1 : 2, prm, &load_bar, fault)) return;
   if (r.nsub == 3) r3_dif_stage<T2, T>(s, r.M, tw3, r.tws3);
-  dif_smem_stages(s, r.M, r.log2M, r.small, tw, r.tws, r.nsub);
+  dif_smem_stages(s, r.M, r.log2M, r.small, tw, r.nsub);
   for (int g = r.warp; g < r.ngroups; g += r.nw) {
     if (r.wide) {
       T2 x[4];
@@ -984,7 +1015,7 @@ __global__ void __launch_bounds__(kFftThreads, sizeof(T) == 4 ? 3 : 1) fft_conv_
     if (r.lane_ok) s[e] = x;
   }
   __syncthreads();
-  dit_smem_stages(s, r.M, r.log2M, r.small, tw, r.tws, r.nsub);
+  dit_smem_stages(s, r.M, r.log2M, r.small, tw, r.nsub);
   if (r.nsub == 3) r3_dit_stage<T2, T>(s, r.M, tw3, r.tws3);
   for (int i = threadIdx.x; i < keep; i += blockDim.x) d[i] = s[i];
 }
@@ -1145,12 +1176,14 @@ const typename FitWorkspace<T>::T2* FitWorkspace<T>::twiddles3(int cap_L, cudaSt
 template <class T>
 const typename FitWorkspace<T>::T2* FitWorkspace<T>::twiddles(int L, cudaStream_t s) {
   if (tw_len != L) {
-    std::vector<T2> h(L / 2 > 0 ? L / 2 : 1);
-    for (int k = 0; k < L / 2; ++k) {
-      const double ang = -2.0 * M_PI * (double)k / (double)L;
-      h[k].x = (T)std::cos(ang);
-      h[k].y = (T)std::sin(ang);
-    }
+    // W_S^k = exp(-2 pi i k / S) at S / 2 - 1 + k, for S = 2 .. L
+    std::vector<T2> h(L > 1 ? L - 1 : 1);
+    for (int S = 2; S <= L; S <<= 1)
+      for (int k = 0; k < S / 2; ++k) {
+        const double ang = -2.0 * M_PI * (double)k / (double)S;
+        h[S / 2 - 1 + k].x = (T)std::cos(ang);
+        h[S / 2 - 1 + k].y = (T)std::sin(ang);
+      }
     tw.ensure(h.size() * sizeof(T2));
     // on the stream of the FFTs that read it (the legacy stream would not
     // order against a non-blocking one); the pageable source is staged
@@ -1269,8 +1302,8 @@ void fit_repulsion_cap(FitWorkspace<T>& ws, int D, const T* y, int64_t n, const 
     dim3 tb(32, 8), tg((unsigned)ceil_div(cap, 32), (unsigned)ceil_div(cap / 2 + 1, 32));
     transpose_half_kernel<T><<<tg, tb, 0, s>>>(a, dp, at);
     BHG_LAUNCH_CHECK();
-    kspec_kernel<T><<<(unsigned)(cap / 2), threads, smem, s>>>(1, dp, ws.twiddles(cap, s), ws.twiddles3(cap, s), cap,
-                                                             at, khat);
+    kspec_kernel<T><<<(unsigned)(cap / 4 + 1), threads, smem, s>>>(1, dp, ws.twiddles(cap, s), ws.twiddles3(cap, s),
+                                                                 cap, at, khat);
     BHG_LAUNCH_CHECK();
   }
 
