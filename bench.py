@@ -682,7 +682,8 @@ def run_serving(args, ctx):
     E = args.serve_epochs
     rng = np.random.default_rng(77)
     arrivals = np.cumsum(rng.exponential(1.0 / args.serve_rate, size=len(reqs)))
-    sv = bg.Server(ctx=ctx, perplexity=30.0, theta=0.5, fit_workers=args.serve_fit_workers)
+    budget = int(args.serve_budget_gb * 1e9) if args.serve_budget_gb > 0 else 0
+    sv = bg.Server(ctx=ctx, perplexity=30.0, theta=0.5, fit_workers=args.serve_fit_workers, hbm_budget_bytes=budget)
     ids = [None] * len(reqs)
     w0 = time.perf_counter()
     for i, (X, method, seed) in enumerate(reqs):
@@ -725,7 +726,8 @@ def run_serving(args, ctx):
         "latency_s": {"p50": round(float(np.percentile(lat_s, 50)), 3), "p99": round(float(np.percentile(lat_s, 99)), 3),
                       "plain_p50": round(float(np.percentile(lat_p, 50)), 3),
                       "plain_p99": round(float(np.percentile(lat_p, 99)), 3)},
-        "peak_admitted_bytes": st["peak_bytes"], "mean_batch_points": round(st["mean_batch_points"], 1),
+        "peak_admitted_bytes": st["peak_bytes"], "budget_bytes": budget if budget else "90% of free device memory",
+        "mean_batch_points": round(st["mean_batch_points"], 1),
         "fit_workers": args.serve_fit_workers,
         "server_busy_s": {k: round(st[k], 3) for k in ("round_s", "repack_s", "prepare_s", "fit_worker_s")},
         "kl_gap": {"mean": round(float(gap.mean()), 5), "p99": round(float(np.percentile(gap, 99)), 5),
@@ -864,6 +866,9 @@ def main():
     ap.add_argument("--serve-epochs", type=int, default=750)
     ap.add_argument("--serve-rate", type=float, default=64.0, help="Poisson arrivals per second")
     ap.add_argument("--serve-fit-workers", type=int, default=8, help="server streams for FIt-SNE requests")
+    ap.add_argument("--serve-budget-gb", type=float, default=0.0,
+                    help="server admission budget in GB (0: 90%% of free device memory)")
+    ap.add_argument("--serve-only", action="store_true", help="run only the serving comparison")
     ap.add_argument("--knn-only", action="store_true", help="time only the kNN of the workload at --n points")
     ap.add_argument("--fft-only", action="store_true",
                     help="time only the FIt-SNE repulsion of --n points at the largest grid")
@@ -874,6 +879,10 @@ def main():
         return run_fft_only(args)
     if args.knn_only:
         run_knn_only(args)
+        return
+    if args.serve_only:
+        import bhtsne_gb300 as bg
+        print(json.dumps({"serving": run_serving(args, bg.Context(0))}))
         return
     if args.warmup < 3:
         args.warmup = 3

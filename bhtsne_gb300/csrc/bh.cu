@@ -616,15 +616,14 @@ __global__ void __launch_bounds__(kTraverseMax) bh_traverse_kernel(const T* __re
 #pragma unroll
     for (int a = 0; a < D; ++a) f[a] = T(0);
     T q = T(0);
-    // 2-D single precision: the displacement, its squares and the force
-    // update in paired f32x2 instructions (each half the scalar operation, so
-    // the same values as the per-axis code)
+    // 2-D single precision: the displacement and its squares in paired
+    // f32x2 instructions (each half the scalar operation, so the same values
+    // as the per-axis code). The force update stays scalar: a paired multiply
+    // feeding a paired add was measured to round as one fused multiply-add
+    // despite the .rn modifiers, which the reference's f += m * d never does.
     constexpr bool kPair = D == 2 && std::is_same<T, float>::value;
-    F32x2 q2 = {0ull}, f2 = {0ull};
-    if constexpr (kPair) {
-      q2 = f2_make((float)qv[0], (float)qv[D - 1]);
-      f2 = f2_make(0.0f, 0.0f);
-    }
+    F32x2 q2 = {0ull};
+    if constexpr (kPair) q2 = f2_make((float)qv[0], (float)qv[D - 1]);
     // Software-pipelined walk: both possible successors of the current node
     // (i + 1 if it is opened, its skip target if it is summarised) are loaded
     // before the decision, so the next visit never waits on a dependent load.
@@ -669,15 +668,12 @@ __global__ void __launch_bounds__(kTraverseMax) bh_traverse_kernel(const T* __re
       q += m;
       m = m * inv;
       if constexpr (kPair) {
-        f2 = f2_add(f2, f2_mul(f2_make((float)m, (float)m), d2));
+        f[0] += m * (T)f2_lo(d2);
+        f[D - 1] += m * (T)f2_hi(d2);
       } else {
 #pragma unroll
         for (int a = 0; a < D; ++a) f[a] += m * disp[a];
       }
-    }
-    if constexpr (kPair) {
-      f[0] = (T)f2_lo(f2);
-      f[D - 1] = (T)f2_hi(f2);
     }
 #pragma unroll
     for (int a = 0; a < D; ++a) neg[pi * D + a] = f[a];

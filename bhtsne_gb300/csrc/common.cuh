@@ -64,8 +64,10 @@ __device__ __forceinline__ double rcp_rn(double x) { return __drcp_rn(x); }
 
 // Two single-precision values in one 64-bit register pair, for the paired
 // f32x2 instructions of sm_100 and later: each lane of a paired add, subtract
-// or multiply is the scalar IEEE operation rounded to nearest, so results are
-// those of the two scalar operations (no contraction into a fused multiply-add).
+// or multiply is the scalar IEEE operation rounded to nearest. A paired
+// multiply whose result feeds a paired add can still be fused into one
+// multiply-add by the assembler (measured: f += m * d accumulated with
+// mul.rn.f32x2 / add.rn.f32x2 rounds like fma), so no such chain is written.
 struct F32x2 {
   unsigned long long v;
 };
@@ -85,11 +87,6 @@ __device__ __forceinline__ float f2_hi(F32x2 x) {
   asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(x.v));
   (void)a;
   return b;
-}
-__device__ __forceinline__ F32x2 f2_add(F32x2 x, F32x2 y) {
-  F32x2 r;
-  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r.v) : "l"(x.v), "l"(y.v));
-  return r;
 }
 __device__ __forceinline__ F32x2 f2_sub(F32x2 x, F32x2 y) {
   F32x2 r;

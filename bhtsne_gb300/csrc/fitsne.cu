@@ -54,11 +54,21 @@ struct Cx<double> {
   typedef double2 type;
 };
 
-template <class T2>
-__device__ __forceinline__ T2 cmul(T2 a, T2 b) {
-  T2 r;
-  r.x = a.x * b.x - a.y * b.y;
-  r.y = a.x * b.y + a.y * b.x;
+// Complex arithmetic of the transforms. The FFT is this library's own (the
+// reference uses rustfft), so its rounding is free: the product uses fused
+// multiply-adds, and f32 sums and differences use the paired f32x2
+// instructions (one instruction for both parts). The spread, the kernel
+// values and the gather keep the reference's arithmetic.
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+  float2 r;
+  r.x = __fmaf_rn(a.x, b.x, -__fmul_rn(a.y, b.y));
+  r.y = __fmaf_rn(a.x, b.y, __fmul_rn(a.y, b.x));
+  return r;
+}
+__device__ __forceinline__ double2 cmul(double2 a, double2 b) {
+  double2 r;
+  r.x = __fma_rn(a.x, b.x, -__dmul_rn(a.y, b.y));
+  r.y = __fma_rn(a.x, b.y, __dmul_rn(a.y, b.x));
   return r;
 }
 
@@ -159,7 +169,7 @@ __device__ __forceinline__ void locate(T v, const FitParams<T>& p, const Lagrang
     if (id > last) id = last;
   }
   *box = (int)id;
-  const T local = offset - (T)(double)id;
+  const T local = offset - (T)(int)id;  // id < 1000: exact either way
   lb.weights(local, w);
 }
 
@@ -261,14 +271,28 @@ __global__ void spread_kernel(const T* __restrict__ y, int64_t n, const FitParam
 
 
 
-template <class T2>
-__device__ __forceinline__ T2 cadd(T2 a, T2 b) {
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) {
+  float2 r;
+  asm("{\n\t.reg .b64 pa, pb, pr;\n\tmov.b64 pa, {%2, %3};\n\tmov.b64 pb, {%4, %5};\n\t"
+      "add.rn.f32x2 pr, pa, pb;\n\tmov.b64 {%0, %1}, pr;\n\t}"
+      : "=f"(r.x), "=f"(r.y)
+      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+  return r;
+}
+__device__ __forceinline__ float2 csub(float2 a, float2 b) {
+  float2 r;
+  asm("{\n\t.reg .b64 pa, pb, pr;\n\tmov.b64 pa, {%2, %3};\n\tmov.b64 pb, {%4, %5};\n\t"
+      "sub.rn.f32x2 pr, pa, pb;\n\tmov.b64 {%0, %1}, pr;\n\t}"
+      : "=f"(r.x), "=f"(r.y)
+      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+  return r;
+}
+__device__ __forceinline__ double2 cadd(double2 a, double2 b) {
   a.x += b.x;
   a.y += b.y;
   return a;
 }
-template <class T2>
-__device__ __forceinline__ T2 csub(T2 a, T2 b) {
+__device__ __forceinline__ double2 csub(double2 a, double2 b) {
   a.x -= b.x;
   a.y -= b.y;
   return a;
@@ -639,10 +663,10 @@ __device__ __forceinline__ bool fft_fill_row(typename Cx<T>::type* s, const type
   if (src == 1) {
     const T spacing = prm->spacing;
     const int lr = row <= L / 2 ? row : row - L;
-    const T dr = spacing * (T)(double)lr;
+    const T dr = spacing * (T)lr;
     for (int c = threadIdx.x; c < L; c += blockDim.x) {
       const int lc = c <= L / 2 ? c : c - L;
-      const T dc = spacing * (T)(double)lc;
+      const T dc = spacing * (T)lc;
       T sq = T(0);
       sq = sq + dc * dc;
       if (D == 2) sq = sq + dr * dr;
@@ -785,7 +809,8 @@ __global__ void __launch_bounds__(kFftThreads, sizeof(T) == 4 ? 3 : 1) fft_rows_
     if (r.nsub == 3) r3_dif_stage<T2, T>(s, r.M, tw3, r.tws3);
     dif_smem_stages(s, r.M, r.log2M, r.small, tw, r.nsub);
     // khat_out: the real part scaled by 1 / L^D (the kernel spectrum)
-    const T inv_total = T(1) / (T)(D == 1 ? (double)L : (double)L * (double)L);
+    // (L^D < 2^31 is exact as an int, so no FP64 conversion is needed)
+    const T inv_total = khat_out ? T(1) / (T)(D == 1 ? L : L * L) : T(0);
     T* kr = khat_out ? khat_out + (int64_t)blockIdx.x * L : nullptr;
     for (int g = r.warp; g < r.ngroups; g += r.nw) {
       if (r.wide) {
@@ -873,10 +898,10 @@ __global__ void __launch_bounds__(kFftThreads, sizeof(T) == 4 ? 3 : 1) kspec_ker
   if (pass == 0) {
     const T spacing = prm->spacing;
     const int l1 = r1 <= half ? r1 : r1 - L, l2 = r2 <= half ? r2 : r2 - L;
-    const T d1 = spacing * (T)(double)l1, d2 = spacing * (T)(double)l2;
+    const T d1 = spacing * (T)l1, d2 = spacing * (T)l2;
     for (int c = threadIdx.x; c < L; c += blockDim.x) {
       const int lc = c <= half ? c : c - L;
-      const T dc = spacing * (T)(double)lc;
+      const T dc = spacing * (T)lc;  // |lc| <= L/2: exact in T
       T sq1 = T(0), sq2 = T(0);
       sq1 = sq1 + dc * dc;
       sq1 = sq1 + d1 * d1;
@@ -902,7 +927,7 @@ __global__ void __launch_bounds__(kFftThreads, sizeof(T) == 4 ? 3 : 1) kspec_ker
   __syncthreads();
   if (r.nsub == 3) r3_dif_stage<T2, T>(s, r.M, tw3, r.tws3);
   dif_smem_stages(s, r.M, r.log2M, r.small, tw, r.nsub);
-  const T scale = pass == 0 ? T(1) : T(1) / (T)((double)L * (double)L);
+  const T scale = pass == 0 ? T(1) : T(1) / (T)(L * L);
   T* o1 = out + (int64_t)r1 * L;
   T* o2 = out + (int64_t)r2 * L;
   for (int g = r.warp; g < r.ngroups; g += r.nw) {

@@ -174,10 +174,12 @@ __device__ __forceinline__ float tf32_hi(float x) {
 // [d0, d0 + 16) of Xp (row-major, ld = dim_pad, zero padded), split into hi /
 // lo core-matrix sub-tiles at dst (query hi, query lo, candidate hi, candidate
 // lo); rows >= row_end are 0. All loads are issued before the first store.
-// Four consecutive threads take the four 16-byte pieces of one row's chunk, so
-// a warp loads 8 rows x 64 contiguous bytes (8 cache lines, not 32) and stores
-// 4 whole core matrices (512 contiguous bytes).
+// A warp takes 8 rows x the four 16-byte pieces of their chunk: its loads
+// touch 8 cache lines (not 32), and lanes 8q .. 8q + 7 hold piece q of the 8
+// rows, so each quarter-warp phase of its 16-byte stores fills one whole core
+// matrix (128 contiguous bytes, no bank conflict).
 constexpr int kStageIters = (2 * TQ * (PK / 4) + kProducers - 1) / kProducers;
+static_assert(PK == 16 && TQ % 8 == 0 && kProducers % 32 == 0, "stage_split's lane layout: 4 pieces per row, whole warps");
 
 __device__ __forceinline__ void stage_split(const float* __restrict__ Xp, int64_t q0, int64_t c0, int64_t row_end,
                                             int dim_pad, int d0, unsigned char* dst, int p) {
@@ -188,7 +190,7 @@ __device__ __forceinline__ void stage_split(const float* __restrict__ Xp, int64_
     x[u] = make_float4(0.f, 0.f, 0.f, 0.f);
     if (idx < 2 * TQ * (PK / 4)) {
       const int half = idx / (TQ * (PK / 4)), rem = idx % (TQ * (PK / 4));
-      const int r = rem / (PK / 4), k4 = rem % (PK / 4);
+      const int r = 8 * (rem >> 5) + (rem & 7), k4 = (rem >> 3) & 3;
       const int64_t row = (half ? c0 : q0) + r;
       if (row < row_end) x[u] = __ldg(reinterpret_cast<const float4*>(Xp + row * dim_pad + d0) + k4);
     }
@@ -198,7 +200,7 @@ __device__ __forceinline__ void stage_split(const float* __restrict__ Xp, int64_
     const int idx = p + u * kProducers;
     if (idx < 2 * TQ * (PK / 4)) {
       const int half = idx / (TQ * (PK / 4)), rem = idx % (TQ * (PK / 4));
-      const int r = rem / (PK / 4), k4 = rem % (PK / 4);
+      const int r = 8 * (rem >> 5) + (rem & 7), k4 = (rem >> 3) & 3;
       float4 h, l;
       h.x = tf32_hi(x[u].x);
       h.y = tf32_hi(x[u].y);
