@@ -9,11 +9,11 @@ from ._lib import (BhtsneError, Context, F32, F64, METHOD_BARNES_HUT, METHOD_EXA
 from .batch import Batch
 from .serve import Server
 from .tsne import (Neighbor, SparseAffinities, TSNE, conditional_p, gradient, knn_euclidean, load_csv,
-                   neighbors_to_arrays, symmetrize, update, write_csv)
+                   load_npz, neighbors_to_arrays, symmetrize, update, write_csv)
 
 __all__ = [
     "Batch", "BhtsneError", "Server", "Context", "F32", "F64", "METHOD_BARNES_HUT", "METHOD_EXACT", "METHOD_FIT_SNE", "SIGNATURES",
     "default_context", "library_path", "load", "Neighbor", "SparseAffinities", "TSNE", "conditional_p", "gradient",
-    "knn_euclidean", "load_csv", "neighbors_to_arrays", "symmetrize", "tune_config", "tune_load", "tune_save",
+    "knn_euclidean", "load_csv", "load_npz", "neighbors_to_arrays", "symmetrize", "tune_config", "tune_load", "tune_save",
     "update", "write_csv",
 ]

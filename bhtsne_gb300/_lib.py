@@ -65,6 +65,7 @@ SIGNATURES = {
     "bhtsne_load_csv": (C.c_int, [C.c_char_p, _i32, _i64p, _i64, C.c_int, _vp, _i64p, _i64p]),
     "bhtsne_tsne_write_csv": (C.c_int, [_vp, C.c_char_p]),
     "bhtsne_write_csv": (C.c_int, [_vp, _i64, _i32, C.c_int, C.c_char_p]),
+    "bhtsne_load_npz": (C.c_int, [C.c_char_p, C.c_char_p, C.c_int, _vp, _i64p, C.POINTER(_i32), _i64p]),
     "bhtsne_io_last_error": (C.c_char_p, []),
     "bhtsne_tune": (C.c_int, [_vp, C.c_int, _i32, _i64, _i32, _i32]),
     "bhtsne_tune_config": (C.c_int, [C.c_int, _i32, _i64, C.c_char_p, _i64]),

@@ -14,7 +14,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OBJ = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libbhtsne_gpu.so")
-SOURCES = ["api.cu", "affinity.cu", "batch.cu", "bh.cu", "epoch.cu", "fitsne.cu", "io.cu", "knn.cu", "knn_tc.cu", "noalloc.cu", "serve.cu", "sort.cu", "tune.cu"]
+SOURCES = ["api.cu", "affinity.cu", "batch.cu", "bh.cu", "epoch.cu", "fitsne.cu", "io.cu", "knn.cu", "knn_tc.cu", "noalloc.cu", "npz.cu", "serve.cu", "sort.cu", "tune.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # -fmad=false: every product and sum rounds on its own, as in the Rust reference.
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-Xcompiler", "-fPIC,-O2,-ffp-contract=off"]

@@ -371,6 +371,27 @@ def load_csv(path: str, has_headers: bool = False, skip=None, dtype=np.float32) 
     return out
 
 
+def load_npz(path: str, name: str, dtype=np.float32) -> np.ndarray:
+    """Array `name` of an .npz archive (the input format of the reference's
+    example, examples/mnist_pca_tsne.rs:39-44) in C order, converted to
+    `dtype`, with its shape."""
+    lib = L.load()
+    code = _dtype_code(dtype)
+    count, ndim = C.c_int64(0), C.c_int32(0)
+    shape = (C.c_int64 * 8)()
+    p, nm = os.fsencode(path), name.encode()
+    rc = lib.bhtsne_load_npz(p, nm, code, None, C.byref(count), C.byref(ndim), shape)
+    if rc != L.OK:
+        raise L.BhtsneError(rc, lib.bhtsne_io_last_error().decode())
+    out = np.zeros(count.value, np.dtype(dtype))
+    rc = lib.bhtsne_load_npz(p, nm, code, _ptr(out), C.byref(count), None, None)
+    if rc != L.OK:
+        raise L.BhtsneError(rc, lib.bhtsne_io_last_error().decode())
+    if ndim.value > 8:
+        return out
+    return out.reshape(tuple(shape[k] for k in range(ndim.value)))
+
+
 def write_csv(embedding: np.ndarray, path: str, D: int = 2):
     """write_csv of an embedding held by the caller (n x D values)."""
     lib = L.load()

@@ -173,6 +173,8 @@ extern "C" {
                            out: *mut c_void, count: *mut i64, records: *mut i64) -> c_int;
     pub fn bhtsne_tsne_write_csv(t: *mut bhtsne_tsne, path: *const c_char) -> c_int;
     pub fn bhtsne_write_csv(embedding: *const c_void, n: i64, embed_dim: i32, dtype: c_int, path: *const c_char) -> c_int;
+    pub fn bhtsne_load_npz(path: *const c_char, name: *const c_char, dtype: c_int, out: *mut c_void,
+                           count: *mut i64, ndim: *mut i32, shape: *mut i64) -> c_int;
     pub fn bhtsne_io_last_error() -> *const c_char;
 
     // ---- batches of independent fits

@@ -404,6 +404,34 @@ pub fn load_csv<T: GpuFloat>(path: &str, has_headers: bool, skip: Option<&[usize
     Ok(data)
 }
 
+/// Array `name` of an .npz archive, the input of the reference's example
+/// (examples/mnist_pca_tsne.rs:39-44, `NpzArchive::by_name(..).into_vec()`),
+/// in C order and converted to `T`, with its shape.
+pub fn load_npz<T: GpuFloat>(path: &str, name: &str) -> Result<(Vec<T>, Vec<usize>), Box<dyn std::error::Error>> {
+    let p = std::ffi::CString::new(path)?;
+    let nm = std::ffi::CString::new(name)?;
+    let (mut count, mut ndim) = (0i64, 0i32);
+    let mut shape = [0i64; 8];
+    let fail = || -> Box<dyn std::error::Error> {
+        unsafe { CStr::from_ptr(sys::bhtsne_io_last_error()) }.to_string_lossy().into_owned().into()
+    };
+    if unsafe {
+        sys::bhtsne_load_npz(p.as_ptr(), nm.as_ptr(), T::DTYPE, std::ptr::null_mut(), &mut count, &mut ndim,
+                             shape.as_mut_ptr())
+    } != 0 {
+        return Err(fail());
+    }
+    let mut data = vec![T::default(); count as usize];
+    if unsafe {
+        sys::bhtsne_load_npz(p.as_ptr(), nm.as_ptr(), T::DTYPE, data.as_mut_ptr().cast(), &mut count,
+                             std::ptr::null_mut(), std::ptr::null_mut())
+    } != 0 {
+        return Err(fail());
+    }
+    let dims = shape[..(ndim as usize).min(8)].iter().map(|&v| v as usize).collect();
+    Ok((data, dims))
+}
+
 impl<'data, T: GpuFloat, U, const D: usize> Drop for tSNE<'data, T, U, D> {
     fn drop(&mut self) {
         unsafe {

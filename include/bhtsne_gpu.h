@@ -237,6 +237,18 @@ int bhtsne_tsne_write_csv(bhtsne_tsne* t, const char* path);
 /* No reference counterpart: write_csv of an embedding held by the caller
  * (n x embed_dim values of dtype), e.g. a batch or server result. */
 int bhtsne_write_csv(const void* embedding, int64_t n, int32_t embed_dim, int dtype, const char* path);
+/* The npz input of the reference's example (examples/mnist_pca_tsne.rs:39-44,
+ * npyz 0.9 NpzArchive::open + by_name + into_vec): array `name` (without its
+ * ".npy" suffix) of an .npz archive, entries stored or deflated, ZIP64
+ * included, in C order (Fortran-order arrays are reordered) and converted to
+ * the dtype's float. Element types: little-endian f4, f8, i1..i8, u1..u8, b1.
+ * Call with out == NULL to get *count (values), *ndim and shape[0 .. min(ndim,
+ * 8)) (ndim and shape may be NULL); then with out holding *count values.
+ * Errors: BHTSNE_EIO (file), BHTSNE_EINVAL (not an npz archive, no such array,
+ * unsupported type, corrupt or truncated data), with a message from
+ * bhtsne_io_last_error (per thread). Host only. */
+int bhtsne_load_npz(const char* path, const char* name, int dtype, void* out, int64_t* count, int32_t* ndim,
+                    int64_t* shape);
 const char* bhtsne_io_last_error(void);
 
 /* ---- batches of independent fits (no reference counterpart) --------------- */
