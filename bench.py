@@ -301,23 +301,30 @@ def run_ours(args):
     aff_h = bg.SparseAffinities(rows_h, cols_h, vals_h, aff.perplexity)
     emb = np.empty(n * 2, np.float32)
     emb, _ = pinned_copy(emb)
-    t2 = bg.TSNE(n, D=2, ctx=ctx).epochs(args.steps).stop_lying_epoch(0).momentum(0.8)
     h2d = rows_h.nbytes + cols_h.nbytes + vals_h.nbytes + y_in.nbytes
-    barrier_and_max(0.0, ws)
-    w0 = time.perf_counter()
-    t2.with_affinities(aff_h)
-    t2.initial_embedding(y_in)
-    t2.barnes_hut(theta)
-    t2.embedding_into(emb)
-    e2e_s = time.perf_counter() - w0
-    e2e_s = barrier_and_max(e2e_s, ws)
+    # the whole user-side call sequence, repeated (a single ~50 ms sample is at
+    # the mercy of the host); the median of the repetitions is reported
+    e2e_runs = []
+    for _ in range(args.e2e_reps):
+        t2 = bg.TSNE(n, D=2, ctx=ctx).epochs(args.steps).stop_lying_epoch(0).momentum(0.8)
+        barrier_and_max(0.0, ws)
+        w0 = time.perf_counter()
+        t2.with_affinities(aff_h)
+        t2.initial_embedding(y_in)
+        t2.barnes_hut(theta)
+        t2.embedding_into(emb)
+        e2e_s = time.perf_counter() - w0
+        e2e_runs.append(barrier_and_max(e2e_s, ws))
+        t2.close()
+    e2e_s = statistics.median(e2e_runs)
     e2e = {"value": round(ws * args.steps / e2e_s, 3), "unit": UNIT, "h2d_bytes_per_step": h2d // args.steps,
            "d2h_bytes_per_step": emb.nbytes // args.steps,
+           "samples": [round(ws * args.steps / x, 1) for x in e2e_runs], "statistic": "median",
            "pinned": bool(pin_rows and pin_cols and pin_vals and pin_y),
            "note": "with_affinities(host CSR) + initial_embedding(window start) + barnes_hut(epochs=steps, "
                    "stop_lying_epoch 0, momentum 0.8) + embedding(); affinity normalisation, the warm start's "
                    "re-layout and all copies inside the timed region"}
-    del t2, rows_h, cols_h, vals_h, aff_h
+    del rows_h, cols_h, vals_h, aff_h
 
     parity = None
     if rank == 0 and not args.no_parity:
@@ -416,12 +423,18 @@ def parity_1m(args, ctx, X, aff, y_end, knn_fallback_fit):
     # the reference sums Z sequentially in f32 (src/repulsion.rs:155); the GPU
     # sums it in FP64: both against the FP64 sum of the oracle's per-point terms
     z64 = float(oq.astype(np.float64).sum())
+    # the same Barnes-Hut pass evaluated in f64 by the oracle: the repulsive
+    # forces of both f32 passes (the GPU's FP64 centres of mass, the oracle's
+    # f32 ones) against it
+    oneg64, _, _ = O.bh_repulsion(y.astype(np.float64), 0.5)
     g = pos.astype(np.float64) - neg.astype(np.float64) / z
     og = opos.astype(np.float64) - oneg.astype(np.float64) / oz
     out["c3_gradient"] = {"embedding": "after the timed window (epoch %d)" % (args.burn_in + args.warmup + args.steps),
                           "rel_l2_gradient": float("%.3g" % rel_l2(g, og)),
                           "rel_l2_attractive": float("%.3g" % rel_l2(pos, opos)),
                           "rel_l2_repulsive": float("%.3g" % rel_l2(neg, oneg)),
+                          "rel_l2_repulsive_vs_f64_pass": {"gpu": float("%.3g" % rel_l2(neg, oneg64)),
+                                                          "oracle_f32": float("%.3g" % rel_l2(oneg, oneg64))},
                           "z_rel_vs_fp64_sum": float("%.3g" % (abs(z - z64) / z64)),
                           "oracle_f32_sequential_z_rel_vs_fp64_sum": float("%.3g" % (abs(oz - z64) / z64)),
                           "bar": 1e-4}
@@ -859,6 +872,7 @@ def main():
     ap.add_argument("--burn-in", type=int, default=250, help="untimed epochs before the warm-up")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-parity", action="store_true", help="skip the 1M-point parity checks")
+    ap.add_argument("--e2e-reps", type=int, default=5, help="repetitions of the end-to-end leg (median reported)")
     ap.add_argument("--parity-rows", type=int, default=2000, help="kNN query rows checked against brute force")
     ap.add_argument("--batch-jobs", type=int, default=512, help="batched-fit comparison (0 to skip)")
     ap.add_argument("--batch-epochs", type=int, default=500)

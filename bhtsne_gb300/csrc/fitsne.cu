@@ -606,45 +606,68 @@ __device__ __forceinline__ void r3_dit_stage(T2* s, int M, const T2* __restrict_
   __syncthreads();
 }
 
-// This lane's forward twiddle for each register stage k (span 2^k):
-// W_(2^k)^(lane mod 2^(k-1)).
+// This lane's twiddle for each register stage k (span 2^k): W_(2^k)^(lane
+// mod 2^(k-1)) in the upper lane of each butterfly (lane bit k-1 set), 1 in
+// the lower lane, so both lanes run the same instructions (below).
 template <class T2>
 __device__ __forceinline__ void lane_twiddles(int lane, int small, const T2* __restrict__ tw, T2 (&w)[5]) {
 #pragma unroll
   for (int k = 1; k <= 5; ++k) {
-    w[k - 1].x = 0;
+    w[k - 1].x = 1;
     w[k - 1].y = 0;
-    if (k <= small) w[k - 1] = twid(tw, 1 << k, lane & ((1 << (k - 1)) - 1));
+    if (k <= small && (lane & (1 << (k - 1)))) w[k - 1] = twid(tw, 1 << k, lane & ((1 << (k - 1)) - 1));
   }
 }
 
-// DIF spans 2^small .. 2 on one element per lane (forward twiddles w).
+// +1 in the lower lane of a span-2^k butterfly, -1 in the upper one.
+template <class T>
+__device__ __forceinline__ T lane_sign(int lane, int k) {
+  return (lane & (1 << (k - 1))) ? T(-1) : T(1);
+}
+
+// s x + o for both parts (one rounding each).
+__device__ __forceinline__ float2 sfma2(float s, float2 x, float2 o) {
+  float2 r;
+  r.x = __fmaf_rn(s, x.x, o.x);
+  r.y = __fmaf_rn(s, x.y, o.y);
+  return r;
+}
+__device__ __forceinline__ double2 sfma2(double s, double2 x, double2 o) {
+  double2 r;
+  r.x = __fma_rn(s, x.x, o.x);
+  r.y = __fma_rn(s, x.y, o.y);
+  return r;
+}
+
+// DIF spans 2^small .. 2 on one element per lane (w from lane_twiddles). The
+// lower lane of a butterfly keeps x + o, the upper one (o - x) w: both compute
+// (o + s x) w with s = +-1 and w = 1 in the lower lane, without a branch.
 template <class T2>
 __device__ __forceinline__ T2 dif_reg_stages(T2 x, int lane, int small, const T2 (&w)[5]) {
+  typedef decltype(x.x) T;
 #pragma unroll
   for (int k = 5; k >= 1; --k) {
     if (k > small) continue;
-    const int half = 1 << (k - 1);
-    const T2 o = shfl_xor2(x, half);
-    x = (lane & half) ? cmul(csub(o, x), w[k - 1]) : cadd(x, o);
+    const T2 o = shfl_xor2(x, 1 << (k - 1));
+    x = cmul(sfma2(lane_sign<T>(lane, k), x, o), w[k - 1]);
   }
   return x;
 }
 
-// DIT spans 2 .. 2^small on one element per lane (w: forward twiddles, used
-// conjugated).
+// DIT spans 2 .. 2^small on one element per lane (w from lane_twiddles, used
+// conjugated): the upper lane sends t = x conj(w) and keeps o - t, the lower
+// sends t = x and keeps x + o; both compute t = x conj(w), then o + s t.
 template <class T2>
 __device__ __forceinline__ T2 dit_reg_stages(T2 x, int lane, int small, const T2 (&w)[5]) {
+  typedef decltype(x.x) T;
 #pragma unroll
   for (int k = 1; k <= 5; ++k) {
     if (k > small) continue;
-    const int half = 1 << (k - 1);
-    const bool up = (lane & half) != 0;
     T2 wc = w[k - 1];
     wc.y = -wc.y;
-    const T2 t = up ? cmul(x, wc) : x;
-    const T2 o = shfl_xor2(t, half);
-    x = up ? csub(o, t) : cadd(x, o);
+    const T2 t = cmul(x, wc);
+    const T2 o = shfl_xor2(t, 1 << (k - 1));
+    x = sfma2(lane_sign<T>(lane, k), t, o);
   }
   return x;
 }
