@@ -55,6 +55,7 @@ SIGNATURES = {
     "bhtsne_tsne_profile": (C.c_int, [_vp, _i32]),
     "bhtsne_tsne_phase_times": (C.c_int, [_vp, _dblp, _i64p]),
     "bhtsne_tsne_relayout_times": (C.c_int, [_vp, _dblp, _i64p]),
+    "bhtsne_tsne_layout_info": (C.c_int, [_vp, C.POINTER(_i32), _i64p]),
     "bhtsne_launch_count": (C.c_int64, []),
     "bhtsne_knn_euclidean": (C.c_int, [_vp, C.c_int, _vp, _i64, _i32, _i32, _u32p, _vp]),
     "bhtsne_conditional_p": (C.c_int, [_vp, C.c_int, _vp, _i64, _i32, _dbl, _vp, _i32p]),

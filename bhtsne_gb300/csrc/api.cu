@@ -96,6 +96,13 @@ struct State {
   DevBuf y, uy, gains, pos, neg, zbuf, klbuf, tmp, tmp2;
   DevBuf kidx, kdist, kp, xin, yext, ckpt;
   Renumbering rn;  // locality layout of y/uy/gains (see launch_renumber)
+  // component layout of the current fit (component_order): the points grouped
+  // by connected component of P, laid out once at epoch 0 instead of the
+  // periodic Morton re-layout
+  bool comp_mode = false;
+  int64_t comp_largest = 0;
+  DevBuf comp_order;
+  ComponentScratch comp;
   AttrTasks at;    // attractive-pass tasks of the current CSR layout
   int task_len = kAttrTaskLen;  // the tuned task length of the current fit
   uint64_t layout_gen = 0;
@@ -154,6 +161,8 @@ struct bhtsne_tsne {
   std::vector<unsigned char> init;
   int64_t init_len = 0;
   bool caller_init = false;  // the current fit started from the caller's embedding
+  bool comp_layout = false;  // the last fit used the component layout
+  int64_t comp_largest = 0;
   bool stop_lying_fired = false;
   bool has_cached_perplexity = false;
   double cached_perplexity = 0;
@@ -418,6 +427,25 @@ void advance_impl(bhtsne_tsne* t, int64_t epochs) {
   // CUDA events around each re-layout, read after the loop's final sync.
   std::vector<cudaEvent_t> rl_ev;
   auto maybe_renumber = [&](int64_t epoch) {
+    if (S.comp_mode) {
+      // component layout: once, at the fit's first epoch
+      if (epoch != 0) return;
+      const bool was_active = S.rn.active;
+      rl_ev.resize(rl_ev.size() + 2);
+      BHG_CUDA(cudaEventCreate(&rl_ev[rl_ev.size() - 2]));
+      BHG_CUDA(cudaEventCreate(&rl_ev[rl_ev.size() - 1]));
+      BHG_CUDA(cudaEventRecord(rl_ev[rl_ev.size() - 2], s));
+      launch_renumber<T>(D, S.comp_order.template as<uint32_t>(), n, S.rn, y, S.uy.template as<T>(),
+                         S.gains.template as<T>(), S.pos.template as<T>(), S.neg.template as<T>(),
+                         static_cast<T*>(S.yext.ensure((size_t)n * D * sizeof(T))), S.rows.template as<uint64_t>(),
+                         S.cols.template as<uint32_t>(), S.vals.template as<T>(), S.nnz, s);
+      launch_recenter_bbox<T>(D, y, n, nullptr, false, S.bh, bits, s);
+      ++S.layout_gen;
+      ensure_tasks();
+      BHG_CUDA(cudaEventRecord(rl_ev.back(), s));
+      if (!was_active) t->drop_graph();
+      return;
+    }
     if (!sparse || renumber_every <= 0 || epoch % renumber_every != 0) return;
     // At epoch 0 only a caller's embedding (a warm start) has a layout worth
     // following; the seeded random start has none.
@@ -654,6 +682,27 @@ void run_loop(bhtsne_tsne* t, int kind, double theta) {
   t->drop_graph();
   st<T>(t).rn.active = false;  // the fit starts from y in the caller's order
   ++st<T>(t).layout_gen;
+  // Component layout for Barnes-Hut fits of large, clustered inputs:
+  // when P's graph splits into components of at most n / 4 points, group the
+  // points by component once (every row's columns then lie within its
+  // component's slots) instead of re-laying them out in Morton order every 50
+  // epochs. BHTSNE_COMPONENT_LAYOUT=0 turns it off.
+  {
+    State<T>& S = st<T>(t);
+    const char* cl = getenv("BHTSNE_COMPONENT_LAYOUT");
+    const bool comp_off = cl && atoi(cl) == 0;
+    const bool comp_force = cl && atoi(cl) == 2;
+    S.comp_mode = false;
+    S.comp_largest = 0;
+    if (!comp_off && kind == BHTSNE_METHOD_BARNES_HUT && S.has_sparse && (t->D == 2 || t->D == 3) &&
+        (comp_force || t->n >= kComponentMinN)) {
+      S.comp_mode = component_order(S.rows.template as<uint64_t>(), S.cols.template as<uint32_t>(), t->n,
+                                    S.comp_order, S.comp, &S.comp_largest, t->ctx->stream);
+      S.comp.release();
+    }
+    t->comp_layout = S.comp_mode;
+    t->comp_largest = S.comp_largest;
+  }
   // launch shapes of this fit: tuned for (T, D, N) on this device, or the defaults
   const TuneKnobs kn = tune_lookup(t->dtype, t->D, t->n);
   st<T>(t).task_len = kn.attr_task_len;
@@ -1208,6 +1257,13 @@ int bhtsne_tsne_advance(bhtsne_tsne* t, int64_t epochs) {
 int bhtsne_tsne_profile(bhtsne_tsne* t, int32_t enable) {
   if (!t) return BHTSNE_EINVAL;
   t->profile = enable != 0;
+  return BHTSNE_OK;
+}
+
+int bhtsne_tsne_layout_info(const bhtsne_tsne* t, int32_t* component_layout, int64_t* largest_component) {
+  if (!t) return BHTSNE_EINVAL;
+  if (component_layout) *component_layout = t->comp_layout ? 1 : 0;
+  if (largest_component) *largest_component = t->comp_largest;
   return BHTSNE_OK;
 }
 

@@ -205,6 +205,63 @@ __global__ void renumber_gather_kernel(const uint32_t* __restrict__ order, const
   }
 }
 
+// Connected components by minimum-label propagation (component_order). A
+// warp per row takes the smallest label among the row and its columns; a
+// label only ever decreases, so the fixed point (each component labelled by
+// its smallest index) does not depend on the order in which rows update.
+__global__ void cc_init_kernel(uint32_t* __restrict__ label, int64_t n) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) label[i] = (uint32_t)i;
+}
+
+__global__ void cc_step_kernel(const uint64_t* __restrict__ rows, const uint32_t* __restrict__ cols, int64_t n,
+                               uint32_t* label, int* __restrict__ changed) {
+  const int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (i >= n) return;  // uniform per warp
+  const uint32_t own = label[i];
+  uint32_t m = own;
+  for (uint64_t e = rows[i] + lane; e < rows[i + 1]; e += 32) {
+    const uint32_t l = label[cols[e]];
+    m = l < m ? l : m;
+  }
+  m = __reduce_min_sync(kFull, m);
+  if (lane == 0 && m < own) {
+    atomicMin(&label[i], m);
+    *changed = 1;
+  }
+}
+
+// label[i] = label[label[i]] (pointer jumping: labels fall toward the root
+// of their chain in fewer propagation rounds)
+__global__ void cc_jump_kernel(uint32_t* label, int64_t n, int* __restrict__ changed) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const uint32_t l = label[i];
+  const uint32_t ll = label[l];
+  if (ll < l) {
+    atomicMin(&label[i], ll);
+    *changed = 1;
+  }
+}
+
+__global__ void cc_count_kernel(const uint32_t* __restrict__ label, int64_t n, uint32_t* __restrict__ count,
+                                uint64_t* __restrict__ keys, uint32_t* __restrict__ vals) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  atomicAdd(&count[label[i]], 1u);
+  keys[i] = label[i];
+  vals[i] = (uint32_t)i;
+}
+
+__global__ void cc_max_kernel(const uint32_t* __restrict__ count, int64_t n, unsigned* __restrict__ out) {
+  unsigned m = 0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    m = count[i] > m ? count[i] : m;
+  m = __reduce_max_sync(kFull, m);
+  if ((threadIdx.x & 31) == 0) atomicMax(out, m);
+}
+
 __global__ void invert_kernel(const uint32_t* __restrict__ ext, int64_t n, uint32_t* __restrict__ inv) {
   const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (s < n) inv[ext[s]] = (uint32_t)s;
@@ -722,6 +779,53 @@ void launch_renumber(int D, const uint32_t* order, int64_t n, Renumbering& r, T*
     BHG_LAUNCH_CHECK();
   }
   r.active = true;
+}
+
+bool component_order(const uint64_t* rows, const uint32_t* cols, int64_t n, DevBuf& order, ComponentScratch& cs,
+                     int64_t* largest, cudaStream_t s) {
+  *largest = 0;
+  if (n < 2) return false;
+  const unsigned g = (unsigned)ceil_div(n, 256);
+  uint32_t* label = static_cast<uint32_t*>(cs.label.ensure((size_t)n * 4));
+  int* flag = static_cast<int*>(cs.flag.ensure(64));
+  cc_init_kernel<<<g, 256, 0, s>>>(label, n);
+  BHG_LAUNCH_CHECK();
+  // Each round at least halves the distance of every label chain to its root
+  // or settles; a kNN graph's components have small diameters. Rounds are
+  // bounded, and a graph that has not settled is left in its current layout.
+  bool settled = false;
+  for (int round = 0; round < 64 && !settled; ++round) {
+    BHG_CUDA(cudaMemsetAsync(flag, 0, sizeof(int), s));
+    cc_step_kernel<<<(unsigned)ceil_div(n * 32, 256), 256, 0, s>>>(rows, cols, n, label, flag);
+    BHG_LAUNCH_CHECK();
+    cc_jump_kernel<<<g, 256, 0, s>>>(label, n, flag);
+    BHG_LAUNCH_CHECK();
+    int h = 0;
+    BHG_CUDA(cudaMemcpyAsync(&h, flag, sizeof(int), cudaMemcpyDeviceToHost, s));
+    BHG_CUDA(cudaStreamSynchronize(s));
+    settled = h == 0;
+  }
+  if (!settled) return false;
+  uint32_t* count = static_cast<uint32_t*>(cs.count.ensure((size_t)n * 4));
+  uint64_t* keys = static_cast<uint64_t*>(cs.keys.ensure((size_t)n * 8));
+  uint32_t* vals = static_cast<uint32_t*>(order.ensure((size_t)n * 4));
+  BHG_CUDA(cudaMemsetAsync(count, 0, (size_t)n * 4, s));
+  cc_count_kernel<<<g, 256, 0, s>>>(label, n, count, keys, vals);
+  BHG_LAUNCH_CHECK();
+  unsigned* mx = reinterpret_cast<unsigned*>(flag) + 1;
+  BHG_CUDA(cudaMemsetAsync(mx, 0, sizeof(unsigned), s));
+  cc_max_kernel<<<(unsigned)std::min<int64_t>(g, sm_grid(4, 4096)), 256, 0, s>>>(count, n, mx);
+  BHG_LAUNCH_CHECK();
+  unsigned hmax = 0;
+  BHG_CUDA(cudaMemcpyAsync(&hmax, mx, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+  BHG_CUDA(cudaStreamSynchronize(s));
+  *largest = hmax;
+  if ((int64_t)hmax > n / 4) return false;
+  int bits = 1;
+  while (bits < 32 && ((uint64_t)1 << bits) < (uint64_t)n) ++bits;
+  radix_sort_pairs<uint32_t>(keys, vals, static_cast<uint64_t*>(cs.keys_alt.ensure((size_t)n * 8)),
+                             static_cast<uint32_t*>(cs.vals_alt.ensure((size_t)n * 4)), n, 0, bits, cs.sort_tmp, s);
+  return true;
 }
 
 template <class T>

@@ -19,6 +19,9 @@ struct UpdateScratch {
 // terms are grouped). Built once per CSR layout (one host synchronisation),
 // replayed every epoch.
 constexpr int kAttrTaskLen = 128;  // the default task length
+// Component layout (component_order) for fits of at least this many points:
+// below it y stays in cache whatever the layout.
+constexpr int64_t kComponentMinN = 65536;
 struct AttrTasks {
   DevBuf tasks, off, cnt, longs, nlong_dev, part, scan_tmp;
   int64_t ntasks = 0, nlong = 0, n = 0;
@@ -57,6 +60,30 @@ struct Renumbering {
 template <class T>
 void launch_renumber(int D, const uint32_t* order, int64_t n, Renumbering& r, T* y, T* uy, T* gains, T* tmp_a, T* tmp_b,
                      T* tmp_c, const uint64_t* rows, const uint32_t* cols, const T* vals, int64_t nnz, cudaStream_t s);
+
+// Component layout: the connected components of the (symmetric) CSR graph of
+// P, found by minimum-label propagation. When the graph splits into
+// components of at most n / 4 points each, `order` receives the points
+// grouped by component (the component of the smallest index first), in index
+// order within each, and the call returns true. A layout in that order keeps
+// every row's columns inside its component's slot range, so the attractive
+// pass's gathers of y stay within a few hundred kilobytes. False (order
+// unspecified) for a graph with a larger component; `largest` receives the
+// size of the largest component (0 when propagation did not settle).
+struct ComponentScratch {
+  DevBuf label, count, keys, keys_alt, vals_alt, flag, sort_tmp;
+  void release() {
+    label.release();
+    count.release();
+    keys.release();
+    keys_alt.release();
+    vals_alt.release();
+    flag.release();
+    sort_tmp.release();
+  }
+};
+bool component_order(const uint64_t* rows, const uint32_t* cols, int64_t n, DevBuf& order, ComponentScratch& cs,
+                     int64_t* largest, cudaStream_t s);
 
 // out[ext[s]] = y[s]: back to the caller's point order.
 template <class T>

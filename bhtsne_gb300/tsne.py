@@ -271,6 +271,13 @@ class TSNE:
         self._check(self.lib.bhtsne_tsne_relayout_times(self.handle, C.byref(ms), C.byref(c)))
         return {"ms": ms.value, "count": c.value}
 
+    def layout_info(self):
+        """The last fit's layout (no reference counterpart): whether the points
+        were grouped by connected component of P, and P's largest component."""
+        comp, big = C.c_int32(), C.c_int64()
+        self._check(self.lib.bhtsne_tsne_layout_info(self.handle, C.byref(comp), C.byref(big)))
+        return {"component_layout": bool(comp.value), "largest_component": big.value}
+
     def timings(self):
         a, lp, e = C.c_double(), C.c_double(), C.c_int64()
         self.lib.bhtsne_tsne_timings(self.handle, C.byref(a), C.byref(lp), C.byref(e))

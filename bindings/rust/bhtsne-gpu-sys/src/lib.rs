@@ -143,6 +143,8 @@ extern "C" {
     pub fn bhtsne_tsne_profile(t: *mut bhtsne_tsne, enable: i32) -> c_int;
     pub fn bhtsne_tsne_phase_times(t: *const bhtsne_tsne, ms: *mut f64, epochs: *mut i64) -> c_int;
     pub fn bhtsne_tsne_relayout_times(t: *const bhtsne_tsne, ms: *mut f64, count: *mut i64) -> c_int;
+    pub fn bhtsne_tsne_layout_info(t: *const bhtsne_tsne, component_layout: *mut i32, largest_component: *mut i64)
+                                   -> c_int;
     pub fn bhtsne_launch_count() -> i64;
 
     // ---- stage entry points
