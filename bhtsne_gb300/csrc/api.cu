@@ -99,9 +99,11 @@ struct State {
   // component layout of the current fit (component_order): the points grouped
   // by connected component of P, laid out once at epoch 0 instead of the
   // periodic Morton re-layout
-  bool comp_mode = false;
+  bool comp_mode = false;     // the component layout is active
+  bool comp_decided = false;  // the first periodic re-layout point has chosen the layout
+  bool comp_eligible = false; // this fit may use the component layout
   int64_t comp_largest = 0;
-  DevBuf comp_order;
+  DevBuf comp_order, comp_slots;
   ComponentScratch comp;
   AttrTasks at;    // attractive-pass tasks of the current CSR layout
   int task_len = kAttrTaskLen;  // the tuned task length of the current fit
@@ -427,15 +429,36 @@ void advance_impl(bhtsne_tsne* t, int64_t epochs) {
   // CUDA events around each re-layout, read after the loop's final sync.
   std::vector<cudaEvent_t> rl_ev;
   auto maybe_renumber = [&](int64_t epoch) {
+    if (S.comp_mode) return;  // laid out once by component: no periodic re-layout
+    if (!sparse || renumber_every <= 0 || epoch % renumber_every != 0) return;
+    // The first periodic re-layout point (epoch 50 by default) chooses the
+    // layout for the rest of the fit: grouped by component when P's graph
+    // splits into small components, else the Morton order of the embedding
+    // every period. Fits shorter than a period never pay for the components.
+    if (epoch > 0 && S.comp_eligible && !S.comp_decided) {
+      S.comp_decided = true;
+      S.comp_mode = component_order(S.rows.template as<uint64_t>(), S.cols.template as<uint32_t>(), n, S.comp_order,
+                                    S.comp, &S.comp_largest, s);
+      S.comp.release();
+      t->comp_layout = S.comp_mode;
+      t->comp_largest = S.comp_largest;
+    }
     if (S.comp_mode) {
-      // component layout: once, at the fit's first epoch
-      if (epoch != 0) return;
+      // the state is in the caller's order, or in a Morton layout from epoch 0
+      // (a warm start): the component order is of CSR rows, so compose it
+      // with the current slot map
       const bool was_active = S.rn.active;
       rl_ev.resize(rl_ev.size() + 2);
       BHG_CUDA(cudaEventCreate(&rl_ev[rl_ev.size() - 2]));
       BHG_CUDA(cudaEventCreate(&rl_ev[rl_ev.size() - 1]));
       BHG_CUDA(cudaEventRecord(rl_ev[rl_ev.size() - 2], s));
-      launch_renumber<T>(D, S.comp_order.template as<uint32_t>(), n, S.rn, y, S.uy.template as<T>(),
+      const uint32_t* order = S.comp_order.template as<uint32_t>();
+      if (was_active) {
+        uint32_t* o2 = static_cast<uint32_t*>(S.comp_slots.ensure((size_t)n * 4));
+        launch_compose_order(order, S.rn.inv.template as<uint32_t>(), n, o2, s);
+        order = o2;
+      }
+      launch_renumber<T>(D, order, n, S.rn, y, S.uy.template as<T>(),
                          S.gains.template as<T>(), S.pos.template as<T>(), S.neg.template as<T>(),
                          static_cast<T*>(S.yext.ensure((size_t)n * D * sizeof(T))), S.rows.template as<uint64_t>(),
                          S.cols.template as<uint32_t>(), S.vals.template as<T>(), S.nnz, s);
@@ -446,7 +469,6 @@ void advance_impl(bhtsne_tsne* t, int64_t epochs) {
       if (!was_active) t->drop_graph();
       return;
     }
-    if (!sparse || renumber_every <= 0 || epoch % renumber_every != 0) return;
     // At epoch 0 only a caller's embedding (a warm start) has a layout worth
     // following; the seeded random start has none.
     if (epoch == 0 && !t->caller_init) return;
@@ -682,26 +704,24 @@ void run_loop(bhtsne_tsne* t, int kind, double theta) {
   t->drop_graph();
   st<T>(t).rn.active = false;  // the fit starts from y in the caller's order
   ++st<T>(t).layout_gen;
-  // Component layout for Barnes-Hut fits of large, clustered inputs:
-  // when P's graph splits into components of at most n / 4 points, group the
-  // points by component once (every row's columns then lie within its
-  // component's slots) instead of re-laying them out in Morton order every 50
-  // epochs. BHTSNE_COMPONENT_LAYOUT=0 turns it off.
+  // Component layout for Barnes-Hut fits of large, clustered inputs: at the
+  // first periodic re-layout point, when P's graph splits into components of
+  // at most n / 4 points, the points are grouped by component once (every
+  // row's columns then lie within its component's slots) instead of being
+  // re-laid out in Morton order every 50 epochs (maybe_renumber).
+  // BHTSNE_COMPONENT_LAYOUT=0 turns it off, =2 lifts the size threshold.
   {
     State<T>& S = st<T>(t);
     const char* cl = getenv("BHTSNE_COMPONENT_LAYOUT");
     const bool comp_off = cl && atoi(cl) == 0;
     const bool comp_force = cl && atoi(cl) == 2;
     S.comp_mode = false;
+    S.comp_decided = false;
     S.comp_largest = 0;
-    if (!comp_off && kind == BHTSNE_METHOD_BARNES_HUT && S.has_sparse && (t->D == 2 || t->D == 3) &&
-        (comp_force || t->n >= kComponentMinN)) {
-      S.comp_mode = component_order(S.rows.template as<uint64_t>(), S.cols.template as<uint32_t>(), t->n,
-                                    S.comp_order, S.comp, &S.comp_largest, t->ctx->stream);
-      S.comp.release();
-    }
-    t->comp_layout = S.comp_mode;
-    t->comp_largest = S.comp_largest;
+    S.comp_eligible = !comp_off && kind == BHTSNE_METHOD_BARNES_HUT && S.has_sparse && (t->D == 2 || t->D == 3) &&
+                      (comp_force || t->n >= kComponentMinN);
+    t->comp_layout = false;
+    t->comp_largest = 0;
   }
   // launch shapes of this fit: tuned for (T, D, N) on this device, or the defaults
   const TuneKnobs kn = tune_lookup(t->dtype, t->D, t->n);

@@ -262,6 +262,12 @@ __global__ void cc_max_kernel(const uint32_t* __restrict__ count, int64_t n, uns
   if ((threadIdx.x & 31) == 0) atomicMax(out, m);
 }
 
+__global__ void compose_kernel(const uint32_t* __restrict__ order, const uint32_t* __restrict__ inv, int64_t n,
+                               uint32_t* __restrict__ out) {
+  const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s < n) out[s] = inv[order[s]];
+}
+
 __global__ void invert_kernel(const uint32_t* __restrict__ ext, int64_t n, uint32_t* __restrict__ inv) {
   const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (s < n) inv[ext[s]] = (uint32_t)s;
@@ -779,6 +785,11 @@ void launch_renumber(int D, const uint32_t* order, int64_t n, Renumbering& r, T*
     BHG_LAUNCH_CHECK();
   }
   r.active = true;
+}
+
+void launch_compose_order(const uint32_t* order, const uint32_t* inv, int64_t n, uint32_t* out, cudaStream_t s) {
+  compose_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, s>>>(order, inv, n, out);
+  BHG_LAUNCH_CHECK();
 }
 
 bool component_order(const uint64_t* rows, const uint32_t* cols, int64_t n, DevBuf& order, ComponentScratch& cs,

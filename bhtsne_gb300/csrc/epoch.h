@@ -62,7 +62,8 @@ void launch_renumber(int D, const uint32_t* order, int64_t n, Renumbering& r, T*
                      T* tmp_c, const uint64_t* rows, const uint32_t* cols, const T* vals, int64_t nnz, cudaStream_t s);
 
 // Component layout: the connected components of the (symmetric) CSR graph of
-// P, found by minimum-label propagation. When the graph splits into
+// P, found by minimum-label propagation (called at a fit's first periodic
+// re-layout point). When the graph splits into
 // components of at most n / 4 points each, `order` receives the points
 // grouped by component (the component of the smallest index first), in index
 // order within each, and the call returns true. A layout in that order keeps
@@ -84,6 +85,8 @@ struct ComponentScratch {
 };
 bool component_order(const uint64_t* rows, const uint32_t* cols, int64_t n, DevBuf& order, ComponentScratch& cs,
                      int64_t* largest, cudaStream_t s);
+// out[s] = inv[order[s]]: an order of CSR rows as an order of the current slots.
+void launch_compose_order(const uint32_t* order, const uint32_t* inv, int64_t n, uint32_t* out, cudaStream_t s);
 
 // out[ext[s]] = y[s]: back to the caller's point order.
 template <class T>

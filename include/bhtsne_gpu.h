@@ -151,12 +151,13 @@ int bhtsne_tsne_phase_times(const bhtsne_tsne* t, double* ms, int64_t* epochs);
  * order of the current embedding every 50 epochs (epochs 50, 100, ...). */
 int bhtsne_tsne_relayout_times(const bhtsne_tsne* t, double* ms, int64_t* count);
 /* No reference counterpart: the layout of the last fit. *component_layout is
- * 1 when the points were grouped by connected component of P's graph once at
- * epoch 0 (Barnes-Hut fits of at least 65,536 points whose graph splits into
- * components of at most n / 4 points; no periodic Morton re-layout then), 0
- * otherwise; *largest_component is the size of P's largest component, 0 when
- * it was not computed. BHTSNE_COMPONENT_LAYOUT=0 turns the component layout
- * off, =2 also applies it below 65,536 points. */
+ * 1 when the points were grouped by connected component of P's graph, once,
+ * at the first periodic re-layout point (epoch 50; Barnes-Hut fits of at least
+ * 65,536 points whose graph splits into components of at most n / 4 points;
+ * no Morton re-layout after it), 0 otherwise; *largest_component is the size
+ * of P's largest component, 0 when it was not computed (fits shorter than a
+ * re-layout period, or not eligible). BHTSNE_COMPONENT_LAYOUT=0 turns the
+ * component layout off, =2 also applies it below 65,536 points. */
 int bhtsne_tsne_layout_info(const bhtsne_tsne* t, int32_t* component_layout, int64_t* largest_component);
 /* Number of CUDA kernel launches this library has issued since it was loaded. */
 int64_t bhtsne_launch_count(void);
