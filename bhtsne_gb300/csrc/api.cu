@@ -697,6 +697,10 @@ void advance_impl(bhtsne_tsne* t, int64_t epochs) {
     for (auto& e : ev) cudaEventDestroy(e);
     t->phase_epochs = epochs;
   }
+  // the Barnes-Hut tree builds of large fits sort with look-back waits; one
+  // that ran out (a fault, not slowness) left an unsorted tree: report it
+  if (t->loop_kind == BHTSNE_METHOD_BARNES_HUT && n >= kOnesweepMin && radix_sort_fault_take(s))
+    throw Error(ST_ETIMEDOUT, "error: a radix sort look-back wait timed out.");
 }
 
 template <class T>

@@ -147,8 +147,15 @@ constexpr size_t radix_sort_tmp_bytes(int64_t n) {
              8 +
          256;
 }
+// From kOnesweepMin to kOnesweepMax keys a pass is one kernel (decoupled
+// look-back); `tmp` then grows to hold the look-back words. A look-back wait
+// that runs out (which would mean a fault, not slow progress) raises a
+// library-wide fault word instead of hanging; radix_sort_fault_take reads and
+// clears it (synchronising s).
+constexpr int64_t kOnesweepMin = 131072, kOnesweepMax = (int64_t)1 << 24;
 template <class V>
 void radix_sort_pairs(uint64_t* keys, V* vals, uint64_t* keys_alt, V* vals_alt, int64_t n, int begin_bit,
                       int end_bit, DevBuf& tmp, cudaStream_t s);
+bool radix_sort_fault_take(cudaStream_t s);
 
 }  // namespace bhg

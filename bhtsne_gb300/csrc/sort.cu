@@ -13,6 +13,20 @@
 //    (each warp with __match_any_sync, then one prefix over warps and
 //    digits) and writes them out in sorted order, so that each digit's run
 //    is one contiguous, coalesced store.
+//
+// From 131,072 keys (the Morton codes of a large fit, every epoch) a pass is
+// one kernel instead: one histogram kernel first counts every pass's digits
+// (the key multiset is the same in every pass), and in each pass a tile takes
+// its number from an atomic counter, counts its digits, publishes them, and
+// learns the counts of all earlier tiles by decoupled look-back (Merrill and
+// Garland's single-pass prefix scan): it walks back over the earlier tiles'
+// published words, adding aggregates until it meets an inclusive prefix.
+// Tiles are numbered in the order blocks start, so every tile a block waits
+// on belongs to a block already running. Every wait is bounded; a wait that
+// runs out raises the library's sort fault word (radix_sort_fault_take)
+// instead of hanging.
+#include <cstdlib>
+
 #include "internal.h"
 
 namespace bhg {
@@ -363,7 +377,222 @@ __global__ void __launch_bounds__(kRsThreads, 4) rs_scatter_kernel(const uint64_
   }
 }
 
+// ---- single-pass variant -------------------------------------------------------
+__device__ uint32_t g_radix_fault;  // raised by a look-back wait that ran out
+
+constexpr uint32_t kOsAgg = 1u << 30;  // word holds the tile's own count
+constexpr uint32_t kOsInc = 2u << 30;  // word holds the inclusive prefix through the tile
+constexpr uint32_t kOsMask = (1u << 30) - 1u;
+constexpr long long kOsSpinLimit = 1LL << 22;
+constexpr int kOsMaxPass = 8;
+
+// Digit counts of passes 0 .. npass-1 (digit shift begin_bit + 8 q) in one read.
+__global__ void __launch_bounds__(256) os_hist_kernel(const uint64_t* __restrict__ keys, int64_t n, int begin_bit,
+                                                      int npass, uint32_t* __restrict__ ghist) {
+  __shared__ uint32_t h[kOsMaxPass][256];
+  for (int i = threadIdx.x; i < kOsMaxPass * 256; i += blockDim.x) h[i / 256][i % 256] = 0;
+  __syncthreads();
+  for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x) {
+    const uint64_t k = keys[p];
+    for (int q = 0; q < npass; ++q) atomicAdd(&h[q][(unsigned)(k >> (begin_bit + 8 * q)) & 255u], 1u);
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < npass * 256; i += blockDim.x) {
+    const uint32_t c = h[i / 256][i % 256];
+    if (c) atomicAdd(&ghist[i], c);
+  }
+}
+
+// Exclusive scan of each pass's 256 digit counts (block q: pass q).
+__global__ void __launch_bounds__(256) os_base_kernel(const uint32_t* __restrict__ ghist, uint32_t* __restrict__ base) {
+  __shared__ uint32_t wt[8];
+  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+  const uint32_t v = ghist[blockIdx.x * 256 + tid];
+  uint32_t x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(kFull, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) wt[w] = x;
+  __syncthreads();
+  uint32_t add = 0;
+  for (int q = 0; q < w; ++q) add += wt[q];
+  base[blockIdx.x * 256 + tid] = x - v + add;
+}
+
+__device__ __forceinline__ uint32_t os_load(const uint32_t* p) {
+  uint32_t v;
+  asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void os_store(uint32_t* p, uint32_t v) {
+  asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// One pass: tile number from *ticket, stable rank in shared memory as in
+// rs_scatter_kernel, output offsets from the pass's digit bases plus the
+// counts of the earlier tiles (look-back over status, one word per tile and
+// digit), coalesced write-out.
+template <class V>
+__global__ void __launch_bounds__(kRsThreads, 4) os_pass_kernel(const uint64_t* __restrict__ kin, const V* __restrict__ vin,
+                                                             uint64_t* __restrict__ kout, V* __restrict__ vout, int64_t n,
+                                                             int shift, const uint32_t* __restrict__ dbase,
+                                                             uint32_t* __restrict__ status, uint32_t* __restrict__ ticket) {
+  __shared__ RsSmem<V> sm;
+  __shared__ uint32_t tile_no;
+  const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
+  const unsigned lt = (1u << lane) - 1u;
+  if (tid == 0) tile_no = atomicAdd(ticket, 1u);
+#pragma unroll
+  for (int q = 0; q < kRsWarps; ++q) sm.wcnt[q][tid] = 0;
+  __syncthreads();
+  const int64_t b = tile_no;
+  const int64_t tile = b * kRsTile;
+  const int64_t wbase = tile + (int64_t)w * kRsWarpSpan;
+  uint64_t k[kRsRounds];
+  V v[kRsRounds];
+  uint32_t rk[kRsRounds];
+#pragma unroll
+  for (int r = 0; r < kRsRounds; ++r) {
+    const int64_t p = wbase + r * 32 + lane;
+    k[r] = 0;
+    v[r] = V{};
+    if (p < n) {
+      k[r] = kin[p];
+      v[r] = vin[p];
+    }
+  }
+#pragma unroll
+  for (int r = 0; r < kRsRounds; ++r) {
+    const int64_t p = wbase + r * 32 + lane;
+    const unsigned d = p < n ? ((unsigned)(k[r] >> shift) & 255u) : 256u;
+    const unsigned peers = __match_any_sync(kFull, d);
+    const uint32_t prior = d < 256u ? sm.wcnt[w][d] : 0u;
+    __syncwarp();
+    if (d < 256u && lane == __ffs(peers) - 1) sm.wcnt[w][d] = prior + (uint32_t)__popc(peers);
+    __syncwarp();
+    rk[r] = prior + (uint32_t)__popc(peers & lt);
+  }
+  __syncthreads();
+  // thread tid owns digit tid: the tile's count, offsets across warps
+  uint32_t tot = 0;
+#pragma unroll
+  for (int q = 0; q < kRsWarps; ++q) {
+    const uint32_t c = sm.wcnt[q][tid];
+    sm.wcnt[q][tid] = tot;
+    tot += c;
+  }
+  // publish, look back, publish the inclusive prefix
+  uint32_t* st = status + b * 256 + tid;
+  uint32_t excl = 0;
+  if (b == 0) {
+    os_store(st, kOsInc | tot);
+  } else {
+    os_store(st, kOsAgg | tot);
+    for (int64_t pb = b - 1; pb >= 0; --pb) {
+      const uint32_t* sp = status + pb * 256 + tid;
+      uint32_t word = os_load(sp);
+      long long spins = 0;
+      while ((word & ~kOsMask) == 0u) {
+        if (++spins >= kOsSpinLimit) {
+          atomicExch(&g_radix_fault, 1u);
+          break;
+        }
+        word = os_load(sp);
+      }
+      excl += word & kOsMask;
+      if ((word & ~kOsMask) != kOsAgg) break;  // an inclusive prefix (or a wait that ran out)
+    }
+    os_store(st, kOsInc | (excl + tot));
+  }
+  sm.gbase[tid] = (uint64_t)dbase[tid] + excl;
+  {
+    uint32_t x = tot;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(kFull, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) sm.wtot[w] = x;
+    __syncthreads();
+    uint32_t add = 0;
+    for (int q = 0; q < w; ++q) add += sm.wtot[q];
+    sm.tstart[tid] = x - tot + add;
+  }
+  __syncthreads();
+#pragma unroll
+  for (int r = 0; r < kRsRounds; ++r) {
+    const int64_t p = wbase + r * 32 + lane;
+    if (p < n) {
+      const unsigned d = (unsigned)(k[r] >> shift) & 255u;
+      const uint32_t lp = sm.tstart[d] + sm.wcnt[w][d] + rk[r];
+      sm.key[lp] = k[r];
+      sm.val[lp] = v[r];
+    }
+  }
+  __syncthreads();
+  const int64_t left = n - tile;
+  const int cnt = left < kRsTile ? (int)left : kRsTile;
+#pragma unroll 4
+  for (int i = tid; i < cnt; i += kRsThreads) {
+    const uint64_t key = sm.key[i];
+    const unsigned d = (unsigned)(key >> shift) & 255u;
+    const uint64_t gp = sm.gbase[d] + (uint64_t)(i - (int)sm.tstart[d]);
+    kout[gp] = key;
+    vout[gp] = sm.val[i];
+  }
+}
+
 }  // namespace
+
+// Bytes the single-pass variant keeps in the sort's scratch: the tickets, the
+// digit counts and bases of every pass, then the look-back words of every pass
+// (one per tile and digit).
+static size_t os_tmp_bytes(int64_t n, int npass) {
+  const int64_t nb = ceil_div(n, kRsTile);
+  return 256 + (size_t)2 * kOsMaxPass * 256 * 4 + (size_t)npass * nb * 256 * 4;
+}
+
+bool radix_sort_fault_take(cudaStream_t s) {
+  uint32_t h = 0, zero = 0;
+  BHG_CUDA(cudaMemcpyFromSymbolAsync(&h, g_radix_fault, 4, 0, cudaMemcpyDeviceToHost, s));
+  BHG_CUDA(cudaMemcpyToSymbolAsync(g_radix_fault, &zero, 4, 0, cudaMemcpyHostToDevice, s));
+  BHG_CUDA(cudaStreamSynchronize(s));
+  return h != 0;
+}
+
+template <class V>
+static void radix_sort_onesweep(uint64_t* keys, V* vals, uint64_t* keys_alt, V* vals_alt, int64_t n, int begin_bit,
+                                int end_bit, DevBuf& tmp, cudaStream_t s) {
+  const int npass = (end_bit - begin_bit + 7) / 8;
+  const int64_t nb = ceil_div(n, kRsTile);
+  char* base = static_cast<char*>(tmp.ensure(std::max(os_tmp_bytes(n, npass), radix_sort_tmp_bytes(n))));
+  uint32_t* tickets = reinterpret_cast<uint32_t*>(base) + 8;    // words 8 .. 15
+  uint32_t* ghist = reinterpret_cast<uint32_t*>(base + 256);
+  uint32_t* dbase = ghist + kOsMaxPass * 256;
+  uint32_t* status = dbase + kOsMaxPass * 256;
+  // tickets, counts and look-back words start at zero (one memset; the fault word is left alone)
+  BHG_CUDA(cudaMemsetAsync(tickets, 0, 256 - 32 + (size_t)2 * kOsMaxPass * 256 * 4 + (size_t)npass * nb * 256 * 4, s));
+  os_hist_kernel<<<(unsigned)std::min<int64_t>(ceil_div(n, 256), sm_grid(4, 4096)), 256, 0, s>>>(keys, n, begin_bit,
+                                                                                               npass, ghist);
+  BHG_LAUNCH_CHECK();
+  os_base_kernel<<<(unsigned)npass, 256, 0, s>>>(ghist, dbase);
+  BHG_LAUNCH_CHECK();
+  uint64_t *ki = keys, *ko = keys_alt;
+  V *vi = vals, *vo = vals_alt;
+  for (int q = 0; q < npass; ++q) {
+    os_pass_kernel<V><<<(unsigned)nb, kRsThreads, 0, s>>>(ki, vi, ko, vo, n, begin_bit + 8 * q, dbase + q * 256,
+                                                          status + (int64_t)q * nb * 256, tickets + q);
+    BHG_LAUNCH_CHECK();
+    std::swap(ki, ko);
+    std::swap(vi, vo);
+  }
+  if (npass & 1) {
+    BHG_CUDA(cudaMemcpyAsync(keys, ki, (size_t)n * sizeof(uint64_t), cudaMemcpyDeviceToDevice, s));
+    BHG_CUDA(cudaMemcpyAsync(vals, vi, (size_t)n * sizeof(V), cudaMemcpyDeviceToDevice, s));
+  }
+}
 
 void scan_u32_to_u64(const uint32_t* in, uint64_t* out, int64_t n, DevBuf& tmp, cudaStream_t s) {
   scan_impl<uint32_t>(in, out, n, tmp, s);
@@ -377,6 +606,14 @@ template <class V>
 void radix_sort_pairs(uint64_t* keys, V* vals, uint64_t* keys_alt, V* vals_alt, int64_t n, int begin_bit,
                       int end_bit, DevBuf& tmp, cudaStream_t s) {
   if (n <= 1 || begin_bit >= end_bit) return;
+  // BHTSNE_SORT_ONESWEEP=0 keeps the three-kernel passes at every size (for
+  // comparing the two; both are stable, so they give the same permutation)
+  const char* os_env = getenv("BHTSNE_SORT_ONESWEEP");
+  const bool os_off = os_env && atoi(os_env) == 0;
+  if (!os_off && n >= kOnesweepMin && n <= kOnesweepMax && end_bit - begin_bit <= 8 * kOsMaxPass) {
+    radix_sort_onesweep<V>(keys, vals, keys_alt, vals_alt, n, begin_bit, end_bit, tmp, s);
+    return;
+  }
   static_assert(kRsTile == kRadixTile && kRsSup == kRadixSup && kScanTile == kRadixScanTile,
                 "radix_sort_tmp_bytes describes this layout");
   const int64_t nb = ceil_div(n, kRsTile);
