@@ -470,8 +470,11 @@ void advance_impl(bhtsne_tsne* t, int64_t epochs) {
       return;
     }
     // At epoch 0 only a caller's embedding (a warm start) has a layout worth
-    // following; the seeded random start has none.
-    if (epoch == 0 && !t->caller_init) return;
+    // following; the seeded random start has none. A re-layout costs about as
+    // much as the attractive passes of a re-layout period save, so a warm
+    // start that runs fewer epochs than one period (in this call: a finisher
+    // or an advance) keeps the caller's order.
+    if (epoch == 0 && (!t->caller_init || epochs < renumber_every)) return;
     if (D < 2 || D > 3) return;
     rl_ev.resize(rl_ev.size() + 2);
     BHG_CUDA(cudaEventCreate(&rl_ev[rl_ev.size() - 2]));
