@@ -288,9 +288,9 @@ def run_ours(args):
     }
     achieved = alg[dom] / (per[dom] / 1e3) / 1e9
     # DRAM bytes (read + write) per launch from one ncu capture of the same
-    # kernel at N = 300,000 (429.7 MB for 52.5M CSR entries), scaled by this
-    # run's entries; null for the other phases
-    traffic = {"attractive": int(429.7e6 * nnz / 52.5e6)}
+    # kernel at N = 300,000 in the component layout (435.7 MB for 52,492,156
+    # CSR entries), scaled by this run's entries; null for the other phases
+    traffic = {"attractive": int(435.65e6 * nnz / 52492156)}
     roofline = {"kernel": {"repulsion": "bh_traverse_kernel", "attractive": "attractive_task_kernel+attractive_fixup_kernel",
                            "update": "update_kernel+recenter_bbox_kernel", "tree": "morton+radix sort+tree build"}[dom],
                 "bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
@@ -685,6 +685,24 @@ def run_batched(args, ctx):
     }
 
 
+def run_batched_only(args, ctx):
+    """The batched arm of the 512-job comparison alone (the same jobs, settings
+    and seed as run_batched), for launch lists and profiles."""
+    import bhtsne_gb300 as bg
+    data = make_batch_workload(args.batch_jobs)
+    w0 = time.perf_counter()
+    b = bg.Batch(perplexity=30.0, epochs=args.batch_epochs, theta=0.5, seed=11, ctx=ctx)
+    for X in data:
+        b.add(X)
+    b.fit()
+    for j in range(len(data)):
+        b.embedding(j)
+    aff_ms, loop_ms = b.timings()
+    b.close()
+    return {"jobs": len(data), "points": int(sum(len(x) for x in data)), "epochs": args.batch_epochs,
+            "total_s": round(time.perf_counter() - w0, 3), "affinity_ms": round(aff_ms, 1), "loop_ms": round(loop_ms, 1)}
+
+
 def make_serving_workload(requests, seed=2025):
     """Requests with N log-uniform in [1000, 300000], input dim 50, each a
     10-component Gaussian mixture (centres ~ N(0, 10^2 I), unit variance);
@@ -898,6 +916,7 @@ def main():
     ap.add_argument("--serve-budget-gb", type=float, default=0.0,
                     help="server admission budget in GB (0: 90%% of free device memory)")
     ap.add_argument("--serve-only", action="store_true", help="run only the serving comparison")
+    ap.add_argument("--batch-only", action="store_true", help="run only the batched arm of the batch comparison")
     ap.add_argument("--knn-only", action="store_true", help="time only the kNN of the workload at --n points")
     ap.add_argument("--fft-only", action="store_true",
                     help="time only the FIt-SNE repulsion of --n points at the largest grid")
@@ -912,6 +931,10 @@ def main():
     if args.serve_only:
         import bhtsne_gb300 as bg
         print(json.dumps({"serving": run_serving(args, bg.Context(0))}))
+        return
+    if args.batch_only:
+        import bhtsne_gb300 as bg
+        print(json.dumps({"batched_arm": run_batched_only(args, bg.Context(0))}))
         return
     if args.warmup < 3:
         args.warmup = 3
