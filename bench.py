@@ -884,13 +884,17 @@ def run_knn_only(args):
     """The affinity build's kNN alone on the 1M workload's distribution at --n
     points (k = 90): a 2,000-row warm-up call, then all rows, timed on the host."""
     import bhtsne_gb300 as bg
+    from bhtsne_gb300 import _lib as L
     X, _ = make_workload(args.n, seed=args.seed)
     bg.knn_euclidean(X[:2000], 90)
     w0 = time.perf_counter()
     bg.knn_euclidean(X, 90)
     el = time.perf_counter() - w0
+    staged = os.environ.get("BHTSNE_KNN_TC_STAGED", "0") not in ("", "0")
     print(json.dumps({"metric": "exact kNN seconds (k = 90)", "value": round(el, 4), "unit": "s",
-                      "higher_is_better": False, "config": {"n_points": args.n, "input_dim": 128, "k": 90}}))
+                      "higher_is_better": False, "fallback_rows": L.default_context().knn_fallback_rows(),
+                      "candidate_pass": "staged" if staged else "resident",
+                      "config": {"n_points": args.n, "input_dim": 128, "k": 90}}))
 
 
 def main():

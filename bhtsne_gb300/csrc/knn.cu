@@ -36,6 +36,11 @@ constexpr int CB = 128;   // candidates per tile
 constexpr int DK = 32;    // dimensions per candidate chunk
 constexpr int kThreads = 256;
 constexpr uint32_t SENT = 0xffffffffu;
+// sliced certified fallback: at most kMaxSlices slices of at least kMinSlice
+// candidates, scratch of at most kSliceScratchMax bytes
+constexpr int kMaxSlices = 16;
+constexpr int64_t kMinSlice = 4096;
+constexpr size_t kSliceScratchMax = (size_t)1 << 30;
 
 __global__ void sq_norm_kernel(const float* __restrict__ X, int64_t n, int dim, float* __restrict__ norms,
                                unsigned* __restrict__ max_bits) {
@@ -116,6 +121,12 @@ __device__ void warp_insert(V* lv, uint32_t* li, int* len_p, int cap, V v, uint3
 // independent point sets back to back, set j owning rows seg_off[j]..
 // seg_off[j+1]; block b takes the queries blk_q0[b].. of set blk_job[b] and
 // scans that set's rows only. Indices stay global.
+//
+// Sliced form (slice_len > 0, EXACT with qrows only): block (x, y) scans the
+// candidates y slice_len .. (y + 1) slice_len - 1 only and writes its list of
+// `cap` (index, distance), padded with (SENT, +inf), to row r = x QB + q of
+// slice_idx / slice_val at [(r gridDim.y + y) cap]; slice_merge_kernel then
+// merges the slices' lists.
 template <int C, bool EXACT>
 __global__ void __launch_bounds__(kThreads, 1) knn_tile_kernel(const float* __restrict__ X, int64_t n, int dim,
                                                                const float* __restrict__ norms,
@@ -124,7 +135,10 @@ __global__ void __launch_bounds__(kThreads, 1) knn_tile_kernel(const float* __re
                                                                float* __restrict__ out_val,
                                                                const int64_t* __restrict__ blk_q0 = nullptr,
                                                                const int32_t* __restrict__ blk_job = nullptr,
-                                                               const int64_t* __restrict__ seg_off = nullptr) {
+                                                               const int64_t* __restrict__ seg_off = nullptr,
+                                                               int64_t slice_len = 0,
+                                                               uint32_t* __restrict__ slice_idx = nullptr,
+                                                               float* __restrict__ slice_val = nullptr) {
   extern __shared__ __align__(16) unsigned char smem[];
   float* Qs = reinterpret_cast<float*>(smem);
   float* Cs = Qs + (size_t)dim * QB;
@@ -149,6 +163,10 @@ __global__ void __launch_bounds__(kThreads, 1) knn_tile_kernel(const float* __re
     if (blk_q0) qidx[tid] = r < hi ? r : -1;
     else qidx[tid] = r < nq ? (qrows ? (int64_t)qrows[r] : r) : -1;
     len[tid] = 0;
+  }
+  if (slice_len > 0) {
+    lo = (int64_t)blockIdx.y * slice_len;
+    hi = lo + slice_len < n ? lo + slice_len : n;
   }
   __syncthreads();
   for (int e = tid; e < QB * dim; e += kThreads) {
@@ -276,7 +294,13 @@ __global__ void __launch_bounds__(kThreads, 1) knn_tile_kernel(const float* __re
     const int64_t qi = qidx[q];
     if (qi < 0) continue;
     const int L = len[q];
-    if (EXACT) {
+    if (EXACT && slice_len > 0) {
+      const size_t base = ((size_t)(q0 + q) * gridDim.y + blockIdx.y) * cap;
+      for (int t = lane; t < cap; t += 32) {
+        slice_idx[base + t] = t < L ? li[q * C + t] : SENT;
+        slice_val[base + t] = t < L ? lv[q * C + t] : INFINITY;
+      }
+    } else if (EXACT) {
       for (int t = lane; t < cap; t += 32) {
         out_idx[qi * cap + t] = li[q * C + t];
         out_val[qi * cap + t] = lv[q * C + t];
@@ -284,6 +308,42 @@ __global__ void __launch_bounds__(kThreads, 1) knn_tile_kernel(const float* __re
     } else {
       for (int t = lane; t < C; t += 32) out_idx[qi * C + t] = t < L ? li[q * C + t] : SENT;
       if (lane == 0) out_val[qi] = L == C ? lv[q * C + C - 1] : INFINITY;
+    }
+  }
+}
+
+// Merge of the sliced fallback's lists: one warp per listed row; lane l < S
+// follows slice l's sorted list, and each of the k steps takes the smallest
+// head (distance bits, index) over the warp. Distances are >= 0, so their
+// bit patterns order like the values; (SENT, +inf) pads sort last.
+__global__ void slice_merge_kernel(const uint32_t* __restrict__ slice_idx, const float* __restrict__ slice_val,
+                                   const uint32_t* __restrict__ rows, int64_t nrows, int S, int k,
+                                   uint32_t* __restrict__ out_idx, float* __restrict__ out_dist) {
+  const int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (r >= nrows) return;
+  const int64_t qi = rows[r];
+  const size_t base = ((size_t)r * S + (lane < S ? lane : 0)) * k;
+  int p = 0;
+  auto head = [&]() -> unsigned long long {
+    if (lane >= S || p >= k) return ~0ull;
+    return ((unsigned long long)__float_as_uint(slice_val[base + p]) << 32) | slice_idx[base + p];
+  };
+  unsigned long long h = head();
+  for (int t = 0; t < k; ++t) {
+    unsigned long long m = h;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const unsigned long long x = __shfl_xor_sync(kFull, m, o);
+      m = x < m ? x : m;
+    }
+    if (lane == 0) {
+      out_idx[qi * k + t] = (uint32_t)(m & 0xffffffffull);
+      out_dist[qi * k + t] = __uint_as_float((uint32_t)(m >> 32));
+    }
+    if (h == m) {
+      ++p;
+      h = head();
     }
   }
 }
@@ -673,7 +733,7 @@ int64_t knn_euclidean(const T* X, int64_t n, int dim, int k, uint32_t* out_idx, 
   const unsigned grid = (unsigned)ceil_div(n, QB);
   const double simt_coef = (4.0 * dim + 16.0) / 16777216.0;
   if (C == 128 && (ws.pass == 0 || (ws.pass < 0 && use_tensor_cores()))) {
-    knn_tc_candidates(Xf, n, dim, norms, nullptr, nullptr, nullptr, ceil_div(n, 128), cand, thr, ws.tc, s);
+    knn_tc_candidates(Xf, n, dim, norms, nullptr, nullptr, nullptr, nullptr, ceil_div(n, 128), cand, thr, ws.tc, s);
     knn_rerank_kernel<T, 128><<<(unsigned)ceil_div(n, 4), 128, 0, s>>>(X, n, dim, k, cand, thr, norms, max_bits, out_idx,
                                                                        out_dist, fails, fail_count,
                                                                        knn_tc_error_coef(dim));
@@ -701,19 +761,52 @@ int64_t knn_euclidean(const T* X, int64_t n, int dim, int k, uint32_t* out_idx, 
   unsigned nfail = 0;
   BHG_CUDA(cudaMemcpyAsync(&nfail, fail_count, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
   BHG_CUDA(cudaStreamSynchronize(s));
+  ws.last_fallback_slices = 1;
   if (nfail > 0) {
     if constexpr (std::is_same<T, float>::value) {
       // certified fallback: the same tiled kernel computing the reference's
       // exact distances for the failing rows only
+      // With few failing rows (under a few waves of blocks) the candidate
+      // range is split into S slices, each block scanning one slice, and the
+      // slices' lists merged: S chosen to minimise the waves per slice length.
       const unsigned fgrid = (unsigned)ceil_div(nfail, QB);
+      const int sms = device_sm_count();
+      int S = 1;
+      double best = (double)ceil_div((int64_t)fgrid, sms);
+      for (int cand_s = 2; cand_s <= kMaxSlices; ++cand_s) {
+        if (n / cand_s < kMinSlice || (size_t)nfail * cand_s * k * 8 > kSliceScratchMax) break;
+        const double waves = (double)ceil_div((int64_t)fgrid * cand_s, sms) / cand_s;
+        if (waves < best - 1e-9) {
+          best = waves;
+          S = cand_s;
+        }
+      }
+      int64_t slice_len = 0;
+      uint32_t* sidx = nullptr;
+      float* sval = nullptr;
+      if (S > 1) {
+        slice_len = ceil_div(ceil_div(n, S), CB) * CB;
+        S = (int)ceil_div(n, slice_len);
+        sidx = static_cast<uint32_t*>(ws.slices.ensure((size_t)nfail * S * k * 8));
+        sval = reinterpret_cast<float*>(sidx + (size_t)nfail * S * k);
+      }
+      const dim3 g2(fgrid, (unsigned)S);
       if (C == 128) {
         BHG_CUDA(cudaFuncSetAttribute(knn_tile_kernel<128, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        knn_tile_kernel<128, true><<<fgrid, kThreads, smem, s>>>(X, n, dim, norms, fails, nfail, k, out_idx, out_dist);
+        knn_tile_kernel<128, true><<<g2, kThreads, smem, s>>>(X, n, dim, norms, fails, nfail, k, out_idx, out_dist,
+                                                              nullptr, nullptr, nullptr, slice_len, sidx, sval);
       } else {
         BHG_CUDA(cudaFuncSetAttribute(knn_tile_kernel<256, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        knn_tile_kernel<256, true><<<fgrid, kThreads, smem, s>>>(X, n, dim, norms, fails, nfail, k, out_idx, out_dist);
+        knn_tile_kernel<256, true><<<g2, kThreads, smem, s>>>(X, n, dim, norms, fails, nfail, k, out_idx, out_dist,
+                                                              nullptr, nullptr, nullptr, slice_len, sidx, sval);
       }
       BHG_LAUNCH_CHECK();
+      if (S > 1) {
+        slice_merge_kernel<<<(unsigned)ceil_div((int64_t)nfail * 32, 256), 256, 0, s>>>(sidx, sval, fails, nfail, S, k,
+                                                                                        out_idx, out_dist);
+        BHG_LAUNCH_CHECK();
+      }
+      ws.last_fallback_slices = S;
     } else {
       const size_t esmem = (size_t)4 * k * (sizeof(T) + sizeof(uint32_t));
       if (esmem > 48 * 1024)
@@ -789,7 +882,7 @@ int64_t knn_euclidean_segmented(const T* X, int64_t total, int dim, int k, const
     int32_t* t_bj = reinterpret_cast<int32_t*>(t_q0 + tn);
     BHG_CUDA(cudaMemcpyAsync(t_q0, tq0.data(), (size_t)tn * 8, cudaMemcpyHostToDevice, s));
     BHG_CUDA(cudaMemcpyAsync(t_bj, tbj.data(), (size_t)tn * 4, cudaMemcpyHostToDevice, s));
-    knn_tc_candidates(Xf, total, dim, norms, t_q0, t_bj, d_off, tn, cand, thr, ws.tc, s);
+    knn_tc_candidates(Xf, total, dim, norms, t_q0, t_bj, d_off, &off, tn, cand, thr, ws.tc, s);
     knn_rerank_kernel<T, 128><<<(unsigned)ceil_div(total, 4), 128, 0, s>>>(X, total, dim, k, cand, thr, norms, max_bits,
                                                                            out_idx, out_dist, fails, fail_count,
                                                                            knn_tc_error_coef(dim));

@@ -9,9 +9,10 @@
 namespace bhg {
 
 struct KnnWorkspace {
-  DevBuf xf, norms, cand, thr, fails, counters, blk, tc_blk;
+  DevBuf xf, norms, cand, thr, fails, counters, blk, tc_blk, slices;
   KnnTcScratch tc;
   int64_t last_fallback_rows = 0;
+  int last_fallback_slices = 1;  // candidate slices of the last certified fallback
   // candidate pass: -1 the default (tensor cores unless BHTSNE_KNN_SIMT is
   // set), 0 tensor cores, 1 CUDA cores; both give the same neighbours
   int pass = -1;
@@ -23,6 +24,7 @@ struct KnnWorkspace {
     fails.release();
     blk.release();
     tc_blk.release();
+    slices.release();
     tc.release();
   }
 };

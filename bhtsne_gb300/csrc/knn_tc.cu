@@ -10,14 +10,22 @@
 // this pass's error bound, so the neighbour lists stay exact.
 //
 // One CTA = 128 queries (one per selection thread and per tensor-memory
-// lane) against every candidate row of its point set, in tiles of 128; see
-// knn_tc_pipe_kernel for the warp roles. Operand tiles use the no-swizzle
-// K-major core-matrix layout (8 rows x 16 bytes per core matrix). Every wait
-// on an mbarrier is bounded; on timeout the CTA raises the error flag, stops
-// issuing work and releases its tensor memory.
+// lane) against every candidate row of its point set, in tiles of 128. Two
+// forms compute the same products in the same order:
+//  - resident (rows of at most 128 dimensions): the query tile's hi / lo
+//    parts sit in tensor memory for the whole CTA (the MMA's A operand), and
+//    the candidate tiles come, split into hi / lo in advance, by bulk copies
+//    (TMA engine) into a 4-deep shared-memory ring;
+//  - staged (wider rows): producer warps split query and candidate chunks
+//    from the FP32 rows into a 2-deep ring for every candidate tile.
+// Operand tiles in shared memory use the no-swizzle K-major core-matrix
+// layout (8 rows x 16 bytes per core matrix). Every wait on an mbarrier is
+// bounded; on timeout the CTA raises the error flag, stops issuing work, waits
+// (bounded) for its copies and MMAs in flight and releases its tensor memory.
 #include "knn_tc.h"
 
 #include <cfloat>
+#include <cstdlib>
 
 namespace bhg {
 
@@ -49,11 +57,21 @@ __device__ __forceinline__ uint64_t make_desc(uint32_t addr, uint32_t lbo, uint3
 // K-major, N = TC, M = TQ.
 constexpr uint32_t kIdesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(TC >> 3) << 17) | ((uint32_t)(TQ >> 4) << 24);
 
+// A and B from shared memory
 __device__ __forceinline__ void mma_tf32(uint32_t tmem, uint64_t a, uint64_t b, uint32_t accumulate) {
   asm volatile(
       "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
       "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem),
       "l"(a), "l"(b), "r"(kIdesc), "r"(accumulate));
+}
+
+// A from tensor memory (row i of A in lane i, one element per column), B from
+// shared memory
+__device__ __forceinline__ void mma_tf32_ta(uint32_t tmem, uint32_t a_tmem, uint64_t b, uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::tf32 [%0], [%1], %2, %3, p;\n\t}\n" ::"r"(tmem),
+      "r"(a_tmem), "l"(b), "r"(kIdesc), "r"(accumulate));
 }
 
 __device__ __forceinline__ void mma_commit(uint32_t mbar) {
@@ -70,8 +88,45 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t mbar, uint32_t parity) {
   return ok != 0;
 }
 
+__device__ __forceinline__ void mbar_arrive(uint32_t mbar) {
+  asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}\n" ::"r"(mbar) : "memory");
+}
+
+// Bounded wait; false (and the abort flag raised) when it runs out or
+// another role already aborted.
+__device__ __forceinline__ bool mbar_wait_bounded(uint32_t mbar, uint32_t parity, volatile int* abort_flag, int* err) {
+  long long spins = 0;
+  while (!mbar_try_wait(mbar, parity)) {
+    if (*abort_flag) return false;
+    if (++spins >= kSpinLimit) {
+      *abort_flag = 1;
+      atomicExch(err, 1);
+      return false;
+    }
+  }
+  return true;
+}
+
+// Bounded wait that ignores the abort flag: the exit path's wait for work
+// already in flight (copies, MMAs), which completes whatever the other roles do.
+__device__ __forceinline__ void mbar_drain(uint32_t mbar, uint32_t parity, int* err) {
+  long long spins = 0;
+  while (!mbar_try_wait(mbar, parity)) {
+    if (++spins >= kSpinLimit) {
+      atomicExch(err, 1);
+      return;
+    }
+  }
+}
+
 __device__ __forceinline__ bool lt_vi(float a, uint32_t ai, float b, uint32_t bi) {
   return a < b || (a == b && ai < bi);
+}
+
+__device__ __forceinline__ float tf32_hi(float x) {
+  uint32_t b = __float_as_uint(x);
+  if ((b & 0x7f800000u) != 0x7f800000u) b = (b + 0x1000u) & 0xffffe000u;
+  return __uint_as_float(b);
 }
 
 // Max-heap of (value, index) per thread, element i of thread t at [i * TQ + t].
@@ -116,59 +171,173 @@ __device__ __forceinline__ void heap_push(float* hv, uint32_t* hi, int t, int& c
   hi[i * TQ + t] = x;
 }
 
+constexpr int PK = 16;                     // dimensions per ring stage
+constexpr int kSubTile = TQ * PK * 4;      // 8 KB: 128 rows x 16 dims
+constexpr int kBuf = 32;                   // pending candidates per query between heap merges
+constexpr int kLd = 16;                    // accumulator columns read per tcgen05.ld
+constexpr size_t kSelSmem = (size_t)HEAPC * TQ * 8 + (size_t)kBuf * TQ * 8;  // heaps + pending lists
+
+// staged form
+constexpr int NST = 2;                     // ring depth
+constexpr int kProducers = 96;
+constexpr int kPipeThreads = 256;
+constexpr int kStageBytes = 4 * kSubTile;  // query hi, query lo, candidate hi, candidate lo
+constexpr size_t kPipeSmem = kSelSmem + (size_t)NST * kStageBytes;
+
+// resident form
+constexpr int NSR = 4;                     // ring depth
+constexpr int kResThreads = 192;
+constexpr int kResStage = 2 * kSubTile;    // candidate hi, candidate lo: 16 KB
+constexpr size_t kResSmem = kSelSmem + (size_t)NSR * kResStage;
+constexpr int kResDimMax = 128;
+// tensor-memory columns: accumulators 0 .. 2 TC - 1, then the query tile's hi
+// and lo parts, kResDimMax columns each (512 in all)
+constexpr uint32_t kColQhi = 2 * TC, kColQlo = 2 * TC + kResDimMax, kResCols = 2 * TC + 2 * kResDimMax;
+static_assert(kResCols == 512, "the resident form takes the whole tensor memory of its SM");
+static_assert(kResSmem <= 227 * 1024 && kPipeSmem <= 227 * 1024, "shared memory per CTA");
+
 // ---------------------------------------------------------------------------
-// Pipelined form. 8 warps split the work:
-//   warps 0-3  selection: thread t owns query row t (TMEM lane t), reads the
-//              128 dot products of a finished tile from one of two TMEM
-//              accumulators and keeps its best 128 in a max-heap in shared
-//              memory (the fast path compares against the root in registers);
+// Selection role (warps 0-3, thread t = query row q0 + t = TMEM lane t): reads
+// the 128 dot products d of a finished tile from one of two TMEM accumulators,
+// forms v = (|q|^2 + |c|^2) - 2 d and keeps its best 128 (value, index) in a
+// max-heap in shared memory. Candidates that beat the current 128-th best
+// (the heap root, in registers) are appended to a per-thread pending list;
+// when any lane's list could overflow on the next read, the whole warp merges
+// its lists into the heaps together, so lanes insert in lockstep instead of
+// one divergent heap update per candidate. Tiles that lie wholly inside the
+// point set and do not hold the CTA's own queries (every tile but the
+// diagonal one and a partial last one) take a path without index checks;
+// tnorm, when given, holds each split tile's 128 squared norms (read as
+// float4). Writes the sorted list and the threshold of its query.
+// ---------------------------------------------------------------------------
+__device__ void selection_role(uint32_t tmem, uint64_t* acc_full, uint64_t* acc_free, unsigned char* smem, int64_t q0,
+                               int64_t lo, int64_t hi, int64_t ntiles, const float* __restrict__ norms,
+                               const float* __restrict__ tnorm, int64_t tb, uint32_t* __restrict__ out_idx,
+                               float* __restrict__ out_thr, volatile int* abort_flag, int* err) {
+  float* hv = reinterpret_cast<float*>(smem);
+  uint32_t* hx = reinterpret_cast<uint32_t*>(hv + HEAPC * TQ);
+  uint2* pend = reinterpret_cast<uint2*>(hx + HEAPC * TQ);  // [kBuf][TQ] pending (value bits, index)
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const int64_t qi = q0 + tid;
+  const bool qvalid = qi < hi;
+  const float qn = qvalid ? norms[qi] : 0.f;
+  int cnt = 0, np = 0;
+  float rootv = INFINITY;
+  uint32_t rootx = SENTI;
+  auto merge = [&]() {
+    const int rounds = __reduce_max_sync(0xffffffffu, (unsigned)np);
+    for (int i = 0; i < rounds; ++i) {
+      if (i < np) {
+        const uint2 e = pend[i * TQ + tid];
+        const float v = __uint_as_float(e.x);
+        if (cnt < HEAPC) {
+          heap_push(hv, hx, tid, cnt, v, e.y);
+        } else if (lt_vi(v, e.y, hv[tid], hx[tid])) {
+          hv[tid] = v;
+          hx[tid] = e.y;
+          heap_sift_down(hv, hx, tid, cnt, 0);
+        }
+      }
+    }
+    np = 0;
+    if (cnt == HEAPC) {
+      rootv = hv[tid];
+      rootx = hx[tid];
+    }
+  };
+  for (int64_t t = 0; t < ntiles; ++t) {
+    const int b = (int)(t & 1);
+    if (!mbar_wait_bounded(smem_u32(&acc_full[b]), (uint32_t)((t >> 1) & 1), abort_flag, err)) break;
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const int64_t c0 = lo + t * TC;
+    const bool fast = c0 + TC <= hi && (c0 + TC <= q0 || q0 + TQ <= c0);  // uniform over the CTA
+#pragma unroll 1
+    for (int cb = 0; cb < TC; cb += kLd) {
+      uint32_t r[kLd];
+      const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(b * TC + cb);
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+          : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+            "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+          : "r"(taddr)
+          : "memory");
+      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+      if (__any_sync(0xffffffffu, np > kBuf - kLd)) merge();
+      if (!qvalid) continue;
+      const uint32_t x0 = (uint32_t)(c0 + cb);
+      if (fast) {
+        float cn[kLd];
+        if (tnorm) {
+          const float4* tn = reinterpret_cast<const float4*>(tnorm + (size_t)(tb + t) * TC + cb);
+#pragma unroll
+          for (int i = 0; i < kLd / 4; ++i) {
+            const float4 v4 = __ldg(tn + i);
+            cn[4 * i] = v4.x;
+            cn[4 * i + 1] = v4.y;
+            cn[4 * i + 2] = v4.z;
+            cn[4 * i + 3] = v4.w;
+          }
+        } else {
+#pragma unroll
+          for (int c = 0; c < kLd; ++c) cn[c] = __ldg(norms + x0 + c);
+        }
+#pragma unroll
+        for (int c = 0; c < kLd; ++c) {
+          // 2 d is exact, so this equals (qn + cn) - 2 d rounded once
+          const float v = fmaf(-2.f, __uint_as_float(r[c]), qn + cn[c]);
+          if (v <= rootv && lt_vi(v, x0 + c, rootv, rootx)) {
+            pend[np * TQ + tid] = make_uint2(__float_as_uint(v), x0 + c);
+            ++np;
+          }
+        }
+      } else {
+#pragma unroll
+        for (int c = 0; c < kLd; ++c) {
+          const int64_t j = c0 + cb + c;
+          const bool in = j < hi && j != qi;
+          const float v = fmaf(-2.f, __uint_as_float(r[c]), qn + __ldg(norms + (in ? j : qi)));
+          if (in && lt_vi(v, (uint32_t)j, rootv, rootx)) {
+            pend[np * TQ + tid] = make_uint2(__float_as_uint(v), (uint32_t)j);
+            ++np;
+          }
+        }
+      }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    mbar_arrive(smem_u32(&acc_free[b]));
+  }
+  merge();
+  if (qvalid && !*abort_flag) {
+    const int full = cnt;
+    for (int m = cnt; m > 1; --m) {
+      const float v0 = hv[tid];
+      const uint32_t x0 = hx[tid];
+      hv[tid] = hv[(m - 1) * TQ + tid];
+      hx[tid] = hx[(m - 1) * TQ + tid];
+      hv[(m - 1) * TQ + tid] = v0;
+      hx[(m - 1) * TQ + tid] = x0;
+      heap_sift_down(hv, hx, tid, m - 1, 0);
+    }
+    for (int t = 0; t < HEAPC; ++t) out_idx[qi * HEAPC + t] = t < full ? hx[t * TQ + tid] : SENTI;
+    out_thr[qi] = full == HEAPC ? hv[(HEAPC - 1) * TQ + tid] : INFINITY;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Staged form. 8 warps split the work:
+//   warps 0-3  selection (selection_role);
 //   warp 4     one thread issues the MMAs: per candidate tile and 16-dim
 //              chunk, 2 k-steps x 3 MMAs;
 //   warps 5-7  stage 16-dim chunks of the query and candidate rows, split into
 //              TF32 hi / lo parts on the fly from the FP32 rows, into a
-//              3-deep shared-memory ring.
+//              2-deep shared-memory ring.
 // mbarriers: full[s] (producers -> MMA), empty[s] (MMA commit -> producers),
 // acc_full[b] (MMA commit -> selection), acc_free[b] (selection -> MMA).
 // The selection of tile t overlaps the staging and MMAs of tile t + 1.
 // ---------------------------------------------------------------------------
-constexpr int PK = 16;                     // dimensions per ring stage
-constexpr int NST = 2;                     // ring depth
-constexpr int kProducers = 96;
-constexpr int kPipeThreads = 256;
-constexpr int kSubTile = TQ * PK * 4;      // 8 KB: 128 rows x 16 dims
-constexpr int kStageBytes = 4 * kSubTile;  // query hi, query lo, candidate hi, candidate lo
-constexpr int kBuf = 32;                   // pending candidates per query between heap merges
-constexpr int kLd = 16;                    // accumulator columns read per tcgen05.ld
-constexpr size_t kPipeSmem = (size_t)HEAPC * TQ * 8 + (size_t)kBuf * TQ * 8 + (size_t)NST * kStageBytes;
-
 struct PipeBars {
-  uint64_t full[NST], empty[NST], acc_full[2], acc_free[2];
+  uint64_t full[NST], empty[NST], acc_full[2], acc_free[2], done;
 };
-
-__device__ __forceinline__ void mbar_arrive(uint32_t mbar) {
-  asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}\n" ::"r"(mbar) : "memory");
-}
-
-// Bounded wait; false (and the abort flag raised) when it runs out or
-// another role already aborted.
-__device__ __forceinline__ bool mbar_wait_bounded(uint32_t mbar, uint32_t parity, volatile int* abort_flag, int* err) {
-  long long spins = 0;
-  while (!mbar_try_wait(mbar, parity)) {
-    if (*abort_flag) return false;
-    if (++spins >= kSpinLimit) {
-      *abort_flag = 1;
-      atomicExch(err, 1);
-      return false;
-    }
-  }
-  return true;
-}
-
-__device__ __forceinline__ float tf32_hi(float x) {
-  uint32_t b = __float_as_uint(x);
-  if ((b & 0x7f800000u) != 0x7f800000u) b = (b + 0x1000u) & 0xffffe000u;
-  return __uint_as_float(b);
-}
 
 // Rows [q0, q0 + 128) (queries) and [c0, c0 + 128) (candidates) x dims
 // [d0, d0 + 16) of Xp (row-major, ld = dim_pad, zero padded), split into hi /
@@ -223,10 +392,7 @@ __global__ void __launch_bounds__(kPipeThreads, 1)
                        uint32_t* __restrict__ out_idx, float* __restrict__ out_thr, const int64_t* __restrict__ blk_q0,
                        const int32_t* __restrict__ blk_job, const int64_t* __restrict__ seg_off, int* __restrict__ err) {
   extern __shared__ __align__(1024) unsigned char smem[];
-  float* hv = reinterpret_cast<float*>(smem);
-  uint32_t* hx = reinterpret_cast<uint32_t*>(hv + HEAPC * TQ);
-  uint2* pend = reinterpret_cast<uint2*>(hx + HEAPC * TQ);  // [kBuf][TQ] pending (value bits, index)
-  unsigned char* ring = reinterpret_cast<unsigned char*>(pend + kBuf * TQ);
+  unsigned char* ring = smem + kSelSmem;
   __shared__ __align__(8) PipeBars bars;
   __shared__ uint32_t tmem_slot;
   __shared__ volatile int abort_flag;
@@ -249,7 +415,8 @@ __global__ void __launch_bounds__(kPipeThreads, 1)
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
   if (tid == 0) {
-    abort_flag = 0;
+    // a CTA that starts after another one timed out does no work
+    abort_flag = *reinterpret_cast<volatile int*>(err) ? 1 : 0;
     for (int i = 0; i < NST; ++i) {
       asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&bars.full[i])), "r"(kProducers) : "memory");
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&bars.empty[i])) : "memory");
@@ -258,6 +425,7 @@ __global__ void __launch_bounds__(kPipeThreads, 1)
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&bars.acc_full[b])) : "memory");
       asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&bars.acc_free[b])), "r"(TQ) : "memory");
     }
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&bars.done)) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -316,93 +484,248 @@ __global__ void __launch_bounds__(kPipeThreads, 1)
         if (!ok) break;
         mma_commit(smem_u32(&bars.acc_full[b]));
       }
+      // every MMA issued has completed before the tensor memory is released
+      mma_commit(smem_u32(&bars.done));
+      mbar_drain(smem_u32(&bars.done), 0, err);
     }
   } else {
-    // ---- selection: query row tid. Candidates that beat the current C-th
-    // best (the heap root, in registers) are appended to a per-thread pending
-    // list; when any lane's list could overflow on the next read, the whole
-    // warp merges its lists into the heaps together, so lanes insert in
-    // lockstep instead of one divergent heap update per candidate.
-    const int64_t qi = q0 + tid;
-    const bool qvalid = qi < hi;
-    const float qn = qvalid ? norms[qi] : 0.f;
-    int cnt = 0, np = 0;
-    float rootv = INFINITY;
-    uint32_t rootx = SENTI;
-    auto merge = [&]() {
-      const int rounds = __reduce_max_sync(0xffffffffu, (unsigned)np);
-      for (int i = 0; i < rounds; ++i) {
-        if (i < np) {
-          const uint2 e = pend[i * TQ + tid];
-          const float v = __uint_as_float(e.x);
-          if (cnt < HEAPC) {
-            heap_push(hv, hx, tid, cnt, v, e.y);
-          } else if (lt_vi(v, e.y, hv[tid], hx[tid])) {
-            hv[tid] = v;
-            hx[tid] = e.y;
-            heap_sift_down(hv, hx, tid, cnt, 0);
-          }
-        }
-      }
-      np = 0;
-      if (cnt == HEAPC) {
-        rootv = hv[tid];
-        rootx = hx[tid];
-      }
-    };
-    for (int64_t t = 0; t < ntiles; ++t) {
-      const int b = (int)(t & 1);
-      if (!mbar_wait_bounded(smem_u32(&bars.acc_full[b]), (uint32_t)((t >> 1) & 1), &abort_flag, err)) break;
-      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      const int64_t c0 = lo + t * TC;
-#pragma unroll 1
-      for (int cb = 0; cb < TC; cb += kLd) {
-        uint32_t r[kLd];
-        const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(b * TC + cb);
-        asm volatile(
-            "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-            : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-              "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-            : "r"(taddr)
-            : "memory");
-        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-        if (__any_sync(0xffffffffu, np > kBuf - kLd)) merge();
-        if (qvalid) {
-#pragma unroll
-          for (int c = 0; c < kLd; ++c) {
-            const int64_t j = c0 + cb + c;
-            const float v = qn + __ldg(norms + (j < hi ? j : lo)) - 2.f * __uint_as_float(r[c]);
-            const uint32_t x = (uint32_t)j;
-            if (j < hi && j != qi && lt_vi(v, x, rootv, rootx)) {
-              pend[np * TQ + tid] = make_uint2(__float_as_uint(v), x);
-              ++np;
-            }
-          }
-        }
-      }
-      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-      mbar_arrive(smem_u32(&bars.acc_free[b]));
-    }
-    merge();
-    if (qvalid && !abort_flag) {
-      const int full = cnt;
-      for (int m = cnt; m > 1; --m) {
-        const float v0 = hv[tid];
-        const uint32_t x0 = hx[tid];
-        hv[tid] = hv[(m - 1) * TQ + tid];
-        hx[tid] = hx[(m - 1) * TQ + tid];
-        hv[(m - 1) * TQ + tid] = v0;
-        hx[(m - 1) * TQ + tid] = x0;
-        heap_sift_down(hv, hx, tid, m - 1, 0);
-      }
-      for (int t = 0; t < HEAPC; ++t) out_idx[qi * HEAPC + t] = t < full ? hx[t * TQ + tid] : SENTI;
-      out_thr[qi] = full == HEAPC ? hv[(HEAPC - 1) * TQ + tid] : INFINITY;
-    }
+    selection_role(tmem, bars.acc_full, bars.acc_free, smem, q0, lo, hi, ntiles, norms, nullptr, 0, out_idx, out_thr,
+                   &abort_flag, err);
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   if (warp == 0) {
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * TC) : "memory");
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Resident form. 6 warps:
+//   warps 0-3  write their query rows' hi / lo parts into tensor memory
+//              (columns kColQhi.. and kColQlo..), then selection_role;
+//   warp 4     one thread issues the MMAs (A from tensor memory, B from the
+//              ring): per candidate tile and 16-dim chunk, 2 k-steps x 3 MMAs,
+//              in the staged form's order;
+//   warp 5     one thread issues the bulk copies of the candidate chunks
+//              (16 KB each, hi and lo, from the split tiles) into the ring.
+// mbarriers: full[s] (copy bytes landed -> MMA), empty[s] (MMA commit ->
+// copier), acc_full / acc_free as in the staged form, qready (query in tensor
+// memory -> MMA), done (last MMAs -> exit).
+// ---------------------------------------------------------------------------
+struct ResBars {
+  uint64_t full[NSR], empty[NSR], acc_full[2], acc_free[2], qready, done;
+};
+
+__device__ __forceinline__ void tmem_st16(uint32_t taddr, const uint32_t (&v)[16]) {
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};" ::"r"(
+          taddr),
+      "r"(v[0]), "r"(v[1]), "r"(v[2]), "r"(v[3]), "r"(v[4]), "r"(v[5]), "r"(v[6]), "r"(v[7]), "r"(v[8]), "r"(v[9]),
+      "r"(v[10]), "r"(v[11]), "r"(v[12]), "r"(v[13]), "r"(v[14]), "r"(v[15])
+      : "memory");
+}
+
+// Xs: split candidate tiles, tile T's chunk ch at Xs + (T * nch + ch) * 16 KB
+// (hi sub-tile, then lo), and their squared norms, 128 per tile, in tnorm;
+// tiles of the point set of block b numbered from tile_base[blk_job[b]] (from
+// 0 without a block table).
+__global__ void __launch_bounds__(kResThreads, 1)
+    knn_tc_res_kernel(const float* __restrict__ Xp, const float* __restrict__ Xs, const float* __restrict__ tnorm,
+                      int64_t n, int dim_pad,
+                      const float* __restrict__ norms, uint32_t* __restrict__ out_idx, float* __restrict__ out_thr,
+                      const int64_t* __restrict__ blk_q0, const int32_t* __restrict__ blk_job,
+                      const int64_t* __restrict__ seg_off, const int64_t* __restrict__ tile_base, int* __restrict__ err) {
+  extern __shared__ __align__(1024) unsigned char smem[];
+  unsigned char* ring = smem + kSelSmem;
+  __shared__ __align__(8) ResBars bars;
+  __shared__ uint32_t tmem_slot;
+  __shared__ volatile int abort_flag;
+
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  int64_t q0 = (int64_t)blockIdx.x * TQ, lo = 0, hi = n, tb = 0;
+  if (blk_q0) {
+    const int jb = blk_job[blockIdx.x];
+    q0 = blk_q0[blockIdx.x];
+    lo = seg_off[jb];
+    hi = seg_off[jb + 1];
+    tb = tile_base[jb];
+  }
+  const int64_t ntiles = (hi - lo + TC - 1) / TC;
+  const int nch = dim_pad / PK;
+
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_slot)),
+                 "r"(kResCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  if (tid == 0) {
+    // a CTA that starts after another one timed out does no work
+    abort_flag = *reinterpret_cast<volatile int*>(err) ? 1 : 0;
+    for (int i = 0; i < NSR; ++i) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&bars.full[i])) : "memory");
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&bars.empty[i])) : "memory");
+    }
+    for (int b = 0; b < 2; ++b) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&bars.acc_full[b])) : "memory");
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&bars.acc_free[b])), "r"(TQ) : "memory");
+    }
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&bars.qready)), "r"(TQ) : "memory");
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&bars.done)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = tmem_slot;
+
+  if (warp == 5) {
+    // ---- bulk copies of the candidate chunks (one thread)
+    if (lane == 0) {
+      int64_t it = 0;
+      bool ok = true;
+      for (int64_t t = 0; t < ntiles && ok && !abort_flag; ++t) {
+        const float* tile = Xs + (size_t)(tb + t) * nch * (kResStage / 4);
+        for (int ch = 0; ch < nch; ++ch) {
+          const int st = (int)(it % NSR);
+          const uint32_t par = (uint32_t)(((it / NSR) & 1) ^ 1);
+          if (!mbar_wait_bounded(smem_u32(&bars.empty[st]), par, &abort_flag, err)) {
+            ok = false;
+            break;
+          }
+          const uint32_t fb = smem_u32(&bars.full[st]);
+          asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(fb), "r"(kResStage) : "memory");
+          asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                           smem_u32(ring + (size_t)st * kResStage)),
+                       "l"(tile + (size_t)ch * (kResStage / 4)), "r"(kResStage), "r"(fb)
+                       : "memory");
+          ++it;
+        }
+      }
+      // the copies still in flight land before the CTA exits
+      for (int64_t j = it > NSR ? it - NSR : 0; j < it; ++j)
+        mbar_drain(smem_u32(&bars.full[j % NSR]), (uint32_t)((j / NSR) & 1), err);
+    }
+  } else if (warp == 4) {
+    // ---- MMA issue (one thread)
+    if (lane == 0) {
+      bool ok = mbar_wait_bounded(smem_u32(&bars.qready), 0, &abort_flag, err);
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      int64_t it = 0;
+      for (int64_t t = 0; t < ntiles && ok && !abort_flag; ++t) {
+        const int b = (int)(t & 1);
+        if (!mbar_wait_bounded(smem_u32(&bars.acc_free[b]), (uint32_t)(((t >> 1) & 1) ^ 1), &abort_flag, err)) break;
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const uint32_t dacc = tmem + (uint32_t)(b * TC);
+        for (int ch = 0; ch < nch; ++ch, ++it) {
+          const int st = (int)(it % NSR);
+          if (!mbar_wait_bounded(smem_u32(&bars.full[st]), (uint32_t)((it / NSR) & 1), &abort_flag, err)) {
+            ok = false;
+            break;
+          }
+          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+          const uint32_t bh = smem_u32(ring + (size_t)st * kResStage), bl = bh + kSubTile;
+#pragma unroll
+          for (int ks = 0; ks < PK / 8; ++ks) {
+            const uint32_t koff = (uint32_t)(ks * 2) * 128;
+            const uint32_t sbo = (PK / 4) * 128;
+            const uint64_t dbh = make_desc(bh + koff, 128, sbo);
+            const uint64_t dbl = make_desc(bl + koff, 128, sbo);
+            const uint32_t col = (uint32_t)(ch * PK + ks * 8);
+            mma_tf32_ta(dacc, tmem + kColQhi + col, dbh, (ch > 0 || ks > 0) ? 1u : 0u);
+            mma_tf32_ta(dacc, tmem + kColQhi + col, dbl, 1u);
+            mma_tf32_ta(dacc, tmem + kColQlo + col, dbh, 1u);
+          }
+          mma_commit(smem_u32(&bars.empty[st]));
+        }
+        if (!ok) break;
+        mma_commit(smem_u32(&bars.acc_full[b]));
+      }
+      // every MMA issued has completed before the tensor memory is released
+      mma_commit(smem_u32(&bars.done));
+      mbar_drain(smem_u32(&bars.done), 0, err);
+    }
+  } else {
+    // ---- query row q0 + tid into tensor memory lane tid, then selection
+    const int64_t qi = q0 + tid;
+    const bool qvalid = qi < hi;
+    const float4* xq = reinterpret_cast<const float4*>(Xp + (qvalid ? qi : 0) * dim_pad);
+    const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
+    for (int ch = 0; ch < nch; ++ch) {
+      uint32_t h[16], l[16];
+#pragma unroll
+      for (int i4 = 0; i4 < 4; ++i4) {
+        const float4 v = qvalid ? __ldg(xq + ch * 4 + i4) : make_float4(0.f, 0.f, 0.f, 0.f);
+        const float x[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          const float hx = tf32_hi(x[e]);
+          h[4 * i4 + e] = __float_as_uint(hx);
+          l[4 * i4 + e] = __float_as_uint(x[e] - hx);
+        }
+      }
+      tmem_st16(lane_base + kColQhi + (uint32_t)(ch * PK), h);
+      tmem_st16(lane_base + kColQlo + (uint32_t)(ch * PK), l);
+    }
+    asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    mbar_arrive(smem_u32(&bars.qready));
+    selection_role(tmem, bars.acc_full, bars.acc_free, smem, q0, lo, hi, ntiles, norms, tnorm, tb, out_idx, out_thr,
+                   &abort_flag, err);
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kResCols) : "memory");
+  }
+}
+
+// Candidate tiles split into TF32 hi / lo core-matrix sub-tiles (the resident
+// form's copy source). Tile T covers rows row0(T) .. row0(T) + 127 of its
+// point set (zero beyond the set's end): row0 = 128 T without a set table,
+// else set j = the last with tile_base[j] <= T and row0 = seg_off[j] + 128
+// (T - tile_base[j]). One thread per 16-byte piece of a row; the first piece's
+// thread also copies the row's squared norm into tnorm[128 T + r].
+__global__ void split_tiles_kernel(const float* __restrict__ Xp, const float* __restrict__ norms, int64_t n,
+                                   int dim_pad, const int64_t* __restrict__ seg_off,
+                                   const int64_t* __restrict__ tile_base, int nseg, int64_t ntile,
+                                   float* __restrict__ out, float* __restrict__ tnorm) {
+  const int q4 = dim_pad / 4, nch = dim_pad / PK;
+  const int64_t total = ntile * TC * q4;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    const int q = (int)(e % q4);
+    const int64_t rt = e / q4;
+    const int r = (int)(rt % TC);
+    const int64_t T = rt / TC;
+    int64_t row0 = T * TC, rend = n;
+    if (tile_base) {
+      int a = 0, b = nseg - 1;
+      while (a < b) {
+        const int m = (a + b + 1) >> 1;
+        if (tile_base[m] <= T) a = m;
+        else b = m - 1;
+      }
+      row0 = seg_off[a] + (T - tile_base[a]) * TC;
+      rend = seg_off[a + 1];
+    }
+    const int64_t row = row0 + r;
+    float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (row < rend) v = __ldg(reinterpret_cast<const float4*>(Xp + row * dim_pad) + q);
+    if (q == 0) tnorm[T * TC + r] = row < rend ? norms[row] : 0.f;
+    float4 h, l;
+    h.x = tf32_hi(v.x);
+    h.y = tf32_hi(v.y);
+    h.z = tf32_hi(v.z);
+    h.w = tf32_hi(v.w);
+    l.x = v.x - h.x;
+    l.y = v.y - h.y;
+    l.z = v.z - h.z;
+    l.w = v.w - h.w;
+    const int ch = q >> 2, k4 = q & 3;
+    float* base = out + ((size_t)T * nch + ch) * (kResStage / 4);
+    const int off = (((r >> 3) * (PK / 4) + k4) * 128 + (r & 7) * 16) / 4;
+    *reinterpret_cast<float4*>(base + off) = h;
+    *reinterpret_cast<float4*>(base + kSubTile / 4 + off) = l;
   }
 }
 
@@ -416,11 +739,18 @@ __global__ void pad_rows_kernel(const float* __restrict__ X, int64_t n, int dim,
   }
 }
 
+// BHTSNE_KNN_TC_STAGED=1 selects the staged form for every width (the two
+// forms give the same candidate lists); read on every call.
+bool staged_forced() {
+  const char* e = getenv("BHTSNE_KNN_TC_STAGED");
+  return e && *e && *e != '0';
+}
+
 }  // namespace
 
 void knn_tc_candidates(const float* X, int64_t n, int dim, const float* norms, const int64_t* blk_q0,
-                       const int32_t* blk_job, const int64_t* seg_off, int64_t nblocks, uint32_t* cand, float* thr,
-                       KnnTcScratch& ws, cudaStream_t s) {
+                       const int32_t* blk_job, const int64_t* seg_off, const std::vector<int64_t>* off,
+                       int64_t nblocks, uint32_t* cand, float* thr, KnnTcScratch& ws, cudaStream_t s) {
   const int dim_pad = (dim + PK - 1) / PK * PK;
   int* err = static_cast<int*>(ws.err.ensure(64));
   BHG_CUDA(cudaMemsetAsync(err, 0, 4, s));
@@ -432,10 +762,39 @@ void knn_tc_candidates(const float* X, int64_t n, int dim, const float* norms, c
     BHG_LAUNCH_CHECK();
     Xp = pad;
   }
-  BHG_CUDA(cudaFuncSetAttribute(knn_tc_pipe_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPipeSmem));
-  knn_tc_pipe_kernel<<<(unsigned)nblocks, kPipeThreads, kPipeSmem, s>>>(Xp, n, dim_pad, norms, cand, thr, blk_q0,
-                                                                        blk_job, seg_off, err);
-  BHG_LAUNCH_CHECK();
+  const bool resident = dim_pad <= kResDimMax && !staged_forced();
+  ws.last_resident = resident;
+  if (resident) {
+    // candidate tiles per point set, numbered set after set
+    const int64_t* tbase = nullptr;
+    int64_t ntile = ceil_div(n, TC);
+    int nseg = 0;
+    if (off) {
+      nseg = (int)off->size() - 1;
+      std::vector<int64_t> tb(nseg + 1);
+      tb[0] = 0;
+      for (int j = 0; j < nseg; ++j) tb[j + 1] = tb[j] + ceil_div((*off)[j + 1] - (*off)[j], TC);
+      ntile = tb[nseg];
+      int64_t* d_tb = static_cast<int64_t*>(ws.tile_base.ensure((size_t)(nseg + 1) * 8));
+      BHG_CUDA(cudaMemcpyAsync(d_tb, tb.data(), (size_t)(nseg + 1) * 8, cudaMemcpyHostToDevice, s));
+      tbase = d_tb;
+    }
+    const int nch = dim_pad / PK;
+    float* Xs = static_cast<float*>(ws.split.ensure((size_t)ntile * (nch * kResStage + TC * 4)));
+    float* tnorm = Xs + (size_t)ntile * nch * (kResStage / 4);
+    split_tiles_kernel<<<(unsigned)std::min<int64_t>(ceil_div(ntile * TC * (dim_pad / 4), 256), sm_grid(8, 8192)), 256, 0,
+                         s>>>(Xp, norms, n, dim_pad, seg_off, tbase, nseg, ntile, Xs, tnorm);
+    BHG_LAUNCH_CHECK();
+    BHG_CUDA(cudaFuncSetAttribute(knn_tc_res_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kResSmem));
+    knn_tc_res_kernel<<<(unsigned)nblocks, kResThreads, kResSmem, s>>>(Xp, Xs, tnorm, n, dim_pad, norms, cand, thr,
+                                                                       blk_q0, blk_job, seg_off, tbase, err);
+    BHG_LAUNCH_CHECK();
+  } else {
+    BHG_CUDA(cudaFuncSetAttribute(knn_tc_pipe_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPipeSmem));
+    knn_tc_pipe_kernel<<<(unsigned)nblocks, kPipeThreads, kPipeSmem, s>>>(Xp, n, dim_pad, norms, cand, thr, blk_q0,
+                                                                          blk_job, seg_off, err);
+    BHG_LAUNCH_CHECK();
+  }
   int herr = 0;
   BHG_CUDA(cudaMemcpyAsync(&herr, err, 4, cudaMemcpyDeviceToHost, s));
   BHG_CUDA(cudaStreamSynchronize(s));

@@ -2,6 +2,7 @@
 #pragma once
 
 #include <cmath>
+#include <vector>
 
 #include "internal.h"
 
@@ -9,18 +10,29 @@ namespace bhg {
 
 struct KnnTcScratch {
   DevBuf xhi, err;  // xhi: rows padded to a multiple of 16 dimensions when needed
-  void release() { xhi.release(); }
+  DevBuf split;     // candidate tiles split into TF32 hi / lo (resident form)
+  DevBuf tile_base; // first split tile of each point set (segmented calls)
+  bool last_resident = false;  // the last call ran the resident form
+  void release() {
+    xhi.release();
+    split.release();
+    tile_base.release();
+  }
 };
 
 // Per query of X (n x dim, FP32): the indices of its 128 candidates with the
 // smallest |q|^2 + |c|^2 - 2 q.c (3xTF32 tensor-core dot products), sorted by
 // (value, index), into cand[q * 128 ..], and the 128-th value into thr[q]
 // (INFINITY when fewer candidates exist). Blocks of 128 queries; with a block
-// table (blk_q0, blk_job, seg_off) block b takes queries blk_q0[b].. of set
-// blk_job[b] and scans only that set's rows. Synchronises the stream.
+// table (blk_q0, blk_job, seg_off, and the host copy of the set offsets in
+// off) block b takes queries blk_q0[b].. of set blk_job[b] and scans only
+// that set's rows. Rows of at most 128 dimensions run the resident form
+// (query tile in tensor memory, candidate tiles split once into hi / lo and
+// streamed by bulk copies: 2 n dim_pad floats of scratch), wider rows the
+// staged form. Synchronises the stream.
 void knn_tc_candidates(const float* X, int64_t n, int dim, const float* norms, const int64_t* blk_q0,
-                       const int32_t* blk_job, const int64_t* seg_off, int64_t nblocks, uint32_t* cand, float* thr,
-                       KnnTcScratch& ws, cudaStream_t s);
+                       const int32_t* blk_job, const int64_t* seg_off, const std::vector<int64_t>* off,
+                       int64_t nblocks, uint32_t* cand, float* thr, KnnTcScratch& ws, cudaStream_t s);
 
 // Error coefficient of the tensor-core candidate values: |v - d^2| <= coef *
 // (|q|^2 + r^2) for candidates within radius r of the origin.
