@@ -421,12 +421,12 @@ def parity_1m(args, ctx, X, aff, y_end, knn_fallback_fit):
     out = {}
     rows = np.sort(np.random.default_rng(2026).choice(n, args.parity_rows, replace=False))
     gi, gd = bg.knn_euclidean(X, 90, ctx=ctx)
-    fb = ctx.knn_fallback_rows()
+    fb, fbb = ctx.knn_fallback_rows(), ctx.knn_brute_rows()
     w0 = time.perf_counter()
     oi, od = O.knn_rows(X, 90, rows)
     same = np.all(gi[rows] == oi, axis=1) & np.all(gd[rows] == od, axis=1)
     out["c3_knn"] = {"rows_checked": int(rows.size), "rows_bit_exact": int(same.sum()),
-                     "fallback_rows": int(fb), "fallback_rows_fit": int(knn_fallback_fit),
+                     "fallback_rows": int(fb), "brute_rows": int(fbb), "fallback_rows_fit": int(knn_fallback_fit),
                      "oracle_s": round(time.perf_counter() - w0, 2),
                      "note": "random query rows, brute force over all %d candidates, (distance, index) order" % n}
     del gi, gd
@@ -893,6 +893,7 @@ def run_knn_only(args):
     staged = os.environ.get("BHTSNE_KNN_TC_STAGED", "0") not in ("", "0")
     print(json.dumps({"metric": "exact kNN seconds (k = 90)", "value": round(el, 4), "unit": "s",
                       "higher_is_better": False, "fallback_rows": L.default_context().knn_fallback_rows(),
+                      "brute_rows": L.default_context().knn_brute_rows(),
                       "candidate_pass": "staged" if staged else "resident",
                       "config": {"n_points": args.n, "input_dim": 128, "k": 90}}))
 

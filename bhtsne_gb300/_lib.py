@@ -26,6 +26,7 @@ SIGNATURES = {
     "bhtsne_ctx_destroy": (C.c_int, [_vp]),
     "bhtsne_ctx_last_error": (C.c_char_p, [_vp]),
     "bhtsne_ctx_knn_fallback_rows": (C.c_int, [_vp, _i64p]),
+    "bhtsne_ctx_knn_brute_rows": (C.c_int, [_vp, _i64p]),
     "bhtsne_tsne_new": (C.c_int, [_vp, C.c_int, _i32, _i64, C.POINTER(C.c_void_p)]),
     "bhtsne_tsne_free": (C.c_int, [_vp]),
     "bhtsne_tsne_last_error": (C.c_char_p, [_vp]),
@@ -195,9 +196,15 @@ class Context:
 
     def knn_fallback_rows(self) -> int:
         """Rows of the last Euclidean kNN on this context that failed the
-        tensor-core pass's exactness certificate and were recomputed."""
+        candidate pass's exactness certificate and were recomputed."""
         v = C.c_int64()
         self.check(self.lib.bhtsne_ctx_knn_fallback_rows(self.handle, C.byref(v)))
+        return v.value
+
+    def knn_brute_rows(self) -> int:
+        """Of those, the rows recomputed by exact brute force."""
+        v = C.c_int64()
+        self.check(self.lib.bhtsne_ctx_knn_brute_rows(self.handle, C.byref(v)))
         return v.value
 
     def close(self) -> None:

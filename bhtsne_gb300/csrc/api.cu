@@ -51,7 +51,8 @@ struct bhtsne_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
   std::string err;
-  int64_t knn_fallback_rows = 0;  // rows of the last kNN on this context recomputed by brute force
+  int64_t knn_fallback_rows = 0;  // rows of the last kNN on this context that failed the certificate
+  int64_t knn_brute_rows = 0;     // of those, the rows recomputed by brute force
 };
 
 namespace bhg {
@@ -799,6 +800,7 @@ void fit_euclidean(bhtsne_tsne* t, int kind, double theta, const void* data, int
     S.knn.pass = tune_lookup(t->dtype, t->D, n).knn_pass;
     t->ctx->knn_fallback_rows = knn_euclidean<T>(S.xin.template as<T>(), n, dim, (int)k,
                                                  S.kidx.template as<uint32_t>(), S.kdist.template as<T>(), S.knn, s);
+    t->ctx->knn_brute_rows = S.knn.last_brute_rows;
     S.xin.release();
     S.knn.release();
     build_affinities<T>(t, k);
@@ -1033,6 +1035,12 @@ int bhtsne_tune(bhtsne_ctx* ctx, int dtype, int32_t embed_dim, int64_t n, int32_
 int bhtsne_ctx_knn_fallback_rows(const bhtsne_ctx* ctx, int64_t* rows) {
   if (!ctx || !rows) return BHTSNE_EINVAL;
   *rows = ctx->knn_fallback_rows;
+  return BHTSNE_OK;
+}
+
+int bhtsne_ctx_knn_brute_rows(const bhtsne_ctx* ctx, int64_t* rows) {
+  if (!ctx || !rows) return BHTSNE_EINVAL;
+  *rows = ctx->knn_brute_rows;
   return BHTSNE_OK;
 }
 
@@ -1332,6 +1340,7 @@ int bhtsne_knn_euclidean(bhtsne_ctx* ctx, int dtype, const void* data, int64_t n
       idx.ensure((size_t)n * k * 4);
       dist.ensure((size_t)n * k * sizeof(T));
       ctx->knn_fallback_rows = knn_euclidean<T>(x.as<T>(), n, dim, k, idx.as<uint32_t>(), dist.as<T>(), ws, s);
+      ctx->knn_brute_rows = ws.last_brute_rows;
       BHG_CUDA(cudaMemcpyAsync(indices, idx.ptr, (size_t)n * k * 4, cudaMemcpyDeviceToHost, s));
       BHG_CUDA(cudaMemcpyAsync(distances, dist.ptr, (size_t)n * k * sizeof(T), cudaMemcpyDeviceToHost, s));
       BHG_CUDA(cudaStreamSynchronize(s));

@@ -41,6 +41,10 @@ constexpr uint32_t SENT = 0xffffffffu;
 constexpr int kMaxSlices = 16;
 constexpr int64_t kMinSlice = 4096;
 constexpr size_t kSliceScratchMax = (size_t)1 << 30;
+// bounded re-scan: at most kListCap listed candidates per failing row, lists
+// of at most kListBytesMax bytes in all
+constexpr int kListCap = 2048;
+constexpr size_t kListBytesMax = (size_t)1 << 30;
 
 __global__ void sq_norm_kernel(const float* __restrict__ X, int64_t n, int dim, float* __restrict__ norms,
                                unsigned* __restrict__ max_bits) {
@@ -569,7 +573,8 @@ __global__ void knn_rerank_kernel(const T* __restrict__ X, int64_t n, int dim, i
                                   const float* __restrict__ thr, const float* __restrict__ norms,
                                   const unsigned* __restrict__ max_bits, uint32_t* __restrict__ out_idx,
                                   T* __restrict__ out_dist, uint32_t* __restrict__ fail_list,
-                                  unsigned* __restrict__ fail_count, double ecoef) {
+                                  unsigned* __restrict__ fail_count, double ecoef,
+                                  float* __restrict__ fail_bound = nullptr) {
   constexpr int W = 4;
   __shared__ T sd[W][C];
   __shared__ T sd2[W][C];
@@ -623,6 +628,7 @@ __global__ void knn_rerank_kernel(const T* __restrict__ X, int64_t n, int dim, i
     // >= th. Certified when d2k (inflated by its own rounding) + E < th.
     const float th = thr[qi];
     bool ok = true;
+    double bound = 0.0;
     if (!isinf(th)) {
       const double u = 1.0 / 16777216.0;
       const double g = (dim + 2.0) * u;
@@ -630,9 +636,69 @@ __global__ void knn_rerank_kernel(const T* __restrict__ X, int64_t n, int dim, i
       const double d2k = (double)sd2[w][k - 1] * (1.0 + g) * (1.0 + 16.0 * u);
       const double r = sqrt(qn) + sqrt(d2k);
       const double E = ecoef * (qn + r * r);
-      ok = d2k + E < (double)th;
+      bound = d2k + E;
+      ok = bound < (double)th;
     }
-    if (!ok) fail_list[atomicAdd(fail_count, 1u)] = (uint32_t)qi;
+    if (!ok) {
+      const unsigned f = atomicAdd(fail_count, 1u);
+      fail_list[f] = (uint32_t)qi;
+      // every true neighbour's candidate value is at most bound (rounded up)
+      if (fail_bound) fail_bound[f] = __double2float_ru(bound);
+    }
+  }
+}
+
+// Exact re-rank of a bounded re-scan: one warp per listed row r (row
+// rows[r] of X) over its list of list_cnt[r] candidates (index order), with
+// the sorted list of size k in shared memory by (distance, index). A row
+// whose list overflowed cap (or holds fewer than k others) goes to over[].
+template <class T>
+__global__ void knn_list_rerank_kernel(const T* __restrict__ X, int dim, int k, const uint32_t* __restrict__ rows,
+                                       int64_t nrows, const uint32_t* __restrict__ list,
+                                       const uint32_t* __restrict__ list_cnt, int cap, uint32_t* __restrict__ out_idx,
+                                       T* __restrict__ out_dist, uint32_t* __restrict__ over,
+                                       unsigned* __restrict__ over_count) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  constexpr int W = 4;
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  T* lv = reinterpret_cast<T*>(smem) + (size_t)w * k;
+  uint32_t* li = reinterpret_cast<uint32_t*>(reinterpret_cast<T*>(smem) + (size_t)W * k) + (size_t)w * k;
+  __shared__ int len[W];
+  const int64_t r = (int64_t)blockIdx.x * W + w;
+  if (r >= nrows) return;
+  const int64_t qi = rows[r];
+  const uint32_t cnt = list_cnt[r];
+  if (cnt > (uint32_t)cap) {
+    if (lane == 0) over[atomicAdd(over_count, 1u)] = (uint32_t)qi;
+    return;
+  }
+  if (lane == 0) len[w] = 0;
+  __syncwarp();
+  const T* xq = X + qi * dim;
+  const uint32_t* lr = list + (size_t)r * cap;
+  for (uint32_t b = 0; b < cnt; b += 32) {
+    const uint32_t e = b + lane;
+    const uint32_t j = e < cnt ? lr[e] : 0u;
+    bool ok = e < cnt && (int64_t)j != qi;
+    T d = T(0);
+    if (ok) d = dsqrt(exact_d2<T>(xq, X + (int64_t)j * dim, dim));
+    if (ok && len[w] == k) ok = lt_pair(d, j, lv[k - 1], li[k - 1]);
+    unsigned mask = __ballot_sync(kFull, ok);
+    while (mask) {
+      const int src = __ffs(mask) - 1;
+      mask &= mask - 1;
+      const T dv = __shfl_sync(kFull, d, src);
+      const uint32_t jv = __shfl_sync(kFull, j, src);
+      warp_insert<T>(lv, li, &len[w], k, dv, jv, lane);
+    }
+  }
+  if (len[w] < k) {
+    if (lane == 0) over[atomicAdd(over_count, 1u)] = (uint32_t)qi;
+    return;
+  }
+  for (int t = lane; t < k; t += 32) {
+    out_idx[qi * k + t] = li[t];
+    out_dist[qi * k + t] = lv[t];
   }
 }
 
@@ -690,6 +756,13 @@ bool use_tensor_cores() {
   return !simt;
 }
 
+// BHTSNE_KNN_RESCAN=0 sends every row that fails the certificate straight to
+// the brute force (read on every call).
+bool rescan_enabled() {
+  const char* e = getenv("BHTSNE_KNN_RESCAN");
+  return !(e && e[0] == '0');
+}
+
 size_t sel_smem_bytes(int dim) {
   return ((size_t)dim * QB + DK * CB + QB * (CB + 1)) * 4 + (size_t)QB * 2 * kSelC * 8;
 }
@@ -732,11 +805,13 @@ int64_t knn_euclidean(const T* X, int64_t n, int dim, int k, uint32_t* out_idx, 
   const size_t smem = ((size_t)dim * QB + DK * CB + QB * (CB + 1) + (size_t)QB * C * 2 + 2 * QB) * 4;
   const unsigned grid = (unsigned)ceil_div(n, QB);
   const double simt_coef = (4.0 * dim + 16.0) / 16777216.0;
+  float* fbound = nullptr;  // per failing row: the bound of the bounded re-scan
   if (C == 128 && (ws.pass == 0 || (ws.pass < 0 && use_tensor_cores()))) {
     knn_tc_candidates(Xf, n, dim, norms, nullptr, nullptr, nullptr, nullptr, ceil_div(n, 128), cand, thr, ws.tc, s);
+    if (knn_tc_can_bound(ws.tc, n, dim) && rescan_enabled()) fbound = static_cast<float*>(ws.fbound.ensure((size_t)n * 4));
     knn_rerank_kernel<T, 128><<<(unsigned)ceil_div(n, 4), 128, 0, s>>>(X, n, dim, k, cand, thr, norms, max_bits, out_idx,
                                                                        out_dist, fails, fail_count,
-                                                                       knn_tc_error_coef(dim));
+                                                                       knn_tc_error_coef(dim), fbound);
   } else if (C == 128 && dim <= kSelDimMax) {
     const size_t ssmem = sel_smem_bytes(dim);
     BHG_CUDA(cudaFuncSetAttribute(knn_cand_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ssmem));
@@ -761,20 +836,19 @@ int64_t knn_euclidean(const T* X, int64_t n, int dim, int k, uint32_t* out_idx, 
   unsigned nfail = 0;
   BHG_CUDA(cudaMemcpyAsync(&nfail, fail_count, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
   BHG_CUDA(cudaStreamSynchronize(s));
-  ws.last_fallback_slices = 1;
-  if (nfail > 0) {
+  // Exact brute force for the listed rows: the tiled kernel computing the
+  // reference's exact distances (f32), or one warp per row (f64).
+  auto brute = [&](const uint32_t* rows, unsigned nrows) {
     if constexpr (std::is_same<T, float>::value) {
-      // certified fallback: the same tiled kernel computing the reference's
-      // exact distances for the failing rows only
-      // With few failing rows (under a few waves of blocks) the candidate
-      // range is split into S slices, each block scanning one slice, and the
-      // slices' lists merged: S chosen to minimise the waves per slice length.
-      const unsigned fgrid = (unsigned)ceil_div(nfail, QB);
+      // With few rows (under a few waves of blocks) the candidate range is
+      // split into S slices, each block scanning one slice, and the slices'
+      // lists merged: S chosen to minimise the waves per slice length.
+      const unsigned fgrid = (unsigned)ceil_div(nrows, QB);
       const int sms = device_sm_count();
       int S = 1;
       double best = (double)ceil_div((int64_t)fgrid, sms);
       for (int cand_s = 2; cand_s <= kMaxSlices; ++cand_s) {
-        if (n / cand_s < kMinSlice || (size_t)nfail * cand_s * k * 8 > kSliceScratchMax) break;
+        if (n / cand_s < kMinSlice || (size_t)nrows * cand_s * k * 8 > kSliceScratchMax) break;
         const double waves = (double)ceil_div((int64_t)fgrid * cand_s, sms) / cand_s;
         if (waves < best - 1e-9) {
           best = waves;
@@ -787,22 +861,22 @@ int64_t knn_euclidean(const T* X, int64_t n, int dim, int k, uint32_t* out_idx, 
       if (S > 1) {
         slice_len = ceil_div(ceil_div(n, S), CB) * CB;
         S = (int)ceil_div(n, slice_len);
-        sidx = static_cast<uint32_t*>(ws.slices.ensure((size_t)nfail * S * k * 8));
-        sval = reinterpret_cast<float*>(sidx + (size_t)nfail * S * k);
+        sidx = static_cast<uint32_t*>(ws.slices.ensure((size_t)nrows * S * k * 8));
+        sval = reinterpret_cast<float*>(sidx + (size_t)nrows * S * k);
       }
       const dim3 g2(fgrid, (unsigned)S);
       if (C == 128) {
         BHG_CUDA(cudaFuncSetAttribute(knn_tile_kernel<128, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        knn_tile_kernel<128, true><<<g2, kThreads, smem, s>>>(X, n, dim, norms, fails, nfail, k, out_idx, out_dist,
+        knn_tile_kernel<128, true><<<g2, kThreads, smem, s>>>(X, n, dim, norms, rows, nrows, k, out_idx, out_dist,
                                                               nullptr, nullptr, nullptr, slice_len, sidx, sval);
       } else {
         BHG_CUDA(cudaFuncSetAttribute(knn_tile_kernel<256, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        knn_tile_kernel<256, true><<<g2, kThreads, smem, s>>>(X, n, dim, norms, fails, nfail, k, out_idx, out_dist,
+        knn_tile_kernel<256, true><<<g2, kThreads, smem, s>>>(X, n, dim, norms, rows, nrows, k, out_idx, out_dist,
                                                               nullptr, nullptr, nullptr, slice_len, sidx, sval);
       }
       BHG_LAUNCH_CHECK();
       if (S > 1) {
-        slice_merge_kernel<<<(unsigned)ceil_div((int64_t)nfail * 32, 256), 256, 0, s>>>(sidx, sval, fails, nfail, S, k,
+        slice_merge_kernel<<<(unsigned)ceil_div((int64_t)nrows * 32, 256), 256, 0, s>>>(sidx, sval, rows, nrows, S, k,
                                                                                         out_idx, out_dist);
         BHG_LAUNCH_CHECK();
       }
@@ -811,9 +885,43 @@ int64_t knn_euclidean(const T* X, int64_t n, int dim, int k, uint32_t* out_idx, 
       const size_t esmem = (size_t)4 * k * (sizeof(T) + sizeof(uint32_t));
       if (esmem > 48 * 1024)
         BHG_CUDA(cudaFuncSetAttribute(knn_exact_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)esmem));
-      knn_exact_kernel<T><<<(unsigned)ceil_div(nfail, 4), 128, esmem, s>>>(X, n, dim, k, fails, nullptr, nfail, out_idx,
+      knn_exact_kernel<T><<<(unsigned)ceil_div(nrows, 4), 128, esmem, s>>>(X, n, dim, k, rows, nullptr, nrows, out_idx,
                                                                           out_dist);
       BHG_LAUNCH_CHECK();
+    }
+  };
+  ws.last_fallback_slices = 1;
+  ws.last_brute_rows = 0;
+  if (nfail > 0) {
+    // Bounded re-scan: the rows that failed the certificate take every
+    // candidate whose tensor-core value is within their bound (a superset of
+    // their true neighbours) and re-rank that list exactly; rows whose list
+    // overflows take the brute force.
+    int cap = 0;
+    if (fbound) {
+      cap = (int)std::min<int64_t>(kListCap, (int64_t)(kListBytesMax / ((size_t)nfail * 4)) / 32 * 32);
+      if (cap < 4 * 128) cap = 0;
+    }
+    if (cap > 0) {
+      uint32_t* list = static_cast<uint32_t*>(ws.list.ensure((size_t)nfail * (cap + 1) * 4));
+      uint32_t* list_cnt = list + (size_t)nfail * cap;
+      knn_tc_bounded(n, dim, norms, fails, fbound, nfail, list, list_cnt, cap, ws.tc, s);
+      unsigned* over_count = fail_count + 2;
+      uint32_t* over = static_cast<uint32_t*>(ws.over.ensure((size_t)nfail * 4));
+      const size_t esmem = (size_t)4 * k * (sizeof(T) + sizeof(uint32_t));
+      if (esmem > 48 * 1024)
+        BHG_CUDA(cudaFuncSetAttribute(knn_list_rerank_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)esmem));
+      knn_list_rerank_kernel<T><<<(unsigned)ceil_div(nfail, 4), 128, esmem, s>>>(X, dim, k, fails, nfail, list, list_cnt,
+                                                                                cap, out_idx, out_dist, over, over_count);
+      BHG_LAUNCH_CHECK();
+      unsigned nover = 0;
+      BHG_CUDA(cudaMemcpyAsync(&nover, over_count, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+      BHG_CUDA(cudaStreamSynchronize(s));
+      if (nover > 0) brute(over, nover);
+      ws.last_brute_rows = nover;
+    } else {
+      brute(fails, nfail);
+      ws.last_brute_rows = nfail;
     }
   }
   ws.last_fallback_rows = nfail;

@@ -9,10 +9,11 @@
 namespace bhg {
 
 struct KnnWorkspace {
-  DevBuf xf, norms, cand, thr, fails, counters, blk, tc_blk, slices;
+  DevBuf xf, norms, cand, thr, fails, counters, blk, tc_blk, slices, fbound, list, over;
   KnnTcScratch tc;
   int64_t last_fallback_rows = 0;
-  int last_fallback_slices = 1;  // candidate slices of the last certified fallback
+  int last_fallback_slices = 1;  // candidate slices of the last brute force
+  int64_t last_brute_rows = 0;   // rows of the last call that took the brute force
   // candidate pass: -1 the default (tensor cores unless BHTSNE_KNN_SIMT is
   // set), 0 tensor cores, 1 CUDA cores; both give the same neighbours
   int pass = -1;
@@ -25,6 +26,9 @@ struct KnnWorkspace {
     blk.release();
     tc_blk.release();
     slices.release();
+    fbound.release();
+    list.release();
+    over.release();
     tc.release();
   }
 };

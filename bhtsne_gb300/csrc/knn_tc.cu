@@ -196,6 +196,24 @@ constexpr uint32_t kColQhi = 2 * TC, kColQlo = 2 * TC + kResDimMax, kResCols = 2
 static_assert(kResCols == 512, "the resident form takes the whole tensor memory of its SM");
 static_assert(kResSmem <= 227 * 1024 && kPipeSmem <= 227 * 1024, "shared memory per CTA");
 
+// 16 consecutive accumulator columns of the warp's 32 lanes (asynchronous:
+// tcgen05.wait::ld, then regs_ready, before the registers are read)
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr)
+      : "memory");
+}
+
+// Ties the registers of a tcgen05.ld to the preceding tcgen05.wait::ld, so
+// no read of them is scheduled before the wait.
+__device__ __forceinline__ void regs_ready(uint32_t (&r)[16]) {
+#pragma unroll
+  for (int i = 0; i < 16; ++i) asm volatile("" : "+r"(r[i]));
+}
+
 // ---------------------------------------------------------------------------
 // Selection role (warps 0-3, thread t = query row q0 + t = TMEM lane t): reads
 // the 128 dot products d of a finished tile from one of two TMEM accumulators,
@@ -251,19 +269,10 @@ __device__ void selection_role(uint32_t tmem, uint64_t* acc_full, uint64_t* acc_
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const int64_t c0 = lo + t * TC;
     const bool fast = c0 + TC <= hi && (c0 + TC <= q0 || q0 + TQ <= c0);  // uniform over the CTA
-#pragma unroll 1
-    for (int cb = 0; cb < TC; cb += kLd) {
-      uint32_t r[kLd];
-      const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(b * TC + cb);
-      asm volatile(
-          "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-          : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-            "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-          : "r"(taddr)
-          : "memory");
-      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+    // 16 dot products of columns cb .. cb + 15 against the root
+    auto chunk = [&](const uint32_t* r, int cb) {
       if (__any_sync(0xffffffffu, np > kBuf - kLd)) merge();
-      if (!qvalid) continue;
+      if (!qvalid) return;
       const uint32_t x0 = (uint32_t)(c0 + cb);
       if (fast) {
         float cn[kLd];
@@ -281,13 +290,34 @@ __device__ void selection_role(uint32_t tmem, uint64_t* acc_full, uint64_t* acc_
 #pragma unroll
           for (int c = 0; c < kLd; ++c) cn[c] = __ldg(norms + x0 + c);
         }
+        // all 16 values first (independent), one test of their minimum
+        // against the root, and only then the per-value tests and appends as
+        // predicated stores (no branch per value)
+        float v[kLd];
 #pragma unroll
         for (int c = 0; c < kLd; ++c) {
           // 2 d is exact, so this equals (qn + cn) - 2 d rounded once
-          const float v = fmaf(-2.f, __uint_as_float(r[c]), qn + cn[c]);
-          if (v <= rootv && lt_vi(v, x0 + c, rootv, rootx)) {
-            pend[np * TQ + tid] = make_uint2(__float_as_uint(v), x0 + c);
-            ++np;
+          v[c] = fmaf(-2.f, __uint_as_float(r[c]), qn + cn[c]);
+        }
+        float m8[kLd / 2];
+#pragma unroll
+        for (int c = 0; c < kLd / 2; ++c) m8[c] = fminf(v[2 * c], v[2 * c + 1]);
+#pragma unroll
+        for (int w2 = kLd / 4; w2 >= 1; w2 >>= 1)
+#pragma unroll
+          for (int c = 0; c < w2; ++c) m8[c] = fminf(m8[2 * c], m8[2 * c + 1]);
+        if (m8[0] <= rootv) {
+          uint32_t at = smem_u32(pend + (size_t)np * TQ + tid);
+#pragma unroll
+          for (int c = 0; c < kLd; ++c) {
+            const uint32_t x = x0 + c;
+            const uint32_t a = (v[c] < rootv || (v[c] == rootv && x < rootx)) ? 1u : 0u;
+            asm volatile(
+                "{\n\t.reg .pred q;\n\tsetp.ne.u32 q, %3, 0;\n\t@q st.shared.v2.u32 [%0], {%1, %2};\n\t}\n" ::"r"(at),
+                "r"(__float_as_uint(v[c])), "r"(x), "r"(a)
+                : "memory");
+            np += (int)a;
+            at += a * (uint32_t)(TQ * sizeof(uint2));
           }
         }
       } else {
@@ -302,6 +332,15 @@ __device__ void selection_role(uint32_t tmem, uint64_t* acc_full, uint64_t* acc_
           }
         }
       }
+    };
+    const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(b * TC);
+#pragma unroll 1
+    for (int cb = 0; cb < TC; cb += kLd) {
+      uint32_t r[kLd];
+      tmem_ld16(lane_base + (uint32_t)cb, r);
+      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+      regs_ready(r);
+      chunk(r, cb);
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     mbar_arrive(smem_u32(&acc_free[b]));
@@ -321,6 +360,66 @@ __device__ void selection_role(uint32_t tmem, uint64_t* acc_full, uint64_t* acc_
     for (int t = 0; t < HEAPC; ++t) out_idx[qi * HEAPC + t] = t < full ? hx[t * TQ + tid] : SENTI;
     out_thr[qi] = full == HEAPC ? hv[(HEAPC - 1) * TQ + tid] : INFINITY;
   }
+}
+
+// ---------------------------------------------------------------------------
+// Bounded role (warps 0-3 of the resident form's bounded re-scan, thread t =
+// listed query slot q0 + t): every candidate j < hi whose value v (computed as
+// in selection_role) is <= B goes to the query's list, in index order; the
+// count, which may exceed cap, to *cnt_out.
+// ---------------------------------------------------------------------------
+__device__ void bound_role(uint32_t tmem, uint64_t* acc_full, uint64_t* acc_free, bool qvalid, int64_t hi,
+                           int64_t ntiles, float qn, float B, const float* __restrict__ tnorm,
+                           uint32_t* __restrict__ my_list, int cap, uint32_t* __restrict__ cnt_out,
+                           volatile int* abort_flag, int* err) {
+  const int warp = threadIdx.x >> 5;
+  uint32_t cnt = 0;
+  for (int64_t t = 0; t < ntiles; ++t) {
+    const int b = (int)(t & 1);
+    if (!mbar_wait_bounded(smem_u32(&acc_full[b]), (uint32_t)((t >> 1) & 1), abort_flag, err)) break;
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const int64_t c0 = t * TC;
+    const bool full = c0 + TC <= hi;
+    const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(b * TC);
+#pragma unroll 1
+    for (int cb = 0; cb < TC; cb += kLd) {
+      uint32_t r[kLd];
+      tmem_ld16(lane_base + (uint32_t)cb, r);
+      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+      regs_ready(r);
+      if (!qvalid) continue;
+      const float4* tn = reinterpret_cast<const float4*>(tnorm + (size_t)t * TC + cb);
+      float v[kLd];
+#pragma unroll
+      for (int i = 0; i < kLd / 4; ++i) {
+        const float4 v4 = __ldg(tn + i);
+        v[4 * i] = fmaf(-2.f, __uint_as_float(r[4 * i]), qn + v4.x);
+        v[4 * i + 1] = fmaf(-2.f, __uint_as_float(r[4 * i + 1]), qn + v4.y);
+        v[4 * i + 2] = fmaf(-2.f, __uint_as_float(r[4 * i + 2]), qn + v4.z);
+        v[4 * i + 3] = fmaf(-2.f, __uint_as_float(r[4 * i + 3]), qn + v4.w);
+      }
+      float m8[kLd / 2];
+#pragma unroll
+      for (int c = 0; c < kLd / 2; ++c) m8[c] = fminf(v[2 * c], v[2 * c + 1]);
+#pragma unroll
+      for (int w2 = kLd / 4; w2 >= 1; w2 >>= 1)
+#pragma unroll
+        for (int c = 0; c < w2; ++c) m8[c] = fminf(m8[2 * c], m8[2 * c + 1]);
+      if (m8[0] <= B) {
+#pragma unroll
+        for (int c = 0; c < kLd; ++c) {
+          const int64_t j = c0 + cb + c;
+          if (v[c] <= B && (full || j < hi)) {
+            if (cnt < (uint32_t)cap) my_list[cnt] = (uint32_t)j;
+            ++cnt;
+          }
+        }
+      }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    mbar_arrive(smem_u32(&acc_free[b]));
+  }
+  if (qvalid && !*abort_flag) *cnt_out = cnt;
 }
 
 // ---------------------------------------------------------------------------
@@ -529,12 +628,25 @@ __device__ __forceinline__ void tmem_st16(uint32_t taddr, const uint32_t (&v)[16
 // (hi sub-tile, then lo), and their squared norms, 128 per tile, in tnorm;
 // tiles of the point set of block b numbered from tile_base[blk_job[b]] (from
 // 0 without a block table).
+// BOUND: the bounded re-scan of the listed rows ba.qrows (see bound_role)
+// over every row of X, instead of the candidate lists.
+struct BoundArgs {
+  const uint32_t* qrows = nullptr;
+  const float* qbound = nullptr;
+  int64_t nq = 0;
+  uint32_t* list = nullptr;
+  uint32_t* list_cnt = nullptr;
+  int cap = 0;
+};
+
+template <bool BOUND>
 __global__ void __launch_bounds__(kResThreads, 1)
     knn_tc_res_kernel(const float* __restrict__ Xp, const float* __restrict__ Xs, const float* __restrict__ tnorm,
                       int64_t n, int dim_pad,
                       const float* __restrict__ norms, uint32_t* __restrict__ out_idx, float* __restrict__ out_thr,
                       const int64_t* __restrict__ blk_q0, const int32_t* __restrict__ blk_job,
-                      const int64_t* __restrict__ seg_off, const int64_t* __restrict__ tile_base, int* __restrict__ err) {
+                      const int64_t* __restrict__ seg_off, const int64_t* __restrict__ tile_base, int* __restrict__ err,
+                      BoundArgs ba) {
   extern __shared__ __align__(1024) unsigned char smem[];
   unsigned char* ring = smem + kSelSmem;
   __shared__ __align__(8) ResBars bars;
@@ -543,7 +655,7 @@ __global__ void __launch_bounds__(kResThreads, 1)
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   int64_t q0 = (int64_t)blockIdx.x * TQ, lo = 0, hi = n, tb = 0;
-  if (blk_q0) {
+  if (!BOUND && blk_q0) {
     const int jb = blk_job[blockIdx.x];
     q0 = blk_q0[blockIdx.x];
     lo = seg_off[jb];
@@ -646,9 +758,11 @@ __global__ void __launch_bounds__(kResThreads, 1)
       mbar_drain(smem_u32(&bars.done), 0, err);
     }
   } else {
-    // ---- query row q0 + tid into tensor memory lane tid, then selection
-    const int64_t qi = q0 + tid;
-    const bool qvalid = qi < hi;
+    // ---- query row q0 + tid (listed row ba.qrows[q0 + tid] when BOUND) into
+    // tensor memory lane tid, then selection
+    const int64_t slot = q0 + tid;
+    const bool qvalid = BOUND ? slot < ba.nq : slot < hi;
+    const int64_t qi = BOUND ? (qvalid ? (int64_t)ba.qrows[slot] : 0) : slot;
     const float4* xq = reinterpret_cast<const float4*>(Xp + (qvalid ? qi : 0) * dim_pad);
     const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
     for (int ch = 0; ch < nch; ++ch) {
@@ -670,8 +784,13 @@ __global__ void __launch_bounds__(kResThreads, 1)
     asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     mbar_arrive(smem_u32(&bars.qready));
-    selection_role(tmem, bars.acc_full, bars.acc_free, smem, q0, lo, hi, ntiles, norms, tnorm, tb, out_idx, out_thr,
-                   &abort_flag, err);
+    if (BOUND)
+      bound_role(tmem, bars.acc_full, bars.acc_free, qvalid, hi, ntiles, qvalid ? norms[qi] : 0.f,
+                 qvalid ? ba.qbound[slot] : 0.f, tnorm, ba.list + (size_t)(qvalid ? slot : 0) * ba.cap, ba.cap,
+                 ba.list_cnt + (qvalid ? slot : 0), &abort_flag, err);
+    else
+      selection_role(tmem, bars.acc_full, bars.acc_free, smem, q0, lo, hi, ntiles, norms, tnorm, tb, out_idx, out_thr,
+                     &abort_flag, err);
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
@@ -764,6 +883,10 @@ void knn_tc_candidates(const float* X, int64_t n, int dim, const float* norms, c
   }
   const bool resident = dim_pad <= kResDimMax && !staged_forced();
   ws.last_resident = resident;
+  ws.last_n = n;
+  ws.last_dim = dim;
+  ws.last_segmented = off != nullptr;
+  ws.last_xp = Xp;
   if (resident) {
     // candidate tiles per point set, numbered set after set
     const int64_t* tbase = nullptr;
@@ -785,9 +908,10 @@ void knn_tc_candidates(const float* X, int64_t n, int dim, const float* norms, c
     split_tiles_kernel<<<(unsigned)std::min<int64_t>(ceil_div(ntile * TC * (dim_pad / 4), 256), sm_grid(8, 8192)), 256, 0,
                          s>>>(Xp, norms, n, dim_pad, seg_off, tbase, nseg, ntile, Xs, tnorm);
     BHG_LAUNCH_CHECK();
-    BHG_CUDA(cudaFuncSetAttribute(knn_tc_res_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kResSmem));
-    knn_tc_res_kernel<<<(unsigned)nblocks, kResThreads, kResSmem, s>>>(Xp, Xs, tnorm, n, dim_pad, norms, cand, thr,
-                                                                       blk_q0, blk_job, seg_off, tbase, err);
+    BHG_CUDA(cudaFuncSetAttribute(knn_tc_res_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kResSmem));
+    knn_tc_res_kernel<false><<<(unsigned)nblocks, kResThreads, kResSmem, s>>>(Xp, Xs, tnorm, n, dim_pad, norms, cand, thr,
+                                                                              blk_q0, blk_job, seg_off, tbase, err,
+                                                                              BoundArgs{});
     BHG_LAUNCH_CHECK();
   } else {
     BHG_CUDA(cudaFuncSetAttribute(knn_tc_pipe_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPipeSmem));
@@ -799,6 +923,36 @@ void knn_tc_candidates(const float* X, int64_t n, int dim, const float* norms, c
   BHG_CUDA(cudaMemcpyAsync(&herr, err, 4, cudaMemcpyDeviceToHost, s));
   BHG_CUDA(cudaStreamSynchronize(s));
   if (herr) throw Error(ST_ETIMEDOUT, "error: the tensor-core kNN pass timed out waiting for its MMAs.");
+}
+
+bool knn_tc_can_bound(const KnnTcScratch& ws, int64_t n, int dim) {
+  return ws.last_resident && !ws.last_segmented && ws.last_n == n && ws.last_dim == dim && ws.split.ptr != nullptr;
+}
+
+void knn_tc_bounded(int64_t n, int dim, const float* norms, const uint32_t* qrows, const float* qbound, int64_t nq,
+                    uint32_t* list, uint32_t* list_cnt, int cap, KnnTcScratch& ws, cudaStream_t s) {
+  if (!knn_tc_can_bound(ws, n, dim)) throw Error(ST_EINTERNAL, "error: the bounded kNN re-scan needs the resident pass.");
+  const int dim_pad = (dim + PK - 1) / PK * PK;
+  const int64_t ntile = ceil_div(n, TC);
+  const float* Xs = static_cast<const float*>(ws.split.ptr);
+  const float* tnorm = Xs + (size_t)ntile * (dim_pad / PK) * (kResStage / 4);
+  int* err = static_cast<int*>(ws.err.ensure(64));
+  BHG_CUDA(cudaMemsetAsync(err, 0, 4, s));
+  BoundArgs ba;
+  ba.qrows = qrows;
+  ba.qbound = qbound;
+  ba.nq = nq;
+  ba.list = list;
+  ba.list_cnt = list_cnt;
+  ba.cap = cap;
+  BHG_CUDA(cudaFuncSetAttribute(knn_tc_res_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kResSmem));
+  knn_tc_res_kernel<true><<<(unsigned)ceil_div(nq, TQ), kResThreads, kResSmem, s>>>(
+      ws.last_xp, Xs, tnorm, n, dim_pad, norms, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, err, ba);
+  BHG_LAUNCH_CHECK();
+  int herr = 0;
+  BHG_CUDA(cudaMemcpyAsync(&herr, err, 4, cudaMemcpyDeviceToHost, s));
+  BHG_CUDA(cudaStreamSynchronize(s));
+  if (herr) throw Error(ST_ETIMEDOUT, "error: the tensor-core kNN re-scan timed out waiting for its MMAs.");
 }
 
 }  // namespace bhg

@@ -100,6 +100,7 @@ extern "C" {
     pub fn bhtsne_ctx_last_error(ctx: *const bhtsne_ctx) -> *const c_char;
     pub fn bhtsne_version() -> *const c_char;
     pub fn bhtsne_ctx_knn_fallback_rows(ctx: *const bhtsne_ctx, rows: *mut i64) -> c_int;
+    pub fn bhtsne_ctx_knn_brute_rows(ctx: *const bhtsne_ctx, rows: *mut i64) -> c_int;
 
     // ---- builder: tSNE::new (src/lib.rs:241-266) and its setters (:277-435)
     pub fn bhtsne_tsne_new(ctx: *mut bhtsne_ctx, dtype: c_int, embed_dim: i32, n_samples: i64,

@@ -63,9 +63,14 @@ const char* bhtsne_ctx_last_error(const bhtsne_ctx* ctx);
 const char* bhtsne_version(void);
 /* No reference counterpart: the number of rows of the last Euclidean kNN run
  * on this context (bhtsne_knn_euclidean, or the affinity build of a dense
- * barnes_hut / fit_sne finisher) whose tensor-core candidate list failed the
- * exactness certificate and were recomputed by exact brute force. */
+ * barnes_hut / fit_sne finisher) whose candidate list failed the exactness
+ * certificate and were recomputed exactly: by a bounded re-scan (every
+ * candidate within the row's error bound, re-ranked exactly) after the
+ * tensor-core pass, else by brute force. */
 int bhtsne_ctx_knn_fallback_rows(const bhtsne_ctx* ctx, int64_t* rows);
+/* No reference counterpart: of those rows, the ones recomputed by exact brute
+ * force (their bounded re-scan list overflowed, or no re-scan applied). */
+int bhtsne_ctx_knn_brute_rows(const bhtsne_ctx* ctx, int64_t* rows);
 
 /* ---- builder ------------------------------------------------------------- */
 /* tSNE::new (src/lib.rs:241-266): defaults lr auto, 1000 epochs, momentum

@@ -15,6 +15,15 @@ from conftest import blobs
 pytestmark = pytest.mark.gpu
 
 
+def _manifold(n, dim, seed, shift):
+    """n points uniform in a 10 x 10 x 10 cube, embedded isometrically in dim
+    dimensions and moved by `shift` along every axis: neighbour counts grow
+    with the cube of the radius, and |q|^2 grows with the shift."""
+    rng = np.random.default_rng(seed)
+    Q, _ = np.linalg.qr(rng.normal(size=(dim, 3)))
+    return (rng.uniform(0.0, 10.0, size=(n, 3)) @ Q.T + shift)
+
+
 def _knn(gpu, X, k, staged):
     from bhtsne_gb300 import _lib as L
     old = os.environ.get("BHTSNE_KNN_TC_STAGED")
@@ -65,16 +74,47 @@ def test_resident_form_tail_tile_and_duplicates(gpu, oracle):
     assert np.array_equal(gd, od)
 
 
-def test_sliced_certified_fallback_exact(gpu, oracle):
-    """Points far from the origin: |q|^2 dwarfs the neighbour gaps, so the
-    candidate pass's error bound fails the certificate on most rows, and the
-    fallback (12,000 points: its candidate range split in two slices, merged)
-    recomputes them exactly."""
+@pytest.mark.parametrize("rescan", ["1", "0"])
+def test_certificate_failures_recomputed_exactly(gpu, oracle, rescan):
+    """Points away from the origin: |q|^2 is large next to the gap between the
+    30th and the 128th candidate, so the candidate pass's error bound fails the
+    certificate on most rows. With the
+    bounded re-scan those rows take every candidate within their bound and
+    re-rank it exactly (the rows whose list overflows take the brute force);
+    without it (BHTSNE_KNN_RESCAN=0) they all take the brute force, whose
+    candidate range (12,000 points) is split in two slices and merged. Both
+    equal the oracle's brute force."""
     from bhtsne_gb300 import _lib as L
-    X, _ = blobs(12000, 64, 10, 21, spread=2.0)
-    X = (X + np.float32(1000.0)).astype(np.float32)
+    X = _manifold(12000, 64, 21, 20.0).astype(np.float32)
+    old = os.environ.get("BHTSNE_KNN_RESCAN")
+    os.environ["BHTSNE_KNN_RESCAN"] = rescan
+    try:
+        gi, gd = gpu.knn_euclidean(X, 30)
+    finally:
+        if old is None:
+            del os.environ["BHTSNE_KNN_RESCAN"]
+        else:
+            os.environ["BHTSNE_KNN_RESCAN"] = old
+    ctx = L.default_context()
+    failed, brute = ctx.knn_fallback_rows(), ctx.knn_brute_rows()
+    assert failed > 100
+    if rescan == "0":
+        assert brute == failed
+    else:
+        assert brute < failed
+    oi, od = oracle.knn(X, 30)
+    assert np.array_equal(gi, oi)
+    assert np.array_equal(gd, od)
+
+
+def test_bounded_rescan_f64(gpu, oracle):
+    """The same rows in f64: the candidate pass runs on an f32 copy, the
+    re-scan's lists are re-ranked in f64."""
+    from bhtsne_gb300 import _lib as L
+    X = _manifold(9000, 48, 22, 20.0).astype(np.float64)
     gi, gd = gpu.knn_euclidean(X, 30)
-    assert L.default_context().knn_fallback_rows() > 1000
+    ctx = L.default_context()
+    assert ctx.knn_fallback_rows() > 100 and ctx.knn_brute_rows() < ctx.knn_fallback_rows()
     oi, od = oracle.knn(X, 30)
     assert np.array_equal(gi, oi)
     assert np.array_equal(gd, od)
