@@ -242,6 +242,11 @@ __device__ void selection_role(uint32_t tmem, uint64_t* acc_full, uint64_t* acc_
   int cnt = 0, np = 0;
   float rootv = INFINITY;
   uint32_t rootx = SENTI;
+  // In a tile without the query's own row and past the set's end, every
+  // candidate's index exceeds every heap entry's (the scan runs in index
+  // order), so (v, x) beats the root iff v < rootv once the heap is full, and
+  // always while it is not: the test is v <= lim.
+  float lim = INFINITY;
   auto merge = [&]() {
     const int rounds = __reduce_max_sync(0xffffffffu, (unsigned)np);
     for (int i = 0; i < rounds; ++i) {
@@ -261,6 +266,7 @@ __device__ void selection_role(uint32_t tmem, uint64_t* acc_full, uint64_t* acc_
     if (cnt == HEAPC) {
       rootv = hv[tid];
       rootx = hx[tid];
+      lim = nextafterf(rootv, -INFINITY);
     }
   };
   for (int64_t t = 0; t < ntiles; ++t) {
@@ -306,18 +312,16 @@ __device__ void selection_role(uint32_t tmem, uint64_t* acc_full, uint64_t* acc_
         for (int w2 = kLd / 4; w2 >= 1; w2 >>= 1)
 #pragma unroll
           for (int c = 0; c < w2; ++c) m8[c] = fminf(m8[2 * c], m8[2 * c + 1]);
-        if (m8[0] <= rootv) {
+        if (m8[0] <= lim) {
           uint32_t at = smem_u32(pend + (size_t)np * TQ + tid);
 #pragma unroll
           for (int c = 0; c < kLd; ++c) {
-            const uint32_t x = x0 + c;
-            const uint32_t a = (v[c] < rootv || (v[c] == rootv && x < rootx)) ? 1u : 0u;
             asm volatile(
-                "{\n\t.reg .pred q;\n\tsetp.ne.u32 q, %3, 0;\n\t@q st.shared.v2.u32 [%0], {%1, %2};\n\t}\n" ::"r"(at),
-                "r"(__float_as_uint(v[c])), "r"(x), "r"(a)
+                "{\n\t.reg .pred p;\n\tsetp.le.f32 p, %2, %3;\n\t@p st.shared.v2.u32 [%0], {%4, %5};\n\t"
+                "@p add.u32 %0, %0, %6;\n\t@p add.s32 %1, %1, 1;\n\t}\n"
+                : "+r"(at), "+r"(np)
+                : "f"(v[c]), "f"(lim), "r"(__float_as_uint(v[c])), "r"(x0 + c), "n"(TQ * (int)sizeof(uint2))
                 : "memory");
-            np += (int)a;
-            at += a * (uint32_t)(TQ * sizeof(uint2));
           }
         }
       } else {
