@@ -123,6 +123,27 @@ __device__ __forceinline__ bool lt_vi(float a, uint32_t ai, float b, uint32_t bi
   return a < b || (a == b && ai < bi);
 }
 
+// Paired single-precision add and fused multiply-add (sm_100 and later):
+// each lane is the scalar IEEE operation rounded to nearest.
+__device__ __forceinline__ unsigned long long pk2(float a, float b) {
+  unsigned long long r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+  return r;
+}
+__device__ __forceinline__ void upk2(unsigned long long x, float& a, float& b) {
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(x));
+}
+__device__ __forceinline__ unsigned long long add2(unsigned long long x, unsigned long long y) {
+  unsigned long long r;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(x), "l"(y));
+  return r;
+}
+__device__ __forceinline__ unsigned long long fma2(unsigned long long x, unsigned long long y, unsigned long long z) {
+  unsigned long long r;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(x), "l"(y), "l"(z));
+  return r;
+}
+
 __device__ __forceinline__ float tf32_hi(float x) {
   uint32_t b = __float_as_uint(x);
   if ((b & 0x7f800000u) != 0x7f800000u) b = (b + 0x1000u) & 0xffffe000u;
@@ -299,11 +320,14 @@ __device__ void selection_role(uint32_t tmem, uint64_t* acc_full, uint64_t* acc_
         // all 16 values first (independent), one test of their minimum
         // against the root, and only then the per-value tests and appends as
         // predicated stores (no branch per value)
+        // v = (qn + cn) - 2 d, two values per instruction: qn + cn rounded,
+        // then 2 d is exact, so the fused multiply-add rounds once more
         float v[kLd];
+        const unsigned long long qq = pk2(qn, qn), m2 = pk2(-2.f, -2.f);
 #pragma unroll
-        for (int c = 0; c < kLd; ++c) {
-          // 2 d is exact, so this equals (qn + cn) - 2 d rounded once
-          v[c] = fmaf(-2.f, __uint_as_float(r[c]), qn + cn[c]);
+        for (int c = 0; c < kLd; c += 2) {
+          const unsigned long long s2 = add2(qq, pk2(cn[c], cn[c + 1]));
+          upk2(fma2(m2, pk2(__uint_as_float(r[c]), __uint_as_float(r[c + 1])), s2), v[c], v[c + 1]);
         }
         float m8[kLd / 2];
 #pragma unroll
