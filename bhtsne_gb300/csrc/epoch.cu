@@ -54,6 +54,39 @@ struct AttrTask {
 
 constexpr uint32_t kPartialBit = 0x80000000u;
 
+// The terms of a task's entries lane + 32 u, u < NU, added to acc. Entries
+// past the task's end add exactly zero, so running NU = ceil(len / 32) steps
+// instead of kU gives the same sums.
+template <class T, int D, bool VEC, int NU>
+__device__ __forceinline__ void attr_accumulate(uint64_t begin, int len, int64_t slot, int lane,
+                                                const uint32_t* __restrict__ cols, const T* __restrict__ vals,
+                                                const T* __restrict__ y, const T (&yi)[D], T (&acc)[D]) {
+  uint32_t j[NU];
+  T p[NU];
+  T yj[NU][D];
+#pragma unroll
+  for (int u = 0; u < NU; ++u) {
+    const int e = lane + 32 * u;
+    j[u] = e < len ? __ldcs(cols + begin + e) : (uint32_t)slot;
+    p[u] = e < len ? __ldcs(vals + begin + e) : T(0);
+  }
+#pragma unroll
+  for (int u = 0; u < NU; ++u) load_point<T, D, VEC>(y, (int64_t)j[u], yj[u]);
+#pragma unroll
+  for (int u = 0; u < NU; ++u) {
+    T disp[D];
+    T dist = T(0);
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+      disp[a] = yi[a] - yj[u][a];
+      dist += disp[a] * disp[a];
+    }
+    const T factor = p[u] / (dist + T(1));
+#pragma unroll
+    for (int a = 0; a < D; ++a) acc[a] += factor * disp[a];
+  }
+}
+
 template <class T, int D, bool VEC, int kU>
 __global__ void __launch_bounds__(256) attractive_task_kernel(const AttrTask* __restrict__ tasks, int64_t ntasks,
                                                               const uint32_t* __restrict__ cols,
@@ -71,29 +104,25 @@ __global__ void __launch_bounds__(256) attractive_task_kernel(const AttrTask* __
     yi[a] = y[slot * D + a];
     acc[a] = T(0);
   }
-  uint32_t j[kU];
-  T p[kU];
-  T yj[kU][D];
-#pragma unroll
-  for (int u = 0; u < kU; ++u) {
-    const int e = lane + 32 * u;
-    j[u] = e < len ? __ldcs(cols + tk.begin + e) : (uint32_t)slot;
-    p[u] = e < len ? __ldcs(vals + tk.begin + e) : T(0);
-  }
-#pragma unroll
-  for (int u = 0; u < kU; ++u) load_point<T, D, VEC>(y, (int64_t)j[u], yj[u]);
-#pragma unroll
-  for (int u = 0; u < kU; ++u) {
-    T disp[D];
-    T dist = T(0);
-#pragma unroll
-    for (int a = 0; a < D; ++a) {
-      disp[a] = yi[a] - yj[u][a];
-      dist += disp[a] * disp[a];
-    }
-    const T factor = p[u] / (dist + T(1));
-#pragma unroll
-    for (int a = 0; a < D; ++a) acc[a] += factor * disp[a];
+  // as many steps of 32 entries as the task holds (uniform per warp)
+  switch ((len + 31) >> 5) {
+    case 0:
+      break;
+    case 1:
+      attr_accumulate<T, D, VEC, 1>(tk.begin, len, slot, lane, cols, vals, y, yi, acc);
+      break;
+    case 2:
+      if constexpr (kU >= 2) attr_accumulate<T, D, VEC, 2>(tk.begin, len, slot, lane, cols, vals, y, yi, acc);
+      break;
+    case 3:
+      if constexpr (kU >= 3) attr_accumulate<T, D, VEC, 3>(tk.begin, len, slot, lane, cols, vals, y, yi, acc);
+      break;
+    case 4:
+      if constexpr (kU >= 4) attr_accumulate<T, D, VEC, 4>(tk.begin, len, slot, lane, cols, vals, y, yi, acc);
+      break;
+    default:
+      if constexpr (kU > 4) attr_accumulate<T, D, VEC, kU>(tk.begin, len, slot, lane, cols, vals, y, yi, acc);
+      break;
   }
 #pragma unroll
   for (int a = 0; a < D; ++a) {
