@@ -120,8 +120,17 @@ __global__ void __launch_bounds__(256) attractive_task_kernel(const AttrTask* __
     case 4:
       if constexpr (kU >= 4) attr_accumulate<T, D, VEC, 4>(tk.begin, len, slot, lane, cols, vals, y, yi, acc);
       break;
+    case 5:
+      if constexpr (kU >= 5) attr_accumulate<T, D, VEC, 5>(tk.begin, len, slot, lane, cols, vals, y, yi, acc);
+      break;
+    case 6:
+      if constexpr (kU >= 6) attr_accumulate<T, D, VEC, 6>(tk.begin, len, slot, lane, cols, vals, y, yi, acc);
+      break;
+    case 7:
+      if constexpr (kU >= 7) attr_accumulate<T, D, VEC, 7>(tk.begin, len, slot, lane, cols, vals, y, yi, acc);
+      break;
     default:
-      if constexpr (kU > 4) attr_accumulate<T, D, VEC, kU>(tk.begin, len, slot, lane, cols, vals, y, yi, acc);
+      if constexpr (kU >= 8) attr_accumulate<T, D, VEC, 8>(tk.begin, len, slot, lane, cols, vals, y, yi, acc);
       break;
   }
 #pragma unroll
