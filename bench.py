@@ -880,6 +880,24 @@ def run_fft_only(args):
                                    "note": "host wall time per call, including the copies of y in and forces out"}}))
 
 
+def run_fit_only(args):
+    """The 1M FIt-SNE configuration alone (2-D, the bh2d workload's affinities at
+    --n points, seeded start): --burn-in, --warmup and --steps epochs, then a
+    profiled pass for the phase split, as in the configurations leg."""
+    import bhtsne_gb300 as bg
+    ctx = bg.Context(0)
+    X, _ = make_workload(args.n, seed=args.seed)
+    t0 = bg.TSNE(X, D=2, ctx=ctx).perplexity(30.0).epochs(0).initial_embedding(initial_embedding(args.n))
+    t0.barnes_hut(0.5)
+    aff = t0.affinities()
+    t0.close()
+    t = bg.TSNE(args.n, D=2, ctx=ctx).with_affinities(aff).epochs(0).initial_embedding(initial_embedding(args.n))
+    t.fit_sne()
+    eps, ph = timed_epochs(t, args)
+    print(json.dumps({"fitsne2d": {"n_points": args.n, "epochs_per_s": eps, "phase_ms_per_epoch": ph,
+                                   "burn_in_epochs": args.burn_in, "steps": args.steps}}))
+
+
 def run_knn_only(args):
     """The affinity build's kNN alone on the 1M workload's distribution at --n
     points (k = 90): a 2,000-row warm-up call, then all rows, timed on the host."""
@@ -923,6 +941,8 @@ def main():
     ap.add_argument("--serve-only", action="store_true", help="run only the serving comparison")
     ap.add_argument("--batch-only", action="store_true", help="run only the batched arm of the batch comparison")
     ap.add_argument("--knn-only", action="store_true", help="time only the kNN of the workload at --n points")
+    ap.add_argument("--fit-only", action="store_true",
+                    help="time only the 2-D FIt-SNE configuration on the workload's affinities at --n points")
     ap.add_argument("--fft-only", action="store_true",
                     help="time only the FIt-SNE repulsion of --n points at the largest grid")
     ap.add_argument("--no-configs", dest="configs", action="store_false",
@@ -932,6 +952,9 @@ def main():
         return run_fft_only(args)
     if args.knn_only:
         run_knn_only(args)
+        return
+    if args.fit_only:
+        run_fit_only(args)
         return
     if args.serve_only:
         import bhtsne_gb300 as bg

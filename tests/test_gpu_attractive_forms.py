@@ -67,3 +67,4 @@ def test_short_and_empty_rows(gpu, oracle):
     opos = oracle.edge_forces(y, rows, cols, vals)
     assert rel_l2(pos, opos) < 1e-5
     assert np.all(pos[3] == 0)
+
