@@ -21,9 +21,17 @@
 //  * normalize_p_values: src/tsne/mod.rs:284-293; stop_lying: :525-531.
 #include "affinity.h"
 
+#include <cmath>
+#include <mutex>
+
 namespace bhg {
 
 namespace {
+
+// 2^(i / 256), i < 256, in double: the table of exp_table_f32 (filled once per
+// device by launch_search_beta).
+constexpr int kExpTab = 256;
+__device__ double g_exp2_tab[kExpTab];
 
 // ---------------------------------------------------------------------------
 // search_beta: one warp per row. The lanes evaluate the kernel values of the
@@ -37,6 +45,41 @@ namespace {
 template <class T>
 __device__ __forceinline__ T exp_rn(T x) {
   return (T)exp((double)x);
+}
+
+// exp(x) of a single-precision x <= 0, computed in FP64 with few FP64
+// operations by Tang's table-driven method: x = (256 m + i) ln2 / 256 + r
+// with |r| <= ln2 / 512 (i and m from a single-precision product, whose
+// rounding moves that bound by under 0.5 %), exp(x) = 2^m 2^(i/256) exp(r),
+// and exp(r) - 1 by its Taylor series to r^4 (the next term is below 2^-54
+// relative). The FP64 value is within a few units in its last place of
+// exp(x), so its rounding to single precision is the correctly rounded result
+// but when exp(x) lies that close to a rounding boundary, as with exp((double)x)
+// itself. Below -110 the result rounds to zero.
+__device__ __forceinline__ float exp_table_f32(float x) {
+  if (!(x >= -110.f)) return x != x ? x : 0.f;
+  const float tf = x * 369.32993046757463f;  // 256 / ln 2
+  const int nn = __float2int_rn(tf);
+  const int i = nn & (kExpTab - 1), m = nn >> 8;
+  // r = x - nn ln2 / 256, ln2 / 256 as a double pair (Cody and Waite)
+  const double ln2_256_hi = 0.0027076061740622863, ln2_256_lo = 9.058776616587108e-20;
+  double r = fma(-(double)nn, ln2_256_hi, (double)x);
+  r = fma(-(double)nn, ln2_256_lo, r);
+  double q = fma(r, 1.0 / 24.0, 1.0 / 6.0);
+  q = fma(q, r, 0.5);
+  q = fma(q, r, 1.0);
+  const double pr = q * r;  // exp(r) - 1
+  const double ti = __ldg(g_exp2_tab + i);
+  const double y = fma(ti, pr, ti);
+  return (float)(y * __hiloint2double((m + 1023) << 20, 0));
+}
+template <class T>
+__device__ __forceinline__ T exp_beta(T x) {
+  return exp_rn<T>(x);
+}
+template <>
+__device__ __forceinline__ float exp_beta<float>(float x) {
+  return exp_table_f32(x);
 }
 template <class T>
 __device__ __forceinline__ T log_rn(T x) {
@@ -61,7 +104,7 @@ __global__ void search_beta_kernel(const T* __restrict__ dist, int64_t n, int64_
   while (!found && iteration < 200) {
     for (int64_t j = lane; j < k; j += 32) {
       const T dj = d[j];
-      out[j] = exp_rn(-beta * (dj * dj));
+      out[j] = exp_beta<T>(-beta * (dj * dj));
     }
     __syncwarp();
     T s = T(0), e = T(0);
@@ -275,6 +318,20 @@ constexpr int kSumBlocksMax = 1024;  // partials of launch_sum (two blocks per S
 template <class T>
 void launch_search_beta(const T* dist, int64_t n, int64_t k, T perplexity, T* p, int32_t* iters, cudaStream_t s) {
   if (n <= 0) return;
+  {
+    // the exp table of this device, once
+    static std::mutex mu;
+    static bool filled[256] = {};
+    int dev = 0;
+    BHG_CUDA(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lk(mu);
+    if (dev >= 0 && dev < 256 && !filled[dev]) {
+      double tab[kExpTab];
+      for (int i = 0; i < kExpTab; ++i) tab[i] = std::exp2((double)i / kExpTab);
+      BHG_CUDA(cudaMemcpyToSymbol(g_exp2_tab, tab, sizeof tab));
+      filled[dev] = true;
+    }
+  }
   const int threads = 256;
   const unsigned grid = (unsigned)ceil_div(n * 32, threads);
   search_beta_kernel<T><<<grid, threads, 0, s>>>(dist, n, k, perplexity, p, iters);

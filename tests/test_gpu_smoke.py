@@ -45,6 +45,23 @@ def test_conditional_p(gpu, oracle):
     gp, _ = gpu.conditional_p(od, 30.0)
     op, _ = oracle.search_beta(od, 30.0)
     assert np.max(np.abs(gp - op) / np.maximum(op, 1e-30)) < 1e-5
+    # single precision: exp by the table-driven FP64 method; the values match
+    # the oracle's libm expf bit for bit but for the rare rounding-boundary case
+    assert np.mean(gp == op) > 0.999
+
+
+def test_conditional_p_large_and_tiny_betas(gpu, oracle):
+    """Rows whose bisection drives beta far up (tight neighbourhoods: most
+    kernel values underflow) and far down (spread-out ones)."""
+    rng = np.random.default_rng(12)
+    d = np.sort(rng.random((3000, 90)).astype(np.float32), axis=1)
+    d[:1000] *= np.float32(1e-3)
+    d[1000:2000] *= np.float32(1e3)
+    gp, gi = gpu.conditional_p(d, 30.0)
+    op, oi = oracle.search_beta(d, 30.0)
+    assert np.mean(gi == oi) > 0.999
+    assert np.max(np.abs(gp - op) / np.maximum(op, 1e-30)) < 1e-5
+    assert np.mean(gp == op) > 0.999
 
 
 def test_symmetrize_bit_exact(gpu, oracle):
