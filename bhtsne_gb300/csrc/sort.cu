@@ -385,6 +385,7 @@ constexpr uint32_t kOsInc = 2u << 30;  // word holds the inclusive prefix throug
 constexpr uint32_t kOsMask = (1u << 30) - 1u;
 constexpr long long kOsSpinLimit = 1LL << 22;
 constexpr int kOsMaxPass = 8;
+constexpr int kOsLook = 4;  // earlier tiles' words a look-back step loads at once
 
 // Digit counts of passes 0 .. npass-1 (digit shift begin_bit + 8 q) in one read.
 __global__ void __launch_bounds__(256) os_hist_kernel(const uint64_t* __restrict__ keys, int64_t n, int begin_bit,
@@ -490,19 +491,30 @@ __global__ void __launch_bounds__(kRsThreads, 4) os_pass_kernel(const uint64_t* 
     os_store(st, kOsInc | tot);
   } else {
     os_store(st, kOsAgg | tot);
-    for (int64_t pb = b - 1; pb >= 0; --pb) {
-      const uint32_t* sp = status + pb * 256 + tid;
-      uint32_t word = os_load(sp);
-      long long spins = 0;
-      while ((word & ~kOsMask) == 0u) {
-        if (++spins >= kOsSpinLimit) {
-          atomicExch(&g_radix_fault, 1u);
-          break;
+    // Walk back kOsLook tiles per step: their words are loaded together, then
+    // taken in tile order (a word read early is at worst an aggregate where
+    // the tile has since published its prefix: the sum is the same). Tile 0
+    // always holds an inclusive prefix, so the walk ends there at the latest.
+    bool done = false;
+    for (int64_t pb = b - 1; !done; pb -= kOsLook) {
+      uint32_t wv[kOsLook];
+#pragma unroll
+      for (int i = 0; i < kOsLook; ++i) wv[i] = pb - i >= 0 ? os_load(status + (pb - i) * 256 + tid) : kOsInc;
+#pragma unroll
+      for (int i = 0; i < kOsLook; ++i) {
+        if (done) break;
+        uint32_t word = wv[i];
+        long long spins = 0;
+        while ((word & ~kOsMask) == 0u) {
+          if (++spins >= kOsSpinLimit) {
+            atomicExch(&g_radix_fault, 1u);
+            break;
+          }
+          word = os_load(status + (pb - i) * 256 + tid);
         }
-        word = os_load(sp);
+        excl += word & kOsMask;
+        done = (word & ~kOsMask) != kOsAgg;  // an inclusive prefix (or a wait that ran out)
       }
-      excl += word & kOsMask;
-      if ((word & ~kOsMask) != kOsAgg) break;  // an inclusive prefix (or a wait that ran out)
     }
     os_store(st, kOsInc | (excl + tot));
   }
