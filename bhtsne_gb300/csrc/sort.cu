@@ -385,7 +385,7 @@ constexpr uint32_t kOsInc = 2u << 30;  // word holds the inclusive prefix throug
 constexpr uint32_t kOsMask = (1u << 30) - 1u;
 constexpr long long kOsSpinLimit = 1LL << 22;
 constexpr int kOsMaxPass = 8;
-constexpr int kOsLook = 4;  // earlier tiles' words a look-back step loads at once
+constexpr int kOsLook = 8;  // earlier tiles' words a look-back step loads at once
 
 // Digit counts of passes 0 .. npass-1 (digit shift begin_bit + 8 q) in one read.
 __global__ void __launch_bounds__(256) os_hist_kernel(const uint64_t* __restrict__ keys, int64_t n, int begin_bit,
